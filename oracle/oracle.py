@@ -1,0 +1,197 @@
+"""Python driver for the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Loads oracle/_build/libdfg_oracle.so (the C restatement in dfg_oracle.c,
+built by ``make -C oracle port``) and runs the whole hot path of the
+reference on a ``delfem_gb300.meshgen.Problem``: pattern, assembly,
+extra loads, Dirichlet finalize, ILU(0), PCG.  Only tests/, the smoke test
+and bench.py's CPU-baseline leg import this module; the product never does.
+
+``run_reference_harness`` executes the reference itself (oracle/_ref,
+compiled from the reference sources) on the same problem; it exists only
+where that build exists.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libdfg_oracle.so")
+HARNESS = os.path.join(HERE, "_ref", "ref_harness")
+
+_lib = None
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+
+
+def build() -> None:
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.dfo_pattern.restype = ctypes.c_long
+        L.dfo_pattern.argtypes = [_I, _I, _I, _P, _P, _P]
+        L.dfo_diaind.argtypes = [_I, _P, _P, _P]
+        for nm in ("dfo_assemble_poisson2d", "dfo_assemble_poisson3d"):
+            getattr(L, nm).argtypes = [_I, _P, _P, _I, _P, _P, _P, _D, _D, _P, _P, _P, _P]
+        L.dfo_assemble_diffusion2d.argtypes = [_I, _P, _P, _I, _P, _P, _P, _D, _D, _D, _D, _D, _P, _P, _P, _P, _P]
+        L.dfo_assemble_solid2d.argtypes = [_I, _P, _P, _I, _P, _P, _P, _D, _D, _D, _D, _D, _P, _P, _P, _P]
+        L.dfo_assemble_solid3d.argtypes = [_I, _P, _P, _I, _P, _P, _P, _D, _D, _D, _D, _D, _D, _P, _P, _P, _P]
+        L.dfo_finalize.restype = _D
+        L.dfo_finalize.argtypes = [_I, _I, _P, _P, _P, _P, _P, _P]
+        L.dfo_ilu0.argtypes = [_I, _I, _P, _P, _P, _P, _P]
+        L.dfo_forward.argtypes = [_I, _I, _P, _P, _P, _P, _P, _P]
+        L.dfo_backward.argtypes = [_I, _I, _P, _P, _P, _P, _P]
+        L.dfo_matvec.argtypes = [_I, _I, _P, _P, _P, _P, _D, _P, _D, _P]
+        L.dfo_pcg.argtypes = [_I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                              ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_uint), _P]
+        L.dfo_now.restype = _D
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def pattern(nnode: int, conn: np.ndarray):
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    L = lib()
+    nnz = L.dfo_pattern(nnode, conn.shape[0], conn.shape[1], _p(conn), None, None)
+    if nnz < 0:
+        raise ValueError("bad connectivity")
+    rowptr = np.zeros(nnode + 1, dtype=np.int32)
+    colind = np.zeros(max(nnz, 1), dtype=np.int32)
+    L.dfo_pattern(nnode, conn.shape[0], conn.shape[1], _p(conn), _p(rowptr), _p(colind))
+    return rowptr, colind[:nnz]
+
+
+def diaind(rowptr, colind):
+    n = rowptr.size - 1
+    d = np.zeros(n, dtype=np.int32)
+    lib().dfo_diaind(n, _p(rowptr), _p(colind), _p(d))
+    return d
+
+
+def assemble(p, rowptr, colind):
+    """Returns (diag, offd, res) before loads / Dirichlet finalize."""
+    from delfem_gb300 import meshgen as mg
+    n, b = p.nnode, p.b
+    bs = b * b
+    diag = np.zeros(n * bs)
+    offd = np.zeros(max(colind.size, 1) * bs)
+    res = np.zeros(n * b)
+    L = lib()
+    coords = np.ascontiguousarray(p.coords, dtype=np.float64)
+    conn = np.ascontiguousarray(p.conn, dtype=np.int32)
+    coef = None if p.coef is None else np.ascontiguousarray(p.coef, dtype=np.float64)
+    u = None if p.u is None else np.ascontiguousarray(p.u, dtype=np.float64)
+    v = None if p.v is None else np.ascontiguousarray(p.v, dtype=np.float64)
+    P = [float(x) for x in p.params]
+    common = (n, _p(rowptr), _p(colind), p.nelem, _p(conn), _p(coords), _p(coef))
+    if p.kind == mg.POISSON2D:
+        rc = L.dfo_assemble_poisson2d(*common, P[0], P[1], _p(u), _p(diag), _p(offd), _p(res))
+    elif p.kind == mg.POISSON3D:
+        rc = L.dfo_assemble_poisson3d(*common, P[0], P[1], _p(u), _p(diag), _p(offd), _p(res))
+    elif p.kind == mg.DIFFUSION2D:
+        rc = L.dfo_assemble_diffusion2d(*common, P[0], P[1], P[2], P[3], P[4], _p(u), _p(v),
+                                        _p(diag), _p(offd), _p(res))
+    elif p.kind == mg.SOLID2D:
+        rc = L.dfo_assemble_solid2d(*common, P[0], P[1], P[2], P[3], P[4], _p(u),
+                                    _p(diag), _p(offd), _p(res))
+    elif p.kind == mg.SOLID3D:
+        rc = L.dfo_assemble_solid3d(*common, P[0], P[1], P[2], P[3], P[4], P[5], _p(u),
+                                    _p(diag), _p(offd), _p(res))
+    else:
+        raise ValueError(p.kind)
+    if rc != 0:
+        raise ValueError("assembly failed")
+    return diag, offd[: colind.size * bs], res
+
+
+def solve(p, tol=None, maxit=None, stop_after_ilu=False) -> dict:
+    """The reference's whole path on the CPU; returns every intermediate."""
+    L = lib()
+    t0 = L.dfo_now()
+    rowptr, colind = pattern(p.nnode, p.conn)
+    n, b = p.nnode, p.b
+    bs = b * b
+    diag, offd, res = assemble(p, rowptr, colind)
+    if p.load is not None:
+        res = res + np.asarray(p.load, dtype=np.float64)
+    t1 = L.dfo_now()
+    bc = np.ascontiguousarray(p.bcflag, dtype=np.int32)
+    offd_c = np.ascontiguousarray(offd) if offd.size else np.zeros(1)
+    norm_res = L.dfo_finalize(n, b, _p(rowptr), _p(colind), _p(bc), _p(diag), _p(offd_c), _p(res))
+    offd = offd_c[: colind.size * bs]
+    rhs = res.copy()
+    dind = diaind(rowptr, colind)
+    fdiag = diag.copy()
+    foffd = offd.copy() if offd.size else np.zeros(1)
+    t2 = L.dfo_now()
+    ilu_rc = L.dfo_ilu0(n, b, _p(rowptr), _p(colind), _p(dind), _p(fdiag), _p(foffd))
+    t3 = L.dfo_now()
+    out = dict(n=n, b=b, nnz=colind.size, rowptr=rowptr, colind=colind, diaind=dind,
+               diag=diag, offd=offd, rhs=rhs, norm_res=norm_res, ilu_rc=ilu_rc,
+               fdiag=fdiag, foffd=foffd[: colind.size * bs], t_assemble=t1 - t0, t_ilu=t3 - t2)
+    if stop_after_ilu:
+        return out
+    r = rhs.copy()
+    x = np.zeros(n * b)
+    work = np.zeros(2 * n * b)
+    conv = ctypes.c_double(p.tol if tol is None else tol)
+    it = ctypes.c_uint(p.maxit if maxit is None else maxit)
+    offd_a = offd if offd.size else np.zeros(1)
+    t4 = L.dfo_now()
+    ok = L.dfo_pcg(n, b, _p(rowptr), _p(colind), _p(dind), _p(diag), _p(offd_a), _p(fdiag), _p(foffd),
+                   _p(r), _p(x), ctypes.byref(conv), ctypes.byref(it), _p(work))
+    t5 = L.dfo_now()
+    out.update(x=x, conv=conv.value, iter=it.value, converged=bool(ok), t_pcg=t5 - t4)
+    return out
+
+
+def matvec(n, b, rowptr, colind, diag, offd, x, alpha=1.0, beta=0.0, y=None):
+    y = np.zeros(n * b) if y is None else y.copy()
+    offd_a = offd if offd.size else np.zeros(1)
+    lib().dfo_matvec(n, b, _p(rowptr), _p(colind), _p(diag), _p(offd_a), alpha, _p(x), beta, _p(y))
+    return y
+
+
+def precond(n, b, rowptr, colind, dind, fdiag, foffd, r):
+    z = np.array(r, dtype=np.float64, copy=True)
+    fo = foffd if foffd.size else np.zeros(1)
+    lib().dfo_forward(n, b, _p(rowptr), _p(colind), _p(dind), _p(fdiag), _p(fo), _p(z))
+    lib().dfo_backward(n, b, _p(rowptr), _p(colind), _p(dind), _p(fo), _p(z))
+    return z
+
+
+def true_residual(out: dict, x: np.ndarray) -> float:
+    """||b - A x|| / ||b|| in FP64 with the assembled (post-BC) matrix."""
+    Ax = matvec(out["n"], out["b"], out["rowptr"], out["colind"], out["diag"], out["offd"], x)
+    bn = float(np.linalg.norm(out["rhs"]))
+    return float(np.linalg.norm(out["rhs"] - Ax)) / (bn if bn > 0 else 1.0)
+
+
+def harness_available() -> bool:
+    return os.path.exists(HARNESS)
+
+
+def run_reference_harness(p) -> dict:
+    """Runs the reference code itself (oracle/_ref/ref_harness) on ``p``."""
+    from delfem_gb300 import meshgen as mg
+    with tempfile.TemporaryDirectory() as td:
+        fi, fo = os.path.join(td, "p.bin"), os.path.join(td, "r.bin")
+        mg.write_problem(p, fi)
+        subprocess.run([HARNESS, fi, fo], check=True, stdout=subprocess.DEVNULL)
+        return mg.read_result(fo)
