@@ -1,0 +1,119 @@
+"""ctypes binding of libdfg's C ABI (include/dfg.h).
+
+The library is loaded from the package directory (built in-tree by
+``delfem_gb300.build``).  There is no fallback: if the shared library is
+missing or cannot be loaded, ``lib()`` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdfg.so")
+HEADER = os.path.join(HERE, "..", "include", "dfg.h")
+
+DFG_OK = 0
+DFG_NOT_CONVERGED = 1
+DFG_SINGULAR_PIVOT = 2
+DFG_NAN_DETECTED = 3
+DFG_OOM_REJECTED = 4
+DFG_TIMEOUT = 5
+DFG_INVALID_ARGUMENT = 6
+DFG_CUDA_ERROR = 7
+DFG_NOT_READY = 8
+STATUS_NAMES = {0: "OK", 1: "NOT_CONVERGED", 2: "SINGULAR_PIVOT", 3: "NAN_DETECTED", 4: "OOM_REJECTED",
+                5: "TIMEOUT", 6: "INVALID_ARGUMENT", 7: "CUDA_ERROR", 8: "NOT_READY"}
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+_U = ctypes.c_uint
+_LL = ctypes.c_longlong
+_PI = ctypes.POINTER(ctypes.c_int)
+_PD = ctypes.POINTER(ctypes.c_double)
+_PU = ctypes.POINTER(ctypes.c_uint)
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "dfg_ctx_create": (_I, [_I, ctypes.POINTER(_P)]),
+    "dfg_ctx_destroy": (_I, [_P]),
+    "dfg_last_error": (ctypes.c_char_p, [_P]),
+    "dfg_version": (ctypes.c_char_p, []),
+    "dfg_ctx_synchronize": (_I, [_P]),
+    "dfg_ctx_kernel_launches": (_LL, [_P]),
+    "dfg_system_create": (_I, [_P, _I, _I, _P, _P, ctypes.POINTER(_P)]),
+    "dfg_system_create_from_elements": (_I, [_P, _I, _I, _I, _I, _P, ctypes.POINTER(_P)]),
+    "dfg_system_destroy": (_I, [_P]),
+    "dfg_system_info": (_I, [_P, _PI, _PI, ctypes.POINTER(_LL)]),
+    "dfg_system_get_pattern": (_I, [_P, _P, _P]),
+    "dfg_system_set_mesh": (_I, [_P, _I, _P, _I, _I, _P]),
+    "dfg_system_set_coef": (_I, [_P, _P]),
+    "dfg_system_set_field": (_I, [_P, _P, _P]),
+    "dfg_set_bcflags": (_I, [_P, _P]),
+    "dfg_initialize_marge": (_I, [_P]),
+    "dfg_assemble_poisson": (_I, [_P, _D, _D]),
+    "dfg_assemble_diffusion": (_I, [_P, _D, _D, _D, _D, _D]),
+    "dfg_assemble_solid2d": (_I, [_P, _D, _D, _D, _D, _D]),
+    "dfg_assemble_solid3d": (_I, [_P, _D, _D, _D, _D, _D, _D]),
+    "dfg_add_residual": (_I, [_P, _P]),
+    "dfg_finalize_marge": (_I, [_P, _PD]),
+    "dfg_get_matrix": (_I, [_P, _P, _P]),
+    "dfg_set_matrix": (_I, [_P, _P, _P]),
+    "dfg_get_vector": (_I, [_P, _I, _P]),
+    "dfg_set_vector": (_I, [_P, _I, _P]),
+    "dfg_get_tmp_vector_size": (_I, [_P, _PU]),
+    "dfg_resize_tmp_vec": (_I, [_P, _U]),
+    "dfg_dot": (_I, [_P, _I, _I, _PD]),
+    "dfg_copy": (_I, [_P, _I, _I]),
+    "dfg_scal": (_I, [_P, _D, _I]),
+    "dfg_axpy": (_I, [_P, _D, _I, _I]),
+    "dfg_matvec": (_I, [_P, _D, _I, _D, _I]),
+    "dfg_precond_create": (_I, [_P, ctypes.POINTER(_P)]),
+    "dfg_precond_destroy": (_I, [_P]),
+    "dfg_precond_set_fill_level": (_I, [_P, _I]),
+    "dfg_precond_set_linear_system": (_I, [_P, _P]),
+    "dfg_precond_set_value": (_I, [_P, _P]),
+    "dfg_precond_solve": (_I, [_P, _P, _I]),
+    "dfg_precond_get_factor": (_I, [_P, _P, _P]),
+    "dfg_solve_pcg": (_I, [_P, _P, _PD, _PU]),
+    "dfg_solve_pcg_mixed": (_I, [_P, _P, _PD, _PU, _PU]),
+    "dfg_true_residual": (_I, [_P, _P, _PD]),
+}
+
+_lib = None
+
+
+def header_symbols() -> list[str]:
+    """Every function the public header declares."""
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(dfg_[a-z0-9_]+)\s*\(", txt)))
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libdfg is not built ({LIB_PATH} missing); run delfem_gb300.build.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+class DfgError(RuntimeError):
+    def __init__(self, status: int, where: str, msg: str):
+        super().__init__(f"{where}: {STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def check(ctx, status: int, where: str) -> int:
+    if status != DFG_OK:
+        msg = lib().dfg_last_error(ctx).decode(errors="replace") if ctx else ""
+        raise DfgError(status, where, msg)
+    return status

@@ -1,0 +1,1154 @@
+// capi.cu -- the extern "C" entry points of libdfg (declared in include/dfg.h).
+//
+// Host-side orchestration only: argument checks, device memory, symbolic
+// set-up (sched.cpp) and kernel launches on the context's stream.  The PCG
+// loop runs device-resident: a chunk of iterations is captured once into a
+// CUDA graph and replayed until the device-side state reports convergence.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "dfg_internal.h"
+#include "k_assemble.h"
+#include "k_ilu.h"
+#include "k_solve.h"
+#include "k_sweep.h"
+
+using namespace dfg;
+
+#define DFG_VERSION "dfg 0.1.0 (sm_103a)"
+
+namespace dfg {
+
+void DBuf::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+}
+
+}  // namespace dfg
+
+namespace {
+
+struct Fail {
+  int status;
+};
+
+inline void set_err(dfg_ctx c, const std::string& m) {
+  if (c) c->last_error = m;
+}
+
+#define CK(call)                                                                            \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess) {                                                                \
+      set_err(ctx_, std::string("CUDA error: ") + cudaGetErrorString(e_) + " at " #call);  \
+      throw Fail{e_ == cudaErrorMemoryAllocation ? DFG_OOM_REJECTED : DFG_CUDA_ERROR};    \
+    }                                                                                       \
+  } while (0)
+
+#define REQUIRE(cond, status, msg)   \
+  do {                               \
+    if (!(cond)) {                   \
+      set_err(ctx_, msg);            \
+      throw Fail{status};            \
+    }                                \
+  } while (0)
+
+template <class F>
+int guarded(dfg_ctx ctx, F&& f) {
+  try {
+    if (ctx) {
+      cudaError_t e = cudaSetDevice(ctx->device);
+      if (e != cudaSuccess) {
+        ctx->last_error = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+        return DFG_CUDA_ERROR;
+      }
+    }
+    return f();
+  } catch (const Fail& x) {
+    return x.status;
+  } catch (const std::bad_alloc&) {
+    set_err(ctx, "host allocation failed");
+    return DFG_OOM_REJECTED;
+  } catch (...) {
+    set_err(ctx, "unexpected host exception");
+    return DFG_CUDA_ERROR;
+  }
+}
+
+void dalloc(dfg_ctx ctx_, DBuf& b, size_t bytes) {
+  if (b.p && b.bytes >= bytes) return;
+  b.release();
+  if (bytes == 0) bytes = 16;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_err(ctx_, "device allocation of " + std::to_string(bytes) + " bytes refused: " + cudaGetErrorString(e));
+    throw Fail{DFG_OOM_REJECTED};
+  }
+  b.p = p;
+  b.bytes = bytes;
+}
+
+template <class T>
+void upload(dfg_ctx ctx_, DBuf& b, const T* h, size_t count, size_t slack = 0) {
+  dalloc(ctx_, b, count * sizeof(T) + slack);
+  if (count) CK(cudaMemcpyAsync(b.p, h, count * sizeof(T), cudaMemcpyHostToDevice, ctx_->stream));
+}
+
+void launched(dfg_ctx c, long long n = 1) { c->launches += n; }
+
+// scratch layout in ctx->scratch: [partials kRedGrid doubles][counters 16][results 16 doubles][tickets 16 ints]
+struct Scratch {
+  double* partials;
+  unsigned* counters;
+  double* results;
+  int* tickets;
+};
+Scratch scratch_of(dfg_ctx c) {
+  char* base = c->scratch.as<char>();
+  Scratch s;
+  s.partials = reinterpret_cast<double*>(base);
+  s.counters = reinterpret_cast<unsigned*>(base + kRedGrid * 8);
+  s.results = reinterpret_cast<double*>(base + kRedGrid * 8 + 16 * 4);
+  s.tickets = reinterpret_cast<int*>(base + kRedGrid * 8 + 16 * 4 + 16 * 8);
+  return s;
+}
+Red red_of(dfg_ctx c, int channel = 0) {
+  Scratch s = scratch_of(c);
+  return Red{s.partials, s.counters + channel, s.results + channel};
+}
+
+double* vec_ptr(dfg_ctx ctx_, dfg_system s, int iv) {
+  if (iv == -1) return s->res.as<double>();
+  if (iv == -2) return s->upd.as<double>();
+  REQUIRE(iv >= 0 && iv < (int)s->tmp.size(), DFG_INVALID_ARGUMENT, "vector slot " + std::to_string(iv) + " out of range");
+  return s->tmp[iv].as<double>();
+}
+
+MatView view64(dfg_system s) {
+  return MatView{s->n, s->b, s->rowptr.as<int>(), s->colind.as<int>(), s->diag.p, s->offd.p};
+}
+
+size_t vec_bytes(dfg_system s, size_t elem) { return (size_t)s->n * s->b * elem + 64; }
+
+void system_alloc(dfg_ctx ctx_, dfg_system s) {
+  const size_t bs = (size_t)s->b * s->b;
+  dalloc(ctx_, s->diag, (size_t)s->n * bs * 8);
+  dalloc(ctx_, s->offd, (size_t)std::max<long long>(s->nnz, 1) * bs * 8);
+  dalloc(ctx_, s->res, vec_bytes(s, 8));
+  dalloc(ctx_, s->upd, vec_bytes(s, 8));
+  CK(cudaMemsetAsync(s->diag.p, 0, s->diag.bytes, ctx_->stream));
+  CK(cudaMemsetAsync(s->offd.p, 0, s->offd.bytes, ctx_->stream));
+  CK(cudaMemsetAsync(s->res.p, 0, s->res.bytes, ctx_->stream));
+  CK(cudaMemsetAsync(s->upd.p, 0, s->upd.bytes, ctx_->stream));
+  s->h_diaind.resize(s->n);
+  for (int i = 0; i < s->n; ++i) {
+    int d = s->h_rowptr[i + 1];
+    for (int c = s->h_rowptr[i]; c < s->h_rowptr[i + 1]; ++c)
+      if (s->h_colind[c] > i) { d = c; break; }
+    s->h_diaind[i] = d;
+  }
+  upload(ctx_, s->rowptr, s->h_rowptr.data(), s->h_rowptr.size());
+  upload(ctx_, s->colind, s->h_colind.data(), s->h_colind.size());
+  upload(ctx_, s->diaind, s->h_diaind.data(), s->h_diaind.size());
+}
+
+void check_pattern(dfg_ctx ctx_, int n, const int* rowptr, const int* colind) {
+  REQUIRE(rowptr[0] == 0, DFG_INVALID_ARGUMENT, "rowptr[0] must be 0");
+  for (int i = 0; i < n; ++i) {
+    REQUIRE(rowptr[i + 1] >= rowptr[i], DFG_INVALID_ARGUMENT, "rowptr must be non-decreasing");
+    for (int c = rowptr[i]; c < rowptr[i + 1]; ++c) {
+      REQUIRE(colind[c] >= 0 && colind[c] < n, DFG_INVALID_ARGUMENT, "column index out of range");
+      REQUIRE(colind[c] != i, DFG_INVALID_ARGUMENT, "pattern must not hold the diagonal block (CMatDia_BlkCrs::AddPattern)");
+      REQUIRE(c == rowptr[i] || colind[c] > colind[c - 1], DFG_INVALID_ARGUMENT, "columns must be strictly ascending within a row");
+    }
+  }
+}
+
+int read_state(dfg_ctx ctx_, PcgState* d_state, PcgState& h) {
+  CK(cudaMemcpyAsync(&h, d_state, sizeof(PcgState), cudaMemcpyDeviceToHost, ctx_->stream));
+  CK(cudaStreamSynchronize(ctx_->stream));
+  return 0;
+}
+
+int read_err(dfg_ctx ctx_) {
+  int e = 0;
+  CK(cudaMemcpyAsync(&e, ctx_->err_word.p, sizeof(int), cudaMemcpyDeviceToHost, ctx_->stream));
+  CK(cudaStreamSynchronize(ctx_->stream));
+  return e;
+}
+
+}  // namespace
+
+// ===================================================================== context
+
+extern "C" const char* dfg_version(void) { return DFG_VERSION; }
+
+extern "C" int dfg_ctx_create(int device, dfg_ctx* out) {
+  if (!out) return DFG_INVALID_ARGUMENT;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return DFG_CUDA_ERROR;
+  }
+  dfg_ctx c = new (std::nothrow) dfg_ctx_s;
+  if (!c) return DFG_OOM_REJECTED;
+  c->device = device;
+  int rc = guarded(c, [&]() -> int {
+    dfg_ctx ctx_ = c;
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device));
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    c->smem_optin = (size_t)optin;
+    dalloc(c, c->err_word, 64);
+    dalloc(c, c->scratch, kRedGrid * 8 + 16 * 4 + 16 * 8 + 16 * 4 + 256);
+    CK(cudaMemsetAsync(c->err_word.p, 0, 64, c->stream));
+    CK(cudaMemsetAsync(c->scratch.p, 0, c->scratch.bytes, c->stream));
+    CK(sweep_set_smem_limits(c->smem_optin));
+    CK(cudaStreamSynchronize(c->stream));
+    return DFG_OK;
+  });
+  if (rc != DFG_OK) {
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return rc;
+  }
+  *out = c;
+  return DFG_OK;
+}
+
+extern "C" int dfg_ctx_destroy(dfg_ctx ctx) {
+  if (!ctx) return DFG_INVALID_ARGUMENT;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->err_word.release();
+  ctx->scratch.release();
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return DFG_OK;
+}
+
+extern "C" const char* dfg_last_error(dfg_ctx ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+extern "C" int dfg_ctx_synchronize(dfg_ctx ctx) {
+  if (!ctx) return DFG_INVALID_ARGUMENT;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return DFG_OK;
+  });
+}
+
+extern "C" long long dfg_ctx_kernel_launches(dfg_ctx ctx) { return ctx ? ctx->launches : -1; }
+
+// ===================================================================== system
+
+extern "C" int dfg_system_create(dfg_ctx ctx, int nblk, int blklen, const int* rowptr, const int* colind,
+                                 dfg_system* out) {
+  if (!ctx || !out) return DFG_INVALID_ARGUMENT;
+  *out = nullptr;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    REQUIRE(nblk >= 0 && rowptr, DFG_INVALID_ARGUMENT, "bad nblk / rowptr");
+    REQUIRE(blklen >= 1 && blklen <= 3, DFG_INVALID_ARGUMENT, "block length must be 1, 2 or 3");
+    check_pattern(ctx, nblk, rowptr, colind);
+    dfg_system s = new dfg_system_s;
+    s->ctx = ctx;
+    s->n = nblk;
+    s->b = blklen;
+    s->nnz = rowptr[nblk];
+    s->h_rowptr.assign(rowptr, rowptr + nblk + 1);
+    s->h_colind.assign(colind, colind + s->nnz);
+    try {
+      system_alloc(ctx, s);
+      CK(cudaStreamSynchronize(ctx->stream));
+    } catch (...) {
+      delete s;
+      throw;
+    }
+    *out = s;
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_system_create_from_elements(dfg_ctx ctx, int nblk, int blklen, int nelem, int nnoel,
+                                               const int* conn, dfg_system* out) {
+  if (!ctx || !out) return DFG_INVALID_ARGUMENT;
+  *out = nullptr;
+  std::vector<int> rp, ci;
+  int rc = guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    REQUIRE(nblk >= 0 && nelem >= 0 && nnoel >= 1 && (conn || nelem == 0), DFG_INVALID_ARGUMENT, "bad element arguments");
+    for (long long k = 0; k < (long long)nelem * nnoel; ++k)
+      REQUIRE(conn[k] >= 0 && conn[k] < nblk, DFG_INVALID_ARGUMENT, "connectivity index out of range");
+    pattern_from_elements(nblk, nelem, nnoel, conn, rp, ci);
+    return DFG_OK;
+  });
+  if (rc != DFG_OK) return rc;
+  return dfg_system_create(ctx, nblk, blklen, rp.data(), ci.data(), out);
+}
+
+extern "C" int dfg_system_destroy(dfg_system sys) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  cudaSetDevice(sys->ctx->device);
+  cudaStreamSynchronize(sys->ctx->stream);
+  delete sys;
+  return DFG_OK;
+}
+
+extern "C" int dfg_system_info(dfg_system sys, int* nblk, int* blklen, long long* nnz) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  if (nblk) *nblk = sys->n;
+  if (blklen) *blklen = sys->b;
+  if (nnz) *nnz = sys->nnz;
+  return DFG_OK;
+}
+
+extern "C" int dfg_system_get_pattern(dfg_system sys, int* rowptr, int* colind) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  if (rowptr) std::memcpy(rowptr, sys->h_rowptr.data(), sys->h_rowptr.size() * sizeof(int));
+  if (colind) std::memcpy(colind, sys->h_colind.data(), sys->h_colind.size() * sizeof(int));
+  return DFG_OK;
+}
+
+extern "C" int dfg_system_set_mesh(dfg_system sys, int ndim, const double* coords, int nelem, int nnoel,
+                                   const int* conn) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    REQUIRE(ndim == 2 || ndim == 3, DFG_INVALID_ARGUMENT, "ndim must be 2 or 3");
+    REQUIRE((ndim == 2 && nnoel == 3) || (ndim == 3 && nnoel == 4), DFG_INVALID_ARGUMENT,
+            "elements must be P1 triangles (2D) or P1 tetrahedra (3D)");
+    REQUIRE(nelem >= 0 && coords && (conn || nelem == 0), DFG_INVALID_ARGUMENT, "bad mesh arguments");
+    GatherMap G;
+    std::string err;
+    REQUIRE(build_gather_map(sys->n, sys->h_rowptr.data(), sys->h_colind.data(), nelem, nnoel, conn, G, err),
+            DFG_INVALID_ARGUMENT, err);
+    sys->ndim = ndim;
+    sys->nelem = nelem;
+    sys->nnoel = nnoel;
+    upload(ctx, sys->coords, coords, (size_t)sys->n * ndim);
+    upload(ctx, sys->conn, conn, (size_t)nelem * nnoel);
+    upload(ctx, sys->slot_ptr, G.slot_ptr.data(), G.slot_ptr.size());
+    upload(ctx, sys->slot_src, G.slot_src.data(), G.slot_src.size());
+    upload(ctx, sys->res_ptr, G.res_ptr.data(), G.res_ptr.size());
+    upload(ctx, sys->res_src, G.res_src.data(), G.res_src.size());
+    CK(cudaStreamSynchronize(ctx->stream));
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_system_set_coef(dfg_system sys, const double* coef) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    REQUIRE(sys->conn.p || sys->nelem == 0, DFG_NOT_READY, "set the mesh before the coefficients");
+    if (!coef) { sys->has_coef = false; return DFG_OK; }
+    upload(ctx, sys->coef, coef, (size_t)sys->nelem);
+    CK(cudaStreamSynchronize(ctx->stream));
+    sys->has_coef = true;
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_system_set_field(dfg_system sys, const double* u, const double* v) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    const size_t m = (size_t)sys->n * sys->b;
+    sys->has_u = u != nullptr;
+    sys->has_v = v != nullptr;
+    if (u) upload(ctx, sys->fu, u, m);
+    if (v) upload(ctx, sys->fv, v, m);
+    CK(cudaStreamSynchronize(ctx->stream));
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_set_bcflags(dfg_system sys, const int* flags) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    const size_t m = (size_t)sys->n * sys->b;
+    if (!flags) {
+      dalloc(ctx, sys->bcflag, m * 4 + 16);
+      CK(cudaMemsetAsync(sys->bcflag.p, 0, sys->bcflag.bytes, ctx->stream));
+    } else {
+      upload(ctx, sys->bcflag, flags, m);
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    sys->has_bc = true;
+    return DFG_OK;
+  });
+}
+
+// ===================================================================== assembly
+
+extern "C" int dfg_initialize_marge(dfg_system sys) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    CK(cudaMemsetAsync(sys->diag.p, 0, sys->diag.bytes, ctx->stream));
+    CK(cudaMemsetAsync(sys->offd.p, 0, sys->offd.bytes, ctx->stream));
+    CK(cudaMemsetAsync(sys->res.p, 0, sys->res.bytes, ctx->stream));
+    CK(cudaMemsetAsync(sys->upd.p, 0, sys->upd.bytes, ctx->stream));
+    sys->mat32_valid = false;
+    sys->rhs0_valid = false;
+    return DFG_OK;
+  });
+}
+
+static int assemble(dfg_system sys, int kind, int need_b, int need_ndim, const double* p, int np) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    REQUIRE(sys->conn.p && sys->nelem >= 0, DFG_NOT_READY, "dfg_system_set_mesh must come before assembly");
+    REQUIRE(sys->b == need_b, DFG_INVALID_ARGUMENT, "block length does not match the equation");
+    REQUIRE(need_ndim == 0 || sys->ndim == need_ndim, DFG_INVALID_ARGUMENT, "mesh dimension does not match the equation");
+    const int k = sys->nnoel, bs = sys->b * sys->b;
+    dalloc(ctx, sys->em, (size_t)sys->nelem * k * k * bs * 8);
+    dalloc(ctx, sys->er, (size_t)sys->nelem * k * sys->b * 8);
+    ElemArgs a{};
+    a.nelem = sys->nelem;
+    a.conn = sys->conn.as<int>();
+    a.coords = sys->coords.as<double>();
+    a.coef = sys->has_coef ? sys->coef.as<double>() : nullptr;
+    a.u = sys->has_u ? sys->fu.as<double>() : nullptr;
+    a.v = sys->has_v ? sys->fv.as<double>() : nullptr;
+    for (int i = 0; i < 8; ++i) a.p[i] = i < np ? p[i] : 0.0;
+    a.em = sys->em.as<double>();
+    a.er = sys->er.as<double>();
+    CK(launch_elem(kind, a, ctx->stream));
+    GatherArgs g{};
+    g.n = sys->n;
+    g.nnz = sys->nnz;
+    g.b = sys->b;
+    g.bs = bs;
+    g.slot_ptr = sys->slot_ptr.as<long long>();
+    g.slot_src = sys->slot_src.as<int>();
+    g.res_ptr = sys->res_ptr.as<long long>();
+    g.res_src = sys->res_src.as<int>();
+    g.em = a.em;
+    g.er = a.er;
+    g.diag = sys->diag.as<double>();
+    g.offd = sys->offd.as<double>();
+    g.res = sys->res.as<double>();
+    CK(launch_gather(g, ctx->stream));
+    launched(ctx, 3);
+    sys->mat32_valid = false;
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_assemble_poisson(dfg_system sys, double alpha, double source) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  const double p[2] = {alpha, source};
+  return assemble(sys, sys->ndim == 3 ? 2 : 1, 1, 0, p, 2);
+}
+extern "C" int dfg_assemble_diffusion(dfg_system sys, double dt, double gamma, double rho, double alpha,
+                                      double source) {
+  const double p[5] = {rho, alpha, source, gamma, dt};
+  return assemble(sys, 3, 1, 2, p, 5);
+}
+extern "C" int dfg_assemble_solid2d(dfg_system sys, double lambda, double myu, double rho, double g_x,
+                                    double g_y) {
+  const double p[5] = {lambda, myu, rho, g_x, g_y};
+  return assemble(sys, 4, 2, 2, p, 5);
+}
+extern "C" int dfg_assemble_solid3d(dfg_system sys, double lambda, double myu, double rho, double g_x,
+                                    double g_y, double g_z) {
+  const double p[6] = {lambda, myu, rho, g_x, g_y, g_z};
+  return assemble(sys, 5, 3, 3, p, 6);
+}
+
+extern "C" int dfg_add_residual(dfg_system sys, const double* f) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    REQUIRE(f, DFG_INVALID_ARGUMENT, "null load vector");
+    const size_t m = (size_t)sys->n * sys->b;
+    DBuf tmp;
+    upload(ctx, tmp, f, m);
+    CK(launch_add_vec((long long)m, tmp.as<double>(), sys->res.as<double>(), ctx->stream));
+    launched(ctx);
+    CK(cudaStreamSynchronize(ctx->stream));
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_finalize_marge(dfg_system sys, double* norm_res) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    if (sys->has_bc) {
+      BcArgs a{};
+      a.n = sys->n;
+      a.nnz = sys->nnz;
+      a.b = sys->b;
+      a.rowptr = sys->rowptr.as<int>();
+      a.colind = sys->colind.as<int>();
+      a.flag = sys->bcflag.as<int>();
+      a.diag = sys->diag.as<double>();
+      a.offd = sys->offd.as<double>();
+      a.res = sys->res.as<double>();
+      CK(launch_bc(a, ctx->stream));
+      launched(ctx, 2);
+    }
+    const size_t m = (size_t)sys->n * sys->b;
+    dalloc(ctx, sys->rhs0, vec_bytes(sys, 8));
+    CK(cudaMemcpyAsync(sys->rhs0.p, sys->res.p, m * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    sys->rhs0_valid = true;
+    sys->mat32_valid = false;
+    Red r = red_of(ctx, 0);
+    CK(api_dot((long long)m, sys->res.as<double>(), sys->res.as<double>(), r, ctx->stream));
+    launched(ctx);
+    double s = 0.0;
+    CK(cudaMemcpyAsync(&s, r.result, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (norm_res) *norm_res = std::sqrt(s);
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_get_matrix(dfg_system sys, double* diag, double* offd) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    const size_t bs = (size_t)sys->b * sys->b;
+    if (diag) CK(cudaMemcpyAsync(diag, sys->diag.p, (size_t)sys->n * bs * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if (offd && sys->nnz) CK(cudaMemcpyAsync(offd, sys->offd.p, (size_t)sys->nnz * bs * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_set_matrix(dfg_system sys, const double* diag, const double* offd) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    const size_t bs = (size_t)sys->b * sys->b;
+    if (diag) CK(cudaMemcpyAsync(sys->diag.p, diag, (size_t)sys->n * bs * 8, cudaMemcpyHostToDevice, ctx->stream));
+    if (offd && sys->nnz) CK(cudaMemcpyAsync(sys->offd.p, offd, (size_t)sys->nnz * bs * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    sys->mat32_valid = false;
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_get_vector(dfg_system sys, int iv, double* out) {
+  if (!sys || !out) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    double* p = vec_ptr(ctx, sys, iv);
+    CK(cudaMemcpyAsync(out, p, (size_t)sys->n * sys->b * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_set_vector(dfg_system sys, int iv, const double* in) {
+  if (!sys || !in) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    double* p = vec_ptr(ctx, sys, iv);
+    CK(cudaMemcpyAsync(p, in, (size_t)sys->n * sys->b * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return DFG_OK;
+  });
+}
+
+// ============================================================ solver interface
+
+extern "C" int dfg_get_tmp_vector_size(dfg_system sys, unsigned* size) {
+  if (!sys || !size) return DFG_INVALID_ARGUMENT;
+  *size = (unsigned)sys->tmp.size();
+  return DFG_OK;
+}
+
+extern "C" int dfg_resize_tmp_vec(dfg_system sys, unsigned size) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    while (sys->tmp.size() > size) sys->tmp.pop_back();
+    while (sys->tmp.size() < size) {
+      sys->tmp.emplace_back();
+      dalloc(ctx, sys->tmp.back(), vec_bytes(sys, 8));
+      CK(cudaMemsetAsync(sys->tmp.back().p, 0, sys->tmp.back().bytes, ctx->stream));
+    }
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_dot(dfg_system sys, int iv1, int iv2, double* out) {
+  if (!sys || !out) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    const double* a = vec_ptr(ctx, sys, iv1);
+    const double* b = vec_ptr(ctx, sys, iv2);
+    Red r = red_of(ctx, 0);
+    CK(api_dot((long long)sys->n * sys->b, a, b, r, ctx->stream));
+    launched(ctx);
+    CK(cudaMemcpyAsync(out, r.result, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_copy(dfg_system sys, int iv1, int iv2) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  if (iv1 == iv2) return DFG_OK;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    const double* a = vec_ptr(ctx, sys, iv1);
+    double* b = vec_ptr(ctx, sys, iv2);
+    CK(cudaMemcpyAsync(b, a, (size_t)sys->n * sys->b * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_scal(dfg_system sys, double alpha, int iv1) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    CK(api_scal((long long)sys->n * sys->b, alpha, vec_ptr(ctx, sys, iv1), ctx->stream));
+    launched(ctx);
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_axpy(dfg_system sys, double alpha, int iv1, int iv2) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    if (alpha == 0) return DFG_OK;  // CLinearSystem::AXPY returns early
+    REQUIRE(iv1 != iv2, DFG_INVALID_ARGUMENT, "AXPY on one slot (the reference asserts)");
+    CK(api_axpy((long long)sys->n * sys->b, alpha, vec_ptr(ctx, sys, iv1), vec_ptr(ctx, sys, iv2), ctx->stream));
+    launched(ctx);
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_matvec(dfg_system sys, double alpha, int iv1, double beta, int iv2) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    double* y = vec_ptr(ctx, sys, iv2);
+    if (alpha == 0.0) {  // CLinearSystem::MATVEC -> SCAL(beta, iv2)
+      CK(api_scal((long long)sys->n * sys->b, beta, y, ctx->stream));
+      launched(ctx);
+      return DFG_OK;
+    }
+    REQUIRE(iv1 != iv2, DFG_INVALID_ARGUMENT, "MATVEC on one slot (the reference asserts)");
+    CK(api_matvec(view64(sys), alpha, vec_ptr(ctx, sys, iv1), beta, y, ctx->stream));
+    launched(ctx);
+    return DFG_OK;
+  });
+}
+
+// =============================================================== preconditioner
+
+namespace {
+
+// Host-assembled static parts of the step records (header, row ids,
+// dependency codes); the value regions are filled on the device by k_pack.
+void build_records(dfg_ctx ctx_, SweepDev& S, int elem, DBuf& rec, DBuf& rec_off, long long& total, long long& max_rec) {
+  const SweepPlan& P = S.plan;
+  const int bs = P.b * P.b;
+  std::vector<long long> off(P.nsteps + 1, 0);
+  max_rec = 0;
+  for (int s = 0; s < P.nsteps; ++s) {
+    const long long rb = rec_bytes(P.step_nent[s], bs, elem, P.forward);
+    off[s + 1] = off[s] + rb;
+    max_rec = std::max(max_rec, rb);
+  }
+  total = off[P.nsteps];
+  std::vector<unsigned char> h((size_t)total, 0);
+  for (int s = 0; s < P.nsteps; ++s) {
+    unsigned char* r = h.data() + off[s];
+    const int nent = P.step_nent[s];
+    std::memcpy(r, &nent, 4);
+    std::memcpy(r + 16, &P.step_rows[(size_t)s * 32], 128);
+    if (nent) std::memcpy(r + 144, &P.ent_src[(size_t)P.ent_off[s] * 32], (size_t)nent * 128);
+  }
+  upload(ctx_, rec, h.data(), h.size(), 64);
+  upload(ctx_, rec_off, off.data(), off.size());
+}
+
+void setup_sweep(dfg_ctx ctx_, SweepDev& S, const dfg_system sys, bool forward) {
+  S.plan = choose_sweep_plan(sys->n, sys->b, sys->h_rowptr.data(), sys->h_colind.data(), sys->h_diaind.data(),
+                             forward, 32, 8);
+  const SweepPlan& P = S.plan;
+  build_records(ctx_, S, 8, S.rec64, S.rec_off64, S.rec_total64, S.max_rec64);
+  build_records(ctx_, S, 4, S.rec32, S.rec_off32, S.rec_total32, S.max_rec32);
+  upload(ctx_, S.range_steps, P.range_steps.data(), P.range_steps.size());
+  upload(ctx_, S.ent_off, P.ent_off.data(), P.ent_off.size());
+  upload(ctx_, S.ent_slot, P.ent_slot.data(), std::max<size_t>(P.ent_slot.size(), 1));
+  upload(ctx_, S.step_rows, P.step_rows.data(), std::max<size_t>(P.step_rows.size(), 1));
+}
+
+void pack_sweep(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, bool fp32) {
+  PackArgs a{};
+  a.nsteps = S.plan.nsteps;
+  a.rec = fp32 ? S.rec32.as<unsigned char>() : S.rec64.as<unsigned char>();
+  a.rec_off = fp32 ? S.rec_off32.as<long long>() : S.rec_off64.as<long long>();
+  a.ent_off = S.ent_off.as<long long>();
+  a.ent_slot = S.ent_slot.as<int>();
+  a.step_rows = S.step_rows.as<int>();
+  a.fdiag = pr->fdiag.as<double>();
+  a.foffd = pr->foffd.as<double>();
+  CK(launch_pack(S.plan.forward, fp32, pr->b, a, ctx_->stream));
+  launched(ctx_);
+}
+
+struct SweepLaunch {
+  SweepArgs args;
+  int grid;
+  int K;
+  size_t smem;
+};
+
+SweepLaunch sweep_launch(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, bool fp32, const void* in, void* out,
+                         int* ticket, const int* done) {
+  const int elem = fp32 ? 4 : 8;
+  SweepLaunch L{};
+  SweepArgs& a = L.args;
+  a.rec = fp32 ? S.rec32.as<unsigned char>() : S.rec64.as<unsigned char>();
+  a.rec_off = fp32 ? S.rec_off32.as<long long>() : S.rec_off64.as<long long>();
+  a.range_steps = S.range_steps.as<int>();
+  a.nranges = S.plan.nranges;
+  a.in = in;
+  a.out = out;
+  a.ticket = ticket;
+  a.err = ctx_->err_word.as<int>();
+  a.done = done;
+  a.rec_stage = (int)((fp32 ? S.max_rec32 : S.max_rec64) + 15) / 16 * 16;
+  a.val_stage = sweep_val_stage(S.plan.max_nent, pr->b, elem);
+  a.R = S.plan.R;
+  L.K = 4;
+  L.smem = sweep_smem_bytes(L.K, a.rec_stage, a.val_stage, a.R, pr->b, elem);
+  if (L.smem > 64 * 1024) {
+    L.K = 2;
+    L.smem = sweep_smem_bytes(L.K, a.rec_stage, a.val_stage, a.R, pr->b, elem);
+  }
+  REQUIRE(L.smem <= ctx_->smem_optin, DFG_INVALID_ARGUMENT, "sweep records exceed shared memory");
+  int per_sm_bytes = 0;
+  cudaDeviceGetAttribute(&per_sm_bytes, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx_->device);
+  int per_sm = std::max(1, std::min(32, (int)(per_sm_bytes / (L.smem + 1024))));
+  L.grid = std::max(1, std::min(S.plan.nranges, ctx_->nsm * per_sm));
+  return L;
+}
+
+void run_sweep(dfg_ctx ctx_, bool forward, int b, bool fp32, const SweepLaunch& L) {
+  CK(launch_sweep(forward, fp32, b, L.K, L.args, L.grid, L.smem, ctx_->stream));
+  launched(ctx_);
+}
+
+}  // namespace
+
+extern "C" int dfg_precond_create(dfg_ctx ctx, dfg_precond* out) {
+  if (!ctx || !out) return DFG_INVALID_ARGUMENT;
+  dfg_precond p = new (std::nothrow) dfg_precond_s;
+  if (!p) return DFG_OOM_REJECTED;
+  p->ctx = ctx;
+  *out = p;
+  return DFG_OK;
+}
+
+extern "C" int dfg_precond_destroy(dfg_precond prec) {
+  if (!prec) return DFG_INVALID_ARGUMENT;
+  cudaSetDevice(prec->ctx->device);
+  cudaStreamSynchronize(prec->ctx->stream);
+  delete prec;
+  return DFG_OK;
+}
+
+extern "C" int dfg_precond_set_fill_level(dfg_precond prec, int lev) {
+  if (!prec) return DFG_INVALID_ARGUMENT;
+  if (lev != 0) {
+    prec->ctx->last_error = "only fill-in level 0 is implemented";
+    return DFG_INVALID_ARGUMENT;
+  }
+  prec->lev = lev;
+  return DFG_OK;
+}
+
+extern "C" int dfg_precond_set_linear_system(dfg_precond prec, dfg_system sys) {
+  if (!prec || !sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = prec->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    REQUIRE(sys->ctx == ctx, DFG_INVALID_ARGUMENT, "system and preconditioner belong to different contexts");
+    prec->sys = sys;
+    prec->n = sys->n;
+    prec->b = sys->b;
+    prec->nnz = sys->nnz;
+    const size_t bs = (size_t)sys->b * sys->b;
+    dalloc(ctx, prec->fdiag, (size_t)sys->n * bs * 8);
+    dalloc(ctx, prec->foffd, (size_t)std::max<long long>(sys->nnz, 1) * bs * 8);
+    prec->lev_fwd = build_levels(sys->n, sys->h_rowptr.data(), sys->h_colind.data(), sys->h_diaind.data(), true);
+    upload(ctx, prec->lev_rows, prec->lev_fwd.rows.data(), std::max<size_t>(prec->lev_fwd.rows.size(), 1));
+    setup_sweep(ctx, prec->fwd, sys, true);
+    setup_sweep(ctx, prec->bwd, sys, false);
+    dalloc(ctx, prec->ybuf64, vec_bytes(sys, 8));
+    dalloc(ctx, prec->ybuf32, vec_bytes(sys, 4));
+    CK(cudaStreamSynchronize(ctx->stream));
+    prec->symbolic = true;
+    prec->numeric = prec->numeric32 = false;
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_precond_set_value(dfg_precond prec, dfg_system sys) {
+  if (!prec || !sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = prec->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    REQUIRE(prec->symbolic && prec->sys == sys, DFG_NOT_READY, "dfg_precond_set_linear_system must come first");
+    const size_t bs = (size_t)sys->b * sys->b;
+    // SetValue_Initialize: copy A into the factor storage
+    CK(cudaMemcpyAsync(prec->fdiag.p, sys->diag.p, (size_t)sys->n * bs * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (sys->nnz)
+      CK(cudaMemcpyAsync(prec->foffd.p, sys->offd.p, (size_t)sys->nnz * bs * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    Scratch sc = scratch_of(ctx);
+    int* nsing = sc.tickets + 8;
+    CK(cudaMemsetAsync(nsing, 0, sizeof(int), ctx->stream));
+    const Levels& L = prec->lev_fwd;
+    const int nl = (int)L.ptr.size() - 1;
+    for (int l = 0; l < nl; ++l)
+      CK(launch_ilu_level(sys->b, prec->lev_rows.as<int>() + L.ptr[l], L.ptr[l + 1] - L.ptr[l], sys->rowptr.as<int>(),
+                          sys->colind.as<int>(), sys->diaind.as<int>(), prec->fdiag.as<double>(),
+                          prec->foffd.as<double>(), nsing, ctx->stream));
+    launched(ctx, nl);
+    int h_nsing = 0;
+    CK(cudaMemcpyAsync(&h_nsing, nsing, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    pack_sweep(ctx, prec, prec->fwd, false);
+    pack_sweep(ctx, prec, prec->bwd, false);
+    CK(cudaStreamSynchronize(ctx->stream));
+    prec->numeric = true;
+    prec->numeric32 = false;
+    if (h_nsing > 10) {
+      set_err(ctx, "ILU(0): " + std::to_string(h_nsing) + " singular pivots (more than 10)");
+      return DFG_SINGULAR_PIVOT;
+    }
+    return DFG_OK;
+  });
+}
+
+namespace {
+void ensure_numeric32(dfg_ctx ctx_, dfg_precond prec) {
+  if (prec->numeric32) return;
+  pack_sweep(ctx_, prec, prec->fwd, true);
+  pack_sweep(ctx_, prec, prec->bwd, true);
+  prec->numeric32 = true;
+}
+}  // namespace
+
+extern "C" int dfg_precond_solve(dfg_precond prec, dfg_system sys, int iv) {
+  if (!prec || !sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = prec->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    REQUIRE(prec->numeric && prec->sys == sys, DFG_NOT_READY, "dfg_precond_set_value must come first");
+    double* v = vec_ptr(ctx, sys, iv);
+    const long long m = (long long)sys->n * sys->b;
+    Scratch sc = scratch_of(ctx);
+    CK(cudaMemsetAsync(sc.tickets, 0, 2 * sizeof(int), ctx->stream));
+    CK(fill_sentinel(m, prec->ybuf64.p, false, ctx->stream));
+    SweepLaunch F = sweep_launch(ctx, prec, prec->fwd, false, v, prec->ybuf64.p, sc.tickets, nullptr);
+    run_sweep(ctx, true, sys->b, false, F);
+    CK(fill_sentinel(m, v, false, ctx->stream));
+    SweepLaunch B = sweep_launch(ctx, prec, prec->bwd, false, prec->ybuf64.p, v, sc.tickets + 1, nullptr);
+    run_sweep(ctx, false, sys->b, false, B);
+    launched(ctx, 2);  // the two sentinel fills
+    if (read_err(ctx) != 0) {
+      CK(cudaMemsetAsync(ctx->err_word.p, 0, sizeof(int), ctx->stream));
+      set_err(ctx, "a triangular-sweep wait timed out");
+      return DFG_TIMEOUT;
+    }
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_precond_get_factor(dfg_precond prec, double* fdiag, double* foffd) {
+  if (!prec) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = prec->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    REQUIRE(prec->numeric, DFG_NOT_READY, "no numeric factor yet");
+    const size_t bs = (size_t)prec->b * prec->b;
+    if (fdiag) CK(cudaMemcpyAsync(fdiag, prec->fdiag.p, (size_t)prec->n * bs * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if (foffd && prec->nnz) CK(cudaMemcpyAsync(foffd, prec->foffd.p, (size_t)prec->nnz * bs * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return DFG_OK;
+  });
+}
+
+// ===================================================================== solvers
+
+namespace {
+
+struct Chunk {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ~Chunk() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+  }
+};
+
+int timeout_status(dfg_ctx ctx_) {
+  CK(cudaMemsetAsync(ctx_->err_word.p, 0, sizeof(int), ctx_->stream));
+  CK(cudaStreamSynchronize(ctx_->stream));
+  set_err(ctx_, "a triangular-sweep wait timed out");
+  return DFG_TIMEOUT;
+}
+
+}  // namespace
+
+extern "C" int dfg_solve_pcg(dfg_system sys, dfg_precond prec, double* conv_ratio, unsigned* iteration) {
+  if (!sys || !prec || !conv_ratio || !iteration) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    REQUIRE(prec->numeric && prec->sys == sys, DFG_NOT_READY, "preconditioner value not set for this system");
+    const long long m = (long long)sys->n * sys->b;
+    dalloc(ctx, sys->w_p, vec_bytes(sys, 8));
+    dalloc(ctx, sys->w_q, vec_bytes(sys, 8));
+    dalloc(ctx, sys->w_z, vec_bytes(sys, 8));
+    dalloc(ctx, sys->w_state, sizeof(PcgState));
+    PcgState* st = sys->w_state.as<PcgState>();
+    Scratch sc = scratch_of(ctx);
+    Red red = red_of(ctx, 1);
+    PcgVecs v{sys->res.as<double>(), sys->upd.as<double>(), sys->w_p.as<double>(), sys->w_q.as<double>(),
+              prec->ybuf64.as<double>(), sys->w_z.as<double>(), m};
+    const int* done = reinterpret_cast<const int*>(reinterpret_cast<const char*>(st) + offsetof(PcgState, done));
+    SweepLaunch F = sweep_launch(ctx, prec, prec->fwd, false, v.r, v.y, sc.tickets, done);
+    SweepLaunch B = sweep_launch(ctx, prec, prec->bwd, false, v.y, v.z, sc.tickets + 1, done);
+    const int maxit = (int)std::min<unsigned>(*iteration, 0x7fffffffu);
+    // prologue (solver_ls_iter.cpp:106-128)
+    CK(pcg_init(v, st, red, *conv_ratio, maxit, sc.tickets, ctx->stream));
+    run_sweep(ctx, true, sys->b, false, F);
+    run_sweep(ctx, false, sys->b, false, B);
+    CK(pcg_after_precond0(v, st, red, ctx->stream));
+    launched(ctx, 2);
+    PcgState h{};
+    read_state(ctx, st, h);
+    // iterations: a graph of `chunk` iterations, replayed until done
+    const int chunk = m < 200000 ? 8 : 32;
+    Chunk g;
+    if (!h.done) {
+      CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      const MatView A = view64(sys);
+      for (int c = 0; c < chunk; ++c) {
+        pcg_spmv_pap(A, v, st, red, ctx->stream);
+        pcg_update_rx(v, st, red, sc.tickets, ctx->stream);
+        launch_sweep(true, false, sys->b, F.K, F.args, F.grid, F.smem, ctx->stream);
+        launch_sweep(false, false, sys->b, B.K, B.args, B.grid, B.smem, ctx->stream);
+        pcg_rz_beta(v, st, red, ctx->stream);
+        pcg_update_p(v, st, ctx->stream);
+      }
+      CK(cudaStreamEndCapture(ctx->stream, &g.graph));
+      CK(cudaGraphInstantiate(&g.exec, g.graph, 0));
+    }
+    long long guard = 0;
+    while (!h.done) {
+      CK(cudaGraphLaunch(g.exec, ctx->stream));
+      launched(ctx, 6LL * chunk);
+      read_state(ctx, st, h);
+      if (read_err(ctx) != 0) return timeout_status(ctx);
+      if (++guard > (long long)maxit / chunk + 4) break;
+    }
+    *conv_ratio = h.conv;
+    if (h.done == 1) {
+      *iteration = (unsigned)h.iter_out;
+      return DFG_OK;
+    }
+    if (h.done == 3) {
+      set_err(ctx, "NaN in the residual");
+      return DFG_NAN_DETECTED;
+    }
+    set_err(ctx, "PCG did not converge within the iteration limit");
+    return DFG_NOT_CONVERGED;
+  });
+}
+
+// Mixed precision: PCG whose SpMV, factor, sweeps and vectors are FP32, with
+// the reductions and alpha/beta in FP64 and the solution accumulated in FP64.
+// Whenever the FP32 recursive residual has dropped by 10x since the last
+// refinement point -- or below the tolerance -- the solution absorbs the
+// FP64 correction, the FP64 true residual b - A x is recomputed, and the
+// recursion continues from it with the current search direction (iterative
+// refinement by residual replacement, without restarting the Krylov space).
+extern "C" int dfg_solve_pcg_mixed(dfg_system sys, dfg_precond prec, double* conv_ratio, unsigned* iteration,
+                                   unsigned* outer) {
+  if (!sys || !prec || !conv_ratio || !iteration) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    REQUIRE(prec->numeric && prec->sys == sys, DFG_NOT_READY, "preconditioner value not set for this system");
+    REQUIRE(sys->rhs0_valid, DFG_NOT_READY, "dfg_finalize_marge must come before the mixed solve");
+    const long long m = (long long)sys->n * sys->b;
+    const size_t bs = (size_t)sys->b * sys->b;
+    if (!sys->mat32_valid) {
+      dalloc(ctx, sys->diag32, (size_t)sys->n * bs * 4 + 64);
+      dalloc(ctx, sys->offd32, (size_t)std::max<long long>(sys->nnz, 1) * bs * 4 + 64);
+      CK(to_fp32((long long)sys->n * bs, sys->diag.as<double>(), sys->diag32.as<float>(), ctx->stream));
+      CK(to_fp32(sys->nnz * (long long)bs, sys->offd.as<double>(), sys->offd32.as<float>(), ctx->stream));
+      launched(ctx, 2);
+      sys->mat32_valid = true;
+    }
+    ensure_numeric32(ctx, prec);
+    dalloc(ctx, sys->w_rd, vec_bytes(sys, 8));
+    dalloc(ctx, sys->w_d, vec_bytes(sys, 8));
+    dalloc(ctx, sys->w_r32, vec_bytes(sys, 4));
+    dalloc(ctx, sys->w_p32, vec_bytes(sys, 4));
+    dalloc(ctx, sys->w_q32, vec_bytes(sys, 4));
+    dalloc(ctx, sys->w_z32, vec_bytes(sys, 4));
+    dalloc(ctx, sys->w_state, sizeof(PcgState));
+    PcgState* st = sys->w_state.as<PcgState>();
+    Scratch sc = scratch_of(ctx);
+    Red red = red_of(ctx, 2);
+    MixVecs v{sys->rhs0.as<double>(), sys->upd.as<double>(), sys->w_rd.as<double>(), sys->w_d.as<double>(),
+              sys->w_r32.as<float>(), sys->w_p32.as<float>(), sys->w_q32.as<float>(), prec->ybuf32.as<float>(),
+              sys->w_z32.as<float>(), m};
+    const MatView A64 = view64(sys);
+    const MatView A32{sys->n, sys->b, sys->rowptr.as<int>(), sys->colind.as<int>(), sys->diag32.p, sys->offd32.p};
+    const int* done = reinterpret_cast<const int*>(reinterpret_cast<const char*>(st) + offsetof(PcgState, done));
+    SweepLaunch F = sweep_launch(ctx, prec, prec->fwd, true, v.r, v.y, sc.tickets, done);
+    SweepLaunch B = sweep_launch(ctx, prec, prec->bwd, true, v.y, v.z, sc.tickets + 1, done);
+    CK(cudaMemsetAsync(v.x, 0, (size_t)m * 8, ctx->stream));
+    CK(cudaMemsetAsync(v.d, 0, (size_t)m * 8, ctx->stream));
+    CK(api_dot(m, v.b, v.b, red, ctx->stream));
+    launched(ctx);
+    double bb = 0.0;
+    CK(cudaMemcpyAsync(&bb, red.result, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const double tol = *conv_ratio;
+    const int maxit = (int)std::min<unsigned>(*iteration, 0x7fffffffu);
+    if (bb < 1.0e-30) {
+      *conv_ratio = 0.0;
+      *iteration = 0;
+      if (outer) *outer = 0;
+      return DFG_OK;
+    }
+    CK(mix_start(st, tol, bb, 0.1, maxit, ctx->stream));
+    // true residual of x = 0 is b; start the recursion from it
+    CK(mix_true_residual(A64, v, st, red, ctx->stream));
+    CK(mix_replace(v, st, sc.tickets, ctx->stream));
+    run_sweep(ctx, true, sys->b, true, F);
+    run_sweep(ctx, false, sys->b, true, B);
+    CK(mix_after_precond0(v, st, red, ctx->stream));
+    launched(ctx, 4);
+    const int chunk = m < 200000 ? 8 : 32;
+    Chunk g;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    for (int c = 0; c < chunk; ++c) {
+      mix_spmv_pap(A32, v, st, red, ctx->stream);
+      mix_update_rx(v, st, red, sc.tickets, ctx->stream);
+      launch_sweep(true, true, sys->b, F.K, F.args, F.grid, F.smem, ctx->stream);
+      launch_sweep(false, true, sys->b, B.K, B.args, B.grid, B.smem, ctx->stream);
+      mix_rz_beta(v, st, red, ctx->stream);
+      mix_update_p(v, st, ctx->stream);
+    }
+    CK(cudaStreamEndCapture(ctx->stream, &g.graph));
+    CK(cudaGraphInstantiate(&g.exec, g.graph, 0));
+    PcgState h{};
+    unsigned refinements = 0;
+    double rel = 1.0;
+    int status = DFG_NOT_CONVERGED;
+    long long guard = 0;
+    for (;;) {
+      CK(cudaGraphLaunch(g.exec, ctx->stream));
+      launched(ctx, 6LL * chunk);
+      read_state(ctx, st, h);
+      if (read_err(ctx) != 0) return timeout_status(ctx);
+      if (h.done == 0) {
+        if (++guard > (long long)maxit / chunk + 64) break;
+        continue;
+      }
+      if (h.done == 3) { status = DFG_NAN_DETECTED; set_err(ctx, "NaN in the residual"); break; }
+      // refinement point: fold the correction in, recompute the true residual
+      CK(mix_accumulate(v, ctx->stream));
+      CK(mix_true_residual(A64, v, st, red, ctx->stream));
+      launched(ctx, 2);
+      ++refinements;
+      PcgState t{};
+      read_state(ctx, st, t);
+      rel = std::sqrt(t.rr / bb);
+      if (!(rel == rel)) { status = DFG_NAN_DETECTED; set_err(ctx, "NaN in the residual"); break; }
+      if (rel <= tol) { status = DFG_OK; break; }
+      if (h.done == 2) { set_err(ctx, "mixed PCG did not converge within the iteration limit"); break; }
+      // continue the recursion from the true residual: finish this iteration
+      // (preconditioner, beta, direction) and resume the graph
+      CK(mix_replace(v, st, sc.tickets, ctx->stream));
+      run_sweep(ctx, true, sys->b, true, F);
+      run_sweep(ctx, false, sys->b, true, B);
+      CK(mix_rz_beta(v, st, red, ctx->stream));
+      CK(mix_update_p(v, st, ctx->stream));
+      launched(ctx, 3);
+    }
+    *conv_ratio = rel;
+    *iteration = (unsigned)h.iter_out;
+    if (outer) *outer = refinements;
+    return status;
+  });
+}
+
+extern "C" int dfg_true_residual(dfg_system sys, const double* b, double* rel) {
+  if (!sys || !rel) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    const long long m = (long long)sys->n * sys->b;
+    DBuf bb, rr;
+    const double* bp;
+    if (b) {
+      upload(ctx, bb, b, (size_t)m);
+      bp = bb.as<double>();
+    } else {
+      REQUIRE(sys->rhs0_valid, DFG_NOT_READY, "no finalized right-hand side");
+      bp = sys->rhs0.as<double>();
+    }
+    dalloc(ctx, rr, (size_t)m * 8 + 64);
+    CK(cudaMemcpyAsync(rr.p, bp, (size_t)m * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(api_matvec(view64(sys), -1.0, sys->upd.as<double>(), 1.0, rr.as<double>(), ctx->stream));
+    Red red = red_of(ctx, 0);
+    CK(api_dot(m, rr.as<double>(), rr.as<double>(), red, ctx->stream));
+    double r2 = 0.0, b2 = 0.0;
+    CK(cudaMemcpyAsync(&r2, red.result, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(api_dot(m, bp, bp, red, ctx->stream));
+    CK(cudaMemcpyAsync(&b2, red.result, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    launched(ctx, 3);
+    *rel = b2 > 0 ? std::sqrt(r2 / b2) : std::sqrt(r2);
+    return DFG_OK;
+  });
+}

@@ -1,0 +1,169 @@
+// dfg_internal.h -- host-side structures of libdfg (not part of the ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/dfg.h"
+
+namespace dfg {
+
+// ------------------------------------------------------------------ errors
+
+struct Error {
+  int status;
+  std::string msg;
+};
+
+// ------------------------------------------------------------ device buffer
+
+struct DBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) { release(); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  void release();
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// --------------------------------------------------------------- schedules
+
+// Forward/backward sweep over the rows of a block-triangular factor, cut into
+// contiguous "ranges" (one warp each) and, inside a range, into "steps" of up
+// to 32 rows whose intra-range dependencies all sit in earlier steps.  Each
+// dependency is encoded as
+//   src >= 0        : ring slot (step % R)*32 + lane of a row of the same range
+//                     finished fewer than R steps ago (read from shared memory)
+//   src == kSrcPad  : padding
+//   otherwise       : -(row+1), a row read from the global output buffer
+//                     (another range, or an old row of the same range)
+struct SweepPlan {
+  static constexpr int kSrcPad = INT32_MIN;
+  bool forward = true;
+  int n = 0, b = 1;
+  int nranges = 0, nsteps = 0, R = 32, max_nent = 0;
+  std::vector<int> range_steps;      // nranges+1
+  std::vector<int> step_nent;        // nsteps
+  std::vector<long long> ent_off;    // nsteps+1, in units of 32-lane entries
+  std::vector<int> step_rows;        // nsteps*32, -1 = empty lane
+  std::vector<int> ent_src;          // ent_off[nsteps]*32
+  std::vector<int> ent_slot;         // CRS slot of the block (-1 for padding)
+  double est_cost = 0.0;             // model makespan (steps), for range-size choice
+};
+
+// byte layout of one step record for element size `sz`:
+//   [hdr 16][row 32*4][src nent*32*4][blk nent*32*bs*sz][dinv 32*bs*sz (forward only)]
+inline long long rec_bytes(int nent, int bs, int sz, bool forward) {
+  return 16 + 128 + (long long)nent * 128 + (long long)nent * 32 * bs * sz + (forward ? 32LL * bs * sz : 0);
+}
+
+// level sets of the triangular dependency DAG (rows sorted by level, then row)
+struct Levels {
+  std::vector<int> level;   // per row
+  std::vector<int> ptr;     // nlevels+1
+  std::vector<int> rows;    // n
+};
+
+Levels build_levels(int n, const int* rowptr, const int* colind, const int* diaind, bool forward);
+SweepPlan build_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind,
+                           bool forward, int range_rows, int R);
+SweepPlan choose_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind,
+                            bool forward, int R, int elem_size);
+
+// node-to-node pattern from elements, no diagonal, ascending (MakePattern_FEM)
+void pattern_from_elements(int nnode, int nelem, int nnoel, const int* conn,
+                           std::vector<int>& rowptr, std::vector<int>& colind);
+
+// Element-to-slot gather map.  Slot s < n is diagonal block s, slot n+c is
+// off-diagonal CRS block c.  slot_src lists, in increasing element order,
+// the element-matrix block index e*k*k + i*k + j contributing to that slot;
+// res_src lists e*k + i for each node.  Summing in this order reproduces the
+// reference's CMatDia_BlkCrs::Mearge / CVector_Blk::AddValue order exactly.
+struct GatherMap {
+  std::vector<long long> slot_ptr;  // n+nnz+1
+  std::vector<int> slot_src;
+  std::vector<long long> res_ptr;   // n+1
+  std::vector<int> res_src;
+};
+bool build_gather_map(int n, const int* rowptr, const int* colind, int nelem, int nnoel,
+                      const int* conn, GatherMap& out, std::string& err);
+
+// --------------------------------------------------------------- handles
+
+struct Ctx;
+
+struct PcgState;  // device-side solver state (defined in solve.cu)
+
+struct SweepDev {
+  // one packed record buffer per precision
+  DBuf rec64, rec32;
+  DBuf rec_off64, rec_off32;       // long long per step (+1)
+  DBuf step_nent, range_steps;
+  DBuf ent_slot, ent_off, step_rows;
+  long long rec_total64 = 0, rec_total32 = 0;
+  long long max_rec64 = 0, max_rec32 = 0;
+  SweepPlan plan;
+};
+
+}  // namespace dfg
+
+struct dfg_ctx_s {
+  int device = 0;
+  int nsm = 0;
+  size_t smem_optin = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  long long launches = 0;
+  dfg::DBuf err_word;     // int, device error word (dfg::kErr*)
+  dfg::DBuf scratch;      // reduction partials + scalars
+  int* h_pinned = nullptr;  // small pinned host area for status reads
+};
+
+struct dfg_system_s {
+  dfg_ctx ctx = nullptr;
+  int n = 0, b = 1;
+  long long nnz = 0;
+  std::vector<int> h_rowptr, h_colind, h_diaind;
+  dfg::DBuf rowptr, colind, diaind;
+  dfg::DBuf diag, offd;            // FP64 matrix, reference layout
+  dfg::DBuf diag32, offd32;        // FP32 copy (mixed precision)
+  bool mat32_valid = false;
+  dfg::DBuf res, upd, rhs0;        // slots -1, -2 and the finalized right-hand side
+  bool rhs0_valid = false;
+  std::vector<dfg::DBuf> tmp;      // slots >= 0
+  dfg::DBuf bcflag;
+  bool has_bc = false;
+  // mesh
+  int ndim = 0, nelem = 0, nnoel = 0;
+  dfg::DBuf coords, conn, coef, fu, fv;
+  bool has_coef = false, has_u = false, has_v = false;
+  dfg::DBuf slot_ptr, slot_src, res_ptr, res_src;
+  dfg::DBuf em, er;                // element matrices / residuals (assembly scratch)
+  // solver workspace (allocated on first solve)
+  dfg::DBuf w_p, w_q, w_z, w_state;          // FP64 PCG
+  dfg::DBuf w_rd, w_d, w_r32, w_p32, w_q32, w_z32;  // mixed
+};
+
+struct dfg_precond_s {
+  dfg_ctx ctx = nullptr;
+  int lev = 0;
+  dfg_system sys = nullptr;        // system of the symbolic set-up
+  bool symbolic = false, numeric = false, numeric32 = false;
+  int n = 0, b = 1;
+  long long nnz = 0;
+  dfg::DBuf fdiag, foffd;          // factor, reference layout (FP64)
+  dfg::Levels lev_fwd;
+  dfg::DBuf lev_rows;
+  dfg::SweepDev fwd, bwd;
+  dfg::DBuf ybuf64, ybuf32;        // forward-sweep outputs
+};

@@ -1,0 +1,91 @@
+// k_solve.h -- launch interface of the SpMV / BLAS-1 / PCG kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace dfg {
+
+// device-resident Krylov state (one per solve)
+struct PcgState {
+  double rz, alpha, beta, rr, inv_rr0, tol2, conv, rr0;
+  double pap;
+  double rr_ref;   // mixed: recursive residual norm^2 at the last reliable update
+  double delta2;   // mixed: reliable update once rr < delta2 * rr_ref
+  double tolb2;    // mixed: tol^2 * ||b||^2
+  int it, maxit, done, iter_out;
+  int pad[4];
+};
+// done codes: 0 running, 1 converged, 2 iteration limit, 3 NaN,
+//             4 reliable update due (mixed), 5 recursive residual below tol (mixed)
+
+// deterministic reductions: fixed grid, per-block partials, the last block
+// to finish sums the partials in index order
+struct Red {
+  double* partials;     // >= kRedGrid
+  unsigned* counter;    // one counter per concurrent reduction channel
+  double* result;       // where the finished sum goes (may be nullptr)
+};
+constexpr int kRedGrid = 304;   // 2 x 152 SMs
+constexpr int kRedTpb = 256;
+
+struct MatView {
+  int n, b;
+  const int* rowptr;
+  const int* colind;
+  const void* diag;   // double or float
+  const void* offd;
+};
+
+// ---- FP64 PCG (plain path) -------------------------------------------------
+struct PcgVecs {
+  double* r;   // residual slot
+  double* x;   // update slot
+  double* p;
+  double* q;   // A p
+  double* y;   // forward-sweep output
+  double* z;   // backward-sweep output (preconditioned residual)
+  long long m; // n*b
+};
+cudaError_t pcg_init(const PcgVecs& v, PcgState* st, Red red, double tol, int maxit, int* tickets, cudaStream_t s);
+cudaError_t pcg_after_precond0(const PcgVecs& v, PcgState* st, Red red, cudaStream_t s);
+cudaError_t pcg_spmv_pap(const MatView& A, const PcgVecs& v, PcgState* st, Red red, cudaStream_t s);
+cudaError_t pcg_update_rx(const PcgVecs& v, PcgState* st, Red red, int* tickets, cudaStream_t s);
+cudaError_t pcg_rz_beta(const PcgVecs& v, PcgState* st, Red red, cudaStream_t s);
+cudaError_t pcg_update_p(const PcgVecs& v, PcgState* st, cudaStream_t s);
+
+// ---- mixed precision ----------------------------------------------------
+struct MixVecs {
+  double* b;       // right-hand side (FP64)
+  double* x;       // solution (FP64)
+  double* rd;      // FP64 true residual b - A x at the last reliable update
+  double* d;       // FP64 correction accumulated since the last reliable update
+  float* r;        // inner residual
+  float* p;
+  float* q;
+  float* y;
+  float* z;
+  long long m;
+};
+// rd = b - A64 x; rr = rd.rd (FP64)
+cudaError_t mix_true_residual(const MatView& A64, const MixVecs& v, PcgState* st, Red red, cudaStream_t s);
+// r32 = rd; rr_ref = rr; done = 0; sweep outputs refilled; tickets reset
+cudaError_t mix_replace(const MixVecs& v, PcgState* st, int* tickets, cudaStream_t s);
+// first call: state reset for a solve (tolerance, limits)
+cudaError_t mix_start(PcgState* st, double tol, double bb, double delta, int maxit, cudaStream_t s);
+cudaError_t mix_after_precond0(const MixVecs& v, PcgState* st, Red red, cudaStream_t s);
+cudaError_t mix_spmv_pap(const MatView& A32, const MixVecs& v, PcgState* st, Red red, cudaStream_t s);
+cudaError_t mix_update_rx(const MixVecs& v, PcgState* st, Red red, int* tickets, cudaStream_t s);
+cudaError_t mix_rz_beta(const MixVecs& v, PcgState* st, Red red, cudaStream_t s);
+cudaError_t mix_update_p(const MixVecs& v, PcgState* st, cudaStream_t s);
+// x += d; d = 0
+cudaError_t mix_accumulate(const MixVecs& v, cudaStream_t s);
+cudaError_t mix_clear_done(PcgState* st, cudaStream_t s);
+cudaError_t to_fp32(long long m, const double* a, float* b, cudaStream_t s);
+
+// ---- strict drop-in BLAS (k_api.cu, bit-exact elementwise ops) ------------
+cudaError_t api_matvec(const MatView& A, double alpha, const double* x, double beta, double* y, cudaStream_t s);
+cudaError_t api_axpy(long long m, double alpha, const double* x, double* y, cudaStream_t s);
+cudaError_t api_scal(long long m, double alpha, double* x, cudaStream_t s);
+cudaError_t api_dot(long long m, const double* x, const double* y, Red red, cudaStream_t s);
+cudaError_t fill_sentinel(long long m, void* p, bool fp32, cudaStream_t s);
+
+}  // namespace dfg

@@ -1,0 +1,51 @@
+// k_sweep.h -- launch interface of the triangular-sweep kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace dfg {
+
+struct SweepArgs {
+  const unsigned char* rec;   // packed step records
+  const long long* rec_off;   // nsteps+1 byte offsets
+  const int* range_steps;     // nranges+1
+  int nranges;
+  const void* in;             // right-hand side, n*B of T
+  void* out;                  // result, n*B of T, pre-filled with the sentinel (+32 B slack)
+  int* ticket;                // range ticket counter (0 at launch)
+  int* err;                   // device error word
+  const int* done;            // optional: skip the launch when *done != 0
+  int rec_stage;              // bytes per record slot (>= the largest record)
+  int val_stage;              // bytes per value slot
+  int R;                      // ring depth in steps
+};
+
+// smem bytes a launch needs
+inline size_t sweep_smem_bytes(int K, int rec_stage, int val_stage, int R, int B, int elem) {
+  return (size_t)2 * K * rec_stage + (size_t)(K + 1) * val_stage + (size_t)R * B * 32 * elem;
+}
+// bytes of one value slot: right-hand sides + raw 32-byte windows per global dependency
+inline int sweep_val_stage(int max_nent, int B, int elem) {
+  int v = B * 32 * elem;
+  v = (v + 15) / 16 * 16;
+  return v + max_nent * 32 * 32;
+}
+
+// launchers (k_sweep.cu)
+cudaError_t launch_sweep(bool forward, bool fp32, int B, int K, const SweepArgs& a, int grid,
+                         size_t smem, cudaStream_t st);
+cudaError_t sweep_set_smem_limits(size_t max_smem);
+
+// packing the factor into step records (k_sweep.cu)
+struct PackArgs {
+  int nsteps;
+  unsigned char* rec;
+  const long long* rec_off;
+  const long long* ent_off;   // nsteps+1
+  const int* ent_slot;        // per 32-lane entry
+  const int* step_rows;       // nsteps*32
+  const double* fdiag;
+  const double* foffd;
+};
+cudaError_t launch_pack(bool forward, bool fp32, int B, const PackArgs& a, cudaStream_t st);
+
+}  // namespace dfg

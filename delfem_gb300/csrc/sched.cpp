@@ -1,0 +1,258 @@
+// sched.cpp -- host-side symbolic work: patterns, level sets, sweep
+// schedules and the assembly gather map.  Runs once per mesh / pattern.
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <numeric>
+
+#include "dfg_internal.h"
+
+namespace dfg {
+
+// CElemAry::MakePattern_FEM (src/femfield/elem_ary.cpp:225-245): elements
+// surrounding each point, then the points of those elements except the point
+// itself, sorted ascending (Com::CIndexedArray::Sort).
+void pattern_from_elements(int nnode, int nelem, int nnoel, const int* conn,
+                           std::vector<int>& rowptr, std::vector<int>& colind) {
+  std::vector<int> esup_ptr(nnode + 1, 0);
+  for (long long k = 0; k < (long long)nelem * nnoel; ++k) esup_ptr[conn[k] + 1]++;
+  for (int i = 0; i < nnode; ++i) esup_ptr[i + 1] += esup_ptr[i];
+  std::vector<int> esup(esup_ptr[nnode]);
+  std::vector<int> fill(esup_ptr.begin(), esup_ptr.end() - 1);
+  for (int e = 0; e < nelem; ++e)
+    for (int k = 0; k < nnoel; ++k) esup[fill[conn[(long long)e * nnoel + k]]++] = e;
+  std::vector<int> mark(nnode, -1);
+  rowptr.assign(nnode + 1, 0);
+  colind.clear();
+  colind.reserve((size_t)nnode * 8);
+  std::vector<int> tmp;
+  for (int i = 0; i < nnode; ++i) {
+    tmp.clear();
+    for (int p = esup_ptr[i]; p < esup_ptr[i + 1]; ++p) {
+      const int e = esup[p];
+      for (int k = 0; k < nnoel; ++k) {
+        const int j = conn[(long long)e * nnoel + k];
+        if (j == i || mark[j] == i) continue;
+        mark[j] = i;
+        tmp.push_back(j);
+      }
+    }
+    std::sort(tmp.begin(), tmp.end());
+    colind.insert(colind.end(), tmp.begin(), tmp.end());
+    rowptr[i + 1] = (int)colind.size();
+  }
+}
+
+static inline void deps_of(int row, bool forward, const int* rowptr, const int* diaind, int& c0, int& c1) {
+  if (forward) { c0 = rowptr[row]; c1 = diaind[row]; }
+  else { c0 = diaind[row]; c1 = rowptr[row + 1]; }
+}
+
+Levels build_levels(int n, const int* rowptr, const int* colind, const int* diaind, bool forward) {
+  Levels L;
+  L.level.assign(n, 0);
+  int maxlev = -1;
+  for (int p = 0; p < n; ++p) {
+    const int row = forward ? p : n - 1 - p;
+    int c0, c1;
+    deps_of(row, forward, rowptr, diaind, c0, c1);
+    int lv = 0;
+    for (int c = c0; c < c1; ++c) lv = std::max(lv, L.level[colind[c]] + 1);
+    L.level[row] = lv;
+    maxlev = std::max(maxlev, lv);
+  }
+  const int nl = maxlev + 1;
+  L.ptr.assign(nl + 1, 0);
+  for (int i = 0; i < n; ++i) L.ptr[L.level[i] + 1]++;
+  for (int l = 0; l < nl; ++l) L.ptr[l + 1] += L.ptr[l];
+  L.rows.assign(n, 0);
+  std::vector<int> fill(L.ptr.begin(), L.ptr.end() - 1);
+  for (int p = 0; p < n; ++p) {
+    const int row = forward ? p : n - 1 - p;
+    L.rows[fill[L.level[row]]++] = row;
+  }
+  return L;
+}
+
+SweepPlan build_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind,
+                           bool forward, int range_rows, int R) {
+  SweepPlan P;
+  P.forward = forward;
+  P.n = n;
+  P.b = b;
+  P.R = R;
+  range_rows = std::max(1, range_rows);
+  P.nranges = (n + range_rows - 1) / range_rows;
+  P.range_steps.assign(P.nranges + 1, 0);
+  std::vector<int> llev(n, 0);          // local level per row
+  std::vector<int> row_step(n, 0), row_lane(n, 0), row_range(n, 0);
+  std::vector<int> cnt;
+  // pass 1: steps per range
+  for (int r = 0; r < P.nranges; ++r) {
+    const int p0 = r * range_rows, p1 = std::min(n, p0 + range_rows);
+    int maxl = 0;
+    for (int p = p0; p < p1; ++p) {
+      const int row = forward ? p : n - 1 - p;
+      int c0, c1;
+      deps_of(row, forward, rowptr, diaind, c0, c1);
+      int lv = 0;
+      for (int c = c0; c < c1; ++c) {
+        const int k = colind[c];
+        const int pk = forward ? k : n - 1 - k;
+        if (pk >= p0) lv = std::max(lv, llev[k] + 1);
+      }
+      llev[row] = lv;
+      row_range[row] = r;
+      maxl = std::max(maxl, lv);
+    }
+    cnt.assign(maxl + 2, 0);
+    for (int p = p0; p < p1; ++p) cnt[llev[forward ? p : n - 1 - p] + 1]++;
+    // steps: ceil(level size / 32) per level, in level order, rows in position order
+    int s = P.nsteps;
+    std::vector<int> lvl_first_step(maxl + 1), lvl_fill(maxl + 1, 0);
+    for (int l = 0; l <= maxl; ++l) {
+      lvl_first_step[l] = s;
+      s += (cnt[l + 1] + 31) / 32;
+    }
+    for (int p = p0; p < p1; ++p) {
+      const int row = forward ? p : n - 1 - p;
+      const int l = llev[row];
+      const int q = lvl_fill[l]++;
+      row_step[row] = lvl_first_step[l] + q / 32;
+      row_lane[row] = q % 32;
+    }
+    P.range_steps[r] = P.nsteps;
+    P.nsteps = s;
+  }
+  P.range_steps[P.nranges] = P.nsteps;
+  // pass 2: rows per step and entry counts
+  P.step_rows.assign((size_t)P.nsteps * 32, -1);
+  P.step_nent.assign(P.nsteps, 0);
+  for (int row = 0; row < n; ++row) {
+    P.step_rows[(size_t)row_step[row] * 32 + row_lane[row]] = row;
+    int c0, c1;
+    deps_of(row, forward, rowptr, diaind, c0, c1);
+    P.step_nent[row_step[row]] = std::max(P.step_nent[row_step[row]], c1 - c0);
+  }
+  P.ent_off.assign(P.nsteps + 1, 0);
+  for (int s = 0; s < P.nsteps; ++s) {
+    P.ent_off[s + 1] = P.ent_off[s] + P.step_nent[s];
+    P.max_nent = std::max(P.max_nent, P.step_nent[s]);
+  }
+  const long long nent_total = P.ent_off[P.nsteps];
+  P.ent_src.assign((size_t)nent_total * 32, SweepPlan::kSrcPad);
+  P.ent_slot.assign((size_t)nent_total * 32, -1);
+  for (int row = 0; row < n; ++row) {
+    const int s = row_step[row], lane = row_lane[row], r = row_range[row];
+    const int local = s - P.range_steps[r];
+    int c0, c1;
+    deps_of(row, forward, rowptr, diaind, c0, c1);
+    for (int c = c0; c < c1; ++c) {
+      const int k = colind[c];
+      const long long e = P.ent_off[s] + (c - c0);
+      int src;
+      if (row_range[k] == r && local - (row_step[k] - P.range_steps[r]) < R) {
+        const int lk = row_step[k] - P.range_steps[r];
+        src = (lk % R) * 32 + row_lane[k];
+      } else {
+        src = -(k + 1);
+      }
+      P.ent_src[(size_t)e * 32 + lane] = src;
+      P.ent_slot[(size_t)e * 32 + lane] = c;
+    }
+  }
+  // makespan model: a step takes one unit once its range's previous step and
+  // every producer step (+ a hop of kHop units between ranges) are done
+  {
+    const double kHop = 12.0;
+    std::vector<double> step_end(P.nsteps, 0.0);
+    double makespan = 0.0;
+    for (int r = 0; r < P.nranges; ++r) {
+      double t = 0.0;
+      for (int s = P.range_steps[r]; s < P.range_steps[r + 1]; ++s) {
+        double start = t;
+        for (long long e = P.ent_off[s]; e < P.ent_off[s + 1]; ++e)
+          for (int lane = 0; lane < 32; ++lane) {
+            const int src = P.ent_src[(size_t)e * 32 + lane];
+            if (src == SweepPlan::kSrcPad || src >= 0) continue;
+            const int k = -src - 1;
+            const double ready = step_end[row_step[k]] + (row_range[k] == r ? 0.0 : kHop);
+            start = std::max(start, ready);
+          }
+        int nrow = 0;
+        for (int lane = 0; lane < 32; ++lane) nrow += P.step_rows[(size_t)s * 32 + lane] >= 0;
+        t = start + 1.0 + 0.002 * nrow * (P.step_nent[s] + 1) * b * b;
+        step_end[s] = t;
+      }
+      makespan = std::max(makespan, t);
+    }
+    P.est_cost = makespan;
+  }
+  return P;
+}
+
+SweepPlan choose_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind,
+                            bool forward, int R, int /*elem_size*/) {
+  SweepPlan best;
+  bool have = false;
+  for (long long rr = 256; ; rr *= 2) {
+    const int range_rows = (int)std::min<long long>(rr, std::max(n, 1));
+    SweepPlan P = build_sweep_plan(n, b, rowptr, colind, diaind, forward, range_rows, R);
+    if (!have || P.est_cost < best.est_cost * 0.97) { best = std::move(P); have = true; }
+    if (range_rows >= n) break;
+  }
+  return best;
+}
+
+bool build_gather_map(int n, const int* rowptr, const int* colind, int nelem, int nnoel,
+                      const int* conn, GatherMap& G, std::string& err) {
+  const long long nnz = rowptr[n];
+  const int k = nnoel;
+  G.slot_ptr.assign(n + nnz + 1, 0);
+  G.res_ptr.assign(n + 1, 0);
+  // count
+  for (int e = 0; e < nelem; ++e) {
+    const int* no = conn + (long long)e * k;
+    for (int i = 0; i < k; ++i) {
+      if (no[i] < 0 || no[i] >= n) { err = "connectivity index out of range"; return false; }
+      G.res_ptr[no[i] + 1]++;
+      for (int j = 0; j < k; ++j) {
+        if (i == j) { G.slot_ptr[no[i] + 1]++; continue; }
+        const int* b0 = colind + rowptr[no[i]];
+        const int* b1 = colind + rowptr[no[i] + 1];
+        const int* f = std::lower_bound(b0, b1, no[j]);
+        if (f == b1 || *f != no[j]) continue;  // Mearge skips blocks outside the pattern
+        G.slot_ptr[n + (f - colind) + 1]++;
+      }
+    }
+  }
+  for (long long s = 0; s < n + nnz; ++s) G.slot_ptr[s + 1] += G.slot_ptr[s];
+  for (int i = 0; i < n; ++i) G.res_ptr[i + 1] += G.res_ptr[i];
+  if (G.slot_ptr[n + nnz] > INT32_MAX || (long long)nelem * k * k > INT32_MAX) {
+    err = "mesh too large for 32-bit element-block indices";
+    return false;
+  }
+  G.slot_src.assign(G.slot_ptr[n + nnz], 0);
+  G.res_src.assign(G.res_ptr[n], 0);
+  std::vector<long long> sf(G.slot_ptr.begin(), G.slot_ptr.end() - 1);
+  std::vector<long long> rf(G.res_ptr.begin(), G.res_ptr.end() - 1);
+  // fill in element order, so each list is sorted by element
+  for (int e = 0; e < nelem; ++e) {
+    const int* no = conn + (long long)e * k;
+    for (int i = 0; i < k; ++i) {
+      G.res_src[rf[no[i]]++] = e * k + i;
+      for (int j = 0; j < k; ++j) {
+        const int blk = (e * k + i) * k + j;
+        if (i == j) { G.slot_src[sf[no[i]]++] = blk; continue; }
+        const int* b0 = colind + rowptr[no[i]];
+        const int* b1 = colind + rowptr[no[i] + 1];
+        const int* f = std::lower_bound(b0, b1, no[j]);
+        if (f == b1 || *f != no[j]) continue;
+        G.slot_src[sf[n + (f - colind)]++] = blk;
+      }
+    }
+  }
+  return true;
+}
+
+}  // namespace dfg

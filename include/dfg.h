@@ -1,0 +1,203 @@
+/*
+ * dfg.h -- C ABI of libdfg, the GB300 (sm_103a) implementation of DelFEM's
+ * finite-element assembly + block ILU(0) preconditioned CG hot path.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, and
+ * returns an int status (DFG_OK == 0).  Host pointers passed in are copied
+ * before the call returns and never retained.  Device memory is owned by
+ * the handles.  All work of one context is ordered on that context's CUDA
+ * stream; calls that hand data back to the host synchronise that stream.
+ * A context is used from one host thread at a time.
+ *
+ * Conventions follow the reference (paths relative to the DelFEM tree):
+ *  - block-CRS with the diagonal blocks kept apart from the off-diagonal CRS
+ *    blocks, each block b x b row-major (include/delfem/matvec/matdia_blkcrs.h:118-123);
+ *    rowptr[nblk+1] / colind[nnz] are what the reference calls m_colInd_Blk /
+ *    m_rowPtr_Blk; columns ascending within a row, no diagonal entry;
+ *  - vector slots of the solver interface: -1 = residual (right-hand side in,
+ *    recursive residual out), -2 = update (solution), >= 0 = work vectors
+ *    (include/delfem/ls/linearsystem_interface_solver.h:39-82);
+ *  - the ILU factor keeps D^-1 in the diagonal slots, the unscaled L in the
+ *    strictly lower part and D^-1 U in the strictly upper part
+ *    (src/matvec/matdiafrac_blkcrs.cpp:862-1046).
+ */
+#ifndef DFG_H
+#define DFG_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+enum {
+  DFG_OK = 0,
+  DFG_NOT_CONVERGED = 1,   /* Solve_PCG returned false (solver_ls_iter.cpp:168-171) */
+  DFG_SINGULAR_PIVOT = 2,  /* more than 10 pivots below 1e-30 (matdiafrac_blkcrs.cpp:779-780) */
+  DFG_NAN_DETECTED = 3,
+  DFG_OOM_REJECTED = 4,    /* device allocation refused */
+  DFG_TIMEOUT = 5,         /* a bounded device-side wait gave up */
+  DFG_INVALID_ARGUMENT = 6,
+  DFG_CUDA_ERROR = 7,
+  DFG_NOT_READY = 8        /* call order violated (e.g. solve before the preconditioner value) */
+};
+
+/* vector precision / solver modes */
+enum {
+  DFG_PREC_FP64 = 0,       /* plain FP64 path */
+  DFG_PREC_MIXED = 1       /* FP32 factor / sweeps / SpMV inside FP64 iterative refinement */
+};
+
+typedef struct dfg_ctx_s* dfg_ctx;
+typedef struct dfg_system_s* dfg_system;
+typedef struct dfg_precond_s* dfg_precond;
+
+/* ---------------------------------------------------------------- context */
+
+/* Creates a context on CUDA device `device` with its own stream. */
+int dfg_ctx_create(int device, dfg_ctx* out);
+int dfg_ctx_destroy(dfg_ctx ctx);
+/* Text of the last error raised through this context (never NULL). */
+const char* dfg_last_error(dfg_ctx ctx);
+/* Library version string. */
+const char* dfg_version(void);
+/* Blocks until all work queued on the context's stream has finished. */
+int dfg_ctx_synchronize(dfg_ctx ctx);
+/* Number of kernels this library has launched through the context. */
+long long dfg_ctx_kernel_launches(dfg_ctx ctx);
+
+/* ------------------------------------------------- linear system (pattern) */
+
+/* Square block-CRS system with a caller-supplied pattern.
+ * Replaces CLinearSystem::AddLinSysSeg + CMatDia_BlkCrs::AddPattern
+ * (src/ls/linearsystem.cpp:138-167, src/matvec/matdia_blkcrs.cpp:346-505). */
+int dfg_system_create(dfg_ctx ctx, int nblk, int blklen,
+                      const int* rowptr, const int* colind, dfg_system* out);
+/* Same, with the node-to-node pattern built from element connectivity
+ * (CElemAry::MakePattern_FEM, src/femfield/elem_ary.cpp:225-245, through
+ * CLinearSystem_Field::AddPattern_Field, src/femls/linearsystem_field.cpp:196-280). */
+int dfg_system_create_from_elements(dfg_ctx ctx, int nblk, int blklen, int nelem, int nnoel,
+                                    const int* conn, dfg_system* out);
+int dfg_system_destroy(dfg_system sys);
+/* nblk, block length and number of off-diagonal blocks. */
+int dfg_system_info(dfg_system sys, int* nblk, int* blklen, long long* nnz);
+/* Copies the pattern out (rowptr: nblk+1 ints, colind: nnz ints). */
+int dfg_system_get_pattern(dfg_system sys, int* rowptr, int* colind);
+
+/* Mesh the element routines read: coordinates (nnode x ndim doubles, node
+ * order == block order) and connectivity (nelem x nnoel ints; 3 = P1
+ * triangle, 4 = P1 tetrahedron).  Builds the element-to-slot gather map.
+ * Stands in for the CFieldWorld node / element segments the reference's
+ * AddLinSys_* routines read (CElemSeg::GetNodes, CNodeSeg::GetValue). */
+int dfg_system_set_mesh(dfg_system sys, int ndim, const double* coords,
+                        int nelem, int nnoel, const int* conn);
+/* Per-element coefficient multiplier (nelem doubles) or NULL for none.
+ * The reference has one scalar per element array; with a multiplier, alpha
+ * (Poisson/diffusion) or lambda and myu (elasticity) become value*coef[e].
+ * A multiplier of exactly 1.0 reproduces the reference bit-for-bit. */
+int dfg_system_set_coef(dfg_system sys, const double* coef);
+/* Current field values u and velocities v (nblk*blklen doubles each, NULL = 0),
+ * read by the element routines as the reference reads the field node segments. */
+int dfg_system_set_field(dfg_system sys, const double* u, const double* v);
+/* Dirichlet flags, one int per DOF (1 = fixed).  Replaces
+ * CLinearSystem_Field::SetFixedBoundaryCondition_Field -> CBCFlag::SetBC
+ * (src/femls/linearsystem_field.cpp:618-710, include/delfem/matvec/bcflag_blk.h:153-164). */
+int dfg_set_bcflags(dfg_system sys, const int* flags);
+
+/* --------------------------------------------------------------- assembly */
+
+/* Zeroes matrix, residual and update (CLinearSystem::InitializeMarge,
+ * src/ls/linearsystem.cpp:74-88). */
+int dfg_initialize_marge(dfg_system sys);
+/* Fem::Eqn::AddLinSys_Poisson (src/femeqn/eqn_poisson.cpp:428-470): P1 triangle
+ * (:49-125) or P1 tetrahedron (:249-323) according to the mesh. */
+int dfg_assemble_poisson(dfg_system sys, double alpha, double source);
+/* Fem::Eqn::AddLinSys_Diffusion (src/femeqn/eqn_diffusion.cpp:348-400), P1 triangle (:240-347). */
+int dfg_assemble_diffusion(dfg_system sys, double dt, double gamma,
+                           double rho, double alpha, double source);
+/* Fem::Eqn::AddLinSys_LinearSolid2D_Static (src/femeqn/eqn_linear_solid2d.cpp:215-266),
+ * P1 triangle (:505-598). */
+int dfg_assemble_solid2d(dfg_system sys, double lambda, double myu,
+                         double rho, double g_x, double g_y);
+/* Fem::Eqn::AddLinSys_LinearSolid3D_Static (src/femeqn/eqn_linear_solid3d.cpp:162-194),
+ * P1 tetrahedron (:241-334). */
+int dfg_assemble_solid3d(dfg_system sys, double lambda, double myu,
+                         double rho, double g_x, double g_y, double g_z);
+/* residual += f (nblk*blklen doubles): extra nodal loads such as the traction
+ * CEqnSystem_Solid2D::SetLoad stores (src/femeqn/eqnsys_solid.cpp:894-907);
+ * equivalent to CVector_Blk::AddValue on every DOF. */
+int dfg_add_residual(dfg_system sys, const double* f);
+/* Dirichlet rows/columns, residual zeroed on fixed DOFs; *norm_res = ||r||_2
+ * (CLinearSystem::FinalizeMarge, src/ls/linearsystem.cpp:92-128). */
+int dfg_finalize_marge(dfg_system sys, double* norm_res);
+
+/* Host copies of the matrix (diag: nblk*b*b, offd: nnz*b*b doubles) and of the
+ * solver vectors (CLinearSystem_Field::GetMatrix / GetResidual / GetUpdate,
+ * src/femls/linearsystem_field.cpp:577-616). */
+int dfg_get_matrix(dfg_system sys, double* diag, double* offd);
+int dfg_set_matrix(dfg_system sys, const double* diag, const double* offd);
+int dfg_get_vector(dfg_system sys, int iv, double* out);
+int dfg_set_vector(dfg_system sys, int iv, const double* in);
+
+/* ---------------------------------------- solver interface (ILinearSystem_Sol) */
+
+int dfg_get_tmp_vector_size(dfg_system sys, unsigned* size);
+int dfg_resize_tmp_vec(dfg_system sys, unsigned size);
+/* *out = {v1}.{v2} (CLinearSystem::DOT, src/ls/linearsystem.cpp:335-360) */
+int dfg_dot(dfg_system sys, int iv1, int iv2, double* out);
+/* {v2} := {v1} (COPY :366-392) */
+int dfg_copy(dfg_system sys, int iv1, int iv2);
+/* {v1} := alpha*{v1} (SCAL :398-415) */
+int dfg_scal(dfg_system sys, double alpha, int iv1);
+/* {v2} := alpha*{v1} + {v2} (AXPY :298-329; no-op when alpha == 0) */
+int dfg_axpy(dfg_system sys, double alpha, int iv1, int iv2);
+/* {v2} := alpha*[A]{v1} + beta*{v2} (MATVEC :250-292 -> CMatDia_BlkCrs::MatVec,
+ * src/matvec/matdia_blkcrs.cpp:921-1094) */
+int dfg_matvec(dfg_system sys, double alpha, int iv1, double beta, int iv2);
+
+/* ------------------------------------------------------- ILU(0) preconditioner */
+
+/* LsSol::CPreconditioner_ILU (include/delfem/ls/preconditioner.h:59-108). */
+int dfg_precond_create(dfg_ctx ctx, dfg_precond* out);
+int dfg_precond_destroy(dfg_precond prec);
+/* SetFillInLevel (preconditioner.h:77-84); only level 0 is implemented. */
+int dfg_precond_set_fill_level(dfg_precond prec, int lev);
+/* Symbolic set-up: pattern copy, split index, level sets and sweep schedules
+ * (CPreconditioner_ILU::SetLinearSystem, src/ls/preconditioner.cpp:57-211;
+ * CMatDiaFrac_BlkCrs(0,A), src/matvec/matdiafrac_blkcrs.cpp:171-225). */
+int dfg_precond_set_linear_system(dfg_precond prec, dfg_system sys);
+/* Numeric factorisation of the system's current matrix
+ * (CPreconditioner_ILU::SetValue, src/ls/preconditioner.cpp:217-297 ->
+ * DoILUDecomp, src/matvec/matdiafrac_blkcrs.cpp:774-1107).  Returns
+ * DFG_SINGULAR_PIVOT when the reference would return false. */
+int dfg_precond_set_value(dfg_precond prec, dfg_system sys);
+/* {iv} := (LU)^-1 {iv} (CPreconditioner_ILU::SolvePrecond, src/ls/preconditioner.cpp:301-335). */
+int dfg_precond_solve(dfg_precond prec, dfg_system sys, int iv);
+/* Host copy of the factor in the reference layout. */
+int dfg_precond_get_factor(dfg_precond prec, double* fdiag, double* foffd);
+
+/* ------------------------------------------------------------------- solvers */
+
+/* LsSol::Solve_PCG (src/ls/solver_ls_iter.cpp:100-172) run device-resident:
+ * residual slot in = right-hand side, out = recursive residual; update slot
+ * out = solution.  *conv_ratio: tolerance in, achieved ||r||/||r0|| out;
+ * *iteration: maximum in, 0-based iteration of convergence out.
+ * Returns DFG_OK when converged, DFG_NOT_CONVERGED otherwise. */
+int dfg_solve_pcg(dfg_system sys, dfg_precond prec, double* conv_ratio, unsigned* iteration);
+
+/* Mixed-precision form of the same solve: FP32 factor, sweeps and SpMV
+ * inside FP64 iterative refinement (FP64 outer residual r = b - A x, FP64
+ * alpha/beta reductions and FP64 solution accumulation).  *conv_ratio: target
+ * true relative residual ||b - A x|| / ||b|| in, achieved out; *iteration:
+ * maximum total inner iterations in, total inner iterations out;
+ * *outer: number of refinement passes out (may be NULL). */
+int dfg_solve_pcg_mixed(dfg_system sys, dfg_precond prec, double* conv_ratio,
+                        unsigned* iteration, unsigned* outer);
+
+/* ||b - A x||_2 / ||b||_2 in FP64 for the system's current matrix, with
+ * b = the given host right-hand side and x = the update slot. */
+int dfg_true_residual(dfg_system sys, const double* b, double* rel);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DFG_H */

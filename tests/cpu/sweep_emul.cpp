@@ -1,0 +1,115 @@
+// sweep_emul.cpp -- TEST INFRASTRUCTURE: executes a sweep schedule built by
+// the library's host scheduler (delfem_gb300/csrc/sched.cpp) sequentially on
+// the CPU, with exactly the dependency encoding the GPU kernel decodes
+// (ring slots for recent same-range rows, global reads otherwise), and
+// checks the properties the kernel relies on:
+//   * every row is scheduled exactly once;
+//   * a ring reference points at the slot the dependency was written to and
+//     that slot has not been overwritten since;
+//   * a global reference points at a row that an earlier range (or an older
+//     step of the same range) has finished -- so ranges claimed in order
+//     can never wait on a range that has not started (no deadlock).
+// Built by tests/test_cpu_schedule.py with g++; never part of libdfg.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../delfem_gb300/csrc/dfg_internal.h"
+
+using namespace dfg;
+
+extern "C" int emul_sweep(int n, int b, const int* rowptr, const int* colind, int forward, int range_rows, int R,
+                          const double* fdiag, const double* foffd, const double* rhs, double* out, long long* info) {
+  std::vector<int> diaind(n);
+  for (int i = 0; i < n; ++i) {
+    int d = rowptr[i + 1];
+    for (int c = rowptr[i]; c < rowptr[i + 1]; ++c)
+      if (colind[c] > i) { d = c; break; }
+    diaind[i] = d;
+  }
+  SweepPlan P = range_rows > 0 ? build_sweep_plan(n, b, rowptr, colind, diaind.data(), forward != 0, range_rows, R)
+                               : choose_sweep_plan(n, b, rowptr, colind, diaind.data(), forward != 0, R, 8);
+  const int bs = b * b;
+  info[0] = P.nranges;
+  info[1] = P.nsteps;
+  info[2] = P.max_nent;
+  info[3] = 0;  // errors
+  std::vector<int> seen(n, 0), done(n, 0), range_of(n, -1);
+  for (int r = 0; r < P.nranges; ++r)
+    for (int s = P.range_steps[r]; s < P.range_steps[r + 1]; ++s)
+      for (int l = 0; l < 32; ++l) {
+        const int row = P.step_rows[(size_t)s * 32 + l];
+        if (row >= 0) { seen[row]++; range_of[row] = r; }
+      }
+  for (int i = 0; i < n; ++i)
+    if (seen[i] != 1) { info[3] = 1; return 1; }
+  std::vector<double> ring((size_t)P.R * 32 * b, NAN);
+  std::vector<int> ring_row((size_t)P.R * 32, -1);
+  for (int r = 0; r < P.nranges; ++r) {
+    std::fill(ring_row.begin(), ring_row.end(), -1);
+    for (int s = P.range_steps[r]; s < P.range_steps[r + 1]; ++s) {
+      const int loc = s - P.range_steps[r];
+      const int nent = P.step_nent[s];
+      // rows of one step are computed from state before the step (as on the GPU)
+      std::vector<double> yv(32 * b, 0.0);
+      std::vector<int> rows(32, -1);
+      for (int l = 0; l < 32; ++l) {
+        const int row = P.step_rows[(size_t)s * 32 + l];
+        rows[l] = row;
+        if (row < 0) continue;
+        double t[3];
+        for (int d = 0; d < b; ++d) t[d] = rhs[(size_t)row * b + d];
+        int c0 = forward ? rowptr[row] : diaind[row];
+        int c1 = forward ? diaind[row] : rowptr[row + 1];
+        if (c1 - c0 > nent) { info[3] = 2; return 2; }
+        for (int e = 0; e < nent; ++e) {
+          const int src = P.ent_src[(size_t)(P.ent_off[s] + e) * 32 + l];
+          const int slot = P.ent_slot[(size_t)(P.ent_off[s] + e) * 32 + l];
+          if (src == SweepPlan::kSrcPad) {
+            if (e < c1 - c0) { info[3] = 3; return 3; }
+            continue;
+          }
+          if (slot != c0 + e) { info[3] = 4; return 4; }
+          const int k = colind[slot];
+          double v[3];
+          if (src >= 0) {
+            const int ss = src >> 5, ln = src & 31;
+            if (ss >= P.R || ring_row[(size_t)ss * 32 + ln] != k) { info[3] = 5; return 5; }
+            for (int d = 0; d < b; ++d) v[d] = ring[((size_t)ss * b + d) * 32 + ln];
+          } else {
+            if (-src - 1 != k) { info[3] = 6; return 6; }
+            if (!done[k]) { info[3] = 7; return 7; }          // would spin forever
+            if (range_of[k] > r) { info[3] = 8; return 8; }   // waits on a later range
+            for (int d = 0; d < b; ++d) v[d] = out[(size_t)k * b + d];
+          }
+          const double* L = foffd + (size_t)slot * bs;
+          for (int p = 0; p < b; ++p)
+            for (int q = 0; q < b; ++q) t[p] -= L[p * b + q] * v[q];
+        }
+        if (forward) {
+          const double* D = fdiag + (size_t)row * bs;
+          for (int p = 0; p < b; ++p) {
+            double acc = 0.0;
+            for (int q = 0; q < b; ++q) acc += D[p * b + q] * t[q];
+            yv[l * b + p] = acc;
+          }
+        } else {
+          for (int p = 0; p < b; ++p) yv[l * b + p] = t[p];
+        }
+      }
+      const int rs = loc % P.R;
+      for (int l = 0; l < 32; ++l) {
+        const int row = rows[l];
+        ring_row[(size_t)rs * 32 + l] = row;
+        if (row < 0) continue;
+        for (int d = 0; d < b; ++d) {
+          ring[((size_t)rs * b + d) * 32 + l] = yv[l * b + d];
+          out[(size_t)row * b + d] = yv[l * b + d];
+        }
+        done[row] = 1;
+      }
+    }
+  }
+  info[4] = (long long)P.est_cost;
+  return 0;
+}

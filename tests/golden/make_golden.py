@@ -1,0 +1,74 @@
+"""Generates the golden fixtures in this directory by running the reference
+itself (the DelFEM sources compiled headless into oracle/_ref/ref_harness by
+``make -C oracle ref``) on small seeded problems.
+
+Each fixture <name>.npz holds the problem (mesh, coefficients, loads,
+Dirichlet flags, parameters) and the reference's outputs: the block pattern,
+the assembled matrix and right-hand side after FinalizeMarge, the ILU(0)
+factor, and the result of LsSol::Solve_PCG (iterations, ratio, solution).
+
+Harness problem file (little-endian): int32 magic 0x44464731, kind, nnode,
+ndim, nelem, nnoel, b; f64 coords[nnode*ndim]; i32 conn[nelem*nnoel];
+i32 has_coef (+ f64 coef[nelem]); f64 params[8]; i32 bcflag[nnode*b];
+i32 has_load (+ f64 load[nnode*b]); i32 has_u (+ f64 u); i32 has_v (+ f64 v);
+f64 tol; i32 maxit.  The result file layout is read by meshgen.read_result.
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), "..", ".."))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from delfem_gb300 import meshgen as mg  # noqa: E402
+import oracle as O  # noqa: E402
+
+
+def cases():
+    return [
+        mg.poisson2d_square(8, seed=11),
+        mg.poisson2d_square(12, seed=12, coef_sigma=0.5),
+        mg.solid2d_cantilever(10, 5, seed=13, coef_sigma=0.5),
+        mg.solid2d_cantilever(6, 3, seed=14, coef_sigma=0.0),
+        mg.solid3d_cube(3, seed=15, coef_sigma=1.0),
+        mg.solid3d_cube(4, seed=16, coef_sigma=0.0, jitter=0.15),
+        mg.poisson3d_cube(4, seed=17),
+        mg.poisson3d_cube(5, seed=18, coef_sigma=1.0),
+        mg.diffusion2d_square(6, seed=19),
+    ]
+
+
+def fixture_name(p: mg.Problem, k: int) -> str:
+    tag = "coef" if p.coef is not None else "uniform"
+    return f"{k:02d}_{p.name.replace('^', 'c')}_{tag}"
+
+
+def main():
+    if not O.harness_available():
+        raise SystemExit("oracle/_ref/ref_harness is missing: run `make -C oracle ref` where the reference exists")
+    here = os.path.dirname(os.path.abspath(__file__))
+    for k, p in enumerate(cases()):
+        R = O.run_reference_harness(p)
+        d = dict(kind=p.kind, coords=p.coords, conn=p.conn, params=p.params, bcflag=p.bcflag, tol=p.tol,
+                 maxit=p.maxit)
+        for nm in ("coef", "load", "u", "v"):
+            a = getattr(p, nm)
+            if a is not None:
+                d[nm] = a
+        for nm in ("rowptr", "colind", "diag", "offd", "rhs", "fdiag", "foffd", "x"):
+            d["ref_" + nm] = R[nm]
+        for nm in ("norm_res", "ilu_ok", "converged", "iter", "conv"):
+            d["ref_" + nm] = np.array(R[nm])
+        path = os.path.join(here, fixture_name(p, k) + ".npz")
+        np.savez_compressed(path, **d)
+        print(f"{path}: n={R['n']} b={R['b']} nnz={R['nnz']} iter={R['iter']} conv={R['conv']:.3e}")
+
+
+if __name__ == "__main__":
+    main()

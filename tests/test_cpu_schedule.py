@@ -1,0 +1,61 @@
+"""The host sweep scheduler (delfem_gb300/csrc/sched.cpp), executed by a
+sequential CPU emulator of the GPU kernel's dependency decoding
+(tests/cpu/sweep_emul.cpp): complete coverage, valid ring references, no
+wait on a later range, and forward/backward results equal to the oracle's
+substitutions up to summation order."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+EMUL_SO = os.path.join(ROOT, "tests", "cpu", "_build", "libsweep_emul.so")
+
+
+@pytest.fixture(scope="module")
+def emul():
+    os.makedirs(os.path.dirname(EMUL_SO), exist_ok=True)
+    srcs = [os.path.join(ROOT, "tests", "cpu", "sweep_emul.cpp"), os.path.join(ROOT, "delfem_gb300", "csrc", "sched.cpp")]
+    inc = [d for d in ("/usr/local/cuda/include",) if os.path.isdir(d)]
+    subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", *[f"-I{d}" for d in inc], "-o", EMUL_SO, *srcs],
+                   check=True)
+    L = ctypes.CDLL(EMUL_SO)
+    P = ctypes.c_void_p
+    L.emul_sweep.argtypes = [ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P, P]
+    return L
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _problems():
+    from delfem_gb300 import meshgen as mg
+    return [mg.poisson2d_square(20, seed=3), mg.solid2d_cantilever(30, 12, seed=4), mg.solid3d_cube(6, seed=5),
+            mg.poisson3d_cube(7, seed=6, coef_sigma=1.0)]
+
+
+@pytest.mark.parametrize("idx", range(4))
+@pytest.mark.parametrize("range_rows", [0, 1, 37, 256, 100000])
+@pytest.mark.parametrize("R", [2, 8, 32])
+def test_sweep_schedule(emul, oracle_lib, idx, range_rows, R):
+    p = _problems()[idx]
+    out = oracle_lib.solve(p, stop_after_ilu=True)
+    n, b = out["n"], out["b"]
+    rhs = np.random.default_rng(idx).standard_normal(n * b)
+    fo = out["foffd"] if out["foffd"].size else np.zeros(1)
+    # forward then backward through the emulator
+    y = np.full(n * b, np.nan)
+    info = np.zeros(8, dtype=np.int64)
+    rc = emul.emul_sweep(n, b, _p(out["rowptr"]), _p(out["colind"]), 1, range_rows, R, _p(out["fdiag"]), _p(fo),
+                         _p(rhs), _p(y), _p(info))
+    assert rc == 0, f"forward schedule check failed with code {rc}"
+    z = np.full(n * b, np.nan)
+    rc = emul.emul_sweep(n, b, _p(out["rowptr"]), _p(out["colind"]), 0, range_rows, R, _p(out["fdiag"]), _p(fo),
+                         _p(y), _p(z), _p(info))
+    assert rc == 0, f"backward schedule check failed with code {rc}"
+    ref = oracle_lib.precond(n, b, out["rowptr"], out["colind"], out["diaind"], out["fdiag"], out["foffd"], rhs)
+    np.testing.assert_allclose(z, ref, rtol=1e-11, atol=1e-12 * np.abs(ref).max())
