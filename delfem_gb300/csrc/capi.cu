@@ -250,6 +250,12 @@ extern "C" int dfg_ctx_synchronize(dfg_ctx ctx) {
 
 extern "C" long long dfg_ctx_kernel_launches(dfg_ctx ctx) { return ctx ? ctx->launches : -1; }
 
+extern "C" int dfg_ctx_get_stream(dfg_ctx ctx, void** stream) {
+  if (!ctx || !stream) return DFG_INVALID_ARGUMENT;
+  *stream = (void*)ctx->stream;
+  return DFG_OK;
+}
+
 // ===================================================================== system
 
 extern "C" int dfg_system_create(dfg_ctx ctx, int nblk, int blklen, const int* rowptr, const int* colind,
@@ -1149,6 +1155,94 @@ extern "C" int dfg_true_residual(dfg_system sys, const double* b, double* rel) {
     CK(cudaStreamSynchronize(ctx->stream));
     launched(ctx, 3);
     *rel = b2 > 0 ? std::sqrt(r2 / b2) : std::sqrt(r2);
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_profile_kernels(dfg_system sys, dfg_precond prec, int mode, int reps, double* ms, double* bytes) {
+  if (!sys || !prec || !ms || reps < 1) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    const bool fp32 = mode == DFG_PREC_MIXED;
+    REQUIRE(prec->numeric && prec->sys == sys, DFG_NOT_READY, "preconditioner value not set for this system");
+    REQUIRE(fp32 ? (sys->w_r32.p && sys->mat32_valid && prec->numeric32) : (sys->w_p.p != nullptr), DFG_NOT_READY,
+            "run a solve of this mode before profiling it");
+    const long long m = (long long)sys->n * sys->b;
+    Scratch sc = scratch_of(ctx);
+    Red red = red_of(ctx, 3);
+    dalloc(ctx, sys->w_state, sizeof(PcgState));
+    PcgState* st = sys->w_state.as<PcgState>();
+    // a state that never reports done, with benign scalars
+    PcgState h{};
+    h.rz = 1.0; h.alpha = 1e-30; h.beta = 1e-30; h.inv_rr0 = 1.0; h.tol2 = 0.0; h.maxit = 1 << 30;
+    h.rr_ref = 1e300; h.delta2 = 0.0; h.tolb2 = 0.0;
+    CK(cudaMemcpyAsync(st, &h, sizeof(PcgState), cudaMemcpyHostToDevice, ctx->stream));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    const MatView A64 = view64(sys);
+    const MatView A32{sys->n, sys->b, sys->rowptr.as<int>(), sys->colind.as<int>(), sys->diag32.p, sys->offd32.p};
+    PcgVecs v{sys->res.as<double>(), sys->upd.as<double>(), sys->w_p.as<double>(), sys->w_q.as<double>(),
+              prec->ybuf64.as<double>(), sys->w_z.as<double>(), m};
+    MixVecs w{sys->rhs0.as<double>(), sys->upd.as<double>(), sys->w_rd.as<double>(), sys->w_d.as<double>(),
+              sys->w_r32.as<float>(), sys->w_p32.as<float>(), sys->w_q32.as<float>(), prec->ybuf32.as<float>(),
+              sys->w_z32.as<float>(), m};
+    const void* rin = fp32 ? (const void*)w.r : (const void*)v.r;
+    void* ybuf = fp32 ? (void*)w.y : (void*)v.y;
+    void* zbuf = fp32 ? (void*)w.z : (void*)v.z;
+    SweepLaunch F = sweep_launch(ctx, prec, prec->fwd, fp32, rin, ybuf, sc.tickets, nullptr);
+    SweepLaunch B = sweep_launch(ctx, prec, prec->bwd, fp32, ybuf, zbuf, sc.tickets + 1, nullptr);
+    auto timed = [&](int slot, auto&& pre, auto&& body) {
+      for (int r = 0; r < reps + 1; ++r) {
+        pre();
+        CK(cudaEventRecord(e0, ctx->stream));
+        body();
+        CK(cudaEventRecord(e1, ctx->stream));
+        CK(cudaEventSynchronize(e1));
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, e0, e1));
+        if (r > 0) acc[slot] += t;  // first launch is a warm-up
+      }
+    };
+    auto nop = [] {};
+    if (fp32) {
+      timed(0, nop, [&] { CK(mix_spmv_pap(A32, w, st, red, ctx->stream)); });
+    } else {
+      timed(0, nop, [&] { CK(pcg_spmv_pap(A64, v, st, red, ctx->stream)); });
+    }
+    timed(1, [&] {
+        CK(fill_sentinel(m, ybuf, fp32, ctx->stream));
+        CK(cudaMemsetAsync(sc.tickets, 0, 2 * sizeof(int), ctx->stream));
+      }, [&] { run_sweep(ctx, true, sys->b, fp32, F); });
+    timed(2, [&] {
+        CK(fill_sentinel(m, zbuf, fp32, ctx->stream));
+        CK(cudaMemsetAsync(sc.tickets, 0, 2 * sizeof(int), ctx->stream));
+      }, [&] { run_sweep(ctx, false, sys->b, fp32, B); });
+    // the update kernels rewrite r, x, p: time them last, on copies of nothing that matters
+    if (fp32) {
+      timed(3, nop, [&] { CK(mix_update_rx(w, st, red, sc.tickets, ctx->stream)); });
+      timed(4, nop, [&] { CK(mix_rz_beta(w, st, red, ctx->stream)); });
+      timed(5, nop, [&] { CK(mix_update_p(w, st, ctx->stream)); });
+    } else {
+      timed(3, nop, [&] { CK(pcg_update_rx(v, st, red, sc.tickets, ctx->stream)); });
+      timed(4, nop, [&] { CK(pcg_rz_beta(v, st, red, ctx->stream)); });
+      timed(5, nop, [&] { CK(pcg_update_p(v, st, ctx->stream)); });
+    }
+    launched(ctx, 8LL * (reps + 1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (int k = 0; k < 6; ++k) ms[k] = acc[k] / reps;
+    if (bytes) {
+      const double sz = fp32 ? 4.0 : 8.0, bs = (double)sys->b * sys->b, N = sys->n, Z = (double)sys->nnz;
+      long long zl = 0;
+      for (int i = 0; i < sys->n; ++i) zl += sys->h_diaind[i] - sys->h_rowptr[i];
+      const double Zl = (double)zl, Zu = Z - Zl, vec = N * sys->b * sz;
+      bytes[0] = (Z + N) * bs * sz + 4.0 * (Z + N + 1) + 2.0 * vec;          // values, indices, x, y
+      bytes[1] = (Zl + N) * bs * sz + 4.0 * (Zl + N + 1) + 2.0 * vec;        // L, D^-1, indices, in, out
+      bytes[2] = Zu * bs * sz + 4.0 * (Zu + N + 1) + 2.0 * vec;              // U', indices, in, out
+    }
     return DFG_OK;
   });
 }

@@ -64,6 +64,9 @@ const char* dfg_version(void);
 int dfg_ctx_synchronize(dfg_ctx ctx);
 /* Number of kernels this library has launched through the context. */
 long long dfg_ctx_kernel_launches(dfg_ctx ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that time or order
+ * their own work against the library's. */
+int dfg_ctx_get_stream(dfg_ctx ctx, void** stream);
 
 /* ------------------------------------------------- linear system (pattern) */
 
@@ -192,6 +195,14 @@ int dfg_solve_pcg(dfg_system sys, dfg_precond prec, double* conv_ratio, unsigned
  * *outer: number of refinement passes out (may be NULL). */
 int dfg_solve_pcg_mixed(dfg_system sys, dfg_precond prec, double* conv_ratio,
                         unsigned* iteration, unsigned* outer);
+
+/* Times each kernel of one PCG iteration on its own (CUDA events on the
+ * context's stream, averaged over `reps` launches) with the system's current
+ * matrix, factor and solver vectors; call after a solve of the same mode.
+ * mode: DFG_PREC_FP64 or DFG_PREC_MIXED.  ms[0..5] = SpMV + p.Ap, forward
+ * sweep, backward sweep, r/x update + r.r, r.z + beta, p update (ms per launch);
+ * bytes[0..2] = algorithmic bytes of one SpMV, forward and backward sweep. */
+int dfg_profile_kernels(dfg_system sys, dfg_precond prec, int mode, int reps, double* ms, double* bytes);
 
 /* ||b - A x||_2 / ||b||_2 in FP64 for the system's current matrix, with
  * b = the given host right-hand side and x = the update slot. */
