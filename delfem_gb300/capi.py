@@ -58,6 +58,7 @@ SIGNATURES = {
     "dfg_assemble_solid2d": (_I, [_P, _D, _D, _D, _D, _D]),
     "dfg_assemble_solid3d": (_I, [_P, _D, _D, _D, _D, _D, _D]),
     "dfg_add_residual": (_I, [_P, _P]),
+    "dfg_system_set_load": (_I, [_P, _P]),
     "dfg_finalize_marge": (_I, [_P, _PD]),
     "dfg_get_matrix": (_I, [_P, _P, _P]),
     "dfg_set_matrix": (_I, [_P, _P, _P]),

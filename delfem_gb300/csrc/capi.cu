@@ -498,11 +498,28 @@ extern "C" int dfg_add_residual(dfg_system sys, const double* f) {
   });
 }
 
+extern "C" int dfg_system_set_load(dfg_system sys, const double* f) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    if (!f) { sys->has_load = false; return DFG_OK; }
+    upload(ctx, sys->load, f, (size_t)sys->n * sys->b);
+    CK(cudaStreamSynchronize(ctx->stream));
+    sys->has_load = true;
+    return DFG_OK;
+  });
+}
+
 extern "C" int dfg_finalize_marge(dfg_system sys, double* norm_res) {
   if (!sys) return DFG_INVALID_ARGUMENT;
   dfg_ctx ctx = sys->ctx;
   return guarded(ctx, [&]() -> int {
     dfg_ctx ctx_ = ctx;
+    if (sys->has_load) {
+      CK(launch_add_vec((long long)sys->n * sys->b, sys->load.as<double>(), sys->res.as<double>(), ctx->stream));
+      launched(ctx);
+    }
     if (sys->has_bc) {
       BcArgs a{};
       a.n = sys->n;
@@ -682,27 +699,10 @@ extern "C" int dfg_matvec(dfg_system sys, double alpha, int iv1, double beta, in
 
 namespace {
 
-// Host-assembled static parts of the step records (header, row ids,
-// dependency codes); the value regions are filled on the device by k_pack.
 void build_records(dfg_ctx ctx_, SweepDev& S, int elem, DBuf& rec, DBuf& rec_off, long long& total, long long& max_rec) {
-  const SweepPlan& P = S.plan;
-  const int bs = P.b * P.b;
-  std::vector<long long> off(P.nsteps + 1, 0);
-  max_rec = 0;
-  for (int s = 0; s < P.nsteps; ++s) {
-    const long long rb = rec_bytes(P.step_nent[s], bs, elem, P.forward);
-    off[s + 1] = off[s] + rb;
-    max_rec = std::max(max_rec, rb);
-  }
-  total = off[P.nsteps];
-  std::vector<unsigned char> h((size_t)total, 0);
-  for (int s = 0; s < P.nsteps; ++s) {
-    unsigned char* r = h.data() + off[s];
-    const int nent = P.step_nent[s];
-    std::memcpy(r, &nent, 4);
-    std::memcpy(r + 16, &P.step_rows[(size_t)s * 32], 128);
-    if (nent) std::memcpy(r + 144, &P.ent_src[(size_t)P.ent_off[s] * 32], (size_t)nent * 128);
-  }
+  std::vector<long long> off;
+  const std::vector<unsigned char> h = pack_record_headers(S.plan, elem, off, max_rec);
+  total = off.back();
   upload(ctx_, rec, h.data(), h.size(), 64);
   upload(ctx_, rec_off, off.data(), off.size());
 }
@@ -736,7 +736,6 @@ void pack_sweep(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, bool fp32) {
 struct SweepLaunch {
   SweepArgs args;
   int grid;
-  int K;
   size_t smem;
 };
 
@@ -757,22 +756,22 @@ SweepLaunch sweep_launch(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, bool fp32, c
   a.rec_stage = (int)((fp32 ? S.max_rec32 : S.max_rec64) + 15) / 16 * 16;
   a.val_stage = sweep_val_stage(S.plan.max_nent, pr->b, elem);
   a.R = S.plan.R;
-  L.K = 4;
-  L.smem = sweep_smem_bytes(L.K, a.rec_stage, a.val_stage, a.R, pr->b, elem);
-  if (L.smem > 64 * 1024) {
-    L.K = 2;
-    L.smem = sweep_smem_bytes(L.K, a.rec_stage, a.val_stage, a.R, pr->b, elem);
-  }
+  // pipeline depth: as deep as 16 stages while the CTA fits in ~200 KB
+  const size_t budget = std::min<size_t>(ctx_->smem_optin, 200 * 1024);
+  int NS = 16;
+  while (NS > 2 && sweep_smem_bytes(NS, a.rec_stage, a.val_stage, a.R, pr->b, elem) > budget) --NS;
+  a.NS = NS;
+  L.smem = sweep_smem_bytes(NS, a.rec_stage, a.val_stage, a.R, pr->b, elem);
   REQUIRE(L.smem <= ctx_->smem_optin, DFG_INVALID_ARGUMENT, "sweep records exceed shared memory");
   int per_sm_bytes = 0;
   cudaDeviceGetAttribute(&per_sm_bytes, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx_->device);
-  int per_sm = std::max(1, std::min(32, (int)(per_sm_bytes / (L.smem + 1024))));
+  int per_sm = std::max(1, std::min(16, (int)(per_sm_bytes / (L.smem + 1024))));
   L.grid = std::max(1, std::min(S.plan.nranges, ctx_->nsm * per_sm));
   return L;
 }
 
 void run_sweep(dfg_ctx ctx_, bool forward, int b, bool fp32, const SweepLaunch& L) {
-  CK(launch_sweep(forward, fp32, b, L.K, L.args, L.grid, L.smem, ctx_->stream));
+  CK(launch_sweep(forward, fp32, b, L.args, L.grid, L.smem, ctx_->stream));
   launched(ctx_);
 }
 
@@ -975,8 +974,8 @@ extern "C" int dfg_solve_pcg(dfg_system sys, dfg_precond prec, double* conv_rati
       for (int c = 0; c < chunk; ++c) {
         pcg_spmv_pap(A, v, st, red, ctx->stream);
         pcg_update_rx(v, st, red, sc.tickets, ctx->stream);
-        launch_sweep(true, false, sys->b, F.K, F.args, F.grid, F.smem, ctx->stream);
-        launch_sweep(false, false, sys->b, B.K, B.args, B.grid, B.smem, ctx->stream);
+        launch_sweep(true, false, sys->b, F.args, F.grid, F.smem, ctx->stream);
+        launch_sweep(false, false, sys->b, B.args, B.grid, B.smem, ctx->stream);
         pcg_rz_beta(v, st, red, ctx->stream);
         pcg_update_p(v, st, ctx->stream);
       }
@@ -1078,8 +1077,8 @@ extern "C" int dfg_solve_pcg_mixed(dfg_system sys, dfg_precond prec, double* con
     for (int c = 0; c < chunk; ++c) {
       mix_spmv_pap(A32, v, st, red, ctx->stream);
       mix_update_rx(v, st, red, sc.tickets, ctx->stream);
-      launch_sweep(true, true, sys->b, F.K, F.args, F.grid, F.smem, ctx->stream);
-      launch_sweep(false, true, sys->b, B.K, B.args, B.grid, B.smem, ctx->stream);
+      launch_sweep(true, true, sys->b, F.args, F.grid, F.smem, ctx->stream);
+      launch_sweep(false, true, sys->b, B.args, B.grid, B.smem, ctx->stream);
       mix_rz_beta(v, st, red, ctx->stream);
       mix_update_p(v, st, ctx->stream);
     }
@@ -1184,10 +1183,22 @@ extern "C" int dfg_profile_kernels(dfg_system sys, dfg_precond prec, int mode, i
     double acc[6] = {0, 0, 0, 0, 0, 0};
     const MatView A64 = view64(sys);
     const MatView A32{sys->n, sys->b, sys->rowptr.as<int>(), sys->colind.as<int>(), sys->diag32.p, sys->offd32.p};
-    PcgVecs v{sys->res.as<double>(), sys->upd.as<double>(), sys->w_p.as<double>(), sys->w_q.as<double>(),
+    // the update kernels run on copies, so the caller's residual, solution and
+    // direction stay as the last solve left them
+    DBuf tr, tx, tp, td;
+    const size_t esz = fp32 ? 4 : 8;
+    dalloc(ctx, tr, vec_bytes(sys, esz));
+    dalloc(ctx, tx, vec_bytes(sys, 8));
+    dalloc(ctx, tp, vec_bytes(sys, esz));
+    dalloc(ctx, td, vec_bytes(sys, 8));
+    CK(cudaMemcpyAsync(tr.p, fp32 ? sys->w_r32.p : sys->res.p, (size_t)m * esz, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(tx.p, sys->upd.p, (size_t)m * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(tp.p, fp32 ? sys->w_p32.p : sys->w_p.p, (size_t)m * esz, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemsetAsync(td.p, 0, (size_t)m * 8, ctx->stream));
+    PcgVecs v{tr.as<double>(), tx.as<double>(), tp.as<double>(), sys->w_q.as<double>(),
               prec->ybuf64.as<double>(), sys->w_z.as<double>(), m};
-    MixVecs w{sys->rhs0.as<double>(), sys->upd.as<double>(), sys->w_rd.as<double>(), sys->w_d.as<double>(),
-              sys->w_r32.as<float>(), sys->w_p32.as<float>(), sys->w_q32.as<float>(), prec->ybuf32.as<float>(),
+    MixVecs w{sys->rhs0.as<double>(), tx.as<double>(), sys->w_rd.as<double>(), td.as<double>(),
+              tr.as<float>(), tp.as<float>(), sys->w_q32.as<float>(), prec->ybuf32.as<float>(),
               sys->w_z32.as<float>(), m};
     const void* rin = fp32 ? (const void*)w.r : (const void*)v.r;
     void* ybuf = fp32 ? (void*)w.y : (void*)v.y;
@@ -1231,6 +1242,7 @@ extern "C" int dfg_profile_kernels(dfg_system sys, dfg_precond prec, int mode, i
       timed(5, nop, [&] { CK(pcg_update_p(v, st, ctx->stream)); });
     }
     launched(ctx, 8LL * (reps + 1));
+    CK(cudaStreamSynchronize(ctx->stream));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     for (int k = 0; k < 6; ++k) ms[k] = acc[k] / reps;

@@ -61,11 +61,22 @@ struct SweepPlan {
   double est_cost = 0.0;             // model makespan (steps), for range-size choice
 };
 
-// byte layout of one step record for element size `sz`:
-//   [hdr 16][row 32*4][src nent*32*4][blk nent*32*bs*sz][dinv 32*bs*sz (forward only)]
+// byte layout of one step record for element size `sz` (k_sweep.cu):
+//   [hdr 16][row 32*4][code nent*32*4][grow nent*32*4][blk nent*32*bs*sz][dinv 32*bs*sz (forward only)]
 inline long long rec_bytes(int nent, int bs, int sz, bool forward) {
-  return 16 + 128 + (long long)nent * 128 + (long long)nent * 32 * bs * sz + (forward ? 32LL * bs * sz : 0);
+  return 16 + 128 + (long long)nent * 256 + (long long)nent * 32 * bs * sz + (forward ? 32LL * bs * sz : 0);
 }
+
+// Host-assembled static parts of the step records of a plan (header, row
+// ids, dependency codes, dependency rows) for element size `elem`; the value
+// regions stay zero and are filled on the device after each factorisation.
+// A code is a byte offset the compute warp adds to one of two bases without
+// branching: the ring region for a dependency finished by the same range
+// within the last R steps (offset 0 = 32 zero bytes for padding), or -- bit 31
+// set -- the step's value slot, where the loader warp gathers the 16-byte
+// window holding an out-of-range dependency.
+std::vector<unsigned char> pack_record_headers(const SweepPlan& P, int elem, std::vector<long long>& off,
+                                               long long& max_rec);
 
 // level sets of the triangular dependency DAG (rows sorted by level, then row)
 struct Levels {
@@ -143,6 +154,8 @@ struct dfg_system_s {
   std::vector<dfg::DBuf> tmp;      // slots >= 0
   dfg::DBuf bcflag;
   bool has_bc = false;
+  dfg::DBuf load;                  // resident nodal load added at finalize
+  bool has_load = false;
   // mesh
   int ndim = 0, nelem = 0, nnoel = 0;
   dfg::DBuf coords, conn, coef, fu, fv;

@@ -2,34 +2,38 @@
 // (CMatDiaFrac_BlkCrs::ForwardSubstitution / BackwardSubstitution,
 // src/matvec/matdiafrac_blkcrs.cpp:332-669) in the reference's natural order.
 //
-// Schedule (built on the host, sched.cpp): the rows are cut into contiguous
-// ranges, one warp each; inside a range the rows are grouped by their local
-// dependency level into steps of <= 32 rows (one row per lane).  A warp
-// walks its steps in order; rows of one step are independent.
+// Schedule (host, sched.cpp): rows are cut into contiguous ranges; inside a
+// range rows are grouped by local dependency level into steps of <= 32 rows
+// (one row per lane); rows of one step are independent.
 //
-//  * a dependency produced by the same warp fewer than R steps ago is read
-//    from a shared-memory ring;
-//  * any other dependency is read from the output vector in global memory.
-//    The output is pre-filled with a NaN sentinel and every value is written
-//    exactly once, so a consumer that sees a non-sentinel value has the final
-//    value: no flags, no fences.  Ranges are claimed through a ticket counter
-//    in row order, so every range a warp waits on is already being worked on.
+// Execution: a persistent CTA of two warps claims ranges in row order
+// through a ticket counter and walks their steps through an NS-deep
+// shared-memory pipeline:
+//   * loader warp  -- per step, one TMA bulk copy of the packed step record
+//     (cp.async.bulk, completion on an mbarrier with a byte count), then, once
+//     the record has landed, per-lane cp.async gathers of the rows' right-hand
+//     sides and of the 16-byte-aligned windows holding dependencies produced
+//     by other ranges; each lane's gathers arrive on the stage's `full`
+//     mbarrier when they complete (cp.async.mbarrier.arrive.noinc);
+//   * compute warp -- waits for `full`, evaluates the rows (dependency values
+//     come from a ring of its own recent results or from the gathered
+//     windows, selected without branching), writes results to the ring and to
+//     global memory, and releases the stage on its `empty` mbarrier.
+// Cross-range hand-off needs no flags or fences: outputs are pre-filled with
+// a NaN sentinel and written once, so a non-sentinel value is final; a window
+// copied before its producer wrote it still holds the sentinel and the
+// compute warp re-polls that value from global memory (bounded).  Ranges are
+// claimed in order, so a range only ever waits on ranges already running.
+// Every wait is bounded (kSpinLimit); a wait that gives up records
+// kErrTimeout and the launch drains and returns.
 //
-// Data movement per step (two-level cp.async pipeline, K steps deep):
-//  record(t)  -- packed step record (row ids, dependency codes, blocks of the
-//                factor, D^-1): issued at step t-2K;
-//  values(t)  -- the rows' right-hand sides and the 16-byte-aligned windows
-//                holding the global dependency values, whose addresses come
-//                from record(t): issued at step t-K (L1-bypassing .cg copies,
-//                so a window copied before its producer wrote it never
-//                leaves a stale line behind; a sentinel seen in a window is
-//                re-polled from global memory).
-// Every wait is bounded (kSpinLimit polls); a wait that gives up records
-// kErrTimeout in the error word and every warp of the launch then leaves.
-//
-// Record layout (bytes): [hdr int4: nent][rows: 32 int][src: nent x 32 int]
+// Record layout (bytes; see build_records in capi.cu):
+//   [hdr int4: nent][row: 32 int][code: nent x 32 int][grow: nent x 32 int]
 //   [blocks: nent x B*B x 32 of T][D^-1: B*B x 32 of T, forward only]
-// (lane-minor, so shared-memory reads are conflict-free).
+// code: bit 31 clear -> byte offset into the ring region (0 = a zero pad);
+//       bit 31 set   -> byte offset into the stage's value slot.
+// grow: global row of an out-of-range dependency (else -1).
+// Value slot: [rhs: 32 lanes x B of T, 16-byte padded][windows: nent x 32 x 32 B].
 #include <climits>
 
 #include "dfg_common.cuh"
@@ -37,152 +41,223 @@
 
 namespace dfg {
 
-template <typename T, int B, bool FWD, int K>
-__global__ void __launch_bounds__(32) k_sweep(SweepArgs a) {
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(smem_u32(bar)),
+               "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait; returns false (and records a timeout) when it gives up
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int* err) {
+  long long n = 0;
+  while (!mbar_try_wait(bar, parity)) {
+    if (++n > kSpinLimit) {
+      atomicExch(err, kErrTimeout);
+      return false;
+    }
+  }
+  return true;
+}
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void cp_async_arrive_noinc(uint64_t* bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void named_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+template <typename T, int B, bool FWD>
+__global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
   constexpr int BS = B * B;
-  constexpr int NREC = 2 * K, NVAL = K + 1;
-  constexpr int RHS_BYTES = ((B * 32 * (int)sizeof(T)) + 15) / 16 * 16;
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int lane = threadIdx.x;
-  unsigned char* rstage = smem;
-  unsigned char* vstage = smem + (size_t)NREC * a.rec_stage;
-  T* ring = reinterpret_cast<T*>(vstage + (size_t)NVAL * a.val_stage);
+  constexpr int SZ = (int)sizeof(T);
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int NS = a.NS;
+  // layout: [bars: 3*NS u64][rstage: NS x rec_stage][vstage: NS x val_stage][zero 32 B][ring]
+  uint64_t* rec_full = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* full = rec_full + NS;
+  uint64_t* empty = full + NS;
+  unsigned char* rstage = smem + (((size_t)3 * NS * 8 + 127) / 128) * 128;
+  unsigned char* vstage = rstage + (size_t)NS * a.rec_stage;
+  unsigned char* ringreg = vstage + (size_t)NS * a.val_stage;  // 32 zero bytes, then the ring
+  __shared__ int s_range;
   const T* __restrict__ in = reinterpret_cast<const T*>(a.in);
   T* out = reinterpret_cast<T*>(a.out);
 
   if (a.done && *a.done) return;
-
-  auto rec_ptr = [&](int slot) { return rstage + (size_t)slot * a.rec_stage; };
-  auto val_ptr = [&](int slot) { return vstage + (size_t)slot * a.val_stage; };
-
-  auto issue_record = [&](long long t, int slot) {
-    const long long o0 = a.rec_off[t], o1 = a.rec_off[t + 1];
-    const unsigned char* g = a.rec + o0;
-    unsigned char* s = rec_ptr(slot);
-    for (long long o = lane * 16; o < o1 - o0; o += 32 * 16) cp_async16(s + o, g + o);
-  };
-  auto issue_values = [&](int rslot, int vslot) {
-    const unsigned char* r = rec_ptr(rslot);
-    const int nent = reinterpret_cast<const int*>(r)[0];
-    const int row = reinterpret_cast<const int*>(r + 16)[lane];
-    unsigned char* v = val_ptr(vslot);
-    if (row < 0) return;
-    T* rhs = reinterpret_cast<T*>(v);
-#pragma unroll
-    for (int d = 0; d < B; ++d) {
-      if constexpr (sizeof(T) == 8) cp_async8(&rhs[d * 32 + lane], &in[(size_t)row * B + d]);
-      else cp_async4(&rhs[d * 32 + lane], &in[(size_t)row * B + d]);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NS; ++s) {
+      mbar_init(&rec_full[s], 1);
+      mbar_init(&full[s], 32);
+      mbar_init(&empty[s], 1);
     }
-    const int* src = reinterpret_cast<const int*>(r + 144);
-    for (int e = 0; e < nent; ++e) {
-      const int c = src[e * 32 + lane];
-      if (c >= 0 || c == INT_MIN) continue;
-      const uintptr_t addr = reinterpret_cast<uintptr_t>(&out[(size_t)(-c - 1) * B]);
-      const unsigned char* w = reinterpret_cast<const unsigned char*>(addr & ~(uintptr_t)15);
-      unsigned char* dst = v + RHS_BYTES + (size_t)(e * 32 + lane) * 32;
-      cp_async16(dst, w);
-      if ((addr & 15) + B * sizeof(T) > 16) cp_async16(dst + 16, w + 16);
-    }
-  };
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (threadIdx.x < 8) reinterpret_cast<unsigned*>(ringreg)[threadIdx.x] = 0u;
+  __syncthreads();
 
+  long long g = 0;  // steps this CTA has pushed through the pipeline (both warps count alike)
   bool abort = false;
   for (;;) {
-    int r = 0;
-    if (lane == 0) r = atomicAdd(a.ticket, 1);
-    r = __shfl_sync(0xffffffffu, r, 0);
+    if (threadIdx.x == 0) s_range = atomicAdd(a.ticket, 1);
+    named_sync(1, 64);
+    const int r = s_range;
+    named_sync(1, 64);
     if (r >= a.nranges) break;
     const long long s0 = a.range_steps[r], s1 = a.range_steps[r + 1];
-    for (int i = 0; i < K; ++i)
-      if (s0 + i < s1) issue_record(s0 + i, i % NREC);
-    cp_async_commit();
-    cp_async_wait_all();
-    __syncwarp();
-    for (int i = 0; i < K; ++i) {
-      if (s0 + i < s1) issue_values(i % NREC, i % NVAL);
-      if (s0 + K + i < s1) issue_record(s0 + K + i, (K + i) % NREC);
-      cp_async_commit();
-    }
-    for (long long s = s0; s < s1; ++s) {
-      const int loc = (int)(s - s0);
-      cp_async_wait<K - 1>();  // the group carrying values(s) and record(s+K) has landed
-      __syncwarp();
-      if (s + K < s1) issue_values((loc + K) % NREC, (loc + K) % NVAL);
-      const unsigned char* rec = rec_ptr(loc % NREC);
-      const int nent = reinterpret_cast<const int*>(rec)[0];
-      const int row = reinterpret_cast<const int*>(rec + 16)[lane];
-      const int* src = reinterpret_cast<const int*>(rec + 144);
-      const T* blk = reinterpret_cast<const T*>(rec + 144 + nent * 128);
-      const unsigned char* val = val_ptr(loc % NVAL);
-      if (row >= 0 && !abort) {
-        T t[B];
+    const long long nsteps = s1 - s0;
+    if (warp == 1) {
+      // ------------------------------------------------------------ loader
+      auto issue_rec = [&](long long i) {  // step s0+i into stage (g+i)%NS
+        const long long gi = g + i;
+        const int st = (int)(gi % NS);
+        if (gi >= NS) {
+          if (!mbar_wait(&empty[st], (unsigned)(((gi / NS) - 1) & 1), a.err)) abort = true;
+        }
+        if (lane == 0) {
+          const long long o0 = a.rec_off[s0 + i], o1 = a.rec_off[s0 + i + 1];
+          mbar_expect_tx(&rec_full[st], (unsigned)(o1 - o0));
+          tma_load_1d(rstage + (size_t)st * a.rec_stage, a.rec + o0, (unsigned)(o1 - o0), &rec_full[st]);
+        }
+      };
+      const int LA = NS > 3 ? NS / 2 : 1;  // record copies run LA steps ahead of the gathers
+      for (long long i = 0; i < LA && i < nsteps; ++i) issue_rec(i);
+      for (long long i = 0; i < nsteps; ++i) {
+        if (i + LA < nsteps) issue_rec(i + LA);
+        const long long gi = g + i;
+        const int st = (int)(gi % NS);
+        if (!mbar_wait(&rec_full[st], (unsigned)((gi / NS) & 1), a.err)) abort = true;
+        const unsigned char* rec = rstage + (size_t)st * a.rec_stage;
+        unsigned char* val = vstage + (size_t)st * a.val_stage;
+        const int nent = reinterpret_cast<const int*>(rec)[0];
+        const int row = reinterpret_cast<const int*>(rec + 16)[lane];
+        if (row >= 0 && !abort) {
+          T* rhs = reinterpret_cast<T*>(val) + lane * B;
 #pragma unroll
-        for (int d = 0; d < B; ++d) t[d] = reinterpret_cast<const T*>(val)[d * 32 + lane];
-        for (int e = 0; e < nent; ++e) {
-          const int c = src[e * 32 + lane];
-          if (c == INT_MIN) continue;
-          T v[B];
-          if (c >= 0) {
-            const int ss = c >> 5, ln = c & 31;
+          for (int d = 0; d < B; ++d) {
+            if constexpr (SZ == 8) cp_async8(rhs + d, &in[(size_t)row * B + d]);
+            else cp_async4(rhs + d, &in[(size_t)row * B + d]);
+          }
+          const int* code = reinterpret_cast<const int*>(rec + 144);
+          const int* grow = code + nent * 32;
+          for (int e = 0; e < nent; ++e) {
+            const int k = grow[e * 32 + lane];
+            if (k < 0) continue;
+            const unsigned c = (unsigned)code[e * 32 + lane] & 0x7fffffffu;
+            const uintptr_t addr = reinterpret_cast<uintptr_t>(&out[(size_t)k * B]);
+            const unsigned char* w = reinterpret_cast<const unsigned char*>(addr & ~(uintptr_t)15);
+            unsigned char* dst = val + (c & ~15u);
+            cp_async16(dst, w);
+            if ((addr & 15) + B * SZ > 16) cp_async16(dst + 16, w + 16);
+          }
+        }
+        cp_async_arrive_noinc(&full[st]);
+      }
+    } else {
+      // ----------------------------------------------------------- compute
+      for (long long i = 0; i < nsteps; ++i) {
+        const long long gi = g + i;
+        const int st = (int)(gi % NS);
+        const unsigned par = (unsigned)((gi / NS) & 1);
+        if (!mbar_wait(&rec_full[st], par, a.err)) abort = true;
+        if (!mbar_wait(&full[st], par, a.err)) abort = true;
+        const unsigned char* rec = rstage + (size_t)st * a.rec_stage;
+        const unsigned char* val = vstage + (size_t)st * a.val_stage;
+        const int nent = reinterpret_cast<const int*>(rec)[0];
+        const int row = reinterpret_cast<const int*>(rec + 16)[lane];
+        const int* code = reinterpret_cast<const int*>(rec + 144);
+        const int* grow = code + nent * 32;
+        const T* blk = reinterpret_cast<const T*>(rec + 144 + nent * 256);
+        if (row >= 0 && !abort) {
+          T t[B];
 #pragma unroll
-            for (int d = 0; d < B; ++d) v[d] = ring[(ss * B + d) * 32 + ln];
-          } else {
-            const size_t k = (size_t)(-c - 1);
-            const uintptr_t addr = reinterpret_cast<uintptr_t>(&out[k * B]);
-            const unsigned char* w = val + RHS_BYTES + (size_t)(e * 32 + lane) * 32 + (addr & 15);
+          for (int d = 0; d < B; ++d) t[d] = reinterpret_cast<const T*>(val)[lane * B + d];
+          for (int e = 0; e < nent; ++e) {
+            const int c = code[e * 32 + lane];
+            const unsigned char* base = (c < 0) ? val : ringreg;
+            const T* vp = reinterpret_cast<const T*>(base + (c & 0x7fffffff));
+            T v[B];
 #pragma unroll
-            for (int d = 0; d < B; ++d) {
-              T x = *reinterpret_cast<const T*>(w + d * sizeof(T));
-              if (is_sentinel(x)) {
+            for (int d = 0; d < B; ++d) v[d] = vp[d];
+            bool stale = false;
+#pragma unroll
+            for (int d = 0; d < B; ++d) stale |= is_sentinel(v[d]);
+            if (stale) {  // produced after the window was copied: poll the value itself
+              const size_t k = (size_t)grow[e * 32 + lane];
+              for (int d = 0; d < B; ++d) {
                 long long spins = 0;
-                for (;;) {
-                  x = ld_relaxed(&out[k * B + d]);
-                  if (!is_sentinel(x)) break;
+                while (is_sentinel(v[d])) {
+                  v[d] = ld_relaxed(&out[k * B + d]);
                   if ((++spins & 1023) == 0) {
-                    if (ld_relaxed_int(a.err) != 0) { abort = true; break; }
-                    if (spins > kSpinLimit) { atomicExch(a.err, kErrTimeout); abort = true; break; }
+                    if (ld_relaxed_int(a.err) != 0 || spins > kSpinLimit) {
+                      if (spins > kSpinLimit) atomicExch(a.err, kErrTimeout);
+                      abort = true;
+                      break;
+                    }
                   }
                 }
               }
-              v[d] = x;
+            }
+#pragma unroll
+            for (int p = 0; p < B; ++p) {
+              T acc = t[p];
+#pragma unroll
+              for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[q];
+              t[p] = acc;
             }
           }
+          T y[B];
+          if constexpr (FWD) {
+            const T* dinv = blk + nent * BS * 32;
 #pragma unroll
-          for (int p = 0; p < B; ++p) {
-            T acc = t[p];
+            for (int p = 0; p < B; ++p) {
+              T acc = dinv[(p * B) * 32 + lane] * t[0];
 #pragma unroll
-            for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[q];
-            t[p] = acc;
+              for (int q = 1; q < B; ++q) acc += dinv[(p * B + q) * 32 + lane] * t[q];
+              y[p] = acc;
+            }
+          } else {
+#pragma unroll
+            for (int p = 0; p < B; ++p) y[p] = t[p];
+          }
+          T* rg = reinterpret_cast<T*>(ringreg + 32) + ((size_t)((i % a.R) * 32 + lane)) * B;
+#pragma unroll
+          for (int d = 0; d < B; ++d) {
+            rg[d] = y[d];
+            st_relaxed(&out[(size_t)row * B + d], y[d]);
           }
         }
-        T y[B];
-        if constexpr (FWD) {
-          const T* dinv = blk + nent * BS * 32;
-#pragma unroll
-          for (int p = 0; p < B; ++p) {
-            T acc = dinv[(p * B) * 32 + lane] * t[0];
-#pragma unroll
-            for (int q = 1; q < B; ++q) acc += dinv[(p * B + q) * 32 + lane] * t[q];
-            y[p] = acc;
-          }
-        } else {
-#pragma unroll
-          for (int p = 0; p < B; ++p) y[p] = t[p];
-        }
-        const int rs = loc % a.R;
-#pragma unroll
-        for (int d = 0; d < B; ++d) {
-          ring[(rs * B + d) * 32 + lane] = y[d];
-          st_relaxed(&out[(size_t)row * B + d], y[d]);
-        }
+        abort = __any_sync(0xffffffffu, abort);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[st]);
       }
-      abort = __any_sync(0xffffffffu, abort);
-      __syncwarp();
-      if (s + 2 * K < s1) issue_record(s + 2 * K, loc % NREC);
-      cp_async_commit();
     }
-    cp_async_wait_all();
-    __syncwarp();
-    if (abort) break;
+    g += nsteps;
+    if (__any_sync(0xffffffffu, abort)) {
+      if (lane == 0) atomicExch(a.err, a.err[0] ? a.err[0] : kErrTimeout);
+    }
+    named_sync(1, 64);
+    if (ld_relaxed_int(a.err) != 0) break;
   }
   cp_async_wait_all();
 }
@@ -198,7 +273,7 @@ __global__ void k_pack(PackArgs a) {
   if (s >= a.nsteps) return;
   unsigned char* rec = a.rec + a.rec_off[s];
   const int nent = (int)(a.ent_off[s + 1] - a.ent_off[s]);
-  T* blk = reinterpret_cast<T*>(rec + 144 + nent * 128);
+  T* blk = reinterpret_cast<T*>(rec + 144 + nent * 256);
   const int* slots = a.ent_slot + a.ent_off[s] * 32;
   for (int idx = threadIdx.x; idx < nent * BS * 32; idx += blockDim.x) {
     const int lane = idx & 31, m = (idx >> 5) % BS, e = (idx >> 5) / BS;
@@ -217,44 +292,33 @@ __global__ void k_pack(PackArgs a) {
 
 // ------------------------------------------------------------------ launchers
 
-template <typename T, int B, bool FWD>
-static cudaError_t launch_k(int K, const SweepArgs& a, int grid, size_t smem, cudaStream_t st) {
-  switch (K) {
-    case 2: k_sweep<T, B, FWD, 2><<<grid, 32, smem, st>>>(a); break;
-    case 4: k_sweep<T, B, FWD, 4><<<grid, 32, smem, st>>>(a); break;
+template <typename T, bool FWD>
+static cudaError_t launch_b(int B, const SweepArgs& a, int grid, size_t smem, cudaStream_t st) {
+  switch (B) {
+    case 1: k_sweep<T, 1, FWD><<<grid, 64, smem, st>>>(a); break;
+    case 2: k_sweep<T, 2, FWD><<<grid, 64, smem, st>>>(a); break;
+    case 3: k_sweep<T, 3, FWD><<<grid, 64, smem, st>>>(a); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
 
-template <typename T, bool FWD>
-static cudaError_t launch_b(int B, int K, const SweepArgs& a, int grid, size_t smem, cudaStream_t st) {
-  switch (B) {
-    case 1: return launch_k<T, 1, FWD>(K, a, grid, smem, st);
-    case 2: return launch_k<T, 2, FWD>(K, a, grid, smem, st);
-    case 3: return launch_k<T, 3, FWD>(K, a, grid, smem, st);
-    default: return cudaErrorInvalidValue;
-  }
+cudaError_t launch_sweep(bool forward, bool fp32, int B, const SweepArgs& a, int grid, size_t smem,
+                         cudaStream_t st) {
+  if (fp32) return forward ? launch_b<float, true>(B, a, grid, smem, st) : launch_b<float, false>(B, a, grid, smem, st);
+  return forward ? launch_b<double, true>(B, a, grid, smem, st) : launch_b<double, false>(B, a, grid, smem, st);
 }
 
-cudaError_t launch_sweep(bool forward, bool fp32, int B, int K, const SweepArgs& a, int grid,
-                         size_t smem, cudaStream_t st) {
-  if (fp32) return forward ? launch_b<float, true>(B, K, a, grid, smem, st) : launch_b<float, false>(B, K, a, grid, smem, st);
-  return forward ? launch_b<double, true>(B, K, a, grid, smem, st) : launch_b<double, false>(B, K, a, grid, smem, st);
-}
-
-template <typename T, int B, bool FWD, int K>
+template <typename T, int B, bool FWD>
 static cudaError_t set_attr(size_t max_smem) {
-  return cudaFuncSetAttribute(k_sweep<T, B, FWD, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+  return cudaFuncSetAttribute(k_sweep<T, B, FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
 }
 
 cudaError_t sweep_set_smem_limits(size_t max_smem) {
   cudaError_t e = cudaSuccess;
-#define DFG_ATTR(T, B)                                                                  \
-  if (e == cudaSuccess) e = set_attr<T, B, true, 2>(max_smem);                          \
-  if (e == cudaSuccess) e = set_attr<T, B, true, 4>(max_smem);                          \
-  if (e == cudaSuccess) e = set_attr<T, B, false, 2>(max_smem);                         \
-  if (e == cudaSuccess) e = set_attr<T, B, false, 4>(max_smem);
+#define DFG_ATTR(T, B)                                        \
+  if (e == cudaSuccess) e = set_attr<T, B, true>(max_smem);   \
+  if (e == cudaSuccess) e = set_attr<T, B, false>(max_smem);
   DFG_ATTR(double, 1) DFG_ATTR(double, 2) DFG_ATTR(double, 3)
   DFG_ATTR(float, 1) DFG_ATTR(float, 2) DFG_ATTR(float, 3)
 #undef DFG_ATTR

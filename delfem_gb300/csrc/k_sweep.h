@@ -17,22 +17,23 @@ struct SweepArgs {
   int rec_stage;              // bytes per record slot (>= the largest record)
   int val_stage;              // bytes per value slot
   int R;                      // ring depth in steps
+  int NS;                     // pipeline stages
 };
 
-// smem bytes a launch needs
-inline size_t sweep_smem_bytes(int K, int rec_stage, int val_stage, int R, int B, int elem) {
-  return (size_t)2 * K * rec_stage + (size_t)(K + 1) * val_stage + (size_t)R * B * 32 * elem;
+// smem bytes a launch needs: mbarriers, NS record slots, NS value slots,
+// a 32-byte zero pad and the ring
+inline size_t sweep_smem_bytes(int NS, int rec_stage, int val_stage, int R, int B, int elem) {
+  return ((size_t)3 * NS * 8 + 127) / 128 * 128 + (size_t)NS * rec_stage + (size_t)NS * val_stage + 32 +
+         (size_t)R * B * 32 * elem;
 }
-// bytes of one value slot: right-hand sides + raw 32-byte windows per global dependency
-inline int sweep_val_stage(int max_nent, int B, int elem) {
-  int v = B * 32 * elem;
-  v = (v + 15) / 16 * 16;
-  return v + max_nent * 32 * 32;
-}
+// bytes of the right-hand-side part of a value slot
+inline int sweep_rhs_bytes(int B, int elem) { return (B * 32 * elem + 15) / 16 * 16; }
+// bytes of one value slot: right-hand sides + 32-byte windows per dependency entry
+inline int sweep_val_stage(int max_nent, int B, int elem) { return sweep_rhs_bytes(B, elem) + max_nent * 32 * 32; }
 
 // launchers (k_sweep.cu)
-cudaError_t launch_sweep(bool forward, bool fp32, int B, int K, const SweepArgs& a, int grid,
-                         size_t smem, cudaStream_t st);
+cudaError_t launch_sweep(bool forward, bool fp32, int B, const SweepArgs& a, int grid, size_t smem,
+                         cudaStream_t st);
 cudaError_t sweep_set_smem_limits(size_t max_smem);
 
 // packing the factor into step records (k_sweep.cu)

@@ -6,6 +6,7 @@
 #include <numeric>
 
 #include "dfg_internal.h"
+#include "k_sweep.h"
 
 namespace dfg {
 
@@ -74,6 +75,46 @@ Levels build_levels(int n, const int* rowptr, const int* colind, const int* diai
   return L;
 }
 
+// Range boundaries.  A cut right after a row that the next rows depend on
+// makes the next range wait for the end of this one, so cuts go only where
+// the row at the cut does not depend on the g rows just before it (line or
+// plane starts in the natural order of a structured mesh); among those, the
+// one closest above the target size wins.
+static std::vector<int> range_cuts(int n, const int* rowptr, const int* colind, const int* diaind, bool forward,
+                                   int target) {
+  std::vector<char> cand(n + 1, 0);
+  const int g = 2;
+  for (int p = 0; p < n; ++p) {
+    const int row = forward ? p : n - 1 - p;
+    int c0, c1;
+    deps_of(row, forward, rowptr, diaind, c0, c1);
+    int nearest = -1;  // largest dependency position
+    for (int c = c0; c < c1; ++c) {
+      const int k = colind[c];
+      nearest = std::max(nearest, forward ? k : n - 1 - k);
+    }
+    cand[p] = (nearest < 0 || p - nearest > g) ? 1 : 0;
+  }
+  std::vector<int> cuts{0};
+  int a = 0;
+  while (a < n) {
+    const int want = a + target;
+    if (want >= n) break;
+    int pick = -1;
+    const int hi = std::min(n - 1, a + 2 * target);
+    for (int p = want; p <= hi; ++p)
+      if (cand[p]) { pick = p; break; }
+    if (pick < 0)
+      for (int p = want - 1; p > a + target / 2; --p)
+        if (cand[p]) { pick = p; break; }
+    if (pick < 0) pick = want;
+    cuts.push_back(pick);
+    a = pick;
+  }
+  cuts.push_back(n);
+  return cuts;
+}
+
 SweepPlan build_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind,
                            bool forward, int range_rows, int R) {
   SweepPlan P;
@@ -82,14 +123,15 @@ SweepPlan build_sweep_plan(int n, int b, const int* rowptr, const int* colind, c
   P.b = b;
   P.R = R;
   range_rows = std::max(1, range_rows);
-  P.nranges = (n + range_rows - 1) / range_rows;
+  const std::vector<int> cuts = range_cuts(n, rowptr, colind, diaind, forward, range_rows);
+  P.nranges = (int)cuts.size() - 1;
   P.range_steps.assign(P.nranges + 1, 0);
   std::vector<int> llev(n, 0);          // local level per row
   std::vector<int> row_step(n, 0), row_lane(n, 0), row_range(n, 0);
   std::vector<int> cnt;
   // pass 1: steps per range
   for (int r = 0; r < P.nranges; ++r) {
-    const int p0 = r * range_rows, p1 = std::min(n, p0 + range_rows);
+    const int p0 = cuts[r], p1 = cuts[r + 1];
     int maxl = 0;
     for (int p = p0; p < p1; ++p) {
       const int row = forward ? p : n - 1 - p;
@@ -202,6 +244,46 @@ SweepPlan choose_sweep_plan(int n, int b, const int* rowptr, const int* colind, 
     if (range_rows >= n) break;
   }
   return best;
+}
+
+std::vector<unsigned char> pack_record_headers(const SweepPlan& P, int elem, std::vector<long long>& off,
+                                               long long& max_rec) {
+  const int b = P.b, bs = b * b;
+  const int rhs_bytes = sweep_rhs_bytes(b, elem);
+  off.assign(P.nsteps + 1, 0);
+  max_rec = 0;
+  for (int s = 0; s < P.nsteps; ++s) {
+    const long long rb = rec_bytes(P.step_nent[s], bs, elem, P.forward);
+    off[s + 1] = off[s] + rb;
+    max_rec = std::max(max_rec, rb);
+  }
+  std::vector<unsigned char> h((size_t)off[P.nsteps], 0);
+  for (int s = 0; s < P.nsteps; ++s) {
+    unsigned char* r = h.data() + off[s];
+    const int nent = P.step_nent[s];
+    std::memcpy(r, &nent, 4);
+    std::memcpy(r + 16, &P.step_rows[(size_t)s * 32], 128);
+    int* code = reinterpret_cast<int*>(r + 144);
+    int* grow = code + nent * 32;
+    for (int e = 0; e < nent; ++e)
+      for (int lane = 0; lane < 32; ++lane) {
+        const int src = P.ent_src[(size_t)(P.ent_off[s] + e) * 32 + lane];
+        int c = 0, gr = -1;
+        if (src == SweepPlan::kSrcPad) {
+          c = 0;
+        } else if (src >= 0) {
+          const int ss = src >> 5, ln = src & 31;
+          c = 32 + (ss * 32 + ln) * b * elem;
+        } else {
+          const long long k = -(long long)src - 1;
+          gr = (int)k;
+          c = (int)(0x80000000u | (unsigned)(rhs_bytes + (e * 32 + lane) * 32 + (int)((k * b * elem) & 15)));
+        }
+        code[e * 32 + lane] = c;
+        grow[e * 32 + lane] = gr;
+      }
+  }
+  return h;
 }
 
 bool build_gather_map(int n, const int* rowptr, const int* colind, int nelem, int nnoel,

@@ -50,6 +50,12 @@ class Context:
         check(self.h, lib().dfg_ctx_synchronize(self.h), "dfg_ctx_synchronize")
 
     @property
+    def stream(self) -> int:
+        h = ctypes.c_void_p()
+        check(self.h, lib().dfg_ctx_get_stream(self.h, ctypes.byref(h)), "dfg_ctx_get_stream")
+        return int(h.value or 0)
+
+    @property
     def kernel_launches(self) -> int:
         return int(lib().dfg_ctx_kernel_launches(self.h))
 
@@ -109,6 +115,11 @@ class LinearSystemField:
         u = None if u is None else _f64(u)
         v = None if v is None else _f64(v)
         check(self.ctx.h, lib().dfg_system_set_field(self.h, _p(u), _p(v)), "dfg_system_set_field")
+
+    def SetLoad(self, f):
+        """Resident nodal load added at every FinalizeMarge (None clears it)."""
+        ff = None if f is None else _f64(f)
+        check(self.ctx.h, lib().dfg_system_set_load(self.h, _p(ff)), "dfg_system_set_load")
 
     def SetFixedBoundaryCondition(self, flags):
         f = _i32(flags)
@@ -361,3 +372,14 @@ def Solve_PCG_reference_loop(conv_ratio: float, iteration: int, lsp: LinearSyste
         lsp.AXPY(1.0, iz, ip)
     sq = lsp.DOT(ir, ir)
     return False, float(np.sqrt(sq * inv0)), mx
+
+
+def profile_kernels(ls: LinearSystemField, prec: PreconditionerILU, mode: str = "fp64", reps: int = 20):
+    """Per-launch device time (ms) of the kernels of one PCG iteration and the
+    algorithmic bytes of the SpMV and the two sweeps."""
+    ms = np.zeros(6)
+    by = np.zeros(3)
+    m = 1 if mode == "mixed" else 0
+    check(ls.ctx.h, lib().dfg_profile_kernels(ls.h, prec.h, m, reps, _p(ms), _p(by)), "dfg_profile_kernels")
+    names = ["spmv", "sweep_fwd", "sweep_bwd", "update_rx", "rz_beta", "update_p"]
+    return dict(zip(names, ms.tolist())), dict(zip(names[:3], by.tolist()))

@@ -26,6 +26,8 @@ class FESolve:
         if p.u is not None or p.v is not None:
             self.ls.set_field(p.u, p.v)
         self.ls.SetFixedBoundaryCondition(p.bcflag)
+        if p.load is not None:
+            self.ls.SetLoad(p.load)
         self.prec = L.PreconditionerILU(ctx)
         self.prec.SetFillInLevel(0)
         self.prec.SetLinearSystem(self.ls)
@@ -42,9 +44,7 @@ class FESolve:
             L.AddLinSys_LinearSolid2D_Static(ls, P[0], P[1], P[2], P[3], P[4])
         elif p.kind == mg.SOLID3D:
             L.AddLinSys_LinearSolid3D_Static(ls, P[0], P[1], P[2], P[3], P[4], P[5])
-        if p.load is not None:
-            ls.AddResidual(p.load)
-        return ls.FinalizeMarge()
+        return ls.FinalizeMarge()  # adds the resident load, then the Dirichlet rows
 
     def factor(self) -> bool:
         return self.prec.SetValue(self.ls)

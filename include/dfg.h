@@ -129,6 +129,13 @@ int dfg_assemble_solid3d(dfg_system sys, double lambda, double myu,
  * CEqnSystem_Solid2D::SetLoad stores (src/femeqn/eqnsys_solid.cpp:894-907);
  * equivalent to CVector_Blk::AddValue on every DOF. */
 int dfg_add_residual(dfg_system sys, const double* f);
+/* Stores a nodal load (nblk*blklen doubles, NULL clears it) on the device;
+ * every later dfg_finalize_marge adds it to the residual before the
+ * Dirichlet rows are applied, so a fixed load stays resident across solves.
+ * Counterpart of CEqnSystem_Solid2D::SetLoad (src/femeqn/eqnsys_solid.cpp:894-907),
+ * which keeps the load with the equation system; the addition is the
+ * element-wise one of dfg_add_residual. */
+int dfg_system_set_load(dfg_system sys, const double* f);
 /* Dirichlet rows/columns, residual zeroed on fixed DOFs; *norm_res = ||r||_2
  * (CLinearSystem::FinalizeMarge, src/ls/linearsystem.cpp:92-128). */
 int dfg_finalize_marge(dfg_system sys, double* norm_res);

@@ -1,0 +1,182 @@
+// dfg_delfem.hpp -- C++ adapter for DelFEM code that drives libdfg.
+//
+// Header-only; include it in a DelFEM build (it needs DelFEM's headers on the
+// include path) and link libdfg.so.  It is the reference-side binding of the
+// C ABI in dfg.h:
+//
+//  * CLinearSystem_FieldGPU mirrors Fem::Ls::CLinearSystem_Field
+//    (include/delfem/femls/linearsystem_field.h:67-172) for one field: the
+//    pattern and the mesh come from the same CFieldWorld segments the
+//    reference's AddPattern_Field and AddLinSys_* read, and it implements
+//    LsSol::ILinearSystemPreconditioner_Sol
+//    (include/delfem/ls/linearsystem_interface_solver.h:61-82), so the
+//    reference's own LsSol::Solve_PCG can drive it unchanged (strict drop-in);
+//  * the AddLinSys_* overloads take the GPU system with the reference's
+//    parameter lists (eqn_poisson.h:71-76, eqn_diffusion.h:68-73,
+//    eqn_linear_solid2d.h:68-72, eqn_linear_solid3d.h:59-64);
+//  * DfgDelFEM::Solve_PCG is the device-resident fast path with the
+//    in/out semantics of LsSol::Solve_PCG (solver_ls_iter.h:38-39).
+#ifndef DFG_DELFEM_HPP
+#define DFG_DELFEM_HPP
+
+#include <cassert>
+#include <string>
+#include <vector>
+
+#include "dfg.h"
+#include "delfem/elem_ary.h"
+#include "delfem/field.h"
+#include "delfem/field_world.h"
+#include "delfem/ls/linearsystem_interface_solver.h"
+#include "delfem/node_ary.h"
+
+namespace DfgDelFEM {
+
+class CLinearSystem_FieldGPU : public LsSol::ILinearSystemPreconditioner_Sol {
+ public:
+  explicit CLinearSystem_FieldGPU(dfg_ctx ctx) : ctx_(ctx) {}
+  virtual ~CLinearSystem_FieldGPU() {
+    if (prec_) dfg_precond_destroy(prec_);
+    if (sys_) dfg_system_destroy(sys_);
+  }
+
+  // CLinearSystem_Field::AddPattern_Field (linearsystem_field.cpp:196-280):
+  // node-to-node pattern of the field's corner segments, plus the mesh the
+  // element routines read (CElemSeg::GetNodes / CNodeSeg::GetValue).
+  bool AddPattern_Field(unsigned int id_field, const Fem::Field::CFieldWorld& world) {
+    using namespace Fem::Field;
+    if (!world.IsIdField(id_field)) return false;
+    const CField& f = world.GetField(id_field);
+    const CNodeAry::CNodeSeg& ns_co = f.GetNodeSeg(CORNER, false, world);
+    const CNodeAry::CNodeSeg& ns_va = f.GetNodeSeg(CORNER, true, world);
+    const unsigned int nnode = ns_co.Size(), ndim = ns_co.Length();
+    blklen_ = (int)ns_va.Length();
+    nnode_ = (int)nnode;
+    std::vector<double> coords((size_t)nnode * ndim);
+    for (unsigned int i = 0; i < nnode; ++i) ns_co.GetValue(i, &coords[(size_t)i * ndim]);
+    std::vector<int> conn;
+    int nnoel = 0;
+    const std::vector<unsigned int> aIdEA = f.GetAryIdEA();
+    for (unsigned int k = 0; k < aIdEA.size(); ++k) {
+      const CElemAry::CElemSeg& es = f.GetElemSeg(aIdEA[k], CORNER, true, world);
+      nnoel = (int)es.Length();
+      std::vector<unsigned int> no(nnoel);
+      for (unsigned int e = 0; e < es.Size(); ++e) {
+        es.GetNodes(e, no.data());
+        for (int q = 0; q < nnoel; ++q) conn.push_back((int)no[q]);
+      }
+    }
+    nelem_ = nnoel ? (int)(conn.size() / nnoel) : 0;
+    if (dfg_system_create_from_elements(ctx_, nnode_, blklen_, nelem_, nnoel, conn.data(), &sys_) != DFG_OK) return false;
+    return dfg_system_set_mesh(sys_, (int)ndim, coords.data(), nelem_, nnoel, conn.data()) == DFG_OK;
+  }
+
+  // SetFixedBoundaryCondition_Field (linearsystem_field.cpp:618-710): every
+  // DOF of every node of the partial field's element segments is fixed.
+  bool SetFixedBoundaryCondition_Field(unsigned int id_field_fix, const Fem::Field::CFieldWorld& world) {
+    using namespace Fem::Field;
+    if (!sys_ || !world.IsIdField(id_field_fix)) return false;
+    if (flags_.empty()) flags_.assign((size_t)nnode_ * blklen_, 0);
+    const CField& f = world.GetField(id_field_fix);
+    const std::vector<unsigned int> aIdEA = f.GetAryIdEA();
+    for (unsigned int k = 0; k < aIdEA.size(); ++k) {
+      const CElemAry::CElemSeg& es = f.GetElemSeg(aIdEA[k], CORNER, true, world);
+      std::vector<unsigned int> no(es.Length());
+      for (unsigned int e = 0; e < es.Size(); ++e) {
+        es.GetNodes(e, no.data());
+        for (unsigned int q = 0; q < no.size(); ++q)
+          for (int d = 0; d < blklen_; ++d) flags_[(size_t)no[q] * blklen_ + d] = 1;
+      }
+    }
+    return dfg_set_bcflags(sys_, flags_.data()) == DFG_OK;
+  }
+
+  void InitializeMarge() { dfg_initialize_marge(sys_); }
+  double FinalizeMarge() {
+    double r = 0.0;
+    dfg_finalize_marge(sys_, &r);
+    return r;
+  }
+
+  // UpdateValueOfField (linearsystem_field.cpp:716-794): field += update
+  bool UpdateValueOfField(unsigned int id_field, Fem::Field::CFieldWorld& world,
+                          Fem::Field::FIELD_DERIVATION_TYPE fdt = Fem::Field::VALUE) {
+    using namespace Fem::Field;
+    std::vector<double> x((size_t)nnode_ * blklen_);
+    if (dfg_get_vector(sys_, -2, x.data()) != DFG_OK) return false;
+    CNodeAry::CNodeSeg& ns = world.GetField(id_field).GetNodeSeg(CORNER, true, world, fdt);
+    for (int i = 0; i < nnode_; ++i)
+      for (int d = 0; d < blklen_; ++d) ns.AddValue(i, d, x[(size_t)i * blklen_ + d]);
+    return true;
+  }
+
+  // ---- CPreconditioner_ILU (preconditioner.h:59-108), owned by the system
+  bool SetFillInLevel(int lev) {
+    if (!prec_ && dfg_precond_create(ctx_, &prec_) != DFG_OK) return false;
+    return dfg_precond_set_fill_level(prec_, lev) == DFG_OK;
+  }
+  bool SetPreconditionerLinearSystem() {
+    if (!prec_ && dfg_precond_create(ctx_, &prec_) != DFG_OK) return false;
+    return dfg_precond_set_linear_system(prec_, sys_) == DFG_OK;
+  }
+  bool SetPreconditionerValue() { return dfg_precond_set_value(prec_, sys_) == DFG_OK; }
+
+  // ---- LsSol::ILinearSystemPreconditioner_Sol
+  unsigned int GetTmpVectorArySize() const {
+    unsigned int n = 0;
+    dfg_get_tmp_vector_size(sys_, &n);
+    return n;
+  }
+  bool ReSizeTmpVecSolver(unsigned int size_new) { return dfg_resize_tmp_vec(sys_, size_new) == DFG_OK; }
+  double DOT(int iv1, int iv2) {
+    double r = 0.0;
+    dfg_dot(sys_, iv1, iv2, &r);
+    return r;
+  }
+  bool COPY(int iv1, int iv2) { return dfg_copy(sys_, iv1, iv2) == DFG_OK; }
+  bool SCAL(double alpha, int iv1) { return dfg_scal(sys_, alpha, iv1) == DFG_OK; }
+  bool AXPY(double alpha, int iv1, int iv2) { return dfg_axpy(sys_, alpha, iv1, iv2) == DFG_OK; }
+  bool MATVEC(double alpha, int iv1, double beta, int iv2) { return dfg_matvec(sys_, alpha, iv1, beta, iv2) == DFG_OK; }
+  bool SolvePrecond(int iv) { return dfg_precond_solve(prec_, sys_, iv) == DFG_OK; }
+
+  dfg_system system() const { return sys_; }
+  dfg_precond preconditioner() const { return prec_; }
+  int BlockLength() const { return blklen_; }
+
+ private:
+  dfg_ctx ctx_ = nullptr;
+  dfg_system sys_ = nullptr;
+  dfg_precond prec_ = nullptr;
+  int nnode_ = 0, blklen_ = 0, nelem_ = 0;
+  std::vector<int> flags_;
+};
+
+// ---- Fem::Eqn element routines with the reference's parameter lists
+inline bool AddLinSys_Poisson(CLinearSystem_FieldGPU& ls, double alpha, double source) {
+  return dfg_assemble_poisson(ls.system(), alpha, source) == DFG_OK;
+}
+inline bool AddLinSys_Diffusion(double dt, double gamma, CLinearSystem_FieldGPU& ls, double rho, double alpha,
+                                double source) {
+  return dfg_assemble_diffusion(ls.system(), dt, gamma, rho, alpha, source) == DFG_OK;
+}
+inline bool AddLinSys_LinearSolid2D_Static(CLinearSystem_FieldGPU& ls, double lambda, double myu, double rho,
+                                           double g_x, double g_y) {
+  return dfg_assemble_solid2d(ls.system(), lambda, myu, rho, g_x, g_y) == DFG_OK;
+}
+inline bool AddLinSys_LinearSolid3D_Static(CLinearSystem_FieldGPU& ls, double lambda, double myu, double rho,
+                                           double g_x, double g_y, double g_z) {
+  return dfg_assemble_solid3d(ls.system(), lambda, myu, rho, g_x, g_y, g_z) == DFG_OK;
+}
+
+// ---- device-resident LsSol::Solve_PCG
+inline bool Solve_PCG(double& conv_ratio, unsigned int& iteration, CLinearSystem_FieldGPU& ls) {
+  return dfg_solve_pcg(ls.system(), ls.preconditioner(), &conv_ratio, &iteration) == DFG_OK;
+}
+inline bool Solve_PCG_Mixed(double& conv_ratio, unsigned int& iteration, CLinearSystem_FieldGPU& ls) {
+  unsigned int outer = 0;
+  return dfg_solve_pcg_mixed(ls.system(), ls.preconditioner(), &conv_ratio, &iteration, &outer) == DFG_OK;
+}
+
+}  // namespace DfgDelFEM
+
+#endif  // DFG_DELFEM_HPP

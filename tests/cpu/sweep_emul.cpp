@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../delfem_gb300/csrc/dfg_internal.h"
+#include "../../delfem_gb300/csrc/k_sweep.h"
 
 using namespace dfg;
 
@@ -111,5 +112,44 @@ extern "C" int emul_sweep(int n, int b, const int* rowptr, const int* colind, in
     }
   }
   info[4] = (long long)P.est_cost;
+  // decode the packed record headers the GPU kernel reads, for both element
+  // sizes, and check every code against the plan
+  for (int elem = 4; elem <= 8; elem += 4) {
+    std::vector<long long> off;
+    long long max_rec = 0;
+    const std::vector<unsigned char> h = pack_record_headers(P, elem, off, max_rec);
+    const int rhs_bytes = sweep_rhs_bytes(b, elem);
+    const int val_stage = sweep_val_stage(P.max_nent, b, elem);
+    for (int r = 0; r < P.nranges; ++r)
+      for (int s = P.range_steps[r]; s < P.range_steps[r + 1]; ++s) {
+        const unsigned char* rec = h.data() + off[s];
+        const int nent = *reinterpret_cast<const int*>(rec);
+        if (nent != P.step_nent[s] || off[s + 1] - off[s] > max_rec || (off[s + 1] - off[s]) % 16) { info[3] = 20; return 20; }
+        const int* rows = reinterpret_cast<const int*>(rec + 16);
+        const int* code = reinterpret_cast<const int*>(rec + 144);
+        const int* grow = code + nent * 32;
+        const int loc = s - P.range_steps[r];
+        for (int l = 0; l < 32; ++l) {
+          if (rows[l] != P.step_rows[(size_t)s * 32 + l]) { info[3] = 21; return 21; }
+          for (int e = 0; e < nent; ++e) {
+            const int src = P.ent_src[(size_t)(P.ent_off[s] + e) * 32 + l];
+            const int c = code[e * 32 + l], g = grow[e * 32 + l];
+            if (src == SweepPlan::kSrcPad) {
+              if (c != 0 || g != -1) { info[3] = 22; return 22; }
+            } else if (src >= 0) {
+              const int off_ring = c - 32;
+              if (c < 32 || g != -1 || off_ring % (b * elem)) { info[3] = 23; return 23; }
+              const int slot = off_ring / (b * elem), ss = slot / 32, ln = slot % 32;
+              if (ss >= P.R || ss * 32 + ln != src || (loc - ss) % P.R < 0) { info[3] = 24; return 24; }
+            } else {
+              const unsigned o = (unsigned)c & 0x7fffffffu;
+              if (c >= 0 || g != -src - 1) { info[3] = 25; return 25; }
+              if ((int)(o & ~15u) != rhs_bytes + (e * 32 + l) * 32 || (int)(o & 15) != (int)(((long long)g * b * elem) & 15) ||
+                  (int)o + b * elem > val_stage) { info[3] = 26; return 26; }
+            }
+          }
+        }
+      }
+  }
   return 0;
 }

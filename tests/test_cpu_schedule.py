@@ -19,6 +19,7 @@ EMUL_SO = os.path.join(ROOT, "tests", "cpu", "_build", "libsweep_emul.so")
 def emul():
     os.makedirs(os.path.dirname(EMUL_SO), exist_ok=True)
     srcs = [os.path.join(ROOT, "tests", "cpu", "sweep_emul.cpp"), os.path.join(ROOT, "delfem_gb300", "csrc", "sched.cpp")]
+    # (sched.cpp includes the CUDA runtime header for cudaStream_t only; no CUDA code runs)
     inc = [d for d in ("/usr/local/cuda/include",) if os.path.isdir(d)]
     subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", *[f"-I{d}" for d in inc], "-o", EMUL_SO, *srcs],
                    check=True)
