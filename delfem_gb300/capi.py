@@ -23,6 +23,10 @@ DFG_TIMEOUT = 5
 DFG_INVALID_ARGUMENT = 6
 DFG_CUDA_ERROR = 7
 DFG_NOT_READY = 8
+DFG_PREC_FP64 = 0
+DFG_PREC_MIXED = 1
+DFG_PREC_FP32_FACTOR = 2
+MODES = {"fp64": DFG_PREC_FP64, "mixed": DFG_PREC_MIXED, "fp32f": DFG_PREC_FP32_FACTOR}
 STATUS_NAMES = {0: "OK", 1: "NOT_CONVERGED", 2: "SINGULAR_PIVOT", 3: "NAN_DETECTED", 4: "OOM_REJECTED",
                 5: "TIMEOUT", 6: "INVALID_ARGUMENT", 7: "CUDA_ERROR", 8: "NOT_READY"}
 
@@ -80,6 +84,7 @@ SIGNATURES = {
     "dfg_precond_get_factor": (_I, [_P, _P, _P]),
     "dfg_solve_pcg": (_I, [_P, _P, _PD, _PU]),
     "dfg_solve_pcg_mixed": (_I, [_P, _P, _PD, _PU, _PU]),
+    "dfg_solve_pcg_ex": (_I, [_P, _P, _I, _I, _PD, _PU, _PU]),
     "dfg_true_residual": (_I, [_P, _P, _PD]),
     "dfg_ctx_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
     "dfg_profile_kernels": (_I, [_P, _P, _I, _I, _P, _P]),

@@ -191,11 +191,17 @@ int read_err(dfg_ctx ctx_) {
 
 extern "C" const char* dfg_version(void) { return DFG_VERSION; }
 
+// error text of the last failed dfg_ctx_create (there is no context to hold it)
+static thread_local std::string g_create_error = "no error";
+
 extern "C" int dfg_ctx_create(int device, dfg_ctx* out) {
   if (!out) return DFG_INVALID_ARGUMENT;
   *out = nullptr;
   int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+  const cudaError_t ce = cudaGetDeviceCount(&ndev);
+  if (ce != cudaSuccess || device < 0 || device >= ndev) {
+    g_create_error = ce != cudaSuccess ? std::string("cudaGetDeviceCount: ") + cudaGetErrorString(ce)
+                                       : "device index out of range";
     cudaGetLastError();
     return DFG_CUDA_ERROR;
   }
@@ -208,7 +214,9 @@ extern "C" int dfg_ctx_create(int device, dfg_ctx* out) {
     CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device));
     int optin = 0;
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
-    c->smem_optin = (size_t)optin;
+    // dynamic shared memory a kernel may request: the opt-in limit less a
+    // margin for the kernels' own static shared memory
+    c->smem_optin = (size_t)optin - 1024;
     dalloc(c, c->err_word, 64);
     dalloc(c, c->scratch, kRedGrid * 8 + 16 * 4 + 16 * 8 + 16 * 4 + 256);
     CK(cudaMemsetAsync(c->err_word.p, 0, 64, c->stream));
@@ -218,6 +226,7 @@ extern "C" int dfg_ctx_create(int device, dfg_ctx* out) {
     return DFG_OK;
   });
   if (rc != DFG_OK) {
+    g_create_error = c->last_error;
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return rc;
@@ -237,7 +246,7 @@ extern "C" int dfg_ctx_destroy(dfg_ctx ctx) {
   return DFG_OK;
 }
 
-extern "C" const char* dfg_last_error(dfg_ctx ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+extern "C" const char* dfg_last_error(dfg_ctx ctx) { return ctx ? ctx->last_error.c_str() : g_create_error.c_str(); }
 
 extern "C" int dfg_ctx_synchronize(dfg_ctx ctx) {
   if (!ctx) return DFG_INVALID_ARGUMENT;
@@ -937,60 +946,108 @@ int timeout_status(dfg_ctx ctx_) {
 
 }  // namespace
 
-extern "C" int dfg_solve_pcg(dfg_system sys, dfg_precond prec, double* conv_ratio, unsigned* iteration) {
-  if (!sys || !prec || !conv_ratio || !iteration) return DFG_INVALID_ARGUMENT;
+// FP64-vector PCG with an FP64 or FP32 factor (dfg_solve_pcg / _ex).
+static int solve_pcg_f64vec(dfg_system sys, dfg_precond prec, bool fp32z, bool target_true, double* conv_ratio,
+                            unsigned* iteration, unsigned* refinements) {
   dfg_ctx ctx = sys->ctx;
   return guarded(ctx, [&]() -> int {
     dfg_ctx ctx_ = ctx;
     REQUIRE(prec->numeric && prec->sys == sys, DFG_NOT_READY, "preconditioner value not set for this system");
+    REQUIRE(!target_true || sys->rhs0_valid, DFG_NOT_READY, "dfg_finalize_marge must come before a true-residual solve");
     const long long m = (long long)sys->n * sys->b;
+    if (fp32z) ensure_numeric32(ctx, prec);
     dalloc(ctx, sys->w_p, vec_bytes(sys, 8));
     dalloc(ctx, sys->w_q, vec_bytes(sys, 8));
     dalloc(ctx, sys->w_z, vec_bytes(sys, 8));
+    dalloc(ctx, sys->w_rd, vec_bytes(sys, 8));
     dalloc(ctx, sys->w_state, sizeof(PcgState));
+    if (fp32z) {
+      dalloc(ctx, sys->w_r32, vec_bytes(sys, 4));
+      dalloc(ctx, sys->w_z32, vec_bytes(sys, 4));
+    }
     PcgState* st = sys->w_state.as<PcgState>();
     Scratch sc = scratch_of(ctx);
     Red red = red_of(ctx, 1);
-    PcgVecs v{sys->res.as<double>(), sys->upd.as<double>(), sys->w_p.as<double>(), sys->w_q.as<double>(),
-              prec->ybuf64.as<double>(), sys->w_z.as<double>(), m};
+    PcgVecs v{};
+    v.r = sys->res.as<double>();
+    v.x = sys->upd.as<double>();
+    v.p = sys->w_p.as<double>();
+    v.q = sys->w_q.as<double>();
+    v.y = fp32z ? prec->ybuf32.p : prec->ybuf64.p;
+    v.z = fp32z ? sys->w_z32.p : sys->w_z.p;
+    v.m = m;
+    v.r32 = fp32z ? sys->w_r32.as<float>() : nullptr;
+    v.rd = sys->w_rd.as<double>();
+    v.b = sys->rhs0_valid ? sys->rhs0.as<double>() : nullptr;
     const int* done = reinterpret_cast<const int*>(reinterpret_cast<const char*>(st) + offsetof(PcgState, done));
-    SweepLaunch F = sweep_launch(ctx, prec, prec->fwd, false, v.r, v.y, sc.tickets, done);
-    SweepLaunch B = sweep_launch(ctx, prec, prec->bwd, false, v.y, v.z, sc.tickets + 1, done);
+    const void* sweep_in = fp32z ? (const void*)v.r32 : (const void*)v.r;
+    SweepLaunch F = sweep_launch(ctx, prec, prec->fwd, fp32z, sweep_in, v.y, sc.tickets, done);
+    SweepLaunch B = sweep_launch(ctx, prec, prec->bwd, fp32z, v.y, v.z, sc.tickets + 1, done);
     const int maxit = (int)std::min<unsigned>(*iteration, 0x7fffffffu);
+    const double tol = *conv_ratio;
     // prologue (solver_ls_iter.cpp:106-128)
-    CK(pcg_init(v, st, red, *conv_ratio, maxit, sc.tickets, ctx->stream));
-    run_sweep(ctx, true, sys->b, false, F);
-    run_sweep(ctx, false, sys->b, false, B);
-    CK(pcg_after_precond0(v, st, red, ctx->stream));
+    CK(pcg_init(v, st, red, tol, maxit, sc.tickets, fp32z, ctx->stream));
+    run_sweep(ctx, true, sys->b, fp32z, F);
+    run_sweep(ctx, false, sys->b, fp32z, B);
+    CK(pcg_after_precond0(v, st, red, fp32z, ctx->stream));
     launched(ctx, 2);
     PcgState h{};
     read_state(ctx, st, h);
     // iterations: a graph of `chunk` iterations, replayed until done
     const int chunk = m < 200000 ? 8 : 32;
+    const MatView A = view64(sys);
     Chunk g;
-    if (!h.done) {
-      CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      const MatView A = view64(sys);
-      for (int c = 0; c < chunk; ++c) {
-        pcg_spmv_pap(A, v, st, red, ctx->stream);
-        pcg_update_rx(v, st, red, sc.tickets, ctx->stream);
-        launch_sweep(true, false, sys->b, F.args, F.grid, F.smem, ctx->stream);
-        launch_sweep(false, false, sys->b, B.args, B.grid, B.smem, ctx->stream);
-        pcg_rz_beta(v, st, red, ctx->stream);
-        pcg_update_p(v, st, ctx->stream);
-      }
-      CK(cudaStreamEndCapture(ctx->stream, &g.graph));
-      CK(cudaGraphInstantiate(&g.exec, g.graph, 0));
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    for (int c = 0; c < chunk; ++c) {
+      pcg_spmv_pap(A, v, st, red, ctx->stream);
+      pcg_update_rx(v, st, red, sc.tickets, fp32z, ctx->stream);
+      launch_sweep(true, fp32z, sys->b, F.args, F.grid, F.smem, ctx->stream);
+      launch_sweep(false, fp32z, sys->b, B.args, B.grid, B.smem, ctx->stream);
+      pcg_rz_beta(v, st, red, fp32z, ctx->stream);
+      pcg_update_p(v, st, fp32z, ctx->stream);
     }
+    CK(cudaStreamEndCapture(ctx->stream, &g.graph));
+    CK(cudaGraphInstantiate(&g.exec, g.graph, 0));
+    unsigned refin = 0;
     long long guard = 0;
-    while (!h.done) {
-      CK(cudaGraphLaunch(g.exec, ctx->stream));
-      launched(ctx, 6LL * chunk);
+    double bb = 0.0;
+    for (;;) {
+      while (!h.done) {
+        CK(cudaGraphLaunch(g.exec, ctx->stream));
+        launched(ctx, 6LL * chunk);
+        read_state(ctx, st, h);
+        if (read_err(ctx) != 0) return timeout_status(ctx);
+        if (++guard > (long long)maxit / chunk + 64) break;
+      }
+      if (h.done != 1 || !target_true) break;
+      // recursive residual converged: check the true one
+      if (bb == 0.0) {
+        CK(api_dot(m, v.b, v.b, red_of(ctx, 0), ctx->stream));
+        launched(ctx);
+        CK(cudaMemcpyAsync(&bb, red_of(ctx, 0).result, 8, cudaMemcpyDeviceToHost, ctx->stream));
+      }
+      CK(pcg_true_residual(A, v, st, red, ctx->stream));
+      launched(ctx);
+      ++refin;
+      PcgState t{};
+      read_state(ctx, st, t);
+      const double rel = bb > 0 ? std::sqrt(t.rr / bb) : 0.0;
+      h.conv = rel;
+      if (rel <= tol || h.it + 1 >= maxit) {
+        if (rel > tol) h.done = 2;
+        break;
+      }
+      // continue from the true residual: finish this iteration and resume
+      CK(pcg_replace(v, st, sc.tickets, fp32z, ctx->stream));
+      run_sweep(ctx, true, sys->b, fp32z, F);
+      run_sweep(ctx, false, sys->b, fp32z, B);
+      CK(pcg_rz_beta(v, st, red, fp32z, ctx->stream));
+      CK(pcg_update_p(v, st, fp32z, ctx->stream));
+      launched(ctx, 3);
       read_state(ctx, st, h);
-      if (read_err(ctx) != 0) return timeout_status(ctx);
-      if (++guard > (long long)maxit / chunk + 4) break;
     }
     *conv_ratio = h.conv;
+    if (refinements) *refinements = refin;
     if (h.done == 1) {
       *iteration = (unsigned)h.iter_out;
       return DFG_OK;
@@ -1002,6 +1059,11 @@ extern "C" int dfg_solve_pcg(dfg_system sys, dfg_precond prec, double* conv_rati
     set_err(ctx, "PCG did not converge within the iteration limit");
     return DFG_NOT_CONVERGED;
   });
+}
+
+extern "C" int dfg_solve_pcg(dfg_system sys, dfg_precond prec, double* conv_ratio, unsigned* iteration) {
+  if (!sys || !prec || !conv_ratio || !iteration) return DFG_INVALID_ARGUMENT;
+  return solve_pcg_f64vec(sys, prec, false, false, conv_ratio, iteration, nullptr);
 }
 
 // Mixed precision: PCG whose SpMV, factor, sweeps and vectors are FP32, with
@@ -1126,6 +1188,19 @@ extern "C" int dfg_solve_pcg_mixed(dfg_system sys, dfg_precond prec, double* con
   });
 }
 
+extern "C" int dfg_solve_pcg_ex(dfg_system sys, dfg_precond prec, int mode, int target_true, double* conv_ratio,
+                                unsigned* iteration, unsigned* refinements) {
+  if (!sys || !prec || !conv_ratio || !iteration) return DFG_INVALID_ARGUMENT;
+  switch (mode) {
+    case DFG_PREC_FP64: return solve_pcg_f64vec(sys, prec, false, target_true != 0, conv_ratio, iteration, refinements);
+    case DFG_PREC_FP32_FACTOR: return solve_pcg_f64vec(sys, prec, true, target_true != 0, conv_ratio, iteration, refinements);
+    case DFG_PREC_MIXED: return dfg_solve_pcg_mixed(sys, prec, conv_ratio, iteration, refinements);
+    default:
+      sys->ctx->last_error = "unknown precision mode";
+      return DFG_INVALID_ARGUMENT;
+  }
+}
+
 extern "C" int dfg_true_residual(dfg_system sys, const double* b, double* rel) {
   if (!sys || !rel) return DFG_INVALID_ARGUMENT;
   dfg_ctx ctx = sys->ctx;
@@ -1163,10 +1238,13 @@ extern "C" int dfg_profile_kernels(dfg_system sys, dfg_precond prec, int mode, i
   dfg_ctx ctx = sys->ctx;
   return guarded(ctx, [&]() -> int {
     dfg_ctx ctx_ = ctx;
-    const bool fp32 = mode == DFG_PREC_MIXED;
+    const bool mixed = mode == DFG_PREC_MIXED;
+    const bool fp32z = mode != DFG_PREC_FP64;  // sweeps in FP32
+    REQUIRE(mode >= 0 && mode <= 2, DFG_INVALID_ARGUMENT, "unknown precision mode");
     REQUIRE(prec->numeric && prec->sys == sys, DFG_NOT_READY, "preconditioner value not set for this system");
-    REQUIRE(fp32 ? (sys->w_r32.p && sys->mat32_valid && prec->numeric32) : (sys->w_p.p != nullptr), DFG_NOT_READY,
-            "run a solve of this mode before profiling it");
+    REQUIRE(mixed ? (sys->w_p32.p && sys->mat32_valid && prec->numeric32)
+                  : (sys->w_p.p && (!fp32z || (sys->w_r32.p && sys->w_z32.p && prec->numeric32))),
+            DFG_NOT_READY, "run a solve of this mode before profiling it");
     const long long m = (long long)sys->n * sys->b;
     Scratch sc = scratch_of(ctx);
     Red red = red_of(ctx, 3);
@@ -1185,26 +1263,31 @@ extern "C" int dfg_profile_kernels(dfg_system sys, dfg_precond prec, int mode, i
     const MatView A32{sys->n, sys->b, sys->rowptr.as<int>(), sys->colind.as<int>(), sys->diag32.p, sys->offd32.p};
     // the update kernels run on copies, so the caller's residual, solution and
     // direction stay as the last solve left them
-    DBuf tr, tx, tp, td;
-    const size_t esz = fp32 ? 4 : 8;
+    DBuf tr, tx, tp, td, tr32;
+    const size_t esz = mixed ? 4 : 8;
     dalloc(ctx, tr, vec_bytes(sys, esz));
     dalloc(ctx, tx, vec_bytes(sys, 8));
     dalloc(ctx, tp, vec_bytes(sys, esz));
     dalloc(ctx, td, vec_bytes(sys, 8));
-    CK(cudaMemcpyAsync(tr.p, fp32 ? sys->w_r32.p : sys->res.p, (size_t)m * esz, cudaMemcpyDeviceToDevice, ctx->stream));
+    dalloc(ctx, tr32, vec_bytes(sys, 4));
+    CK(cudaMemcpyAsync(tr.p, mixed ? sys->w_r32.p : sys->res.p, (size_t)m * esz, cudaMemcpyDeviceToDevice, ctx->stream));
     CK(cudaMemcpyAsync(tx.p, sys->upd.p, (size_t)m * 8, cudaMemcpyDeviceToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(tp.p, fp32 ? sys->w_p32.p : sys->w_p.p, (size_t)m * esz, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(tp.p, mixed ? sys->w_p32.p : sys->w_p.p, (size_t)m * esz, cudaMemcpyDeviceToDevice, ctx->stream));
     CK(cudaMemsetAsync(td.p, 0, (size_t)m * 8, ctx->stream));
-    PcgVecs v{tr.as<double>(), tx.as<double>(), tp.as<double>(), sys->w_q.as<double>(),
-              prec->ybuf64.as<double>(), sys->w_z.as<double>(), m};
+    if (fp32z && !mixed) CK(cudaMemcpyAsync(tr32.p, sys->w_r32.p, (size_t)m * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    PcgVecs v{};
+    v.r = tr.as<double>(); v.x = tx.as<double>(); v.p = tp.as<double>(); v.q = sys->w_q.as<double>();
+    v.y = fp32z ? prec->ybuf32.p : prec->ybuf64.p;
+    v.z = fp32z ? sys->w_z32.p : sys->w_z.p;
+    v.m = m; v.r32 = tr32.as<float>(); v.rd = td.as<double>(); v.b = sys->rhs0.as<double>();
     MixVecs w{sys->rhs0.as<double>(), tx.as<double>(), sys->w_rd.as<double>(), td.as<double>(),
               tr.as<float>(), tp.as<float>(), sys->w_q32.as<float>(), prec->ybuf32.as<float>(),
               sys->w_z32.as<float>(), m};
-    const void* rin = fp32 ? (const void*)w.r : (const void*)v.r;
-    void* ybuf = fp32 ? (void*)w.y : (void*)v.y;
-    void* zbuf = fp32 ? (void*)w.z : (void*)v.z;
-    SweepLaunch F = sweep_launch(ctx, prec, prec->fwd, fp32, rin, ybuf, sc.tickets, nullptr);
-    SweepLaunch B = sweep_launch(ctx, prec, prec->bwd, fp32, ybuf, zbuf, sc.tickets + 1, nullptr);
+    const void* rin = mixed ? (const void*)w.r : (fp32z ? (const void*)v.r32 : (const void*)v.r);
+    void* ybuf = fp32z ? prec->ybuf32.p : prec->ybuf64.p;
+    void* zbuf = fp32z ? sys->w_z32.p : sys->w_z.p;
+    SweepLaunch F = sweep_launch(ctx, prec, prec->fwd, fp32z, rin, ybuf, sc.tickets, nullptr);
+    SweepLaunch B = sweep_launch(ctx, prec, prec->bwd, fp32z, ybuf, zbuf, sc.tickets + 1, nullptr);
     auto timed = [&](int slot, auto&& pre, auto&& body) {
       for (int r = 0; r < reps + 1; ++r) {
         pre();
@@ -1218,28 +1301,24 @@ extern "C" int dfg_profile_kernels(dfg_system sys, dfg_precond prec, int mode, i
       }
     };
     auto nop = [] {};
-    if (fp32) {
-      timed(0, nop, [&] { CK(mix_spmv_pap(A32, w, st, red, ctx->stream)); });
-    } else {
-      timed(0, nop, [&] { CK(pcg_spmv_pap(A64, v, st, red, ctx->stream)); });
-    }
+    if (mixed) timed(0, nop, [&] { CK(mix_spmv_pap(A32, w, st, red, ctx->stream)); });
+    else timed(0, nop, [&] { CK(pcg_spmv_pap(A64, v, st, red, ctx->stream)); });
     timed(1, [&] {
-        CK(fill_sentinel(m, ybuf, fp32, ctx->stream));
+        CK(fill_sentinel(m, ybuf, fp32z, ctx->stream));
         CK(cudaMemsetAsync(sc.tickets, 0, 2 * sizeof(int), ctx->stream));
-      }, [&] { run_sweep(ctx, true, sys->b, fp32, F); });
+      }, [&] { run_sweep(ctx, true, sys->b, fp32z, F); });
     timed(2, [&] {
-        CK(fill_sentinel(m, zbuf, fp32, ctx->stream));
+        CK(fill_sentinel(m, zbuf, fp32z, ctx->stream));
         CK(cudaMemsetAsync(sc.tickets, 0, 2 * sizeof(int), ctx->stream));
-      }, [&] { run_sweep(ctx, false, sys->b, fp32, B); });
-    // the update kernels rewrite r, x, p: time them last, on copies of nothing that matters
-    if (fp32) {
+      }, [&] { run_sweep(ctx, false, sys->b, fp32z, B); });
+    if (mixed) {
       timed(3, nop, [&] { CK(mix_update_rx(w, st, red, sc.tickets, ctx->stream)); });
       timed(4, nop, [&] { CK(mix_rz_beta(w, st, red, ctx->stream)); });
       timed(5, nop, [&] { CK(mix_update_p(w, st, ctx->stream)); });
     } else {
-      timed(3, nop, [&] { CK(pcg_update_rx(v, st, red, sc.tickets, ctx->stream)); });
-      timed(4, nop, [&] { CK(pcg_rz_beta(v, st, red, ctx->stream)); });
-      timed(5, nop, [&] { CK(pcg_update_p(v, st, ctx->stream)); });
+      timed(3, nop, [&] { CK(pcg_update_rx(v, st, red, sc.tickets, fp32z, ctx->stream)); });
+      timed(4, nop, [&] { CK(pcg_rz_beta(v, st, red, fp32z, ctx->stream)); });
+      timed(5, nop, [&] { CK(pcg_update_p(v, st, fp32z, ctx->stream)); });
     }
     launched(ctx, 8LL * (reps + 1));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -1247,13 +1326,14 @@ extern "C" int dfg_profile_kernels(dfg_system sys, dfg_precond prec, int mode, i
     cudaEventDestroy(e1);
     for (int k = 0; k < 6; ++k) ms[k] = acc[k] / reps;
     if (bytes) {
-      const double sz = fp32 ? 4.0 : 8.0, bs = (double)sys->b * sys->b, N = sys->n, Z = (double)sys->nnz;
+      const double spmv_sz = mixed ? 4.0 : 8.0, sw_sz = fp32z ? 4.0 : 8.0;
+      const double bs = (double)sys->b * sys->b, N = sys->n, Z = (double)sys->nnz;
       long long zl = 0;
       for (int i = 0; i < sys->n; ++i) zl += sys->h_diaind[i] - sys->h_rowptr[i];
-      const double Zl = (double)zl, Zu = Z - Zl, vec = N * sys->b * sz;
-      bytes[0] = (Z + N) * bs * sz + 4.0 * (Z + N + 1) + 2.0 * vec;          // values, indices, x, y
-      bytes[1] = (Zl + N) * bs * sz + 4.0 * (Zl + N + 1) + 2.0 * vec;        // L, D^-1, indices, in, out
-      bytes[2] = Zu * bs * sz + 4.0 * (Zu + N + 1) + 2.0 * vec;              // U', indices, in, out
+      const double Zl = (double)zl, Zu = Z - Zl;
+      bytes[0] = (Z + N) * bs * spmv_sz + 4.0 * (Z + N + 1) + 2.0 * N * sys->b * spmv_sz;   // values, indices, x, y
+      bytes[1] = (Zl + N) * bs * sw_sz + 4.0 * (Zl + N + 1) + 2.0 * N * sys->b * sw_sz;       // L, D^-1, indices, in, out
+      bytes[2] = Zu * bs * sw_sz + 4.0 * (Zu + N + 1) + 2.0 * N * sys->b * sw_sz;             // U', indices, in, out
     }
     return DFG_OK;
   });

@@ -118,15 +118,22 @@ __global__ void k_spmv_pap(MatView Am, const T* __restrict__ p, T* __restrict__ 
 
 // ------------------------------------------------------------- FP64 PCG
 
+template <typename Z>
+__device__ __forceinline__ double zval(const void* z, long long k) {
+  return (double)reinterpret_cast<const Z*>(z)[k];
+}
+
 // x := 0 * x (SCAL(0,x)); rr0 = r.r; early exit below 1e-30; sentinels
+template <typename Z>
 __global__ void k_pcg_init(PcgVecs v, PcgState* st, Red red, double tol, int maxit, int* tickets) {
   double part = 0.0;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < v.m; k += (long long)gridDim.x * blockDim.x) {
     v.x[k] = v.x[k] * 0.0;
     const double r = v.r[k];
     part += r * r;
-    v.y[k] = sentinel_value<double>();
-    v.z[k] = sentinel_value<double>();
+    reinterpret_cast<Z*>(v.y)[k] = sentinel_value<Z>();
+    reinterpret_cast<Z*>(v.z)[k] = sentinel_value<Z>();
+    if constexpr (sizeof(Z) == 4) v.r32[k] = (float)r;
   }
   double tot;
   if (grid_sum(part, red, &tot) && threadIdx.x == 0) {
@@ -149,11 +156,12 @@ __global__ void k_pcg_init(PcgVecs v, PcgState* st, Red red, double tol, int max
 }
 
 // p := z; rz = r.z
+template <typename Z>
 __global__ void k_pcg_after_precond0(PcgVecs v, PcgState* st, Red red) {
   if (st->done) return;
   double part = 0.0;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < v.m; k += (long long)gridDim.x * blockDim.x) {
-    const double z = v.z[k];
+    const double z = zval<Z>(v.z, k);
     v.p[k] = z;
     part += v.r[k] * z;
   }
@@ -163,6 +171,7 @@ __global__ void k_pcg_after_precond0(PcgVecs v, PcgState* st, Red red) {
 
 // r := r - alpha q; x := x + alpha p (AXPY, no-op for alpha == 0); rr = r.r;
 // convergence check; sentinel refill for the sweeps; sweep tickets reset
+template <typename Z>
 __global__ void k_pcg_update_rx(PcgVecs v, PcgState* st, Red red, int* tickets) {
   if (st->done) return;
   const double alpha = st->alpha;
@@ -175,8 +184,9 @@ __global__ void k_pcg_update_rx(PcgVecs v, PcgState* st, Red red, int* tickets) 
       v.x[k] = __dadd_rn(v.x[k], __dmul_rn(alpha, v.p[k]));
     }
     part += r * r;
-    v.y[k] = sentinel_value<double>();
-    v.z[k] = sentinel_value<double>();
+    reinterpret_cast<Z*>(v.y)[k] = sentinel_value<Z>();
+    reinterpret_cast<Z*>(v.z)[k] = sentinel_value<Z>();
+    if constexpr (sizeof(Z) == 4) v.r32[k] = (float)r;
   }
   double tot;
   if (grid_sum(part, red, &tot) && threadIdx.x == 0) {
@@ -201,11 +211,12 @@ __global__ void k_pcg_update_rx(PcgVecs v, PcgState* st, Red red, int* tickets) 
 }
 
 // rz_new = r.z; beta = rz_new / rz
+template <typename Z>
 __global__ void k_pcg_rz_beta(PcgVecs v, PcgState* st, Red red) {
   if (st->done) return;
   double part = 0.0;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < v.m; k += (long long)gridDim.x * blockDim.x)
-    part += v.r[k] * v.z[k];
+    part += v.r[k] * zval<Z>(v.z, k);
   double tot;
   if (grid_sum(part, red, &tot) && threadIdx.x == 0) {
     st->beta = tot / st->rz;
@@ -214,12 +225,50 @@ __global__ void k_pcg_rz_beta(PcgVecs v, PcgState* st, Red red) {
 }
 
 // p := beta p; p := p + 1.0 z (SCAL + AXPY); iteration counter
+template <typename Z>
 __global__ void k_pcg_update_p(PcgVecs v, PcgState* st) {
   if (st->done) return;
   const double beta = st->beta;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < v.m; k += (long long)gridDim.x * blockDim.x)
-    v.p[k] = __dadd_rn(__dmul_rn(v.p[k], beta), v.z[k]);
+    v.p[k] = __dadd_rn(__dmul_rn(v.p[k], beta), zval<Z>(v.z, k));
   if (blockIdx.x == 0 && threadIdx.x == 0) st->it += 1;
+}
+
+// rd = b - A x; st->rr = rd.rd
+template <int B>
+__global__ void k_pcg_true_residual(MatView Am, PcgVecs v, PcgState* st, Red red) {
+  const double* diag = reinterpret_cast<const double*>(Am.diag);
+  const double* offd = reinterpret_cast<const double*>(Am.offd);
+  double part = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < Am.n; i += gridDim.x * blockDim.x) {
+    double y[B];
+    row_mv<double, double, B>(i, Am.rowptr, Am.colind, diag, offd, v.x, y);
+#pragma unroll
+    for (int d = 0; d < B; ++d) {
+      const double r = v.b[(size_t)i * B + d] - y[d];
+      v.rd[(size_t)i * B + d] = r;
+      part += r * r;
+    }
+  }
+  double tot;
+  if (grid_sum(part, red, &tot) && threadIdx.x == 0) st->rr = tot;
+}
+
+// residual replacement: continue the recursion from the true residual
+template <typename Z>
+__global__ void k_pcg_replace(PcgVecs v, PcgState* st, int* tickets) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < v.m; k += (long long)gridDim.x * blockDim.x) {
+    const double r = v.rd[k];
+    v.r[k] = r;
+    if constexpr (sizeof(Z) == 4) v.r32[k] = (float)r;
+    reinterpret_cast<Z*>(v.y)[k] = sentinel_value<Z>();
+    reinterpret_cast<Z*>(v.z)[k] = sentinel_value<Z>();
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->done = 0;
+    tickets[0] = 0;
+    tickets[1] = 0;
+  }
 }
 
 // ----------------------------------------------------------- mixed precision
@@ -363,19 +412,21 @@ __global__ void k_fill_sentinel32(long long m, float* p) {
 
 // ------------------------------------------------------------- launchers
 
-static inline int row_grid(int n, int tpb) {
-  const int g = (n + tpb - 1) / tpb;
-  return g < kRedGrid ? (g > 0 ? g : 1) : kRedGrid;
-}
 // reductions always use the fixed grid (deterministic regardless of timing)
 #define RED_LAUNCH <<<kRedGrid, kRedTpb, 0, s>>>
 
-cudaError_t pcg_init(const PcgVecs& v, PcgState* st, Red red, double tol, int maxit, int* tickets, cudaStream_t s) {
-  k_pcg_init RED_LAUNCH(v, st, red, tol, maxit, tickets);
+#define ZDISPATCH(kern, ...)                               \
+  do {                                                     \
+    if (fp32z) kern<float> RED_LAUNCH(__VA_ARGS__);        \
+    else kern<double> RED_LAUNCH(__VA_ARGS__);             \
+  } while (0)
+
+cudaError_t pcg_init(const PcgVecs& v, PcgState* st, Red red, double tol, int maxit, int* tickets, bool fp32z, cudaStream_t s) {
+  ZDISPATCH(k_pcg_init, v, st, red, tol, maxit, tickets);
   return cudaGetLastError();
 }
-cudaError_t pcg_after_precond0(const PcgVecs& v, PcgState* st, Red red, cudaStream_t s) {
-  k_pcg_after_precond0 RED_LAUNCH(v, st, red);
+cudaError_t pcg_after_precond0(const PcgVecs& v, PcgState* st, Red red, bool fp32z, cudaStream_t s) {
+  ZDISPATCH(k_pcg_after_precond0, v, st, red);
   return cudaGetLastError();
 }
 cudaError_t pcg_spmv_pap(const MatView& A, const PcgVecs& v, PcgState* st, Red red, cudaStream_t s) {
@@ -387,16 +438,29 @@ cudaError_t pcg_spmv_pap(const MatView& A, const PcgVecs& v, PcgState* st, Red r
   }
   return cudaGetLastError();
 }
-cudaError_t pcg_update_rx(const PcgVecs& v, PcgState* st, Red red, int* tickets, cudaStream_t s) {
-  k_pcg_update_rx RED_LAUNCH(v, st, red, tickets);
+cudaError_t pcg_update_rx(const PcgVecs& v, PcgState* st, Red red, int* tickets, bool fp32z, cudaStream_t s) {
+  ZDISPATCH(k_pcg_update_rx, v, st, red, tickets);
   return cudaGetLastError();
 }
-cudaError_t pcg_rz_beta(const PcgVecs& v, PcgState* st, Red red, cudaStream_t s) {
-  k_pcg_rz_beta RED_LAUNCH(v, st, red);
+cudaError_t pcg_rz_beta(const PcgVecs& v, PcgState* st, Red red, bool fp32z, cudaStream_t s) {
+  ZDISPATCH(k_pcg_rz_beta, v, st, red);
   return cudaGetLastError();
 }
-cudaError_t pcg_update_p(const PcgVecs& v, PcgState* st, cudaStream_t s) {
-  k_pcg_update_p RED_LAUNCH(v, st);
+cudaError_t pcg_update_p(const PcgVecs& v, PcgState* st, bool fp32z, cudaStream_t s) {
+  ZDISPATCH(k_pcg_update_p, v, st);
+  return cudaGetLastError();
+}
+cudaError_t pcg_true_residual(const MatView& A, const PcgVecs& v, PcgState* st, Red red, cudaStream_t s) {
+  switch (A.b) {
+    case 1: k_pcg_true_residual<1> RED_LAUNCH(A, v, st, red); break;
+    case 2: k_pcg_true_residual<2> RED_LAUNCH(A, v, st, red); break;
+    case 3: k_pcg_true_residual<3> RED_LAUNCH(A, v, st, red); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+cudaError_t pcg_replace(const PcgVecs& v, PcgState* st, int* tickets, bool fp32z, cudaStream_t s) {
+  ZDISPATCH(k_pcg_replace, v, st, tickets);
   return cudaGetLastError();
 }
 

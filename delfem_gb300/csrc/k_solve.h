@@ -41,16 +41,24 @@ struct PcgVecs {
   double* x;   // update slot
   double* p;
   double* q;   // A p
-  double* y;   // forward-sweep output
-  double* z;   // backward-sweep output (preconditioned residual)
+  void* y;     // forward-sweep output (double, or float with an FP32 factor)
+  void* z;     // backward-sweep output (preconditioned residual)
   long long m; // n*b
+  float* r32;  // FP32 copy of r fed to FP32 sweeps (nullptr with an FP64 factor)
+  double* rd;  // true-residual scratch (b - A x)
+  const double* b;  // finalized right-hand side (true-residual checks)
 };
-cudaError_t pcg_init(const PcgVecs& v, PcgState* st, Red red, double tol, int maxit, int* tickets, cudaStream_t s);
-cudaError_t pcg_after_precond0(const PcgVecs& v, PcgState* st, Red red, cudaStream_t s);
+// fp32z: the preconditioned vectors y, z are float (FP32 factor and sweeps)
+cudaError_t pcg_init(const PcgVecs& v, PcgState* st, Red red, double tol, int maxit, int* tickets, bool fp32z, cudaStream_t s);
+cudaError_t pcg_after_precond0(const PcgVecs& v, PcgState* st, Red red, bool fp32z, cudaStream_t s);
 cudaError_t pcg_spmv_pap(const MatView& A, const PcgVecs& v, PcgState* st, Red red, cudaStream_t s);
-cudaError_t pcg_update_rx(const PcgVecs& v, PcgState* st, Red red, int* tickets, cudaStream_t s);
-cudaError_t pcg_rz_beta(const PcgVecs& v, PcgState* st, Red red, cudaStream_t s);
-cudaError_t pcg_update_p(const PcgVecs& v, PcgState* st, cudaStream_t s);
+cudaError_t pcg_update_rx(const PcgVecs& v, PcgState* st, Red red, int* tickets, bool fp32z, cudaStream_t s);
+cudaError_t pcg_rz_beta(const PcgVecs& v, PcgState* st, Red red, bool fp32z, cudaStream_t s);
+cudaError_t pcg_update_p(const PcgVecs& v, PcgState* st, bool fp32z, cudaStream_t s);
+// rd = b - A x, rr = rd.rd (into st->rr; state otherwise untouched)
+cudaError_t pcg_true_residual(const MatView& A, const PcgVecs& v, PcgState* st, Red red, cudaStream_t s);
+// r = rd (and r32), sentinels, tickets reset, done = 0: continue from the true residual
+cudaError_t pcg_replace(const PcgVecs& v, PcgState* st, int* tickets, bool fp32z, cudaStream_t s);
 
 // ---- mixed precision ----------------------------------------------------
 struct MixVecs {

@@ -43,7 +43,7 @@ class Context:
         h = ctypes.c_void_p()
         st = lib().dfg_ctx_create(device, ctypes.byref(h))
         if st != capi.DFG_OK:
-            raise capi.DfgError(st, "dfg_ctx_create", "no usable CUDA device")
+            raise capi.DfgError(st, "dfg_ctx_create", lib().dfg_last_error(None).decode(errors="replace"))
         self.h = h
 
     def synchronize(self):
@@ -337,6 +337,22 @@ def Solve_PCG_Mixed(conv_ratio: float, iteration: int, ls: LinearSystemField, pr
     return st == capi.DFG_OK, c.value, it.value, outer.value
 
 
+def Solve_PCG_ex(conv_ratio: float, iteration: int, ls: LinearSystemField, prec: PreconditionerILU,
+                 mode: str = "fp64", target_true: bool = False):
+    """dfg_solve_pcg_ex: mode "fp64" (plain), "mixed" (FP32 factor, sweeps, SpMV
+    and vectors inside FP64 refinement) or "fp32f" (FP32 factor and sweeps,
+    FP64 SpMV and vectors).  With target_true the true relative residual must
+    also reach the tolerance.  Returns (converged, ratio, iterations, refinements)."""
+    c = ctypes.c_double(conv_ratio)
+    it = ctypes.c_uint(iteration)
+    refin = ctypes.c_uint(0)
+    st = lib().dfg_solve_pcg_ex(ls.h, prec.h, capi.MODES[mode], 1 if target_true else 0, ctypes.byref(c),
+                                ctypes.byref(it), ctypes.byref(refin))
+    if st not in (capi.DFG_OK, capi.DFG_NOT_CONVERGED):
+        check(ls.ctx.h, st, "dfg_solve_pcg_ex")
+    return st == capi.DFG_OK, c.value, it.value, refin.value
+
+
 def Solve_PCG_reference_loop(conv_ratio: float, iteration: int, lsp: LinearSystemPreconditioner):
     """The reference's Solve_PCG control flow (solver_ls_iter.cpp:100-172)
     written against the ILinearSystemPreconditioner_Sol virtuals: this is how
@@ -379,7 +395,7 @@ def profile_kernels(ls: LinearSystemField, prec: PreconditionerILU, mode: str = 
     algorithmic bytes of the SpMV and the two sweeps."""
     ms = np.zeros(6)
     by = np.zeros(3)
-    m = 1 if mode == "mixed" else 0
+    m = capi.MODES[mode]
     check(ls.ctx.h, lib().dfg_profile_kernels(ls.h, prec.h, m, reps, _p(ms), _p(by)), "dfg_profile_kernels")
     names = ["spmv", "sweep_fwd", "sweep_bwd", "update_rx", "rz_beta", "update_p"]
     return dict(zip(names, ms.tolist())), dict(zip(names[:3], by.tolist()))

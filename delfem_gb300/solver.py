@@ -49,18 +49,24 @@ class FESolve:
     def factor(self) -> bool:
         return self.prec.SetValue(self.ls)
 
-    def solve(self, mode: str = "fp64", tol: float | None = None, maxit: int | None = None) -> dict:
+    def solve(self, mode: str = "fp64", tol: float | None = None, maxit: int | None = None,
+              target_true: bool = False) -> dict:
+        """mode: "fp64" (LsSol::Solve_PCG semantics unless target_true), "mixed"
+        (FP32 factor/sweeps/SpMV/vectors + FP64 refinement, always on the true
+        residual) or "fp32f" (FP32 factor and sweeps only)."""
         tol = self.p.tol if tol is None else tol
         maxit = self.p.maxit if maxit is None else maxit
-        if mode == "fp64":
+        if mode == "fp64" and not target_true:
             ok, conv, it = L.Solve_PCG(tol, maxit, self.ls, self.prec)
             return dict(converged=ok, conv=conv, iter=it, refinements=0)
         if mode == "mixed":
             ok, conv, it, outer = L.Solve_PCG_Mixed(tol, maxit, self.ls, self.prec)
             return dict(converged=ok, conv=conv, iter=it, refinements=outer)
-        raise ValueError(mode)
+        ok, conv, it, refin = L.Solve_PCG_ex(tol, maxit, self.ls, self.prec, mode, target_true)
+        return dict(converged=ok, conv=conv, iter=it, refinements=refin)
 
-    def run(self, mode: str = "fp64", tol: float | None = None, maxit: int | None = None) -> dict:
+    def run(self, mode: str = "fp64", tol: float | None = None, maxit: int | None = None,
+            target_true: bool = False) -> dict:
         t0 = time.perf_counter()
         norm_res = self.assemble()
         self.ctx.synchronize()
@@ -68,7 +74,7 @@ class FESolve:
         ok = self.factor()
         self.ctx.synchronize()
         t2 = time.perf_counter()
-        out = self.solve(mode, tol, maxit)
+        out = self.solve(mode, tol, maxit, target_true)
         t3 = time.perf_counter()
         out.update(norm_res=norm_res, ilu_ok=ok, t_assemble=t1 - t0, t_ilu=t2 - t1, t_solve=t3 - t2)
         return out

@@ -43,8 +43,9 @@ enum {
 
 /* vector precision / solver modes */
 enum {
-  DFG_PREC_FP64 = 0,       /* plain FP64 path */
-  DFG_PREC_MIXED = 1       /* FP32 factor / sweeps / SpMV inside FP64 iterative refinement */
+  DFG_PREC_FP64 = 0,        /* plain FP64 path */
+  DFG_PREC_MIXED = 1,       /* FP32 factor, sweeps, SpMV and Krylov vectors inside FP64 refinement */
+  DFG_PREC_FP32_FACTOR = 2  /* FP32 factor and sweeps; FP64 SpMV, vectors and reductions */
 };
 
 typedef struct dfg_ctx_s* dfg_ctx;
@@ -56,7 +57,8 @@ typedef struct dfg_precond_s* dfg_precond;
 /* Creates a context on CUDA device `device` with its own stream. */
 int dfg_ctx_create(int device, dfg_ctx* out);
 int dfg_ctx_destroy(dfg_ctx ctx);
-/* Text of the last error raised through this context (never NULL). */
+/* Text of the last error raised through this context (never NULL); with
+ * ctx == NULL, the reason the last dfg_ctx_create of this thread failed. */
 const char* dfg_last_error(dfg_ctx ctx);
 /* Library version string. */
 const char* dfg_version(void);
@@ -193,6 +195,17 @@ int dfg_precond_get_factor(dfg_precond prec, double* fdiag, double* foffd);
  * *iteration: maximum in, 0-based iteration of convergence out.
  * Returns DFG_OK when converged, DFG_NOT_CONVERGED otherwise. */
 int dfg_solve_pcg(dfg_system sys, dfg_precond prec, double* conv_ratio, unsigned* iteration);
+
+/* General form of the device-resident PCG.  `mode` is one of DFG_PREC_*.
+ * With target_true != 0 the solve also requires the true relative residual
+ * ||b - A x|| / ||b|| (b = the finalized right-hand side) to be <= the
+ * tolerance: when the recursive residual says converged but the true one does
+ * not, the recursion continues from the true residual.  With target_true == 0
+ * and DFG_PREC_FP64 this is exactly dfg_solve_pcg.  *conv_ratio: tolerance in,
+ * achieved ratio out (the true one when target_true != 0); *iteration: maximum
+ * in, iterations out; *refinements: true-residual recomputations (may be NULL). */
+int dfg_solve_pcg_ex(dfg_system sys, dfg_precond prec, int mode, int target_true, double* conv_ratio,
+                     unsigned* iteration, unsigned* refinements);
 
 /* Mixed-precision form of the same solve: FP32 factor, sweeps and SpMV
  * inside FP64 iterative refinement (FP64 outer residual r = b - A x, FP64

@@ -198,3 +198,26 @@ def test_solution_is_deterministic(gpu_ctx):
     x2 = s.solution()
     assert np.array_equal(bits(x1), bits(x2))
     s.close()
+
+
+@pytest.mark.parametrize("path", golden_files(), ids=GOLDEN_IDS)
+def test_pcg_fp32_factor(gpu_ctx, path):
+    """FP32 factor and sweeps, FP64 SpMV and Krylov vectors, true residual enforced."""
+    p, ref = load_golden(path)
+    s = _solver(gpu_ctx, p)
+    r = s.run("fp32f", tol=1e-8, maxit=5000, target_true=True)
+    assert r["converged"] and r["conv"] <= 1e-8
+    assert s.ls.true_residual() <= 1e-8
+    assert abs(r["iter"] - int(ref["iter"])) <= max(3, int(ref["iter"]) // 10)
+    xr = ref["x"]
+    assert np.linalg.norm(s.solution() - xr) <= 1e-6 * np.linalg.norm(xr)
+    s.close()
+
+
+def test_fp64_true_residual_target(gpu_ctx, oracle_lib):
+    from delfem_gb300 import meshgen as mg
+    p = mg.solid2d_cantilever(60, 30, seed=31)
+    s = _solver(gpu_ctx, p)
+    r = s.run("fp64", target_true=True)
+    assert r["converged"] and r["conv"] <= 1e-8 and s.ls.true_residual() <= 1e-8
+    s.close()
