@@ -117,6 +117,7 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
   __syncthreads();
 
   long long g = 0;  // steps this CTA has pushed through the pipeline (both warps count alike)
+  int g_st = 0, g_ph = 0;  // stage and phase parity of pipeline position g
   bool abort = false;
   for (;;) {
     if (threadIdx.x == 0) s_range = atomicAdd(a.ticket, 1);
@@ -126,27 +127,30 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
     if (r >= a.nranges) break;
     const long long s0 = a.range_steps[r], s1 = a.range_steps[r + 1];
     const long long nsteps = s1 - s0;
+    const int nst = (int)nsteps;
     if (warp == 1) {
       // ------------------------------------------------------------ loader
-      auto issue_rec = [&](long long i) {  // step s0+i into stage (g+i)%NS
-        const long long gi = g + i;
-        const int st = (int)(gi % NS);
-        if (gi >= NS) {
-          if (!mbar_wait(&empty[st], (unsigned)(((gi / NS) - 1) & 1), a.err)) abort = true;
+      // stage / phase of pipeline position g+i, advanced incrementally
+      int rs_st = g_st, rs_ph = g_ph;     // next record to issue
+      int vl_st = g_st, vl_ph = g_ph;     // next step to gather for
+      auto issue_rec = [&](int i) {       // step s0+i into stage rs_st
+        if (g + i >= NS) {
+          if (!mbar_wait(&empty[rs_st], (unsigned)(rs_ph ^ 1), a.err)) abort = true;
         }
         if (lane == 0) {
           const long long o0 = a.rec_off[s0 + i], o1 = a.rec_off[s0 + i + 1];
-          mbar_expect_tx(&rec_full[st], (unsigned)(o1 - o0));
-          tma_load_1d(rstage + (size_t)st * a.rec_stage, a.rec + o0, (unsigned)(o1 - o0), &rec_full[st]);
+          mbar_expect_tx(&rec_full[rs_st], (unsigned)(o1 - o0));
+          tma_load_1d(rstage + (size_t)rs_st * a.rec_stage, a.rec + o0, (unsigned)(o1 - o0), &rec_full[rs_st]);
         }
+        if (++rs_st == NS) { rs_st = 0; rs_ph ^= 1; }
       };
       const int LA = NS > 3 ? NS / 2 : 1;  // record copies run LA steps ahead of the gathers
-      for (long long i = 0; i < LA && i < nsteps; ++i) issue_rec(i);
-      for (long long i = 0; i < nsteps; ++i) {
-        if (i + LA < nsteps) issue_rec(i + LA);
-        const long long gi = g + i;
-        const int st = (int)(gi % NS);
-        if (!mbar_wait(&rec_full[st], (unsigned)((gi / NS) & 1), a.err)) abort = true;
+      for (int i = 0; i < LA && i < nst; ++i) issue_rec(i);
+      for (int i = 0; i < nst; ++i) {
+        if (i + LA < nst) issue_rec(i + LA);
+        const int st = vl_st;
+        if (!mbar_wait(&rec_full[st], (unsigned)vl_ph, a.err)) abort = true;
+        if (++vl_st == NS) { vl_st = 0; vl_ph ^= 1; }
         const unsigned char* rec = rstage + (size_t)st * a.rec_stage;
         unsigned char* val = vstage + (size_t)st * a.val_stage;
         const int nent = reinterpret_cast<const int*>(rec)[0];
@@ -175,12 +179,10 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
       }
     } else {
       // ----------------------------------------------------------- compute
-      for (long long i = 0; i < nsteps; ++i) {
-        const long long gi = g + i;
-        const int st = (int)(gi % NS);
-        const unsigned par = (unsigned)((gi / NS) & 1);
-        if (!mbar_wait(&rec_full[st], par, a.err)) abort = true;
-        if (!mbar_wait(&full[st], par, a.err)) abort = true;
+      int st = g_st, ph = g_ph, rs = 0;
+      for (int i = 0; i < nst; ++i) {
+        if (!mbar_wait(&rec_full[st], (unsigned)ph, a.err)) abort = true;
+        if (!mbar_wait(&full[st], (unsigned)ph, a.err)) abort = true;
         const unsigned char* rec = rstage + (size_t)st * a.rec_stage;
         const unsigned char* val = vstage + (size_t)st * a.val_stage;
         const int nent = reinterpret_cast<const int*>(rec)[0];
@@ -192,16 +194,18 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
           T t[B];
 #pragma unroll
           for (int d = 0; d < B; ++d) t[d] = reinterpret_cast<const T*>(val)[lane * B + d];
+#pragma unroll 4
           for (int e = 0; e < nent; ++e) {
             const int c = code[e * 32 + lane];
             const unsigned char* base = (c < 0) ? val : ringreg;
             const T* vp = reinterpret_cast<const T*>(base + (c & 0x7fffffff));
             T v[B];
-#pragma unroll
-            for (int d = 0; d < B; ++d) v[d] = vp[d];
             bool stale = false;
 #pragma unroll
-            for (int d = 0; d < B; ++d) stale |= is_sentinel(v[d]);
+            for (int d = 0; d < B; ++d) {
+              v[d] = vp[d];
+              stale |= is_sentinel(v[d]);
+            }
             if (stale) {  // produced after the window was copied: poll the value itself
               const size_t k = (size_t)grow[e * 32 + lane];
               for (int d = 0; d < B; ++d) {
@@ -240,7 +244,7 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
 #pragma unroll
             for (int p = 0; p < B; ++p) y[p] = t[p];
           }
-          T* rg = reinterpret_cast<T*>(ringreg + 32) + ((size_t)((i % a.R) * 32 + lane)) * B;
+          T* rg = reinterpret_cast<T*>(ringreg + 32) + (rs * 32 + lane) * B;
 #pragma unroll
           for (int d = 0; d < B; ++d) {
             rg[d] = y[d];
@@ -250,9 +254,13 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
         abort = __any_sync(0xffffffffu, abort);
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[st]);
+        if (++st == NS) { st = 0; ph ^= 1; }
+        if (++rs == a.R) rs = 0;
       }
     }
     g += nsteps;
+    g_st = (int)(g % NS);  // once per range
+    g_ph = (int)((g / NS) & 1);
     if (__any_sync(0xffffffffu, abort)) {
       if (lane == 0) atomicExch(a.err, a.err[0] ? a.err[0] : kErrTimeout);
     }
