@@ -765,6 +765,7 @@ SweepLaunch sweep_launch(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, bool fp32, c
   a.rec_stage = (int)((fp32 ? S.max_rec32 : S.max_rec64) + 15) / 16 * 16;
   a.val_stage = sweep_val_stage(S.plan.max_nent, pr->b, elem);
   a.R = S.plan.R;
+  a.max_nent = S.plan.max_nent;
   // pipeline depth: as deep as 16 stages while the CTA fits in ~200 KB
   const size_t budget = std::min<size_t>(ctx_->smem_optin, 200 * 1024);
   int NS = 16;

@@ -62,8 +62,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
       : "memory");
   return ok != 0;
 }
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
 // bounded wait; returns false (and records a timeout) when it gives up
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int* err) {
+  if (mbar_test_wait(bar, parity)) return true;
   long long n = 0;
   while (!mbar_try_wait(bar, parity)) {
     if (++n > kSpinLimit) {
@@ -86,7 +96,26 @@ __device__ __forceinline__ void named_sync(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-template <typename T, int B, bool FWD>
+// Rare path: a gathered window still held the sentinel (its producer wrote
+// after the copy); poll those values from global memory, bounded.
+template <typename T>
+__device__ __noinline__ T poll_value(const T* p, const int* err, int* abort) {
+  long long spins = 0;
+  T x = ld_relaxed(p);
+  while (is_sentinel(x)) {
+    x = ld_relaxed(p);
+    if ((++spins & 1023) == 0) {
+      if (ld_relaxed_int(err) != 0 || spins > kSpinLimit) {
+        if (spins > kSpinLimit) atomicExch(const_cast<int*>(err), kErrTimeout);
+        *abort = 1;
+        break;
+      }
+    }
+  }
+  return x;
+}
+
+template <typename T, int B, bool FWD, int MAXE>
 __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
   constexpr int BS = B * B;
   constexpr int SZ = (int)sizeof(T);
@@ -194,40 +223,72 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
           T t[B];
 #pragma unroll
           for (int d = 0; d < B; ++d) t[d] = reinterpret_cast<const T*>(val)[lane * B + d];
-#pragma unroll 4
-          for (int e = 0; e < nent; ++e) {
-            const int c = code[e * 32 + lane];
-            const unsigned char* base = (c < 0) ? val : ringreg;
-            const T* vp = reinterpret_cast<const T*>(base + (c & 0x7fffffff));
-            T v[B];
+          if constexpr (MAXE > 0) {
+            // all dependency values first (independent shared-memory loads),
+            // one staleness test, then the FMAs
+            T v[MAXE][B];
             bool stale = false;
 #pragma unroll
-            for (int d = 0; d < B; ++d) {
-              v[d] = vp[d];
-              stale |= is_sentinel(v[d]);
-            }
-            if (stale) {  // produced after the window was copied: poll the value itself
-              const size_t k = (size_t)grow[e * 32 + lane];
-              for (int d = 0; d < B; ++d) {
-                long long spins = 0;
-                while (is_sentinel(v[d])) {
-                  v[d] = ld_relaxed(&out[k * B + d]);
-                  if ((++spins & 1023) == 0) {
-                    if (ld_relaxed_int(a.err) != 0 || spins > kSpinLimit) {
-                      if (spins > kSpinLimit) atomicExch(a.err, kErrTimeout);
-                      abort = true;
-                      break;
-                    }
-                  }
+            for (int e = 0; e < MAXE; ++e) {
+              if (e < nent) {
+                const int c = code[e * 32 + lane];
+                const unsigned char* base = (c < 0) ? val : ringreg;
+                const T* vp = reinterpret_cast<const T*>(base + (c & 0x7fffffff));
+#pragma unroll
+                for (int d = 0; d < B; ++d) {
+                  v[e][d] = vp[d];
+                  stale |= is_sentinel(v[e][d]);
                 }
               }
             }
+            if (stale) {
+              int ab = 0;
 #pragma unroll
-            for (int p = 0; p < B; ++p) {
-              T acc = t[p];
+              for (int e = 0; e < MAXE; ++e)
 #pragma unroll
-              for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[q];
-              t[p] = acc;
+                for (int d = 0; d < B; ++d)
+                  if (e < nent && is_sentinel(v[e][d]))
+                    v[e][d] = poll_value<T>(&out[(size_t)grow[e * 32 + lane] * B + d], a.err, &ab);
+              abort |= ab != 0;
+            }
+#pragma unroll
+            for (int e = 0; e < MAXE; ++e) {
+              if (e < nent) {
+#pragma unroll
+                for (int p = 0; p < B; ++p) {
+                  T acc = t[p];
+#pragma unroll
+                  for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[e][q];
+                  t[p] = acc;
+                }
+              }
+            }
+          } else {
+            for (int e = 0; e < nent; ++e) {
+              const int c = code[e * 32 + lane];
+              const unsigned char* base = (c < 0) ? val : ringreg;
+              const T* vp = reinterpret_cast<const T*>(base + (c & 0x7fffffff));
+              T v[B];
+              bool stale = false;
+#pragma unroll
+              for (int d = 0; d < B; ++d) {
+                v[d] = vp[d];
+                stale |= is_sentinel(v[d]);
+              }
+              if (stale) {
+                int ab = 0;
+#pragma unroll
+                for (int d = 0; d < B; ++d)
+                  if (is_sentinel(v[d])) v[d] = poll_value<T>(&out[(size_t)grow[e * 32 + lane] * B + d], a.err, &ab);
+                abort |= ab != 0;
+              }
+#pragma unroll
+              for (int p = 0; p < B; ++p) {
+                T acc = t[p];
+#pragma unroll
+                for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[q];
+                t[p] = acc;
+              }
             }
           }
           T y[B];
@@ -251,7 +312,6 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
             st_relaxed(&out[(size_t)row * B + d], y[d]);
           }
         }
-        abort = __any_sync(0xffffffffu, abort);
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[st]);
         if (++st == NS) { st = 0; ph ^= 1; }
@@ -300,15 +360,22 @@ __global__ void k_pack(PackArgs a) {
 
 // ------------------------------------------------------------------ launchers
 
+template <typename T, int B, bool FWD>
+static cudaError_t launch_e(const SweepArgs& a, int grid, size_t smem, cudaStream_t st) {
+  if (a.max_nent <= 4) k_sweep<T, B, FWD, 4><<<grid, 64, smem, st>>>(a);
+  else if (a.max_nent <= 8) k_sweep<T, B, FWD, 8><<<grid, 64, smem, st>>>(a);
+  else k_sweep<T, B, FWD, 0><<<grid, 64, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
 template <typename T, bool FWD>
 static cudaError_t launch_b(int B, const SweepArgs& a, int grid, size_t smem, cudaStream_t st) {
   switch (B) {
-    case 1: k_sweep<T, 1, FWD><<<grid, 64, smem, st>>>(a); break;
-    case 2: k_sweep<T, 2, FWD><<<grid, 64, smem, st>>>(a); break;
-    case 3: k_sweep<T, 3, FWD><<<grid, 64, smem, st>>>(a); break;
+    case 1: return launch_e<T, 1, FWD>(a, grid, smem, st);
+    case 2: return launch_e<T, 2, FWD>(a, grid, smem, st);
+    case 3: return launch_e<T, 3, FWD>(a, grid, smem, st);
     default: return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
 }
 
 cudaError_t launch_sweep(bool forward, bool fp32, int B, const SweepArgs& a, int grid, size_t smem,
@@ -319,7 +386,12 @@ cudaError_t launch_sweep(bool forward, bool fp32, int B, const SweepArgs& a, int
 
 template <typename T, int B, bool FWD>
 static cudaError_t set_attr(size_t max_smem) {
-  return cudaFuncSetAttribute(k_sweep<T, B, FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+  cudaError_t e = cudaFuncSetAttribute(k_sweep<T, B, FWD, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_sweep<T, B, FWD, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_sweep<T, B, FWD, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+  return e;
 }
 
 cudaError_t sweep_set_smem_limits(size_t max_smem) {

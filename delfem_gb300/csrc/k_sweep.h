@@ -18,6 +18,7 @@ struct SweepArgs {
   int val_stage;              // bytes per value slot
   int R;                      // ring depth in steps
   int NS;                     // pipeline stages
+  int max_nent;               // most dependency entries of any step (selects the unrolled variant)
 };
 
 // smem bytes a launch needs: mbarriers, NS record slots, NS value slots,

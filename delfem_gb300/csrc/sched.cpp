@@ -76,37 +76,39 @@ Levels build_levels(int n, const int* rowptr, const int* colind, const int* diai
 }
 
 // Range boundaries.  A cut right after a row that the next rows depend on
-// makes the next range wait for the end of this one, so cuts go only where
-// the row at the cut does not depend on the g rows just before it (line or
-// plane starts in the natural order of a structured mesh); among those, the
-// one closest above the target size wins.
+// makes the next range wait for the end of this one, so a cut goes where the
+// row at the cut depends on no row close before it: between half and twice
+// the target size, the candidate whose nearest dependency lies furthest back
+// wins (a plane start beats a line start in a structured 3D mesh), ties going
+// to the candidate closest to the target.
 static std::vector<int> range_cuts(int n, const int* rowptr, const int* colind, const int* diaind, bool forward,
                                    int target) {
-  std::vector<char> cand(n + 1, 0);
-  const int g = 2;
+  std::vector<int> dist(n + 1, 0);  // position distance to the nearest dependency
   for (int p = 0; p < n; ++p) {
     const int row = forward ? p : n - 1 - p;
     int c0, c1;
     deps_of(row, forward, rowptr, diaind, c0, c1);
-    int nearest = -1;  // largest dependency position
+    int nearest = -1;
     for (int c = c0; c < c1; ++c) {
       const int k = colind[c];
       nearest = std::max(nearest, forward ? k : n - 1 - k);
     }
-    cand[p] = (nearest < 0 || p - nearest > g) ? 1 : 0;
+    dist[p] = nearest < 0 ? n : p - nearest;
   }
   std::vector<int> cuts{0};
   int a = 0;
+  const int g = 2;
   while (a < n) {
     const int want = a + target;
     if (want >= n) break;
-    int pick = -1;
-    const int hi = std::min(n - 1, a + 2 * target);
-    for (int p = want; p <= hi; ++p)
-      if (cand[p]) { pick = p; break; }
-    if (pick < 0)
-      for (int p = want - 1; p > a + target / 2; --p)
-        if (cand[p]) { pick = p; break; }
+    const int lo = std::max(a + 1, a + target / 2), hi = std::min(n - 1, a + 2 * target);
+    int pick = -1, best_d = g, best_off = 0;
+    for (int p = lo; p <= hi; ++p) {
+      const int d = dist[p], off = std::abs(p - want);
+      if (d > best_d || (d == best_d && pick >= 0 && off < best_off)) {
+        if (d > g) { pick = p; best_d = d; best_off = off; }
+      }
+    }
     if (pick < 0) pick = want;
     cuts.push_back(pick);
     a = pick;
@@ -206,7 +208,7 @@ SweepPlan build_sweep_plan(int n, int b, const int* rowptr, const int* colind, c
   // makespan model: a step takes one unit once its range's previous step and
   // every producer step (+ a hop of kHop units between ranges) are done
   {
-    const double kHop = 12.0;
+    const double kHop = 40.0;
     std::vector<double> step_end(P.nsteps, 0.0);
     double makespan = 0.0;
     for (int r = 0; r < P.nranges; ++r) {
@@ -223,7 +225,7 @@ SweepPlan build_sweep_plan(int n, int b, const int* rowptr, const int* colind, c
           }
         int nrow = 0;
         for (int lane = 0; lane < 32; ++lane) nrow += P.step_rows[(size_t)s * 32 + lane] >= 0;
-        t = start + 1.0 + 0.002 * nrow * (P.step_nent[s] + 1) * b * b;
+        t = start + 1.0 + 0.0005 * nrow * (P.step_nent[s] + 1) * b * b;
         step_end[s] = t;
       }
       makespan = std::max(makespan, t);
