@@ -208,8 +208,9 @@ def run_gpu(args, rank, world, local):
         r = s.solve(mode, target_true=True)
         return ok, r
 
+    arms_run = [(a, m) for a, m in ARMS if a in args.arms.split(",")]
     results = {}
-    for arm, mode in ARMS:
+    for arm, mode in arms_run:
         for _ in range(args.warmup):
             step(mode)
         barrier()
@@ -247,11 +248,12 @@ def run_gpu(args, rank, world, local):
 
     # per-kernel timing (CUDA events on the library's stream) + algorithmic bytes
     prof = {}
-    for arm, mode in ARMS:
+    for arm, mode in arms_run:
         step(mode)
         ms, by = L.profile_kernels(s.ls, s.prec, mode, reps=10)
         prof[arm] = (ms, by)
-    head = max(("mixed_fp32_factor", "mixed_fp32_all"), key=lambda a: -results[a]["total_ms"])
+    mixed_run = [a for a in ("mixed_fp32_factor", "mixed_fp32_all") if a in results] or list(results)
+    head = max(mixed_run, key=lambda a: -results[a]["total_ms"])
 
     # end to end through the C ABI: per-solve inputs from pinned host memory
     e2e = None
@@ -356,8 +358,8 @@ def compose_line(args, world, p, results, prof, e2e, head):
     dom = max(ms_h, key=ms_h.get)  # every kernel launches once per iteration
     roof_dom = roof(ms_h, by_h, dom) if dom in by_h else roof(ms_h, by_h, "spmv")
     value = arms[head]["value"]
-    plain = arms["plain_fp64"]
-    xp = results["plain_fp64"]["x"]
+    plain = arms.get("plain_fp64", arms[head])
+    xp = results["plain_fp64"]["x"] if "plain_fp64" in results else results[head]["x"]
     line = {
         "metric": METRIC,
         "value": value,
@@ -379,9 +381,9 @@ def compose_line(args, world, p, results, prof, e2e, head):
         "p99_ms": arms[head]["p99_ms"],
         "iterations": arms[head]["iterations"],
         "true_rel_residual": hr["true_rel"],
-        "plain_fp64": plain,
-        "mixed_fp32_factor": arms["mixed_fp32_factor"],
-        "mixed_fp32_all": arms["mixed_fp32_all"],
+        "plain_fp64": arms.get("plain_fp64"),
+        "mixed_fp32_factor": arms.get("mixed_fp32_factor"),
+        "mixed_fp32_all": arms.get("mixed_fp32_all"),
         "mixed_over_plain": round(value / plain["value"], 3),
         "roofline": roof_dom,
         "gpu_launches": int(hr["launches"]),
@@ -393,7 +395,7 @@ def compose_line(args, world, p, results, prof, e2e, head):
         line["e2e"] = {"value": round(e2e["value"], 4), "unit": "solves/s", "h2d_bytes_per_step": int(e2e["h2d"]),
                        "d2h_bytes_per_step": int(e2e["d2h"])}
     if not args.no_cpu_baseline:
-        iters_full = REF_ITERS.get(args.config) or results["plain_fp64"]["iters"][-1]
+        iters_full = REF_ITERS.get(args.config) or results[("plain_fp64" if "plain_fp64" in results else head)]["iters"][-1]
         sample_iters = args.cpu_sample_iters
         rate, t_solve, res = cpu_rate(args.config, iters_full, 1, sample_iters)
         line["cpu_baseline"] = {"value": round(rate, 6), "unit": "solves/s", "cores": 1, "kind": "port",
@@ -444,6 +446,8 @@ def main():
     ap.add_argument("--config", default="solid2d_1000x500", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-iters", type=int, default=60)
+    ap.add_argument("--arms", default=",".join(a for a, _ in ARMS),
+                    help="comma-separated GPU arms to run (profiling runs pick one)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
