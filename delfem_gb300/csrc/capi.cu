@@ -716,9 +716,7 @@ void build_records(dfg_ctx ctx_, SweepDev& S, int elem, DBuf& rec, DBuf& rec_off
   upload(ctx_, rec_off, off.data(), off.size());
 }
 
-void setup_sweep(dfg_ctx ctx_, SweepDev& S, const dfg_system sys, bool forward) {
-  S.plan = choose_sweep_plan(sys->n, sys->b, sys->h_rowptr.data(), sys->h_colind.data(), sys->h_diaind.data(),
-                             forward, 32, 8);
+void setup_sweep_plan(dfg_ctx ctx_, SweepDev& S) {
   const SweepPlan& P = S.plan;
   build_records(ctx_, S, 8, S.rec64, S.rec_off64, S.rec_total64, S.max_rec64);
   build_records(ctx_, S, 4, S.rec32, S.rec_off32, S.rec_total32, S.max_rec32);
@@ -785,6 +783,59 @@ void run_sweep(dfg_ctx ctx_, bool forward, int b, bool fp32, const SweepLaunch& 
   launched(ctx_);
 }
 
+// Schedule choice: the cost model keeps a few candidate range sizes and each
+// is timed on the device with one FP32 sweep of the real structure (values
+// do not change the timing); the fastest wins.
+void setup_sweep(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, const dfg_system sys, bool forward) {
+  std::vector<SweepPlan> cands = candidate_sweep_plans(sys->n, sys->b, sys->h_rowptr.data(), sys->h_colind.data(),
+                                                       sys->h_diaind.data(), forward, 32, 4);
+  size_t best = 0;
+  if (cands.size() > 1) {
+    const long long m = (long long)sys->n * sys->b;
+    DBuf vin, vout;
+    dalloc(ctx_, vin, (size_t)m * 4 + 64);
+    dalloc(ctx_, vout, (size_t)m * 4 + 64);
+    CK(cudaMemsetAsync(vin.p, 0, vin.bytes, ctx_->stream));
+    Scratch sc = scratch_of(ctx_);
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best_ms = 1e30f;
+    for (size_t c = 0; c < cands.size(); ++c) {
+      SweepDev T;
+      T.plan = std::move(cands[c]);
+      build_records(ctx_, T, 4, T.rec32, T.rec_off32, T.rec_total32, T.max_rec32);
+      CK(cudaMemsetAsync(T.rec32.p, 0, T.rec32.bytes, ctx_->stream));  // factor values not packed: zeros
+      upload(ctx_, T.range_steps, T.plan.range_steps.data(), T.plan.range_steps.size());
+      SweepLaunch L = sweep_launch(ctx_, pr, T, true, vin.p, vout.p, sc.tickets + 2, nullptr);
+      float ms_min = 1e30f;
+      for (int rep = 0; rep < 2; ++rep) {
+        CK(fill_sentinel(m, vout.p, true, ctx_->stream));
+        CK(cudaMemsetAsync(sc.tickets + 2, 0, sizeof(int), ctx_->stream));
+        CK(cudaEventRecord(e0, ctx_->stream));
+        CK(launch_sweep(forward, true, sys->b, L.args, L.grid, L.smem, ctx_->stream));
+        CK(cudaEventRecord(e1, ctx_->stream));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        ms_min = std::min(ms_min, ms);
+      }
+      launched(ctx_, 4);
+      if (ms_min < best_ms) { best_ms = ms_min; best = c; }
+      cands[c] = std::move(T.plan);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (read_err(ctx_) != 0) {
+      CK(cudaMemsetAsync(ctx_->err_word.p, 0, sizeof(int), ctx_->stream));
+      set_err(ctx_, "a triangular-sweep wait timed out while choosing the schedule");
+      throw Fail{DFG_TIMEOUT};
+    }
+  }
+  S.plan = std::move(cands[best]);
+  setup_sweep_plan(ctx_, S);
+}
+
 }  // namespace
 
 extern "C" int dfg_precond_create(dfg_ctx ctx, dfg_precond* out) {
@@ -829,8 +880,8 @@ extern "C" int dfg_precond_set_linear_system(dfg_precond prec, dfg_system sys) {
     dalloc(ctx, prec->foffd, (size_t)std::max<long long>(sys->nnz, 1) * bs * 8);
     prec->lev_fwd = build_levels(sys->n, sys->h_rowptr.data(), sys->h_colind.data(), sys->h_diaind.data(), true);
     upload(ctx, prec->lev_rows, prec->lev_fwd.rows.data(), std::max<size_t>(prec->lev_fwd.rows.size(), 1));
-    setup_sweep(ctx, prec->fwd, sys, true);
-    setup_sweep(ctx, prec->bwd, sys, false);
+    setup_sweep(ctx, prec, prec->fwd, sys, true);
+    setup_sweep(ctx, prec, prec->bwd, sys, false);
     dalloc(ctx, prec->ybuf64, vec_bytes(sys, 8));
     dalloc(ctx, prec->ybuf32, vec_bytes(sys, 4));
     CK(cudaStreamSynchronize(ctx->stream));

@@ -90,6 +90,9 @@ SweepPlan build_sweep_plan(int n, int b, const int* rowptr, const int* colind, c
                            bool forward, int range_rows, int R);
 SweepPlan choose_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind,
                             bool forward, int R, int elem_size);
+// the `keep` plans with the lowest model makespan over range sizes 256, 512, ... rows
+std::vector<SweepPlan> candidate_sweep_plans(int n, int b, const int* rowptr, const int* colind, const int* diaind,
+                                             bool forward, int R, int keep);
 
 // node-to-node pattern from elements, no diagonal, ascending (MakePattern_FEM)
 void pattern_from_elements(int nnode, int nelem, int nnoel, const int* conn,

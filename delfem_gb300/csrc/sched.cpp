@@ -235,17 +235,26 @@ SweepPlan build_sweep_plan(int n, int b, const int* rowptr, const int* colind, c
   return P;
 }
 
-SweepPlan choose_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind,
-                            bool forward, int R, int /*elem_size*/) {
-  SweepPlan best;
-  bool have = false;
-  for (long long rr = 256; ; rr *= 2) {
+std::vector<SweepPlan> candidate_sweep_plans(int n, int b, const int* rowptr, const int* colind, const int* diaind,
+                                             bool forward, int R, int keep) {
+  std::vector<SweepPlan> all;
+  for (long long rr = 256;; rr *= 2) {
     const int range_rows = (int)std::min<long long>(rr, std::max(n, 1));
     SweepPlan P = build_sweep_plan(n, b, rowptr, colind, diaind, forward, range_rows, R);
-    if (!have || P.est_cost < best.est_cost * 0.97) { best = std::move(P); have = true; }
+    bool dup = false;
+    for (const SweepPlan& Q : all) dup |= (Q.nranges == P.nranges && Q.nsteps == P.nsteps);
+    if (!dup) all.push_back(std::move(P));
     if (range_rows >= n) break;
   }
-  return best;
+  std::stable_sort(all.begin(), all.end(), [](const SweepPlan& x, const SweepPlan& y) { return x.est_cost < y.est_cost; });
+  if ((int)all.size() > keep) all.resize(keep);
+  return all;
+}
+
+SweepPlan choose_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind,
+                            bool forward, int R, int /*elem_size*/) {
+  std::vector<SweepPlan> c = candidate_sweep_plans(n, b, rowptr, colind, diaind, forward, R, 1);
+  return std::move(c.front());
 }
 
 std::vector<unsigned char> pack_record_headers(const SweepPlan& P, int elem, std::vector<long long>& off,
