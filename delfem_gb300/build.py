@@ -30,6 +30,7 @@ SOURCES = {
     "k_assemble.cu": ["-fmad=false"],
     "k_ilu.cu": ["-fmad=false"],
     "k_api.cu": ["-fmad=false"],
+    "noalloc.cu": [],
 }
 
 

@@ -88,7 +88,9 @@ SIGNATURES = {
     "dfg_true_residual": (_I, [_P, _P, _PD]),
     "dfg_ctx_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
     "dfg_profile_kernels": (_I, [_P, _P, _I, _I, _P, _P]),
+    "dfg_dot_noalloc": (_I, [_P, _P, _LL, _PD, _P]),
 }
+DFG_DOT_NOALLOC_MAX_LEN = 33554432
 
 _lib = None
 

@@ -194,6 +194,11 @@ extern "C" const char* dfg_version(void) { return DFG_VERSION; }
 // error text of the last failed dfg_ctx_create (there is no context to hold it)
 static thread_local std::string g_create_error = "no error";
 
+namespace dfg {
+// errors of entry points that take no context (dfg_dot_noalloc)
+void set_noctx_error(const std::string& m) { g_create_error = m; }
+}  // namespace dfg
+
 extern "C" int dfg_ctx_create(int device, dfg_ctx* out) {
   if (!out) return DFG_INVALID_ARGUMENT;
   *out = nullptr;

@@ -58,7 +58,8 @@ typedef struct dfg_precond_s* dfg_precond;
 int dfg_ctx_create(int device, dfg_ctx* out);
 int dfg_ctx_destroy(dfg_ctx ctx);
 /* Text of the last error raised through this context (never NULL); with
- * ctx == NULL, the reason the last dfg_ctx_create of this thread failed. */
+ * ctx == NULL, the reason the last dfg_ctx_create or dfg_dot_noalloc of this
+ * thread failed. */
 const char* dfg_last_error(dfg_ctx ctx);
 /* Library version string. */
 const char* dfg_version(void);
@@ -156,6 +157,34 @@ int dfg_get_tmp_vector_size(dfg_system sys, unsigned* size);
 int dfg_resize_tmp_vec(dfg_system sys, unsigned size);
 /* *out = {v1}.{v2} (CLinearSystem::DOT, src/ls/linearsystem.cpp:335-360) */
 int dfg_dot(dfg_system sys, int iv1, int iv2, double* out);
+/* Allocation-free dot product.  No counterpart in the reference (its DOT,
+ * src/ls/linearsystem.cpp:335-360, is dfg_dot above).
+ *
+ * *out = x.y for m doubles in device memory of the calling thread's current
+ * CUDA device, computed on `stream` (a cudaStream_t; NULL = the default
+ * stream); the call returns once the result is on the host.  Same
+ * deterministic two-pass sum as dfg_dot (fixed-shape block trees, then the
+ * per-block partials in index order), with 4096-element blocks: the same
+ * inputs give the same bits on every call, and the value agrees with
+ * dfg_dot's to rounding.
+ *
+ * For callers that may not allocate device memory: a serving loop whose
+ * device budget is fully reserved at admission while other solves run
+ * (cudaMalloc could exceed the budget, cudaFree waits for the whole device),
+ * and callers holding vectors in their own device memory without a dfg
+ * context (creating one allocates).  Nothing is allocated: the reduction
+ * scratch is a fixed file-scope device array of 8192 partial sums plus two
+ * words (65,552 bytes per device), so m > DFG_DOT_NOALLOC_MAX_LEN is rejected
+ * with DFG_INVALID_ARGUMENT (reason in dfg_last_error(NULL)).  The arrival
+ * counter is cleared on `stream` before each launch.
+ *
+ * The first call on each device looks up the array's address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture begins.  All calls on one device share the one
+ * array: calls that overlap (several host threads, or several streams at
+ * once) race, and the caller must serialise them. */
+#define DFG_DOT_NOALLOC_MAX_LEN 33554432LL /* 8192 blocks x 4096 elements */
+int dfg_dot_noalloc(const double* x, const double* y, long long m, double* out, void* stream);
 /* {v2} := {v1} (COPY :366-392) */
 int dfg_copy(dfg_system sys, int iv1, int iv2);
 /* {v1} := alpha*{v1} (SCAL :398-415) */
