@@ -31,6 +31,8 @@ SOURCES = {
     "k_ilu.cu": ["-fmad=false"],
     "k_api.cu": ["-fmad=false"],
     "noalloc.cu": [],
+    "k_serve.cu": [],
+    "serve.cu": [],
 }
 
 

@@ -89,7 +89,41 @@ SIGNATURES = {
     "dfg_ctx_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
     "dfg_profile_kernels": (_I, [_P, _P, _I, _I, _P, _P]),
     "dfg_dot_noalloc": (_I, [_P, _P, _LL, _PD, _P]),
+    "dfg_server_create": (_I, [_P, _P, ctypes.POINTER(_P)]),
+    "dfg_server_submit": (_I, [_P, _P, ctypes.POINTER(_LL)]),
+    "dfg_server_wait": (_I, [_P, _LL, _P]),
+    "dfg_server_error_text": (_I, [_P, _LL, ctypes.c_char_p, _I]),
+    "dfg_server_drain": (_I, [_P]),
+    "dfg_server_stats": (_I, [_P, _P]),
+    "dfg_server_destroy": (_I, [_P]),
 }
+
+
+class ServerConfig(ctypes.Structure):
+    """dfg_server_config"""
+    _fields_ = [("mode", _I), ("tol", _D), ("maxit", _I), ("budget_bytes", _LL), ("max_inflight", _I),
+                ("chunk_iters", _I), ("host_threads", _I)]
+
+
+class Request(ctypes.Structure):
+    """dfg_request"""
+    _fields_ = [("kind", _I), ("nnode", _I), ("nelem", _I), ("coords", _P), ("conn", _P), ("coef", _P),
+                ("params", _P), ("nparams", _I), ("bcflag", _P), ("load", _P), ("x_out", _P)]
+
+
+class Result(ctypes.Structure):
+    """dfg_result"""
+    _fields_ = [("id", _LL), ("status", _I), ("iterations", _I), ("conv", _D), ("rel_true", _D),
+                ("t_submit", _D), ("t_admit", _D), ("t_done", _D), ("device_bytes", _LL)]
+
+
+class ServerCounters(ctypes.Structure):
+    """dfg_server_counters"""
+    _fields_ = [("submitted", _LL), ("finished", _LL), ("replays", _LL), ("kernel_launches", _LL),
+                ("graph_builds", _LL), ("peak_inflight", _LL), ("budget_bytes", _LL), ("peak_bytes", _LL),
+                ("busy_seconds", _D), ("now_seconds", _D)]
+
+
 DFG_DOT_NOALLOC_MAX_LEN = 33554432
 
 _lib = None

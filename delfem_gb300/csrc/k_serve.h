@@ -1,0 +1,72 @@
+// k_serve.h -- batched PCG kernels of the serving path: one launch works on
+// every in-flight solve listed in a device-side slot table.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "k_solve.h"
+
+namespace dfg {
+
+constexpr int kSrvRows = 256;       // rows per chunk (one thread per block row)
+constexpr int kSrvMaxSlots = 256;   // in-flight solves per server
+constexpr int kSrvTpb = kSrvRows;
+
+// One in-flight solve.  Its rows are cut into chunks of kSrvRows; chunk k of
+// the slot is chunk chunk0 + k of the launch's chunk space.  Reductions sum a
+// slot's per-chunk partials in chunk order, so a slot's result does not
+// depend on which other solves share the launch.
+struct SrvSlot {
+  int n, b;
+  int chunk0, nchunks;
+  const int* rowptr;
+  const int* colind;
+  const double* diag;   // FP64 matrix, reference layout
+  const double* offd;
+  const double* rhs;    // finalized right-hand side
+  double* r;            // recursive residual
+  double* x;            // solution
+  double* p;
+  double* q;            // A p
+  double* rd;           // true residual b - A x
+  void* y;              // forward-sweep output (sweep precision)
+  void* z;              // backward-sweep output
+  float* r32;           // FP32 sweep input (FP32 factor), else nullptr
+  PcgState* st;
+  unsigned* cnt;        // reduction arrival counter (0 between launches)
+};
+
+struct SrvTable {
+  int nslots;
+  int total_chunks;
+  int chunk_start[kSrvMaxSlots + 1];
+  SrvSlot slot[kSrvMaxSlots];
+};
+
+// What the host reads after each replay, one entry per table slot.
+struct SrvStatus {
+  int done, iter_out, verified, nreplace;
+  double conv;      // recursive sqrt(rr / rr0) at the stop
+  double rel_true;  // ||b - A x|| / ||b|| at the last check (-1 if none)
+};
+
+// fp32z: sweep outputs y, z are float (FP32 factor); tickets: the batched
+// sweep launches' counters, reset once the sweeps of an iteration are over
+cudaError_t srv_rz_beta(const SrvTable* T, double* partials, int* tickets, int ntickets, bool fp32z, int grid,
+                        cudaStream_t s);
+cudaError_t srv_update_p(const SrvTable* T, bool fp32z, int grid, cudaStream_t s);
+cudaError_t srv_spmv_pap(const SrvTable* T, double* partials, int grid, cudaStream_t s);
+cudaError_t srv_update_rx(const SrvTable* T, double* partials, bool fp32z, int grid, cudaStream_t s);
+// for slots with a converged recursion not yet verified: rd = b - A x and the
+// true residual check; failures are marked for replacement
+cudaError_t srv_check_true(const SrvTable* T, double* partials, int grid, cudaStream_t s);
+// slots marked for replacement continue from r = rd
+cudaError_t srv_replace(const SrvTable* T, double* partials, bool fp32z, int grid, cudaStream_t s);
+cudaError_t srv_collect(const SrvTable* T, SrvStatus* out, cudaStream_t s);
+
+// admission: r = rhs, x = p = 0, sweep outputs = sentinel, r32 = r; then the
+// state from rr0 = r.r (computed by the caller into *rr0)
+cudaError_t srv_init_vectors(long long m, const double* rhs, double* r, double* x, double* p, void* y, void* z,
+                             float* r32, bool fp32z, cudaStream_t s);
+cudaError_t srv_init_state(PcgState* st, const double* rr0, double tol, int maxit, cudaStream_t s);
+
+}  // namespace dfg

@@ -13,6 +13,7 @@
 
 #include "dfg_common.cuh"
 #include "k_solve.h"
+#include "k_rowmv.cuh"
 
 namespace dfg {
 
@@ -64,34 +65,6 @@ __device__ bool grid_sum(double v, Red red, double* total) {
 }
 
 // ------------------------------------------------------------------- SpMV
-
-// y_i = sum_j A_ij x_j for one block row; off-diagonal blocks in CRS order,
-// then the diagonal block (the order of CMatDia_BlkCrs::MatVec).
-template <typename T, typename A, int B>
-__device__ __forceinline__ void row_mv(int i, const int* __restrict__ rowptr, const int* __restrict__ colind,
-                                       const T* __restrict__ diag, const T* __restrict__ offd,
-                                       const T* __restrict__ x, A y[B]) {
-  constexpr int BS = B * B;
-#pragma unroll
-  for (int p = 0; p < B; ++p) y[p] = 0;
-  const int c0 = rowptr[i], c1 = rowptr[i + 1];
-  for (int c = c0; c < c1; ++c) {
-    const int j = colind[c];
-    const T* a = offd + (size_t)c * BS;
-    T xv[B];
-#pragma unroll
-    for (int q = 0; q < B; ++q) xv[q] = x[(size_t)j * B + q];
-#pragma unroll
-    for (int p = 0; p < B; ++p)
-#pragma unroll
-      for (int q = 0; q < B; ++q) y[p] += (A)a[p * B + q] * (A)xv[q];
-  }
-  const T* a = diag + (size_t)i * BS;
-#pragma unroll
-  for (int p = 0; p < B; ++p)
-#pragma unroll
-    for (int q = 0; q < B; ++q) y[p] += (A)a[p * B + q] * (A)x[(size_t)i * B + q];
-}
 
 // q = A p and pAp = p.q; the last block sets alpha = rz / pAp
 template <typename T, int B>

@@ -11,8 +11,11 @@ struct PcgState {
   double rr_ref;   // mixed: recursive residual norm^2 at the last reliable update
   double delta2;   // mixed: reliable update once rr < delta2 * rr_ref
   double tolb2;    // mixed: tol^2 * ||b||^2
+  double rr_true;  // serving: ||b - A x||^2 at the last check
   int it, maxit, done, iter_out;
-  int pad[4];
+  int verified;    // serving: the true residual met the tolerance
+  int nreplace;    // serving: residual replacements so far
+  int pad[2];
 };
 // done codes: 0 running, 1 converged, 2 iteration limit, 3 NaN,
 //             4 reliable update due (mixed), 5 recursive residual below tol (mixed)

@@ -19,6 +19,8 @@
 //     come from a ring of its own recent results or from the gathered
 //     windows, selected without branching), writes results to the ring and to
 //     global memory, and releases the stage on its `empty` mbarrier.
+// In a batched launch (SweepArgs::batch) a ticket names a range of one of
+// several independent solves; the pipeline simply continues across them.
 // Cross-range hand-off needs no flags or fences: outputs are pre-filled with
 // a NaN sentinel and written once, so a non-sentinel value is final; a window
 // copied before its producer wrote it still holds the sentinel and the
@@ -129,9 +131,7 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
   unsigned char* rstage = smem + (((size_t)3 * NS * 8 + 127) / 128) * 128;
   unsigned char* vstage = rstage + (size_t)NS * a.rec_stage;
   unsigned char* ringreg = vstage + (size_t)NS * a.val_stage;  // 32 zero bytes, then the ring
-  __shared__ int s_range;
-  const T* __restrict__ in = reinterpret_cast<const T*>(a.in);
-  T* out = reinterpret_cast<T*>(a.out);
+  __shared__ int s_range, s_slot;
 
   if (a.done && *a.done) return;
   if (threadIdx.x == 0) {
@@ -149,12 +149,38 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
   int g_st = 0, g_ph = 0;  // stage and phase parity of pipeline position g
   bool abort = false;
   for (;;) {
-    if (threadIdx.x == 0) s_range = atomicAdd(a.ticket, 1);
+    if (threadIdx.x == 0) {
+      const int t = atomicAdd(a.ticket, 1);
+      int r = -1, j = 0;
+      if (a.batch) {
+        const SweepBatch* bt = a.batch;
+        const int ns = bt->nslots;
+        if (t < bt->range_start[ns]) {
+          int lo = 0, hi = ns - 1;  // last j with range_start[j] <= t
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (bt->range_start[mid] <= t) lo = mid; else hi = mid - 1;
+          }
+          j = lo;
+          r = ld_relaxed_int(bt->slot[j].done) ? -2 : t - bt->range_start[j];
+        }
+      } else if (t < a.nranges) {
+        r = t;
+      }
+      s_range = r;
+      s_slot = j;
+    }
     named_sync(1, 64);
-    const int r = s_range;
+    const int r = s_range, jslot = s_slot;
     named_sync(1, 64);
-    if (r >= a.nranges) break;
-    const long long s0 = a.range_steps[r], s1 = a.range_steps[r + 1];
+    if (r == -1) break;
+    if (r == -2) continue;  // a finished solve: its ranges are skipped
+    const unsigned char* __restrict__ recs = a.batch ? a.batch->slot[jslot].rec : a.rec;
+    const long long* __restrict__ rec_off = a.batch ? a.batch->slot[jslot].rec_off : a.rec_off;
+    const int* __restrict__ range_steps = a.batch ? a.batch->slot[jslot].range_steps : a.range_steps;
+    const T* __restrict__ in = reinterpret_cast<const T*>(a.batch ? a.batch->slot[jslot].in : a.in);
+    T* out = reinterpret_cast<T*>(a.batch ? a.batch->slot[jslot].out : a.out);
+    const long long s0 = range_steps[r], s1 = range_steps[r + 1];
     const long long nsteps = s1 - s0;
     const int nst = (int)nsteps;
     if (warp == 1) {
@@ -167,9 +193,9 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
           if (!mbar_wait(&empty[rs_st], (unsigned)(rs_ph ^ 1), a.err)) abort = true;
         }
         if (lane == 0) {
-          const long long o0 = a.rec_off[s0 + i], o1 = a.rec_off[s0 + i + 1];
+          const long long o0 = rec_off[s0 + i], o1 = rec_off[s0 + i + 1];
           mbar_expect_tx(&rec_full[rs_st], (unsigned)(o1 - o0));
-          tma_load_1d(rstage + (size_t)rs_st * a.rec_stage, a.rec + o0, (unsigned)(o1 - o0), &rec_full[rs_st]);
+          tma_load_1d(rstage + (size_t)rs_st * a.rec_stage, recs + o0, (unsigned)(o1 - o0), &rec_full[rs_st]);
         }
         if (++rs_st == NS) { rs_st = 0; rs_ph ^= 1; }
       };

@@ -4,7 +4,28 @@
 
 namespace dfg {
 
+// Several independent sweeps in one launch (the serving path): a claimed
+// ticket t selects the slot j with range_start[j] <= t < range_start[j+1] and
+// its range t - range_start[j]; ranges of a slot whose *done is non-zero are
+// skipped.  All slots share the launch's stage sizes (rec_stage, val_stage,
+// R, NS), so every slot's records must fit them.
+constexpr int kSweepMaxSlots = 256;
+struct SweepSlot {
+  const unsigned char* rec;
+  const long long* rec_off;
+  const int* range_steps;
+  const void* in;
+  void* out;
+  const int* done;
+};
+struct SweepBatch {
+  int nslots;
+  int range_start[kSweepMaxSlots + 1];
+  SweepSlot slot[kSweepMaxSlots];
+};
+
 struct SweepArgs {
+  const SweepBatch* batch;    // non-null: batched launch (rec .. done below unused)
   const unsigned char* rec;   // packed step records
   const long long* rec_off;   // nsteps+1 byte offsets
   const int* range_steps;     // nranges+1

@@ -1,0 +1,1053 @@
+// serve.cu -- the serving runtime: a persistent request loop that keeps many
+// FE solves resident on the device and advances all of them with batched
+// launches replayed from one captured CUDA graph.
+//
+// Request life cycle:
+//   submit      inputs copied; queued for the symbolic workers
+//   symbolic    host threads: node pattern (MakePattern_FEM), element-to-slot
+//               gather map, ILU level sets, forward/backward sweep schedules
+//               and their record headers, and the request's device memory plan
+//   admission   one thread, FIFO: once the request's bytes fit the device
+//               arena and an in-flight slot is free, it uploads the request and
+//               runs assembly (element kernels + gather), Dirichlet rows, the
+//               ILU(0) factorisation, record packing and the PCG start on its
+//               own low-priority stream; transient buffers are released
+//   iteration   the loop thread adds the solve to the slot table; every replay
+//               of the graph runs `chunk` PCG iterations of all slots (sweeps
+//               per block-size class on parallel branches, then the batched
+//               vector kernels), checks converged slots' true residuals, and
+//               copies a status array back
+//   retire      a finished slot leaves the table; its solution is copied to the
+//               caller's buffer and its memory returns to the arena
+// Nothing on the loop path allocates or frees device memory: the arena is one
+// reservation made at creation.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstddef>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "dfg_internal.h"
+#include "k_assemble.h"
+#include "k_ilu.h"
+#include "k_serve.h"
+#include "k_solve.h"
+#include "k_sweep.h"
+
+using namespace dfg;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+constexpr int kClasses = 9;         // block size 1..3 x dependency entries <= 4, 8, 16
+constexpr int kMaxChunks = 1 << 20; // chunk space of one launch (kSrvRows rows each)
+constexpr int kRingSteps = 32;
+
+struct CudaFail {
+  cudaError_t e;
+  const char* what;
+};
+#define SCK(call)                                   \
+  do {                                              \
+    cudaError_t e_ = (call);                        \
+    if (e_ != cudaSuccess) throw CudaFail{e_, #call}; \
+  } while (0)
+
+// ------------------------------------------------------------------ arena
+
+// First-fit allocator over one device reservation; offsets and sizes are
+// multiples of 256 bytes.
+class Arena {
+ public:
+  void init(size_t bytes) {
+    cap_ = bytes / 256 * 256;
+    free_.clear();
+    if (cap_) free_[0] = cap_;
+  }
+  bool alloc(size_t bytes, size_t* off) {
+    bytes = round(bytes);
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= bytes) {
+        *off = it->first;
+        const size_t rest = it->second - bytes, o = it->first + bytes;
+        free_.erase(it);
+        if (rest) free_[o] = rest;
+        used_ += bytes;
+        peak_ = std::max(peak_, used_);
+        return true;
+      }
+    }
+    return false;
+  }
+  void release(size_t off, size_t bytes) {
+    bytes = round(bytes);
+    used_ -= bytes;
+    auto it = free_.emplace(off, bytes).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_.erase(it);
+      }
+    }
+  }
+  size_t capacity() const { return cap_; }
+  size_t used() const { return used_; }
+  size_t peak() const { return peak_; }
+  static size_t round(size_t b) { return (std::max<size_t>(b, 1) + 255) / 256 * 256; }
+
+ private:
+  std::map<size_t, size_t> free_;
+  size_t cap_ = 0, used_ = 0, peak_ = 0;
+};
+
+struct Layout {
+  size_t total = 0;
+  size_t add(size_t bytes) {
+    const size_t o = total;
+    total += Arena::round(bytes);
+    return o;
+  }
+};
+
+// ---------------------------------------------------------------- requests
+
+struct Req {
+  long long id = 0;
+  int kind = 0, b = 1, ndim = 2, nnoel = 3, n = 0, nelem = 0;
+  std::vector<double> coords, coef, load, params;
+  std::vector<int> conn, bcflag;
+  double* x_out = nullptr;
+  double t_submit = 0, t_admit = 0, t_done = 0;
+  // symbolic set-up
+  std::vector<int> rowptr, colind, diaind;
+  long long nnz = 0;
+  GatherMap gm;
+  Levels lev;
+  SweepPlan pf, pb;
+  std::vector<unsigned char> hf, hb;
+  std::vector<long long> of, ob;
+  long long maxrf = 0, maxrb = 0;
+  int cls = -1, maxe = 0;
+  // device memory plan (offsets into the persistent / transient blocks)
+  Layout P, T;
+  size_t o_rowptr, o_colind, o_diag, o_offd, o_rhs, o_r, o_x, o_p, o_q, o_rd, o_y, o_z, o_r32;
+  size_t o_recf, o_offf, o_rsf, o_recb, o_offb, o_rsb, o_st, o_cnt;
+  size_t t_coords, t_conn, t_coef, t_bc, t_load, t_em, t_er, t_sp, t_ss, t_rp, t_rs, t_dia, t_lev, t_fd, t_fo;
+  size_t t_eof, t_esf, t_srf, t_eob, t_esb, t_srb;
+  size_t pbase = 0, tbase = 0;
+  bool have_p = false, have_t = false;
+  // outcome
+  int status = DFG_OK;
+  std::string error;
+  int iters = 0;
+  double conv = 0, rel_true = -1;
+  bool finished = false;
+};
+
+inline int class_index(int b, int maxe) { return (b - 1) * 3 + (maxe <= 4 ? 0 : maxe <= 8 ? 1 : 2); }
+inline int class_maxe(int c) { return (c % 3) == 0 ? 4 : (c % 3) == 1 ? 8 : 16; }
+inline int class_b(int c) { return c / 3 + 1; }
+
+}  // namespace
+
+struct dfg_server_s {
+  dfg_ctx ctx = nullptr;
+  int device = 0, nsm = 0;
+  int mode = DFG_PREC_FP32_FACTOR;
+  bool fp32 = true;
+  double tol = 1e-8;
+  int maxit = 20000, max_inflight = 128, chunk = 8, nthreads = 4;
+  int vec_grid = 0;
+
+  // device resources (made at creation)
+  void* arena_base = nullptr;
+  Arena arena;
+  SrvTable* d_tab = nullptr;
+  SweepBatch* d_sb = nullptr;   // kClasses x 2 (forward, backward)
+  int* d_tickets = nullptr;     // kClasses x 2
+  double* d_partials = nullptr; // kMaxChunks
+  unsigned char* d_stat = nullptr;  // SrvStatus[kSrvMaxSlots] then the error word
+  double* d_adm = nullptr;      // admission reductions: partials, counter, result, singular-pivot count
+  SrvTable* h_tab = nullptr;    // pinned mirrors
+  SweepBatch* h_sb = nullptr;
+  unsigned char* h_stat = nullptr;
+  int* h_nsing = nullptr;
+  cudaStream_t s_iter = nullptr, s_adm = nullptr, s_copy = nullptr;
+  cudaStream_t s_side[kClasses] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[kClasses] = {};
+  cudaGraphExec_t exec = nullptr;
+  int graph_mask = -1;
+  // per-class sweep launch shape
+  int cls_grid[kClasses] = {}, cls_ns[kClasses][2] = {}, cls_rec_stage[kClasses][2] = {}, cls_val_stage[kClasses] = {};
+  size_t cls_smem[kClasses][2] = {};
+
+  // host state
+  Clock::time_point t0;
+  std::mutex mu;
+  std::condition_variable cv_sym, cv_adm, cv_loop, cv_done;
+  std::deque<Req*> submitted;          // waiting for symbolic set-up
+  std::map<long long, Req*> ready;     // symbolic done, by id (FIFO admission)
+  std::deque<Req*> activated;          // admitted, waiting for a table slot
+  std::unordered_map<long long, std::unique_ptr<Req>> all;
+  long long next_id = 0, n_submitted = 0, n_finished = 0;
+  int inflight = 0;                    // admitted and not yet released
+  bool stopping = false;   // no more submissions; symbolic workers leave when idle
+  bool adm_stop = false;   // set once the workers are gone; admission leaves when idle
+  bool loop_stop = false;  // set once admission is gone; the loop leaves when idle
+  int fatal = DFG_OK;
+  std::string fatal_msg;
+  std::vector<std::thread> workers;
+  std::thread adm_thread, loop_thread;
+  // statistics
+  long long replays = 0, launches = 0, peak_inflight = 0, graph_builds = 0;
+  double busy_s = 0;
+
+  double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+};
+
+namespace {
+
+// ---------------------------------------------------------------- symbolic
+
+// Fills the request's host-side set-up; returns false with r->error on failure.
+bool symbolic(dfg_server_s* S, Req* r) {
+  const int n = r->n;
+  pattern_from_elements(n, r->nelem, r->nnoel, r->conn.data(), r->rowptr, r->colind);
+  r->nnz = (long long)r->colind.size();
+  r->diaind.resize(n);
+  for (int i = 0; i < n; ++i) {
+    int d = r->rowptr[i + 1];
+    for (int c = r->rowptr[i]; c < r->rowptr[i + 1]; ++c)
+      if (r->colind[c] > i) { d = c; break; }
+    r->diaind[i] = d;
+  }
+  std::string err;
+  if (!build_gather_map(n, r->rowptr.data(), r->colind.data(), r->nelem, r->nnoel, r->conn.data(), r->gm, err)) {
+    r->error = err;
+    return false;
+  }
+  r->lev = build_levels(n, r->rowptr.data(), r->colind.data(), r->diaind.data(), true);
+  const int elem = S->fp32 ? 4 : 8;
+  r->pf = choose_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), true, kRingSteps, elem);
+  r->pb = choose_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), false, kRingSteps, elem);
+  r->maxe = std::max(r->pf.max_nent, r->pb.max_nent);
+  if (r->maxe > 16) {
+    r->error = "a row has more than 16 lower or upper neighbours; the serving sweeps take at most 16";
+    return false;
+  }
+  r->cls = class_index(r->b, r->maxe);
+  r->hf = pack_record_headers(r->pf, elem, r->of, r->maxrf);
+  r->hb = pack_record_headers(r->pb, elem, r->ob, r->maxrb);
+
+  const size_t m = (size_t)n * r->b, bs = (size_t)r->b * r->b, Z = (size_t)std::max<long long>(r->nnz, 1);
+  Layout& P = r->P;
+  r->o_rowptr = P.add((n + 1) * 4);
+  r->o_colind = P.add(Z * 4);
+  r->o_diag = P.add(n * bs * 8);
+  r->o_offd = P.add(Z * bs * 8);
+  r->o_rhs = P.add(m * 8);
+  r->o_r = P.add(m * 8);
+  r->o_x = P.add(m * 8);
+  r->o_p = P.add(m * 8);
+  r->o_q = P.add(m * 8);
+  r->o_rd = P.add(m * 8);
+  r->o_y = P.add(m * elem + 64);
+  r->o_z = P.add(m * elem + 64);
+  r->o_r32 = P.add(S->fp32 ? m * 4 + 64 : 16);
+  r->o_recf = P.add(r->hf.size() + 64);
+  r->o_offf = P.add(r->of.size() * 8);
+  r->o_rsf = P.add(r->pf.range_steps.size() * 4);
+  r->o_recb = P.add(r->hb.size() + 64);
+  r->o_offb = P.add(r->ob.size() * 8);
+  r->o_rsb = P.add(r->pb.range_steps.size() * 4);
+  r->o_st = P.add(sizeof(PcgState));
+  r->o_cnt = P.add(16);
+  Layout& T = r->T;
+  const size_t k = r->nnoel;
+  r->t_coords = T.add(r->coords.size() * 8);
+  r->t_conn = T.add(r->conn.size() * 4);
+  r->t_coef = T.add(std::max<size_t>(r->coef.size(), 1) * 8);
+  r->t_bc = T.add(m * 4);
+  r->t_load = T.add(std::max<size_t>(r->load.size(), 1) * 8);
+  r->t_em = T.add((size_t)r->nelem * k * k * bs * 8);
+  r->t_er = T.add((size_t)r->nelem * k * r->b * 8);
+  r->t_sp = T.add(r->gm.slot_ptr.size() * 8);
+  r->t_ss = T.add(std::max<size_t>(r->gm.slot_src.size(), 1) * 4);
+  r->t_rp = T.add(r->gm.res_ptr.size() * 8);
+  r->t_rs = T.add(std::max<size_t>(r->gm.res_src.size(), 1) * 4);
+  r->t_dia = T.add((size_t)n * 4);
+  r->t_lev = T.add(std::max<size_t>(r->lev.rows.size(), 1) * 4);
+  r->t_fd = T.add((size_t)n * bs * 8);
+  r->t_fo = T.add(Z * bs * 8);
+  r->t_eof = T.add(r->pf.ent_off.size() * 8);
+  r->t_esf = T.add(std::max<size_t>(r->pf.ent_slot.size(), 1) * 4);
+  r->t_srf = T.add(std::max<size_t>(r->pf.step_rows.size(), 1) * 4);
+  r->t_eob = T.add(r->pb.ent_off.size() * 8);
+  r->t_esb = T.add(std::max<size_t>(r->pb.ent_slot.size(), 1) * 4);
+  r->t_srb = T.add(std::max<size_t>(r->pb.step_rows.size(), 1) * 4);
+  return true;
+}
+
+template <class T>
+T* at(dfg_server_s* S, size_t base, size_t off) {
+  return reinterpret_cast<T*>(static_cast<unsigned char*>(S->arena_base) + base + off);
+}
+
+template <class T>
+void up(dfg_server_s* S, size_t base, size_t off, const std::vector<T>& v) {
+  if (!v.empty())
+    SCK(cudaMemcpyAsync(at<T>(S, base, off), v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, S->s_adm));
+}
+
+// Device work of one admission on s_adm; returns the ILU singular-pivot count.
+int admit_device(dfg_server_s* S, Req* r) {
+  const size_t pb = r->pbase, tb = r->tbase;
+  const int n = r->n, b = r->b;
+  const long long m = (long long)n * b;
+  const size_t bs = (size_t)b * b;
+  cudaStream_t st = S->s_adm;
+  up(S, pb, r->o_rowptr, r->rowptr);
+  up(S, pb, r->o_colind, r->colind);
+  up(S, tb, r->t_coords, r->coords);
+  up(S, tb, r->t_conn, r->conn);
+  up(S, tb, r->t_coef, r->coef);
+  up(S, tb, r->t_bc, r->bcflag);
+  up(S, tb, r->t_load, r->load);
+  up(S, tb, r->t_sp, r->gm.slot_ptr);
+  up(S, tb, r->t_ss, r->gm.slot_src);
+  up(S, tb, r->t_rp, r->gm.res_ptr);
+  up(S, tb, r->t_rs, r->gm.res_src);
+  up(S, tb, r->t_dia, r->diaind);
+  up(S, tb, r->t_lev, r->lev.rows);
+  up(S, pb, r->o_recf, r->hf);
+  up(S, pb, r->o_offf, r->of);
+  up(S, pb, r->o_rsf, r->pf.range_steps);
+  up(S, pb, r->o_recb, r->hb);
+  up(S, pb, r->o_offb, r->ob);
+  up(S, pb, r->o_rsb, r->pb.range_steps);
+  up(S, tb, r->t_eof, r->pf.ent_off);
+  up(S, tb, r->t_esf, r->pf.ent_slot);
+  up(S, tb, r->t_srf, r->pf.step_rows);
+  up(S, tb, r->t_eob, r->pb.ent_off);
+  up(S, tb, r->t_esb, r->pb.ent_slot);
+  up(S, tb, r->t_srb, r->pb.step_rows);
+  double* diag = at<double>(S, pb, r->o_diag);
+  double* offd = at<double>(S, pb, r->o_offd);
+  double* rhs = at<double>(S, pb, r->o_rhs);
+  SCK(cudaMemsetAsync(diag, 0, n * bs * 8, st));
+  SCK(cudaMemsetAsync(offd, 0, std::max<long long>(r->nnz, 1) * bs * 8, st));
+  SCK(cudaMemsetAsync(rhs, 0, m * 8, st));
+  SCK(cudaMemsetAsync(at<unsigned>(S, pb, r->o_cnt), 0, 16, st));
+  // AddLinSys_*: element kernels, then the gather in element order
+  ElemArgs ea{};
+  ea.nelem = r->nelem;
+  ea.conn = at<int>(S, tb, r->t_conn);
+  ea.coords = at<double>(S, tb, r->t_coords);
+  ea.coef = r->coef.empty() ? nullptr : at<double>(S, tb, r->t_coef);
+  for (int i = 0; i < 8; ++i) ea.p[i] = i < (int)r->params.size() ? r->params[i] : 0.0;
+  ea.em = at<double>(S, tb, r->t_em);
+  ea.er = at<double>(S, tb, r->t_er);
+  SCK(launch_elem(r->kind, ea, st));
+  GatherArgs ga{};
+  ga.n = n;
+  ga.nnz = r->nnz;
+  ga.b = b;
+  ga.bs = (int)bs;
+  ga.slot_ptr = at<long long>(S, tb, r->t_sp);
+  ga.slot_src = at<int>(S, tb, r->t_ss);
+  ga.res_ptr = at<long long>(S, tb, r->t_rp);
+  ga.res_src = at<int>(S, tb, r->t_rs);
+  ga.em = ea.em;
+  ga.er = ea.er;
+  ga.diag = diag;
+  ga.offd = offd;
+  ga.res = rhs;
+  SCK(launch_gather(ga, st));
+  int nl = 3;
+  // FinalizeMarge: resident load, then Dirichlet rows and columns
+  if (!r->load.empty()) {
+    SCK(launch_add_vec(m, at<double>(S, tb, r->t_load), rhs, st));
+    ++nl;
+  }
+  BcArgs bc{};
+  bc.n = n;
+  bc.nnz = r->nnz;
+  bc.b = b;
+  bc.rowptr = at<int>(S, pb, r->o_rowptr);
+  bc.colind = at<int>(S, pb, r->o_colind);
+  bc.flag = at<int>(S, tb, r->t_bc);
+  bc.diag = diag;
+  bc.offd = offd;
+  bc.res = rhs;
+  SCK(launch_bc(bc, st));
+  nl += 2;
+  // ILU(0): SetValue_Initialize (copy), then the levels
+  double* fd = at<double>(S, tb, r->t_fd);
+  double* fo = at<double>(S, tb, r->t_fo);
+  SCK(cudaMemcpyAsync(fd, diag, n * bs * 8, cudaMemcpyDeviceToDevice, st));
+  if (r->nnz) SCK(cudaMemcpyAsync(fo, offd, r->nnz * bs * 8, cudaMemcpyDeviceToDevice, st));
+  int* nsing = reinterpret_cast<int*>(S->d_adm + kRedGrid + 16);
+  SCK(cudaMemsetAsync(nsing, 0, sizeof(int), st));
+  const int nlev = (int)r->lev.ptr.size() - 1;
+  for (int l = 0; l < nlev; ++l)
+    SCK(launch_ilu_level(b, at<int>(S, tb, r->t_lev) + r->lev.ptr[l], r->lev.ptr[l + 1] - r->lev.ptr[l],
+                         bc.rowptr, bc.colind, at<int>(S, tb, r->t_dia), fd, fo, nsing, st));
+  nl += nlev;
+  // the factor into the step records
+  for (int dir = 0; dir < 2; ++dir) {
+    const SweepPlan& pl = dir == 0 ? r->pf : r->pb;
+    PackArgs pa{};
+    pa.nsteps = pl.nsteps;
+    pa.rec = at<unsigned char>(S, pb, dir == 0 ? r->o_recf : r->o_recb);
+    pa.rec_off = at<long long>(S, pb, dir == 0 ? r->o_offf : r->o_offb);
+    pa.ent_off = at<long long>(S, tb, dir == 0 ? r->t_eof : r->t_eob);
+    pa.ent_slot = at<int>(S, tb, dir == 0 ? r->t_esf : r->t_esb);
+    pa.step_rows = at<int>(S, tb, dir == 0 ? r->t_srf : r->t_srb);
+    pa.fdiag = fd;
+    pa.foffd = fo;
+    SCK(launch_pack(dir == 0, S->fp32, b, pa, st));
+    ++nl;
+  }
+  // PCG start: r = b, x = 0, rr0 = r.r
+  SCK(srv_init_vectors(m, rhs, at<double>(S, pb, r->o_r), at<double>(S, pb, r->o_x), at<double>(S, pb, r->o_p),
+                       at<void>(S, pb, r->o_y), at<void>(S, pb, r->o_z),
+                       S->fp32 ? at<float>(S, pb, r->o_r32) : nullptr, S->fp32, st));
+  Red red{S->d_adm, reinterpret_cast<unsigned*>(S->d_adm + kRedGrid), S->d_adm + kRedGrid + 8};
+  SCK(api_dot(m, rhs, rhs, red, st));
+  SCK(srv_init_state(at<PcgState>(S, pb, r->o_st), red.result, S->tol, S->maxit, st));
+  nl += 3;
+  SCK(cudaMemcpyAsync(S->h_nsing, nsing, sizeof(int), cudaMemcpyDeviceToHost, st));
+  SCK(cudaStreamSynchronize(st));
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->launches += nl;
+  }
+  return *S->h_nsing;
+}
+
+void finish_locked(dfg_server_s* S, Req* r) {
+  r->finished = true;
+  r->t_done = S->now();
+  // host set-up data is no longer needed
+  r->coords = {}; r->coef = {}; r->load = {}; r->conn = {}; r->bcflag = {};
+  r->rowptr = {}; r->colind = {}; r->diaind = {};
+  r->gm = GatherMap{}; r->lev = Levels{}; r->pf = SweepPlan{}; r->pb = SweepPlan{};
+  r->hf = {}; r->hb = {}; r->of = {}; r->ob = {};
+  ++S->n_finished;
+  S->cv_done.notify_all();
+}
+
+void release_locked(dfg_server_s* S, Req* r) {
+  if (r->have_p) S->arena.release(r->pbase, r->P.total);
+  if (r->have_t) S->arena.release(r->tbase, r->T.total);
+  const bool was_admitted = r->have_p;
+  r->have_p = r->have_t = false;
+  if (was_admitted) --S->inflight;
+  S->cv_adm.notify_all();
+}
+
+// ------------------------------------------------------------------ threads
+
+void symbolic_worker(dfg_server_s* S) {
+  for (;;) {
+    Req* r = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv_sym.wait(lk, [&] { return S->stopping || !S->submitted.empty(); });
+      if (S->submitted.empty()) return;
+      r = S->submitted.front();
+      S->submitted.pop_front();
+    }
+    bool ok = false;
+    try {
+      ok = symbolic(S, r);
+    } catch (const std::bad_alloc&) {
+      r->error = "host allocation failed during the symbolic set-up";
+    }
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (!ok) {
+      r->status = DFG_INVALID_ARGUMENT;
+      finish_locked(S, r);
+      continue;
+    }
+    if ((size_t)(r->P.total + r->T.total) > S->arena.capacity()) {
+      r->status = DFG_OOM_REJECTED;
+      r->error = "the request needs " + std::to_string(r->P.total + r->T.total) +
+                 " device bytes, more than the whole admission budget";
+      finish_locked(S, r);
+      continue;
+    }
+    S->ready[r->id] = r;
+    S->cv_adm.notify_all();
+  }
+}
+
+void admission_thread(dfg_server_s* S) {
+  cudaSetDevice(S->device);
+  for (;;) {
+    Req* r = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      for (;;) {
+        if (S->fatal != DFG_OK) {
+          // drain: everything not admitted fails with the fatal status
+          for (auto& kv : S->ready) {
+            kv.second->status = S->fatal;
+            kv.second->error = S->fatal_msg;
+            finish_locked(S, kv.second);
+          }
+          S->ready.clear();
+        }
+        if (S->adm_stop && S->ready.empty()) return;
+        if (!S->ready.empty() && S->inflight < S->max_inflight) {
+          Req* h = S->ready.begin()->second;  // lowest id first
+          size_t po = 0, to = 0;
+          if (S->arena.alloc(h->P.total, &po)) {
+            if (S->arena.alloc(h->T.total, &to)) {
+              h->pbase = po;
+              h->tbase = to;
+              h->have_p = h->have_t = true;
+              S->ready.erase(S->ready.begin());
+              ++S->inflight;
+              S->peak_inflight = std::max<long long>(S->peak_inflight, S->inflight);
+              h->t_admit = S->now();
+              r = h;
+              break;
+            }
+            S->arena.release(po, h->P.total);
+          }
+        }
+        S->cv_adm.wait(lk);
+      }
+    }
+    int nsing = 0;
+    try {
+      nsing = admit_device(S, r);
+    } catch (const CudaFail& f) {
+      cudaGetLastError();
+      std::lock_guard<std::mutex> lk(S->mu);
+      r->status = DFG_CUDA_ERROR;
+      r->error = std::string("admission: ") + cudaGetErrorString(f.e) + " at " + f.what;
+      release_locked(S, r);
+      finish_locked(S, r);
+      continue;
+    }
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->arena.release(r->tbase, r->T.total);
+    r->have_t = false;
+    if (nsing > 10) {
+      r->status = DFG_SINGULAR_PIVOT;
+      r->error = "ILU(0): " + std::to_string(nsing) + " singular pivots (more than 10)";
+      release_locked(S, r);
+      finish_locked(S, r);
+      continue;
+    }
+    S->activated.push_back(r);
+    S->cv_loop.notify_all();
+  }
+}
+
+SrvSlot slot_of(dfg_server_s* S, Req* r) {
+  const size_t pb = r->pbase;
+  SrvSlot s{};
+  s.n = r->n;
+  s.b = r->b;
+  s.rowptr = at<int>(S, pb, r->o_rowptr);
+  s.colind = at<int>(S, pb, r->o_colind);
+  s.diag = at<double>(S, pb, r->o_diag);
+  s.offd = at<double>(S, pb, r->o_offd);
+  s.rhs = at<double>(S, pb, r->o_rhs);
+  s.r = at<double>(S, pb, r->o_r);
+  s.x = at<double>(S, pb, r->o_x);
+  s.p = at<double>(S, pb, r->o_p);
+  s.q = at<double>(S, pb, r->o_q);
+  s.rd = at<double>(S, pb, r->o_rd);
+  s.y = at<void>(S, pb, r->o_y);
+  s.z = at<void>(S, pb, r->o_z);
+  s.r32 = S->fp32 ? at<float>(S, pb, r->o_r32) : nullptr;
+  s.st = at<PcgState>(S, pb, r->o_st);
+  s.cnt = at<unsigned>(S, pb, r->o_cnt);
+  return s;
+}
+
+// Rebuilds the pinned table mirrors from the active slots and uploads them;
+// returns the mask of sweep classes present.
+int upload_table(dfg_server_s* S, const std::vector<Req*>& act) {
+  SrvTable* T = S->h_tab;
+  T->nslots = (int)act.size();
+  int c = 0;
+  for (int i = 0; i < (int)act.size(); ++i) {
+    SrvSlot s = slot_of(S, act[i]);
+    s.chunk0 = c;
+    s.nchunks = (act[i]->n + kSrvRows - 1) / kSrvRows;
+    T->chunk_start[i] = c;
+    T->slot[i] = s;
+    c += s.nchunks;
+  }
+  T->chunk_start[act.size()] = c;
+  T->total_chunks = c;
+  int mask = 0;
+  for (int k = 0; k < kClasses; ++k)
+    for (int dir = 0; dir < 2; ++dir) S->h_sb[k * 2 + dir].nslots = 0;
+  for (int i = 0; i < (int)act.size(); ++i) {
+    Req* r = act[i];
+    mask |= 1 << r->cls;
+    for (int dir = 0; dir < 2; ++dir) {
+      SweepBatch& B = S->h_sb[r->cls * 2 + dir];
+      const int j = B.nslots++;
+      const SweepPlan& pl = dir == 0 ? r->pf : r->pb;
+      SweepSlot& w = B.slot[j];
+      w.rec = at<unsigned char>(S, r->pbase, dir == 0 ? r->o_recf : r->o_recb);
+      w.rec_off = at<long long>(S, r->pbase, dir == 0 ? r->o_offf : r->o_offb);
+      w.range_steps = at<int>(S, r->pbase, dir == 0 ? r->o_rsf : r->o_rsb);
+      const SrvSlot& s = T->slot[i];
+      w.in = dir == 0 ? (S->fp32 ? (const void*)s.r32 : (const void*)s.r) : s.y;
+      w.out = dir == 0 ? s.y : s.z;
+      w.done = &s.st->done;
+      B.range_start[j + 1] = (j == 0 ? 0 : B.range_start[j]) + pl.nranges;
+      B.range_start[0] = 0;
+    }
+  }
+  // only the used prefix of each structure travels
+  const size_t tab_bytes = offsetof(SrvTable, slot) + sizeof(SrvSlot) * std::max<size_t>(act.size(), 1);
+  SCK(cudaMemcpyAsync(S->d_tab, S->h_tab, tab_bytes, cudaMemcpyHostToDevice, S->s_iter));
+  SCK(cudaMemcpyAsync(S->d_sb, S->h_sb, sizeof(SweepBatch) * kClasses * 2, cudaMemcpyHostToDevice, S->s_iter));
+  return mask;
+}
+
+SweepArgs class_args(dfg_server_s* S, int k, int dir) {
+  SweepArgs a{};
+  a.batch = S->d_sb + k * 2 + dir;
+  a.ticket = S->d_tickets + k * 2 + dir;
+  a.err = reinterpret_cast<int*>(S->d_stat + sizeof(SrvStatus) * kSrvMaxSlots);
+  a.rec_stage = S->cls_rec_stage[k][dir];
+  a.val_stage = S->cls_val_stage[k];
+  a.R = kRingSteps;
+  a.NS = S->cls_ns[k][dir];
+  a.max_nent = class_maxe(k);
+  return a;
+}
+
+// Captures `chunk` iterations of every class in `mask` plus the stop checks
+// and the status copy.
+void build_graph(dfg_server_s* S, int mask) {
+  if (S->exec) {
+    cudaGraphExecDestroy(S->exec);
+    S->exec = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  SCK(cudaStreamBeginCapture(S->s_iter, cudaStreamCaptureModeThreadLocal));
+  const int grid = S->vec_grid;
+  for (int it = 0; it < S->chunk; ++it) {
+    SCK(cudaEventRecord(S->ev_fork, S->s_iter));
+    for (int k = 0; k < kClasses; ++k) {
+      if (!(mask >> k & 1)) continue;
+      SCK(cudaStreamWaitEvent(S->s_side[k], S->ev_fork, 0));
+      for (int dir = 0; dir < 2; ++dir)
+        SCK(launch_sweep(dir == 0, S->fp32, class_b(k), class_args(S, k, dir), S->cls_grid[k], S->cls_smem[k][dir],
+                         S->s_side[k]));
+      SCK(cudaEventRecord(S->ev_join[k], S->s_side[k]));
+      SCK(cudaStreamWaitEvent(S->s_iter, S->ev_join[k], 0));
+    }
+    SCK(srv_rz_beta(S->d_tab, S->d_partials, S->d_tickets, kClasses * 2, S->fp32, grid, S->s_iter));
+    SCK(srv_update_p(S->d_tab, S->fp32, grid, S->s_iter));
+    SCK(srv_spmv_pap(S->d_tab, S->d_partials, grid, S->s_iter));
+    SCK(srv_update_rx(S->d_tab, S->d_partials, S->fp32, grid, S->s_iter));
+  }
+  SCK(srv_check_true(S->d_tab, S->d_partials, grid, S->s_iter));
+  SCK(srv_replace(S->d_tab, S->d_partials, S->fp32, grid, S->s_iter));
+  SCK(srv_collect(S->d_tab, reinterpret_cast<SrvStatus*>(S->d_stat), S->s_iter));
+  SCK(cudaMemcpyAsync(S->h_stat, S->d_stat, sizeof(SrvStatus) * kSrvMaxSlots + 16, cudaMemcpyDeviceToHost,
+                      S->s_iter));
+  SCK(cudaStreamEndCapture(S->s_iter, &g));
+  const cudaError_t e = cudaGraphInstantiate(&S->exec, g, 0);
+  cudaGraphDestroy(g);
+  SCK(e);
+  S->graph_mask = mask;
+  ++S->graph_builds;
+}
+
+int kernels_per_replay(dfg_server_s* S) {
+  int nc = 0;
+  for (int k = 0; k < kClasses; ++k) nc += (S->graph_mask >> k) & 1;
+  return S->chunk * (2 * nc + 4) + 3;
+}
+
+void loop_thread(dfg_server_s* S) {
+  cudaSetDevice(S->device);
+  std::vector<Req*> act, retiring;
+  bool changed = false;
+  try {
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(S->mu);
+        S->cv_loop.wait(lk, [&] { return !S->activated.empty() || !act.empty() || !retiring.empty() || S->loop_stop; });
+        if (act.empty() && retiring.empty() && S->activated.empty() && S->loop_stop) return;
+        while (!S->activated.empty() && (int)act.size() < kSrvMaxSlots) {
+          act.push_back(S->activated.front());
+          S->activated.pop_front();
+          changed = true;
+        }
+      }
+      if (act.empty()) {
+        // only retirements left
+      } else {
+        const auto tb = Clock::now();
+        if (changed) {
+          const int mask = upload_table(S, act);
+          if (mask != S->graph_mask) build_graph(S, mask);
+          changed = false;
+        }
+        SCK(cudaGraphLaunch(S->exec, S->s_iter));
+        {
+          std::lock_guard<std::mutex> lk(S->mu);
+          ++S->replays;
+          S->launches += kernels_per_replay(S);
+        }
+        // solutions of the slots retired by the previous replay go out while this one runs
+        for (Req* r : retiring)
+          SCK(cudaMemcpyAsync(r->x_out, at<double>(S, r->pbase, r->o_x), (size_t)r->n * r->b * 8,
+                              cudaMemcpyDeviceToHost, S->s_copy));
+        SCK(cudaStreamSynchronize(S->s_copy));
+        {
+          std::lock_guard<std::mutex> lk(S->mu);
+          for (Req* r : retiring) {
+            release_locked(S, r);
+            finish_locked(S, r);
+          }
+        }
+        retiring.clear();
+        SCK(cudaStreamSynchronize(S->s_iter));
+        S->busy_s += std::chrono::duration<double>(Clock::now() - tb).count();
+        const int err = *reinterpret_cast<int*>(S->h_stat + sizeof(SrvStatus) * kSrvMaxSlots);
+        const SrvStatus* stv = reinterpret_cast<const SrvStatus*>(S->h_stat);
+        std::vector<Req*> keep;
+        for (int i = 0; i < (int)act.size(); ++i) {
+          Req* r = act[i];
+          const SrvStatus& s = stv[i];
+          const bool fin = err != 0 || (s.done != 0 && s.done != 6 && (s.done != 1 || s.verified));
+          if (!fin) {
+            keep.push_back(r);
+            continue;
+          }
+          r->iters = s.iter_out;
+          r->conv = s.conv;
+          r->rel_true = s.rel_true;
+          if (err != 0) {
+            r->status = DFG_TIMEOUT;
+            r->error = "a triangular-sweep wait timed out";
+          } else if (s.done == 1) {
+            r->status = DFG_OK;
+          } else if (s.done == 3) {
+            r->status = DFG_NAN_DETECTED;
+          } else {
+            r->status = DFG_NOT_CONVERGED;
+          }
+          retiring.push_back(r);
+          changed = true;
+        }
+        act.swap(keep);
+        if (err != 0) {
+          SCK(cudaMemsetAsync(S->d_stat + sizeof(SrvStatus) * kSrvMaxSlots, 0, 16, S->s_iter));
+          SCK(cudaMemsetAsync(S->d_tickets, 0, sizeof(int) * kClasses * 2, S->s_iter));
+          SCK(cudaStreamSynchronize(S->s_iter));
+        }
+      }
+      if (act.empty() && !retiring.empty()) {
+        for (Req* r : retiring)
+          SCK(cudaMemcpyAsync(r->x_out, at<double>(S, r->pbase, r->o_x), (size_t)r->n * r->b * 8,
+                              cudaMemcpyDeviceToHost, S->s_copy));
+        SCK(cudaStreamSynchronize(S->s_copy));
+        std::lock_guard<std::mutex> lk(S->mu);
+        for (Req* r : retiring) {
+          release_locked(S, r);
+          finish_locked(S, r);
+        }
+        retiring.clear();
+      }
+    }
+  } catch (const CudaFail& f) {
+    cudaGetLastError();
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->fatal = DFG_CUDA_ERROR;
+    S->fatal_msg = std::string("serving loop: ") + cudaGetErrorString(f.e) + " at " + f.what;
+    for (Req* r : act) { r->status = S->fatal; r->error = S->fatal_msg; finish_locked(S, r); }
+    for (Req* r : retiring) { r->status = S->fatal; r->error = S->fatal_msg; finish_locked(S, r); }
+    for (Req* r : S->activated) { r->status = S->fatal; r->error = S->fatal_msg; finish_locked(S, r); }
+    S->activated.clear();
+    S->cv_adm.notify_all();
+  }
+}
+
+void class_shapes(dfg_server_s* S) {
+  const int elem = S->fp32 ? 4 : 8;
+  int per_sm_bytes = 0;
+  cudaDeviceGetAttribute(&per_sm_bytes, cudaDevAttrMaxSharedMemoryPerMultiprocessor, S->device);
+  const size_t budget = std::min<size_t>(S->ctx->smem_optin, 200 * 1024);
+  for (int k = 0; k < kClasses; ++k) {
+    const int b = class_b(k), maxe = class_maxe(k);
+    S->cls_val_stage[k] = sweep_val_stage(maxe, b, elem);
+    size_t worst = 0;
+    for (int dir = 0; dir < 2; ++dir) {
+      const int rs = (int)((rec_bytes(maxe, b * b, elem, dir == 0) + 15) / 16 * 16);
+      int NS = 16;
+      while (NS > 2 && sweep_smem_bytes(NS, rs, S->cls_val_stage[k], kRingSteps, b, elem) > budget) --NS;
+      S->cls_rec_stage[k][dir] = rs;
+      S->cls_ns[k][dir] = NS;
+      S->cls_smem[k][dir] = sweep_smem_bytes(NS, rs, S->cls_val_stage[k], kRingSteps, b, elem);
+      worst = std::max(worst, S->cls_smem[k][dir]);
+    }
+    const int per_sm = std::max(1, std::min(16, (int)(per_sm_bytes / (worst + 1024))));
+    S->cls_grid[k] = S->nsm * per_sm;
+  }
+}
+
+int server_error(dfg_ctx ctx, int status, const std::string& m) {
+  if (ctx) ctx->last_error = m;
+  return status;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+
+extern "C" int dfg_server_create(dfg_ctx ctx, const dfg_server_config* cfg, dfg_server* out) {
+  if (!ctx || !cfg || !out) return DFG_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (cfg->mode != DFG_PREC_FP64 && cfg->mode != DFG_PREC_FP32_FACTOR)
+    return server_error(ctx, DFG_INVALID_ARGUMENT, "serving modes: DFG_PREC_FP64 or DFG_PREC_FP32_FACTOR");
+  if (cfg->max_inflight < 0 || cfg->max_inflight > kSrvMaxSlots || cfg->chunk_iters < 0 || cfg->chunk_iters > 64 ||
+      !(cfg->tol > 0.0) || cfg->maxit < 0 || cfg->budget_bytes < 0)
+    return server_error(ctx, DFG_INVALID_ARGUMENT, "server configuration out of range");
+  std::unique_ptr<dfg_server_s> S(new (std::nothrow) dfg_server_s);
+  if (!S) return DFG_OOM_REJECTED;
+  S->ctx = ctx;
+  S->device = ctx->device;
+  S->nsm = ctx->nsm;
+  S->mode = cfg->mode;
+  S->fp32 = cfg->mode == DFG_PREC_FP32_FACTOR;
+  S->tol = cfg->tol;
+  S->maxit = cfg->maxit > 0 ? cfg->maxit : 20000;
+  S->max_inflight = cfg->max_inflight > 0 ? cfg->max_inflight : 128;
+  S->chunk = cfg->chunk_iters > 0 ? cfg->chunk_iters : 8;
+  const int hw = (int)std::thread::hardware_concurrency();
+  S->nthreads = cfg->host_threads > 0 ? cfg->host_threads : std::max(1, hw - 2);
+  S->vec_grid = S->nsm * 4;
+  S->t0 = Clock::now();
+  try {
+    SCK(cudaSetDevice(S->device));
+    size_t fre = 0, tot = 0;
+    SCK(cudaMemGetInfo(&fre, &tot));
+    size_t budget = cfg->budget_bytes > 0 ? (size_t)cfg->budget_bytes : (size_t)(fre * 0.85);
+    if (budget + (64u << 20) > fre)
+      return server_error(ctx, DFG_OOM_REJECTED,
+                          "admission budget of " + std::to_string(budget) + " bytes exceeds free device memory (" +
+                              std::to_string(fre) + ")");
+    SCK(cudaMalloc(&S->arena_base, budget));
+    S->arena.init(budget);
+    SCK(cudaMalloc(&S->d_tab, sizeof(SrvTable)));
+    SCK(cudaMalloc(&S->d_sb, sizeof(SweepBatch) * kClasses * 2));
+    SCK(cudaMalloc(&S->d_tickets, sizeof(int) * kClasses * 2));
+    SCK(cudaMalloc(&S->d_partials, sizeof(double) * kMaxChunks));
+    SCK(cudaMalloc(&S->d_stat, sizeof(SrvStatus) * kSrvMaxSlots + 64));
+    SCK(cudaMalloc(&S->d_adm, sizeof(double) * (kRedGrid + 32)));
+    SCK(cudaMemset(S->d_tickets, 0, sizeof(int) * kClasses * 2));
+    SCK(cudaMemset(S->d_stat, 0, sizeof(SrvStatus) * kSrvMaxSlots + 64));
+    SCK(cudaMemset(S->d_adm, 0, sizeof(double) * (kRedGrid + 32)));
+    SCK(cudaMemset(S->d_sb, 0, sizeof(SweepBatch) * kClasses * 2));
+    SCK(cudaHostAlloc(&S->h_tab, sizeof(SrvTable), cudaHostAllocDefault));
+    SCK(cudaHostAlloc(&S->h_sb, sizeof(SweepBatch) * kClasses * 2, cudaHostAllocDefault));
+    SCK(cudaHostAlloc(&S->h_stat, sizeof(SrvStatus) * kSrvMaxSlots + 64, cudaHostAllocDefault));
+    SCK(cudaHostAlloc(&S->h_nsing, 64, cudaHostAllocDefault));
+    std::memset(S->h_tab, 0, sizeof(SrvTable));
+    std::memset(S->h_sb, 0, sizeof(SweepBatch) * kClasses * 2);
+    std::memset(S->h_stat, 0, sizeof(SrvStatus) * kSrvMaxSlots + 64);
+    int lo = 0, hi = 0;
+    SCK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    SCK(cudaStreamCreateWithPriority(&S->s_iter, cudaStreamNonBlocking, hi));
+    SCK(cudaStreamCreateWithPriority(&S->s_adm, cudaStreamNonBlocking, lo));
+    SCK(cudaStreamCreateWithPriority(&S->s_copy, cudaStreamNonBlocking, lo));
+    for (int k = 0; k < kClasses; ++k) {
+      SCK(cudaStreamCreateWithPriority(&S->s_side[k], cudaStreamNonBlocking, hi));
+      SCK(cudaEventCreateWithFlags(&S->ev_join[k], cudaEventDisableTiming));
+    }
+    SCK(cudaEventCreateWithFlags(&S->ev_fork, cudaEventDisableTiming));
+    SCK(sweep_set_smem_limits(ctx->smem_optin));
+    class_shapes(S.get());
+  } catch (const CudaFail& f) {
+    cudaGetLastError();
+    const int st = f.e == cudaErrorMemoryAllocation ? DFG_OOM_REJECTED : DFG_CUDA_ERROR;
+    const std::string m = std::string("dfg_server_create: ") + cudaGetErrorString(f.e) + " at " + f.what;
+    dfg_server raw = S.release();
+    dfg_server_destroy(raw);
+    return server_error(ctx, st, m);
+  }
+  dfg_server s = S.release();
+  for (int i = 0; i < s->nthreads; ++i) s->workers.emplace_back(symbolic_worker, s);
+  s->adm_thread = std::thread(admission_thread, s);
+  s->loop_thread = std::thread(loop_thread, s);
+  *out = s;
+  return DFG_OK;
+}
+
+extern "C" int dfg_server_submit(dfg_server s, const dfg_request* q, long long* id) {
+  if (!s || !q || !id) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = s->ctx;
+  if (q->kind < 1 || q->kind > 5 || q->nnode <= 0 || q->nelem < 0 || !q->coords || (q->nelem > 0 && !q->conn) ||
+      !q->params || q->nparams < 0 || q->nparams > 8 || !q->bcflag || !q->x_out)
+    return server_error(ctx, DFG_INVALID_ARGUMENT, "dfg_server_submit: malformed request");
+  std::unique_ptr<Req> r(new (std::nothrow) Req);
+  if (!r) return DFG_OOM_REJECTED;
+  const bool three = q->kind == 2 || q->kind == 5;
+  r->kind = q->kind;
+  r->ndim = three ? 3 : 2;
+  r->nnoel = three ? 4 : 3;
+  r->b = q->kind == 4 ? 2 : q->kind == 5 ? 3 : 1;
+  r->n = q->nnode;
+  r->nelem = q->nelem;
+  const size_t m = (size_t)r->n * r->b;
+  try {
+    r->coords.assign(q->coords, q->coords + (size_t)r->n * r->ndim);
+    r->conn.assign(q->conn, q->conn + (size_t)r->nelem * r->nnoel);
+    if (q->coef) r->coef.assign(q->coef, q->coef + r->nelem);
+    r->params.assign(q->params, q->params + q->nparams);
+    r->bcflag.assign(q->bcflag, q->bcflag + m);
+    if (q->load) r->load.assign(q->load, q->load + m);
+  } catch (const std::bad_alloc&) {
+    return server_error(ctx, DFG_OOM_REJECTED, "dfg_server_submit: host allocation failed");
+  }
+  for (int v : r->conn)
+    if (v < 0 || v >= r->n) return server_error(ctx, DFG_INVALID_ARGUMENT, "dfg_server_submit: node index out of range");
+  r->x_out = q->x_out;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->stopping) return server_error(ctx, DFG_NOT_READY, "the server is shutting down");
+  r->id = s->next_id++;
+  r->t_submit = s->now();
+  *id = r->id;
+  Req* raw = r.get();
+  s->all[raw->id] = std::move(r);
+  ++s->n_submitted;
+  if (s->fatal != DFG_OK) {
+    raw->status = s->fatal;
+    raw->error = s->fatal_msg;
+    finish_locked(s, raw);
+    return DFG_OK;
+  }
+  s->submitted.push_back(raw);
+  s->cv_sym.notify_one();
+  return DFG_OK;
+}
+
+static void fill_result(const Req* r, dfg_result* out) {
+  out->id = r->id;
+  out->status = r->status;
+  out->iterations = r->iters;
+  out->conv = r->conv;
+  out->rel_true = r->rel_true;
+  out->t_submit = r->t_submit;
+  out->t_admit = r->t_admit;
+  out->t_done = r->t_done;
+  out->device_bytes = (long long)(r->P.total + r->T.total);
+}
+
+extern "C" int dfg_server_wait(dfg_server s, long long id, dfg_result* out) {
+  if (!s || !out) return DFG_INVALID_ARGUMENT;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->all.find(id);
+  if (it == s->all.end()) return server_error(s->ctx, DFG_INVALID_ARGUMENT, "unknown request id");
+  Req* r = it->second.get();
+  s->cv_done.wait(lk, [&] { return r->finished; });
+  fill_result(r, out);
+  return DFG_OK;
+}
+
+extern "C" int dfg_server_error_text(dfg_server s, long long id, char* buf, int len) {
+  if (!s || !buf || len <= 0) return DFG_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->all.find(id);
+  if (it == s->all.end()) return DFG_INVALID_ARGUMENT;
+  std::snprintf(buf, (size_t)len, "%s", it->second->error.c_str());
+  return DFG_OK;
+}
+
+extern "C" int dfg_server_drain(dfg_server s) {
+  if (!s) return DFG_INVALID_ARGUMENT;
+  std::unique_lock<std::mutex> lk(s->mu);
+  s->cv_done.wait(lk, [&] { return s->n_finished == s->n_submitted; });
+  return s->fatal;
+}
+
+extern "C" int dfg_server_stats(dfg_server s, dfg_server_counters* out) {
+  if (!s || !out) return DFG_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(s->mu);
+  out->submitted = s->n_submitted;
+  out->finished = s->n_finished;
+  out->replays = s->replays;
+  out->kernel_launches = s->launches;
+  out->graph_builds = s->graph_builds;
+  out->peak_inflight = s->peak_inflight;
+  out->budget_bytes = (long long)s->arena.capacity();
+  out->peak_bytes = (long long)s->arena.peak();
+  out->busy_seconds = s->busy_s;
+  out->now_seconds = s->now();
+  return DFG_OK;
+}
+
+extern "C" int dfg_server_destroy(dfg_server s) {
+  if (!s) return DFG_INVALID_ARGUMENT;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stopping = true;
+  }
+  s->cv_sym.notify_all();
+  s->cv_adm.notify_all();
+  s->cv_loop.notify_all();
+  for (auto& t : s->workers)
+    if (t.joinable()) t.join();
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->adm_stop = true;
+    s->cv_adm.notify_all();
+  }
+  if (s->adm_thread.joinable()) s->adm_thread.join();
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->loop_stop = true;
+    s->cv_loop.notify_all();
+  }
+  if (s->loop_thread.joinable()) s->loop_thread.join();
+  cudaSetDevice(s->device);
+  if (s->s_iter) cudaStreamSynchronize(s->s_iter);
+  if (s->exec) cudaGraphExecDestroy(s->exec);
+  for (int k = 0; k < kClasses; ++k) {
+    if (s->s_side[k]) cudaStreamDestroy(s->s_side[k]);
+    if (s->ev_join[k]) cudaEventDestroy(s->ev_join[k]);
+  }
+  if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+  for (cudaStream_t st : {s->s_iter, s->s_adm, s->s_copy})
+    if (st) cudaStreamDestroy(st);
+  for (void* p : {(void*)s->arena_base, (void*)s->d_tab, (void*)s->d_sb, (void*)s->d_tickets, (void*)s->d_partials,
+                  (void*)s->d_stat, (void*)s->d_adm})
+    if (p) cudaFree(p);
+  for (void* p : {(void*)s->h_tab, (void*)s->h_sb, (void*)s->h_stat, (void*)s->h_nsing})
+    if (p) cudaFreeHost(p);
+  delete s;
+  return DFG_OK;
+}

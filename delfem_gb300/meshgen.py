@@ -252,6 +252,141 @@ def diffusion2d_square(n: int = 32, seed: int = 5, rho: float = 1.0, alpha: floa
 
 
 # --------------------------------------------------------------------------
+# request streams of the serving workloads (seeded)
+# --------------------------------------------------------------------------
+
+SIDES_2D = ("left", "right", "bottom", "top")
+FACES_3D = ("x0", "x1", "y0", "y1", "z0", "z1")
+
+
+def _side_nodes_2d(nx: int, ny: int, side: str) -> np.ndarray:
+    """Node ids along one side of a tri_grid, in order along the side."""
+    if side == "left":
+        return np.arange(ny + 1) * (nx + 1)
+    if side == "right":
+        return np.arange(ny + 1) * (nx + 1) + nx
+    if side == "bottom":
+        return np.arange(nx + 1)
+    return ny * (nx + 1) + np.arange(nx + 1)
+
+
+def rect_problem_2d(kind: int, nnode: int, seed: int, coef_sigma: float = 0.5, jitter: float = 0.2,
+                    tol: float = 1e-8) -> Problem:
+    """One serving request: a jittered triangulated rectangle of about
+    ``nnode`` nodes (aspect ratio log-uniform in [1/4, 4], square cells),
+    Poisson (alpha=1, source=1, u=0 on the Dirichlet sides, unit outward flux on
+    the load side) or plane-strain elasticity (E=1, nu=0.3, clamped Dirichlet
+    sides, traction 1e-3 in a random direction on the load side); 1 to 3 random
+    Dirichlet sides, one load side among the rest; log-normal per-element
+    multiplier."""
+    rng = np.random.default_rng(seed)
+    aspect = float(np.exp(rng.uniform(np.log(0.25), np.log(4.0))))
+    ny = max(2, int(round(np.sqrt(nnode / aspect))) - 1)
+    nx = max(2, int(round(nnode / (ny + 1))) - 1)
+    coords, conn = tri_grid(nx, ny, nx / ny, 1.0, jitter, rng)
+    b = BLOCK[kind]
+    order = rng.permutation(4)
+    ndir = int(rng.integers(1, 4))
+    dsides = [SIDES_2D[k] for k in order[:ndir]]
+    lside = SIDES_2D[order[ndir]]
+    bc = np.zeros(coords.shape[0] * b, dtype=np.int32)
+    for sd in dsides:
+        nodes = _side_nodes_2d(nx, ny, sd)
+        for d in range(b):
+            bc[nodes * b + d] = 1
+    lnodes = _side_nodes_2d(nx, ny, lside)
+    coef = _lognormal(rng, conn.shape[0], coef_sigma) if coef_sigma > 0 else None
+    prm = np.zeros(8)
+    if kind == POISSON2D:
+        load = edge_traction(coords, lnodes, 1, (1.0,))
+        prm[0] = 1.0
+        prm[1] = 1.0
+    elif kind == SOLID2D:
+        ang = rng.uniform(0.0, 2.0 * np.pi)
+        load = edge_traction(coords, lnodes, 2, (1e-3 * np.cos(ang), 1e-3 * np.sin(ang)))
+        lam, myu = lame(1.0, 0.3)
+        prm[0] = lam
+        prm[1] = myu
+        prm[2] = 1.0
+    else:
+        raise ValueError("2D serving requests are Poisson or plane-strain elasticity")
+    load[bc != 0] = 0.0
+    return Problem(kind, coords, conn, prm, bc, coef=coef, load=load, tol=tol,
+                   name=f"{KIND_NAMES[kind]}_{nx}x{ny}")
+
+
+def box_problem_3d(kind: int, nx: int, ny: int, nz: int, seed: int, coef_sigma: float = 1.0,
+                   tol: float = 1e-8) -> Problem:
+    """One 3D serving request: an nx x ny x nz hex grid of unit cells split
+    into Kuhn tetrahedra; Poisson (alpha=1, source=1) or elasticity (E=1,
+    nu=0.3, body force -1e-3 along z); 1 to 3 random Dirichlet faces (u=0 /
+    clamped); log-normal per-element multiplier."""
+    rng = np.random.default_rng(seed)
+    coords, conn = tet_grid(nx, ny, nz, float(nx), float(ny), float(nz))
+    b = BLOCK[kind]
+    order = rng.permutation(6)
+    ndir = int(rng.integers(1, 4))
+    ext = (nx, ny, nz)
+    bcn = np.zeros(coords.shape[0], dtype=bool)
+    for f in order[:ndir]:
+        axis, hi = divmod(int(f), 2)
+        bcn |= coords[:, axis] == (float(ext[axis]) if hi else 0.0)
+    bc = np.repeat(bcn.astype(np.int32), b)
+    coef = _lognormal(rng, conn.shape[0], coef_sigma) if coef_sigma > 0 else None
+    prm = np.zeros(8)
+    if kind == POISSON3D:
+        prm[0] = 1.0
+        prm[1] = 1.0
+    elif kind == SOLID3D:
+        lam, myu = lame(1.0, 0.3)
+        prm[0] = lam
+        prm[1] = myu
+        prm[2] = 1.0
+        prm[5] = -1e-3
+    else:
+        raise ValueError("3D serving requests are Poisson or elasticity")
+    return Problem(kind, coords, conn, prm, bc, coef=coef, tol=tol, name=f"{KIND_NAMES[kind]}_{nx}x{ny}x{nz}")
+
+
+@dataclasses.dataclass
+class StreamItem:
+    arrival: float      # seconds after the stream starts
+    kind: int
+    size: tuple         # 2D: (target nodes,); 3D: (nx, ny, nz)
+    seed: int
+
+    def problem(self) -> Problem:
+        if len(self.size) == 1:
+            return rect_problem_2d(self.kind, self.size[0], self.seed)
+        return box_problem_3d(self.kind, *self.size, seed=self.seed)
+
+
+def serve_stream_2d(nreq: int = 2000, seed: int = 4, rate: float = 200.0, nmin: int = 2000,
+                    nmax: int = 400000) -> list[StreamItem]:
+    """Poisson arrivals at ``rate`` requests/s; 50/50 Poisson and plane-strain
+    elasticity; node counts log-uniform in [nmin, nmax]."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    sizes = np.exp(rng.uniform(np.log(nmin), np.log(nmax), nreq)).astype(int)
+    kinds = np.where(rng.random(nreq) < 0.5, POISSON2D, SOLID2D)
+    seeds = rng.integers(0, 2**31 - 1, nreq)
+    return [StreamItem(float(t[i]), int(kinds[i]), (int(sizes[i]),), int(seeds[i])) for i in range(nreq)]
+
+
+def serve_stream_3d(nreq: int = 500, seed: int = 5, rate: float = 50.0, emin: int = 16,
+                    emax: int = 80) -> list[StreamItem]:
+    """Poisson arrivals; 50/50 3D Poisson and 3D elasticity; hex-grid edge
+    counts per axis uniform in [emin, emax]."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    ext = rng.integers(emin, emax + 1, size=(nreq, 3))
+    kinds = np.where(rng.random(nreq) < 0.5, POISSON3D, SOLID3D)
+    seeds = rng.integers(0, 2**31 - 1, nreq)
+    return [StreamItem(float(t[i]), int(kinds[i]), tuple(int(v) for v in ext[i]), int(seeds[i]))
+            for i in range(nreq)]
+
+
+# --------------------------------------------------------------------------
 # problem file (read by oracle/ref_harness.cpp)
 # --------------------------------------------------------------------------
 

@@ -257,6 +257,84 @@ int dfg_profile_kernels(dfg_system sys, dfg_precond prec, int mode, int reps, do
  * b = the given host right-hand side and x = the update slot. */
 int dfg_true_residual(dfg_system sys, const double* b, double* rel);
 
+/* --------------------------------------------------------------- serving
+ *
+ * No counterpart in the reference (its solves run one at a time on the
+ * caller's thread).  A server keeps many independent FE solves resident on
+ * one device: requests are admitted first-come first-served as device memory
+ * (a fixed admission budget reserved at creation) and in-flight slots free
+ * up, assembled and factorised on a low-priority stream, and iterated
+ * together -- every replay of one captured CUDA graph runs `chunk_iters` PCG
+ * iterations of all in-flight solves through batched launches.  Each solve
+ * follows the reference path (AddLinSys_* -> FinalizeMarge -> ILU(0) ->
+ * Solve_PCG) and stops when its TRUE relative residual ||b-Ax||/||b|| is
+ * <= tol (the recursion continues from the true residual when they disagree).
+ * A solve's arithmetic does not depend on the other solves in flight: the
+ * same request gives the same bits alone and in any mix. */
+
+typedef struct dfg_server_s* dfg_server;
+
+typedef struct {
+  int mode;               /* DFG_PREC_FP64 or DFG_PREC_FP32_FACTOR */
+  double tol;             /* true relative residual target */
+  int maxit;              /* iteration limit per solve; 0 = 20000 */
+  long long budget_bytes; /* device bytes reserved for admitted solves; 0 = 85% of free memory */
+  int max_inflight;       /* solves resident at once, <= 256; 0 = 128 */
+  int chunk_iters;        /* PCG iterations per graph replay, <= 64; 0 = 8 */
+  int host_threads;       /* symbolic set-up threads; 0 = hardware threads - 2 */
+} dfg_server_config;
+
+/* kind: 1 Poisson 2D (P1 triangles), 2 Poisson 3D (P1 tetrahedra),
+ * 3 diffusion 2D, 4 linear solid 2D, 5 linear solid 3D.  params as the
+ * matching dfg_assemble_* takes them, in its argument order (Poisson: alpha,
+ * source; solid 2D: lambda, myu, rho, g_x, g_y; solid 3D: + g_z; diffusion:
+ * rho, alpha, source, gamma, dt).  Block length: 1, 1, 1, 2, 3. */
+typedef struct {
+  int kind;
+  int nnode, nelem;
+  const double* coords;   /* nnode x dim */
+  const int* conn;        /* nelem x (3 or 4) */
+  const double* coef;     /* per-element multiplier, or NULL */
+  const double* params;
+  int nparams;            /* <= 8 */
+  const int* bcflag;      /* per DOF: != 0 fixed at 0 */
+  const double* load;     /* per DOF nodal load added at FinalizeMarge, or NULL */
+  double* x_out;          /* host buffer, nnode x block length: the solution */
+} dfg_request;
+
+typedef struct {
+  long long id;
+  int status;             /* DFG_OK, DFG_NOT_CONVERGED, DFG_SINGULAR_PIVOT, DFG_NAN_DETECTED,
+                             DFG_OOM_REJECTED (larger than the whole budget), DFG_TIMEOUT, ... */
+  int iterations;         /* 0-based iteration of the stop, as Solve_PCG reports it */
+  double conv;            /* recursive residual ratio at the stop */
+  double rel_true;        /* ||b - A x|| / ||b|| of the returned x (-1 if not checked) */
+  double t_submit, t_admit, t_done;  /* seconds since the server was created */
+  long long device_bytes; /* device bytes the solve reserved while admitted */
+} dfg_result;
+
+typedef struct {
+  long long submitted, finished, replays, kernel_launches, graph_builds, peak_inflight;
+  long long budget_bytes, peak_bytes;
+  double busy_seconds;    /* loop-thread time with a replay in flight */
+  double now_seconds;     /* on the clock of dfg_result's times */
+} dfg_server_counters;
+
+/* Creates a server on the context's device (its own streams and threads). */
+int dfg_server_create(dfg_ctx ctx, const dfg_server_config* cfg, dfg_server* out);
+/* Queues one solve (all inputs copied; x_out is written before the request
+ * completes).  Thread-safe. */
+int dfg_server_submit(dfg_server s, const dfg_request* req, long long* id);
+/* Blocks until request `id` has completed and reports its outcome. */
+int dfg_server_wait(dfg_server s, long long id, dfg_result* out);
+/* Text of a failed request's error ("" when it succeeded). */
+int dfg_server_error_text(dfg_server s, long long id, char* buf, int len);
+/* Blocks until every submitted request has completed. */
+int dfg_server_drain(dfg_server s);
+int dfg_server_stats(dfg_server s, dfg_server_counters* out);
+/* Completes the requests in flight, then releases the server. */
+int dfg_server_destroy(dfg_server s);
+
 #ifdef __cplusplus
 }
 #endif
