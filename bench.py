@@ -1,27 +1,29 @@
 #!/usr/bin/env python
 """Throughput benchmark of the FE assembly + ILU(0)-PCG hot path on GB300.
 
-Workload (one "step" = one complete solve): the 2D plane-strain elasticity
-configuration -- 1000 x 500 cells, jittered P1 triangles (501,501 nodes,
-1,003,002 DOF, 2x2 block-CRS in FP64), E = 1 with a seeded log-normal
-(sigma 0.5) per-element multiplier, nu = 0.3, left edge clamped, downward
-traction 1e-3 on the right edge.  A step runs InitializeMarge ->
-AddLinSys_LinearSolid2D_Static -> FinalizeMarge (resident load + Dirichlet)
--> ILU(0) numeric factorisation -> PCG to a 1e-8 relative residual.
+Default workload (``--config serve2d``): the serving stream -- 2,000 solves
+arriving as a seeded Poisson process, 50/50 2D Poisson (1x1 blocks) and 2D
+plane-strain elasticity (2x2 blocks) on jittered triangulated rectangles,
+node counts log-uniform in [2k, 400k], log-normal (sigma 0.5) per-element
+coefficients, 1-3 random Dirichlet sides and one loaded side.  Every request
+runs AddLinSys_* -> FinalizeMarge -> ILU(0) -> PCG to a true relative residual
+<= 1e-8 inside the server (include/dfg.h, dfg_server_*), which admits requests
+by free device memory and iterates all in-flight solves together in batched
+launches replayed from one CUDA graph.  The W + K steps split the stream
+into equal consecutive segments: the first W are served as warm-up, the last
+K are served as one continuous timed stream (requests keep arriving while
+others run).  Arms: served FP32-factor mixed precision (``value``) and served
+plain FP64 (``plain_fp64``), on the same stream.  Requests come from host
+memory and solutions return to host memory, so ``value`` is end to end
+(``e2e`` repeats it with the bytes moved).  Timing is the host clock around
+the timed stream with the device synchronised at both ends (the server runs
+several streams and threads); per-kernel device times come from CUDA events
+inside profiled graph replays.
 
-Three GPU arms solve the same inputs to the same stopping rule (true relative
-residual ||b - A x|| / ||b|| <= 1e-8):
-  * plain FP64 ILU(0)-PCG (``plain_fp64``);
-  * mixed, FP32 factor: FP32 ILU factor and triangular sweeps, FP64 SpMV,
-    vectors and reductions (``mixed_fp32_factor``);
-  * mixed, all FP32: FP32 factor, sweeps, SpMV and Krylov vectors inside FP64
-    refinement with FP64 reductions and solution (``mixed_fp32_all``).
-``value`` is the faster of the two mixed forms (named in config.mixed_form).  Inputs (mesh,
-coefficients, loads) are resident in HBM for ``value``; ``e2e`` repeats the
-step through the C ABI with the per-solve inputs (element coefficients and
-nodal loads) copied in from pinned host memory and the solution copied back.
-The matrix (112 MB), factor records and vectors exceed the 129 MB L2, so no
-separate L2 flush is needed.
+``--config serve3d``: the 3D stream (500 solves, 3D Poisson / elasticity on
+hex grids of 16-80 cells per axis, sigma 1.0, admission budget 120 GB).
+Single-solve configurations (``solid2d_1000x500`` and smaller) time one
+complete solve per step with three precision arms.
 
 ``--impl reference`` times the reference's CPU algorithm (the oracle's
 bit-exact restatement) on all host cores instead.
@@ -42,6 +44,8 @@ sys.path.insert(0, ROOT)
 METRIC = "PCG solves/s at 1e-8 rel. residual, served mixed vs plain FP64 GPU; p50/p99 ms"
 CONFIGS = {
     # name -> (meshgen factory kwargs, description)
+    "serve2d": dict(kind="serve", dim=2, nreq=2000, seed=4, rate=50.0, budget=0),
+    "serve3d": dict(kind="serve", dim=3, nreq=500, seed=5, rate=10.0, budget=120 * 10**9),
     "solid2d_1000x500": dict(kind="solid2d", nx=1000, ny=500),
     "poisson2d_128": dict(kind="poisson2d", n=128),
     "solid3d_96": dict(kind="solid3d", n=96),
@@ -405,12 +409,267 @@ def compose_line(args, world, p, results, prof, e2e, head):
     return line
 
 
+# ------------------------------------------------------------- serving arm
+
+SERVE_ARMS = [("plain_fp64", "fp64"), ("mixed_fp32_factor", "fp32f")]
+
+
+def serve_stream(name):
+    from delfem_gb300 import meshgen as mg
+    c = CONFIGS[name]
+    if c["dim"] == 2:
+        return mg.serve_stream_2d(nreq=c["nreq"], seed=c["seed"], rate=c["rate"])
+    return mg.serve_stream_3d(nreq=c["nreq"], seed=c["seed"], rate=c["rate"])
+
+
+def gen_problems(items, threads=8):
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(threads) as ex:
+        return list(ex.map(lambda it: it.problem(), items))
+
+
+def serve_segment(S, items, probs, t_origin):
+    """Submits the requests at their arrival times (relative to the first),
+    returns the request ids in order."""
+    ids = []
+    a0 = items[0].arrival
+    t0 = time.perf_counter()
+    for it, p in zip(items, probs):
+        dt = (it.arrival - a0) - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        ids.append(S.submit(p))
+    return ids
+
+
+def run_serve(args, rank, world, local):
+    import numpy as np
+    from delfem_gb300 import build as B
+    B.build()
+    from delfem_gb300 import linsys as L
+    from delfem_gb300.serve import Server
+    try:
+        import torch
+    except Exception:
+        torch = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    cfg = CONFIGS[args.config]
+    items = serve_stream(args.config)
+    nseg = args.warmup + args.steps
+    seg = [items[(len(items) * k) // nseg:(len(items) * (k + 1)) // nseg] for k in range(nseg)]
+    warm_items = [it for sg in seg[:args.warmup] for it in sg]
+    timed_items = [it for sg in seg[args.warmup:] for it in sg]
+    t_gen = time.perf_counter()
+    warm_probs = gen_problems(warm_items)
+    timed_probs = gen_problems(timed_items)
+    t_gen = time.perf_counter() - t_gen
+    ctx = L.Context(local)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        ctx.synchronize()
+        if torch is not None:
+            torch.cuda.synchronize(local)
+
+    arms_run = [(a, m) for a, m in SERVE_ARMS if a in args.arms.split(",")]
+    results = {}
+    x_plain = {}
+    for arm, mode in arms_run:
+        with Server(ctx, mode=mode, budget_bytes=cfg["budget"], profile_every=16) as S:
+            wids = serve_segment(S, warm_items, warm_probs, 0.0)
+            for i in wids:
+                S.wait(i)
+                S.release(i)
+            st0 = S.stats()
+            prof0 = S.profile()
+            barrier()
+            with ClockSampler(local) as clk:
+                t0 = time.perf_counter()
+                ids = serve_segment(S, timed_items, timed_probs, t0)
+                S.drain()
+                barrier()
+                wall = time.perf_counter() - t0
+            st1 = S.stats()
+            res = [S.wait(i) for i in ids]
+            prof1 = S.profile()
+            bad = [r for r in res if r["status"] != 0]
+            if bad:
+                raise RuntimeError(f"{arm}: {len(bad)} requests failed, first: {bad[0]}")
+            err = []
+            for k, r in enumerate(res):
+                if arm == "plain_fp64":
+                    x_plain[k] = r["x"].copy()
+                elif k in x_plain:
+                    xp = x_plain[k]
+                    err.append(float(np.linalg.norm(r["x"] - xp) / max(np.linalg.norm(xp), 1e-300)))
+                S.release(r["id"])
+            prof = {}
+            for k, v in prof1.items():
+                v0 = prof0.get(k, {"n": 0, "ms": 0.0, "bytes": 0.0})
+                n = v["n"] - v0["n"]
+                if n <= 0:
+                    continue
+                ms = (v["ms"] * v["n"] - v0["ms"] * v0["n"]) / n
+                by = (v["bytes"] * v["n"] - v0["bytes"] * v0["n"]) / n
+                prof[k] = {"n": n, "ms": ms, "bytes": by}
+        lat = [r["t_done"] - r["t_submit"] for r in res]
+        svc = [r["t_done"] - r["t_admit"] for r in res]
+        results[arm] = dict(
+            mode=mode, wall=wall, n=len(res), lat=lat, svc=svc,
+            iters=[r["iterations"] for r in res], rel_true=max(r["rel_true"] for r in res),
+            launches=st1["kernel_launches"] - st0["kernel_launches"], replays=st1["replays"] - st0["replays"],
+            h2d=st1["h2d_bytes"] - st0["h2d_bytes"], d2h=st1["d2h_bytes"] - st0["d2h_bytes"],
+            peak_inflight=st1["peak_inflight"], peak_bytes=st1["peak_bytes"], budget=st1["budget_bytes"],
+            busy=st1["busy_seconds"] - st0["busy_seconds"], prof=prof, clocks=clk.summary(),
+            err_vs_plain=(max(err) if err else None),
+            dof_iters=sum(p.ndof * (r["iterations"] + 1) for p, r in zip(timed_probs, res)))
+
+    def gmax(v):
+        if world > 1:
+            t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{local}")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            return float(t.item())
+        return v
+
+    for arm in results:
+        results[arm]["wall"] = gmax(results[arm]["wall"])
+    out = None
+    if rank == 0:
+        out = compose_serve_line(args, world, cfg, items, timed_items, timed_probs, results, t_gen)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return out
+
+
+def _cpu_serve_sample(args):
+    """Reference algorithm (oracle) on whole requests of the stream, in a
+    spawned process: returns the seconds each request took."""
+    name, idx = args
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    items = serve_stream(name)
+    out = []
+    for i in idx:
+        p = items[i].problem()
+        t0 = time.perf_counter()
+        r = O.solve(p)
+        out.append((i, time.perf_counter() - t0, int(r["iter"])))
+    return out
+
+
+def cpu_serve_rate(name, procs, per_proc, first=0):
+    """Solves/s of the reference algorithm on `procs` host cores, each solving
+    `per_proc` whole requests of the stream (requests first, first+1, ...)."""
+    import multiprocessing as mp
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    ctx = mp.get_context("spawn")
+    jobs = [(name, [first + k * procs + j for k in range(per_proc)]) for j in range(procs)]
+    t0 = time.perf_counter()
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_cpu_serve_sample, jobs)
+    wall = time.perf_counter() - t0
+    times = [t for r in res for _, t, _ in r]
+    return len(times) / max(sum(times), 1e-9) * procs, times, wall
+
+
+def compose_serve_line(args, world, cfg, items, timed_items, timed_probs, results, t_gen):
+    hbm_peak, peak_kind = load_peaks()
+    steps = args.steps
+
+    def arm_summary(arm):
+        r = results[arm]
+        value = r["n"] * world / r["wall"]
+        return {"value": round(value, 4), "unit": "solves/s",
+                "p50_ms": round(1e3 * _pct(r["lat"], 0.5), 1), "p99_ms": round(1e3 * _pct(r["lat"], 0.99), 1),
+                "service_p50_ms": round(1e3 * _pct(r["svc"], 0.5), 1),
+                "service_p99_ms": round(1e3 * _pct(r["svc"], 0.99), 1),
+                "dof_iterations_per_s": round(r["dof_iters"] * world / r["wall"], 1),
+                "iterations_median": int(_pct(r["iters"], 0.5)), "iterations_max": int(max(r["iters"])),
+                "max_true_rel_residual": r["rel_true"], "gpu_launches": int(r["launches"]),
+                "graph_replays": int(r["replays"]), "peak_inflight": int(r["peak_inflight"]),
+                "peak_device_bytes": int(r["peak_bytes"]),
+                "kernels": {k: {"ms": round(v["ms"], 4), "gbs": round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1)
+                                if v["bytes"] > 0 and v["ms"] > 0 else None}
+                            for k, v in sorted(r["prof"].items(), key=lambda kv: -kv[1]["ms"])}}
+
+    arms = {arm: arm_summary(arm) for arm in results}
+    head = "mixed_fp32_factor" if "mixed_fp32_factor" in results else next(iter(results))
+    hr = results[head]
+    prof = hr["prof"]
+    swept = {k: v for k, v in prof.items() if v["bytes"] > 0}
+    dom = max(swept, key=lambda k: swept[k]["ms"]) if swept else None
+    roof = None
+    if dom is not None:
+        v = swept[dom]
+        achieved = v["bytes"] / (v["ms"] * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                "frac": round(achieved / hbm_peak, 4), "traffic": ncu_traffic(dom), "peak_source": peak_kind,
+                "kernel": dom, "ms_per_launch": round(v["ms"], 4), "algorithmic_bytes": int(v["bytes"]),
+                "launches_timed": int(v["n"])}
+    value = arms[head]["value"]
+    plain = arms.get("plain_fp64")
+    nreq = len(timed_items)
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "solves/s",
+        "n_gpus": world,
+        "steps": steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(1e3 * hr["wall"] / steps, 1),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 factor/sweeps, f64 SpMV/vectors/reductions",
+        "data": "synthetic (seeded request stream: jittered meshes, log-normal coefficients)",
+        "config": {"workload": args.config, "requests": len(items), "requests_timed": nreq,
+                   "requests_per_step": round(nreq / steps, 1), "arrival_rate_per_s": cfg["rate"],
+                   "kinds": "2D Poisson / plane-strain elasticity 50:50" if cfg["dim"] == 2
+                   else "3D Poisson / elasticity 50:50",
+                   "dof_timed": int(sum(p.ndof for p in timed_probs)),
+                   "admission_budget_bytes": int(hr["budget"]), "tol": 1e-8,
+                   "stop": "true relative residual <= tol (every request, both arms)",
+                   "timing": "host clock around the timed stream, device synchronised at both ends",
+                   "l2": "in-flight working set (GBs of matrices, factors, vectors) far above the 129 MB L2; no flush",
+                   "parallelism": f"one server per GPU, x{world}", "generation_s": round(t_gen, 1)},
+        "p50_ms": arms[head]["p50_ms"],
+        "p99_ms": arms[head]["p99_ms"],
+        "plain_fp64": plain,
+        "mixed_fp32_factor": arms.get("mixed_fp32_factor"),
+        "mixed_over_plain": round(value / plain["value"], 3) if plain else None,
+        "error_vs_fp64_rel_l2_max": hr["err_vs_plain"],
+        "roofline": roof,
+        "gpu_launches": int(hr["launches"]),
+        "clocks": hr["clocks"],
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": int(hr["h2d"] / steps),
+                "d2h_bytes_per_step": int(hr["d2h"] / steps),
+                "note": "the served stream itself: requests from host memory, solutions to host memory"},
+    }
+    if not args.no_cpu_baseline:
+        rate, times, wall = cpu_serve_rate(args.config, 1, args.cpu_serve_requests)
+        line["cpu_baseline"] = {"value": round(rate, 4), "unit": "solves/s", "cores": 1, "kind": "port",
+                                "sample": f"the first {len(times)} requests of the stream solved whole (assembly, "
+                                          f"ILU(0), PCG to 1e-8) by the reference algorithm on one host core "
+                                          f"({sum(times):.1f} s)"}
+    return line
+
+
 # ---------------------------------------------------------- reference arm
 
 def run_reference(args, rank, world):
     if rank != 0:
         return None
     procs = os.cpu_count() or 1
+    if CONFIGS[args.config]["kind"] == "serve":
+        return run_reference_serve(args, world, procs)
     iters_full = REF_ITERS.get(args.config)
     if iters_full is None:
         iters_full = 3000
@@ -437,16 +696,48 @@ def run_reference(args, rank, world):
     }
 
 
+def run_reference_serve(args, world, procs):
+    """The reference algorithm serving the stream's requests on all host
+    cores: each step, every core solves `--ref-requests-per-core` whole
+    requests (consecutive requests of the stream, a new set per step)."""
+    per = args.ref_requests_per_core
+    rates = []
+    t_all0 = time.perf_counter()
+    for i in range(args.warmup + args.steps):
+        rate, times, wall = cpu_serve_rate(args.config, procs, per, first=i * procs * per)
+        if i >= args.warmup:
+            rates.append(rate)
+    value = statistics.median(rates)
+    return {
+        "metric": METRIC, "impl": "reference", "value": round(value, 4), "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded request stream)",
+        "config": {"workload": args.config, "tol": 1e-8,
+                   "parallelism": f"{procs} independent single-threaded solvers (one per host core)"},
+        "ms_per_step": round(1e3 * procs * per / value, 1),
+        "cpu_baseline": {"value": round(value, 4), "unit": "solves/s", "cores": procs, "kind": "port",
+                         "sample": f"per step {procs * per} whole requests of the stream ({per} per core), "
+                                   f"the reference algorithm's bit-exact C restatement; rate = cores x requests "
+                                   f"/ summed solve seconds"},
+        "e2e": {"value": round(value, 4), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": round(time.perf_counter() - t_all0, 1),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="solid2d_1000x500", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="serve2d", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-iters", type=int, default=60)
-    ap.add_argument("--arms", default=",".join(a for a, _ in ARMS),
+    ap.add_argument("--cpu-serve-requests", type=int, default=12,
+                    help="requests the one-core CPU baseline solves (serving configs)")
+    ap.add_argument("--ref-requests-per-core", type=int, default=2,
+                    help="requests per host core per step of --impl reference (serving configs)")
+    ap.add_argument("--arms", default=",".join(sorted({a for a, _ in ARMS + SERVE_ARMS})),
                     help="comma-separated GPU arms to run (profiling runs pick one)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -454,6 +745,8 @@ def main():
     rank, world, local = dist_env()
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif CONFIGS[args.config]["kind"] == "serve":
+        line = run_serve(args, rank, world, local)
     else:
         line = run_gpu(args, rank, world, local)
     if rank == 0 and line is not None:

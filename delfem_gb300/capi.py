@@ -96,13 +96,14 @@ SIGNATURES = {
     "dfg_server_drain": (_I, [_P]),
     "dfg_server_stats": (_I, [_P, _P]),
     "dfg_server_destroy": (_I, [_P]),
+    "dfg_server_profile": (_I, [_P, _P]),
 }
 
 
 class ServerConfig(ctypes.Structure):
     """dfg_server_config"""
     _fields_ = [("mode", _I), ("tol", _D), ("maxit", _I), ("budget_bytes", _LL), ("max_inflight", _I),
-                ("chunk_iters", _I), ("host_threads", _I)]
+                ("chunk_iters", _I), ("host_threads", _I), ("profile_every", _I)]
 
 
 class Request(ctypes.Structure):
@@ -121,7 +122,17 @@ class ServerCounters(ctypes.Structure):
     """dfg_server_counters"""
     _fields_ = [("submitted", _LL), ("finished", _LL), ("replays", _LL), ("kernel_launches", _LL),
                 ("graph_builds", _LL), ("peak_inflight", _LL), ("budget_bytes", _LL), ("peak_bytes", _LL),
-                ("busy_seconds", _D), ("now_seconds", _D)]
+                ("h2d_bytes", _LL), ("d2h_bytes", _LL), ("busy_seconds", _D), ("now_seconds", _D)]
+
+
+SERVER_NKERNELS = 24
+SERVER_KERNEL_NAMES = ["rz_beta", "update_p", "spmv_pap", "update_rx", "check_true", "replace"] + [
+    f"sweep_{d}_b{c // 3 + 1}_e{(4, 8, 16)[c % 3]}" for c in range(9) for d in ("fwd", "bwd")]
+
+
+class ServerProfile(ctypes.Structure):
+    """dfg_server_profile_t"""
+    _fields_ = [("ms", _D * SERVER_NKERNELS), ("bytes", _D * SERVER_NKERNELS), ("n", _LL * SERVER_NKERNELS)]
 
 
 DFG_DOT_NOALLOC_MAX_LEN = 33554432

@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <atomic>
 #include <condition_variable>
 #include <cstddef>
 #include <cstdio>
@@ -53,6 +54,7 @@ using Clock = std::chrono::steady_clock;
 constexpr int kClasses = 9;         // block size 1..3 x dependency entries <= 4, 8, 16
 constexpr int kMaxChunks = 1 << 20; // chunk space of one launch (kSrvRows rows each)
 constexpr int kRingSteps = 32;
+constexpr int kServeStages = 3;   // sweep pipeline depth in batched launches
 
 struct CudaFail {
   cudaError_t e;
@@ -145,6 +147,9 @@ struct Req {
   std::vector<long long> of, ob;
   long long maxrf = 0, maxrb = 0;
   int cls = -1, maxe = 0;
+  // algorithmic bytes of one launch of each batched kernel for this solve:
+  // 0 r.z, 1 p update, 2 SpMV, 3 r/x update, then forward and backward sweep
+  double alg[6] = {};
   // device memory plan (offsets into the persistent / transient blocks)
   Layout P, T;
   size_t o_rowptr, o_colind, o_diag, o_offd, o_rhs, o_r, o_x, o_p, o_q, o_rd, o_y, o_z, o_r32;
@@ -192,8 +197,14 @@ struct dfg_server_s {
   cudaStream_t s_iter = nullptr, s_adm = nullptr, s_copy = nullptr;
   cudaStream_t s_side[kClasses] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[kClasses] = {};
-  cudaGraphExec_t exec = nullptr;
+  cudaGraphExec_t exec = nullptr, exec_prof = nullptr;
   int graph_mask = -1;
+  // profiling of every profile_every-th replay (first iteration, per kernel)
+  int profile_every = 0;
+  cudaEvent_t ev_prof[2 * DFG_SERVER_NKERNELS] = {};
+  double prof_ms[DFG_SERVER_NKERNELS] = {}, prof_bytes[DFG_SERVER_NKERNELS] = {};
+  long long prof_n[DFG_SERVER_NKERNELS] = {};
+  std::atomic<long long> h2d{0}, d2h{0};
   // per-class sweep launch shape
   int cls_grid[kClasses] = {}, cls_ns[kClasses][2] = {}, cls_rec_stage[kClasses][2] = {}, cls_val_stage[kClasses] = {};
   size_t cls_smem[kClasses][2] = {};
@@ -257,6 +268,15 @@ bool symbolic(dfg_server_s* S, Req* r) {
   r->hb = pack_record_headers(r->pb, elem, r->ob, r->maxrb);
 
   const size_t m = (size_t)n * r->b, bs = (size_t)r->b * r->b, Z = (size_t)std::max<long long>(r->nnz, 1);
+  {
+    const double dm = (double)m, mat = (n + 1) * 4.0 + r->nnz * 4.0 + ((double)n + r->nnz) * bs * 8.0;
+    r->alg[0] = dm * (8 + elem);
+    r->alg[1] = dm * (16 + elem);
+    r->alg[2] = mat + dm * 16;
+    r->alg[3] = dm * (16 + 8 + 16 + 8 + 2 * elem + (S->fp32 ? 4 : 0));
+    r->alg[4] = (double)r->hf.size() + dm * 2 * elem;
+    r->alg[5] = (double)r->hb.size() + dm * 2 * elem;
+  }
   Layout& P = r->P;
   r->o_rowptr = P.add((n + 1) * 4);
   r->o_colind = P.add(Z * 4);
@@ -312,8 +332,9 @@ T* at(dfg_server_s* S, size_t base, size_t off) {
 
 template <class T>
 void up(dfg_server_s* S, size_t base, size_t off, const std::vector<T>& v) {
-  if (!v.empty())
-    SCK(cudaMemcpyAsync(at<T>(S, base, off), v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, S->s_adm));
+  if (v.empty()) return;
+  SCK(cudaMemcpyAsync(at<T>(S, base, off), v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, S->s_adm));
+  S->h2d += (long long)(v.size() * sizeof(T));
 }
 
 // Device work of one admission on s_adm; returns the ILU singular-pivot count.
@@ -646,42 +667,94 @@ SweepArgs class_args(dfg_server_s* S, int k, int dir) {
 }
 
 // Captures `chunk` iterations of every class in `mask` plus the stop checks
-// and the status copy.
-void build_graph(dfg_server_s* S, int mask) {
-  if (S->exec) {
-    cudaGraphExecDestroy(S->exec);
-    S->exec = nullptr;
-  }
+// and the status copy.  The profiled variant brackets each kernel of the
+// first iteration (and the stop checks) with timing events.
+cudaGraphExec_t capture_graph(dfg_server_s* S, int mask, bool prof) {
   cudaGraph_t g = nullptr;
+  auto mark = [&](int k, int edge, cudaStream_t st) {
+    if (prof) SCK(cudaEventRecordWithFlags(S->ev_prof[2 * k + edge], st, cudaEventRecordExternal));
+  };
   SCK(cudaStreamBeginCapture(S->s_iter, cudaStreamCaptureModeThreadLocal));
   const int grid = S->vec_grid;
   for (int it = 0; it < S->chunk; ++it) {
+    const bool pf = prof && it == 0;
+    auto mk = [&](int k, int edge, cudaStream_t st) {
+      if (pf) mark(k, edge, st);
+    };
     SCK(cudaEventRecord(S->ev_fork, S->s_iter));
     for (int k = 0; k < kClasses; ++k) {
       if (!(mask >> k & 1)) continue;
       SCK(cudaStreamWaitEvent(S->s_side[k], S->ev_fork, 0));
-      for (int dir = 0; dir < 2; ++dir)
+      for (int dir = 0; dir < 2; ++dir) {
+        mk(6 + 2 * k + dir, 0, S->s_side[k]);
         SCK(launch_sweep(dir == 0, S->fp32, class_b(k), class_args(S, k, dir), S->cls_grid[k], S->cls_smem[k][dir],
                          S->s_side[k]));
+        mk(6 + 2 * k + dir, 1, S->s_side[k]);
+      }
       SCK(cudaEventRecord(S->ev_join[k], S->s_side[k]));
       SCK(cudaStreamWaitEvent(S->s_iter, S->ev_join[k], 0));
     }
+    mk(0, 0, S->s_iter);
     SCK(srv_rz_beta(S->d_tab, S->d_partials, S->d_tickets, kClasses * 2, S->fp32, grid, S->s_iter));
+    mk(0, 1, S->s_iter);
+    mk(1, 0, S->s_iter);
     SCK(srv_update_p(S->d_tab, S->fp32, grid, S->s_iter));
+    mk(1, 1, S->s_iter);
+    mk(2, 0, S->s_iter);
     SCK(srv_spmv_pap(S->d_tab, S->d_partials, grid, S->s_iter));
+    mk(2, 1, S->s_iter);
+    mk(3, 0, S->s_iter);
     SCK(srv_update_rx(S->d_tab, S->d_partials, S->fp32, grid, S->s_iter));
+    mk(3, 1, S->s_iter);
   }
+  mark(4, 0, S->s_iter);
   SCK(srv_check_true(S->d_tab, S->d_partials, grid, S->s_iter));
+  mark(4, 1, S->s_iter);
+  mark(5, 0, S->s_iter);
   SCK(srv_replace(S->d_tab, S->d_partials, S->fp32, grid, S->s_iter));
+  mark(5, 1, S->s_iter);
   SCK(srv_collect(S->d_tab, reinterpret_cast<SrvStatus*>(S->d_stat), S->s_iter));
   SCK(cudaMemcpyAsync(S->h_stat, S->d_stat, sizeof(SrvStatus) * kSrvMaxSlots + 16, cudaMemcpyDeviceToHost,
                       S->s_iter));
   SCK(cudaStreamEndCapture(S->s_iter, &g));
-  const cudaError_t e = cudaGraphInstantiate(&S->exec, g, 0);
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
   cudaGraphDestroy(g);
   SCK(e);
+  return exec;
+}
+
+void build_graph(dfg_server_s* S, int mask) {
+  if (S->exec) cudaGraphExecDestroy(S->exec);
+  if (S->exec_prof) cudaGraphExecDestroy(S->exec_prof);
+  S->exec = S->exec_prof = nullptr;
+  S->exec = capture_graph(S, mask, false);
+  if (S->profile_every > 0) S->exec_prof = capture_graph(S, mask, true);
   S->graph_mask = mask;
   ++S->graph_builds;
+}
+
+// Adds a profiled replay's event durations and the algorithmic bytes of the
+// solves it ran (all slots in flight at its start) to the totals.
+void account_profile(dfg_server_s* S, const std::vector<Req*>& act) {
+  double bytes[DFG_SERVER_NKERNELS] = {};
+  for (const Req* r : act) {
+    for (int k = 0; k < 4; ++k) bytes[k] += r->alg[k];
+    bytes[6 + 2 * r->cls] += r->alg[4];
+    bytes[7 + 2 * r->cls] += r->alg[5];
+  }
+  std::lock_guard<std::mutex> lk(S->mu);
+  for (int k = 0; k < DFG_SERVER_NKERNELS; ++k) {
+    if (k >= 6 && !((S->graph_mask >> ((k - 6) / 2)) & 1)) continue;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, S->ev_prof[2 * k], S->ev_prof[2 * k + 1]) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    S->prof_ms[k] += ms;
+    S->prof_bytes[k] += bytes[k];
+    S->prof_n[k] += 1;
+  }
 }
 
 int kernels_per_replay(dfg_server_s* S) {
@@ -715,16 +788,19 @@ void loop_thread(dfg_server_s* S) {
           if (mask != S->graph_mask) build_graph(S, mask);
           changed = false;
         }
-        SCK(cudaGraphLaunch(S->exec, S->s_iter));
+        const bool prof = S->exec_prof && S->replays % S->profile_every == 0;
+        SCK(cudaGraphLaunch(prof ? S->exec_prof : S->exec, S->s_iter));
         {
           std::lock_guard<std::mutex> lk(S->mu);
           ++S->replays;
           S->launches += kernels_per_replay(S);
         }
         // solutions of the slots retired by the previous replay go out while this one runs
-        for (Req* r : retiring)
+        for (Req* r : retiring) {
           SCK(cudaMemcpyAsync(r->x_out, at<double>(S, r->pbase, r->o_x), (size_t)r->n * r->b * 8,
                               cudaMemcpyDeviceToHost, S->s_copy));
+          S->d2h += (long long)r->n * r->b * 8;
+        }
         SCK(cudaStreamSynchronize(S->s_copy));
         {
           std::lock_guard<std::mutex> lk(S->mu);
@@ -736,6 +812,7 @@ void loop_thread(dfg_server_s* S) {
         retiring.clear();
         SCK(cudaStreamSynchronize(S->s_iter));
         S->busy_s += std::chrono::duration<double>(Clock::now() - tb).count();
+        if (prof) account_profile(S, act);
         const int err = *reinterpret_cast<int*>(S->h_stat + sizeof(SrvStatus) * kSrvMaxSlots);
         const SrvStatus* stv = reinterpret_cast<const SrvStatus*>(S->h_stat);
         std::vector<Req*> keep;
@@ -771,9 +848,11 @@ void loop_thread(dfg_server_s* S) {
         }
       }
       if (act.empty() && !retiring.empty()) {
-        for (Req* r : retiring)
+        for (Req* r : retiring) {
           SCK(cudaMemcpyAsync(r->x_out, at<double>(S, r->pbase, r->o_x), (size_t)r->n * r->b * 8,
                               cudaMemcpyDeviceToHost, S->s_copy));
+          S->d2h += (long long)r->n * r->b * 8;
+        }
         SCK(cudaStreamSynchronize(S->s_copy));
         std::lock_guard<std::mutex> lk(S->mu);
         for (Req* r : retiring) {
@@ -796,22 +875,23 @@ void loop_thread(dfg_server_s* S) {
   }
 }
 
+// Sweep launch shape per class.  A batched sweep has many independent
+// ranges in flight, so it trades pipeline depth for CTAs: three stages per
+// CTA and as many CTAs per SM as shared memory allows (measured on GB300 over
+// 150-request streams: depth 3 beat depths 2 and 5-16 in both precisions).
 void class_shapes(dfg_server_s* S) {
   const int elem = S->fp32 ? 4 : 8;
   int per_sm_bytes = 0;
   cudaDeviceGetAttribute(&per_sm_bytes, cudaDevAttrMaxSharedMemoryPerMultiprocessor, S->device);
-  const size_t budget = std::min<size_t>(S->ctx->smem_optin, 200 * 1024);
   for (int k = 0; k < kClasses; ++k) {
     const int b = class_b(k), maxe = class_maxe(k);
     S->cls_val_stage[k] = sweep_val_stage(maxe, b, elem);
     size_t worst = 0;
     for (int dir = 0; dir < 2; ++dir) {
       const int rs = (int)((rec_bytes(maxe, b * b, elem, dir == 0) + 15) / 16 * 16);
-      int NS = 16;
-      while (NS > 2 && sweep_smem_bytes(NS, rs, S->cls_val_stage[k], kRingSteps, b, elem) > budget) --NS;
       S->cls_rec_stage[k][dir] = rs;
-      S->cls_ns[k][dir] = NS;
-      S->cls_smem[k][dir] = sweep_smem_bytes(NS, rs, S->cls_val_stage[k], kRingSteps, b, elem);
+      S->cls_ns[k][dir] = kServeStages;
+      S->cls_smem[k][dir] = sweep_smem_bytes(kServeStages, rs, S->cls_val_stage[k], kRingSteps, b, elem);
       worst = std::max(worst, S->cls_smem[k][dir]);
     }
     const int per_sm = std::max(1, std::min(16, (int)(per_sm_bytes / (worst + 1024))));
@@ -850,6 +930,7 @@ extern "C" int dfg_server_create(dfg_ctx ctx, const dfg_server_config* cfg, dfg_
   const int hw = (int)std::thread::hardware_concurrency();
   S->nthreads = cfg->host_threads > 0 ? cfg->host_threads : std::max(1, hw - 2);
   S->vec_grid = S->nsm * 4;
+  S->profile_every = std::max(0, cfg->profile_every);
   S->t0 = Clock::now();
   try {
     SCK(cudaSetDevice(S->device));
@@ -889,6 +970,8 @@ extern "C" int dfg_server_create(dfg_ctx ctx, const dfg_server_config* cfg, dfg_
       SCK(cudaEventCreateWithFlags(&S->ev_join[k], cudaEventDisableTiming));
     }
     SCK(cudaEventCreateWithFlags(&S->ev_fork, cudaEventDisableTiming));
+    if (S->profile_every > 0)
+      for (int k = 0; k < 2 * DFG_SERVER_NKERNELS; ++k) SCK(cudaEventCreate(&S->ev_prof[k]));
     SCK(sweep_set_smem_limits(ctx->smem_optin));
     class_shapes(S.get());
   } catch (const CudaFail& f) {
@@ -1005,8 +1088,21 @@ extern "C" int dfg_server_stats(dfg_server s, dfg_server_counters* out) {
   out->peak_inflight = s->peak_inflight;
   out->budget_bytes = (long long)s->arena.capacity();
   out->peak_bytes = (long long)s->arena.peak();
+  out->h2d_bytes = s->h2d.load();
+  out->d2h_bytes = s->d2h.load();
   out->busy_seconds = s->busy_s;
   out->now_seconds = s->now();
+  return DFG_OK;
+}
+
+extern "C" int dfg_server_profile(dfg_server s, dfg_server_profile_t* out) {
+  if (!s || !out) return DFG_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(s->mu);
+  for (int k = 0; k < DFG_SERVER_NKERNELS; ++k) {
+    out->ms[k] = s->prof_ms[k];
+    out->bytes[k] = s->prof_bytes[k];
+    out->n[k] = s->prof_n[k];
+  }
   return DFG_OK;
 }
 
@@ -1036,6 +1132,9 @@ extern "C" int dfg_server_destroy(dfg_server s) {
   cudaSetDevice(s->device);
   if (s->s_iter) cudaStreamSynchronize(s->s_iter);
   if (s->exec) cudaGraphExecDestroy(s->exec);
+  if (s->exec_prof) cudaGraphExecDestroy(s->exec_prof);
+  for (cudaEvent_t e : s->ev_prof)
+    if (e) cudaEventDestroy(e);
   for (int k = 0; k < kClasses; ++k) {
     if (s->s_side[k]) cudaStreamDestroy(s->s_side[k]);
     if (s->ev_join[k]) cudaEventDestroy(s->ev_join[k]);

@@ -166,11 +166,15 @@ def edge_traction(coords: np.ndarray, nodes: np.ndarray, b: int, traction) -> np
     (the load the dead code at eqnsys_solid.cpp:558-567 intended)."""
     f = np.zeros(coords.shape[0] * b)
     t = np.asarray(traction, dtype=np.float64)
-    for a, c in zip(nodes[:-1], nodes[1:]):
-        L = float(np.hypot(*(coords[c] - coords[a])))
-        for d in range(b):
-            f[a * b + d] += t[d] * L * 0.5
-            f[c * b + d] += t[d] * L * 0.5
+    nodes = np.asarray(nodes)
+    a, c = nodes[:-1], nodes[1:]
+    dxy = coords[c] - coords[a]
+    L = np.hypot(dxy[:, 0], dxy[:, 1])
+    # a node gets at most two edge halves; 0 + x + y is the same in either order
+    for d in range(b):
+        h = t[d] * L * 0.5
+        np.add.at(f, a * b + d, h)
+        np.add.at(f, c * b + d, h)
     return f
 
 

@@ -26,9 +26,10 @@ def _ptr(a):
 
 class Server:
     def __init__(self, ctx, mode: str = "fp32f", tol: float = 1e-8, maxit: int = 20000, budget_bytes: int = 0,
-                 max_inflight: int = 128, chunk_iters: int = 8, host_threads: int = 0):
+                 max_inflight: int = 128, chunk_iters: int = 8, host_threads: int = 0, profile_every: int = 0):
         self.ctx = ctx
-        cfg = capi.ServerConfig(MODES[mode], tol, maxit, budget_bytes, max_inflight, chunk_iters, host_threads)
+        cfg = capi.ServerConfig(MODES[mode], tol, maxit, budget_bytes, max_inflight, chunk_iters, host_threads,
+                                profile_every)
         h = ctypes.c_void_p()
         check(ctx.h, lib().dfg_server_create(ctx.h, ctypes.byref(cfg), ctypes.byref(h)), "dfg_server_create")
         self.h = h
@@ -76,6 +77,20 @@ class Server:
         c = capi.ServerCounters()
         check(self.ctx.h, lib().dfg_server_stats(self.h, ctypes.byref(c)), "dfg_server_stats")
         return {f: getattr(c, f) for f, _ in capi.ServerCounters._fields_}
+
+    def profile(self) -> dict:
+        """Per batched kernel: launches profiled, mean ms per launch, mean
+        algorithmic bytes per launch and the GB/s they imply."""
+        pr = capi.ServerProfile()
+        check(self.ctx.h, lib().dfg_server_profile(self.h, ctypes.byref(pr)), "dfg_server_profile")
+        out = {}
+        for k, name in enumerate(capi.SERVER_KERNEL_NAMES):
+            n = pr.n[k]
+            if n:
+                ms = pr.ms[k] / n
+                by = pr.bytes[k] / n
+                out[name] = {"n": n, "ms": ms, "bytes": by, "gbs": (by / (ms * 1e-3) / 1e9) if ms > 0 and by > 0 else None}
+        return out
 
     def close(self) -> None:
         if self.h:

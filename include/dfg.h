@@ -282,6 +282,7 @@ typedef struct {
   int max_inflight;       /* solves resident at once, <= 256; 0 = 128 */
   int chunk_iters;        /* PCG iterations per graph replay, <= 64; 0 = 8 */
   int host_threads;       /* symbolic set-up threads; 0 = hardware threads - 2 */
+  int profile_every;      /* every n-th replay times its first iteration per kernel; 0 = never */
 } dfg_server_config;
 
 /* kind: 1 Poisson 2D (P1 triangles), 2 Poisson 3D (P1 tetrahedra),
@@ -316,9 +317,26 @@ typedef struct {
 typedef struct {
   long long submitted, finished, replays, kernel_launches, graph_builds, peak_inflight;
   long long budget_bytes, peak_bytes;
+  long long h2d_bytes;    /* request data uploaded (inputs and derived set-up) */
+  long long d2h_bytes;    /* solutions copied back */
   double busy_seconds;    /* loop-thread time with a replay in flight */
   double now_seconds;     /* on the clock of dfg_result's times */
 } dfg_server_counters;
+
+/* Per-kernel timing of profiled replays (dfg_server_config::profile_every):
+ * for kernel k, ms[k] sums the CUDA-event durations of its launches and
+ * bytes[k] their algorithmic bytes (the solves in flight at that launch),
+ * over n[k] launches.  k: 0 r.z + beta, 1 p update, 2 SpMV + p.Ap,
+ * 3 r/x update + r.r, 4 true-residual check, 5 residual replacement,
+ * 6 + 2*c forward sweep of class c, 7 + 2*c backward sweep of class c, where
+ * class c holds block length c/3 + 1 and at most 4, 8 or 16 (c % 3)
+ * dependency entries per row. */
+#define DFG_SERVER_NKERNELS 24
+typedef struct {
+  double ms[DFG_SERVER_NKERNELS];
+  double bytes[DFG_SERVER_NKERNELS];
+  long long n[DFG_SERVER_NKERNELS];
+} dfg_server_profile_t;
 
 /* Creates a server on the context's device (its own streams and threads). */
 int dfg_server_create(dfg_ctx ctx, const dfg_server_config* cfg, dfg_server* out);
@@ -332,6 +350,7 @@ int dfg_server_error_text(dfg_server s, long long id, char* buf, int len);
 /* Blocks until every submitted request has completed. */
 int dfg_server_drain(dfg_server s);
 int dfg_server_stats(dfg_server s, dfg_server_counters* out);
+int dfg_server_profile(dfg_server s, dfg_server_profile_t* out);
 /* Completes the requests in flight, then releases the server. */
 int dfg_server_destroy(dfg_server s);
 
