@@ -74,8 +74,13 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // error word shared by all kernels of a context (0 = ok)
 enum : int { kErrNone = 0, kErrTimeout = 1, kErrBadIndex = 2 };
 
-// Device-side spin budget: a wait gives up after this many polls, records
-// kErrTimeout and lets every other waiter of the launch leave too.
-constexpr long long kSpinLimit = 1ll << 24;
+// Device-side wait budget: a wait gives up after this many SM clock cycles
+// (about two seconds at 2 GHz), records kErrTimeout with where it happened,
+// and every other waiter of the launch leaves as soon as it sees the record.
+constexpr long long kWaitCycles = 4000000000ll;
+// Bound on waiting for a copy already in flight before a failing CTA leaves.
+constexpr long long kDrainCycles = 2000000ll;
+// wait sites recorded with a timeout (error word [1])
+enum : int { kSiteEmpty = 1, kSiteRecLoad = 2, kSitePoll = 3, kSiteRecCompute = 4, kSiteFull = 5, kSiteRange = 6 };
 
 }  // namespace dfg

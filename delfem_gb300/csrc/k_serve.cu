@@ -3,7 +3,8 @@
 //
 // Each launch walks a global chunk space: chunk c belongs to the slot s with
 // chunk_start[s] <= c < chunk_start[s+1] and covers kSrvRows block rows of
-// it.  Blocks loop over chunks (fixed grid), so a launch's shape does not
+// it (vector kernels: a thread per element; SpMV: lane groups per row, see
+// row_mv_warp).  Blocks loop over chunks (fixed grid), so a launch's shape does not
 // depend on the slots in flight and one captured graph serves every mix.
 // A slot whose state says `done` is skipped.
 //
@@ -19,6 +20,8 @@
 #include "dfg_common.cuh"
 #include "k_rowmv.cuh"
 #include "k_serve.h"
+
+static_assert(dfg::kSrvTpb <= 1024 && dfg::kSrvTpb % 32 == 0, "batched kernels: block size");
 
 namespace dfg {
 
@@ -88,33 +91,55 @@ __device__ __forceinline__ void chunk_elems(const SrvSlot& S, int c, long long& 
   e1 = row1 * S.b;
 }
 
-// q_i = (A p)_i; returns p_i . q_i
+// q = A p over rows [row0, row1) of one chunk (warp-cooperative rows);
+// returns this thread's share of p.q
 template <int B>
-__device__ __forceinline__ double row_q_pap(const SrvSlot& S, int i) {
-  double y[B];
-  row_mv<double, double, B>(i, S.rowptr, S.colind, S.diag, S.offd, S.p, y);
+__device__ __forceinline__ double chunk_q_pap(const SrvSlot& S, int row0, int row1) {
+  constexpr int RPW = RowLanes<B>::RPW;
+  int g, sub;
+  row_lane<B>(threadIdx.x & 31, g, sub);
+  bool writer;
+  const int comp = row_comp<B>(sub, writer);
+  const int warp = threadIdx.x >> 5, nw = kSrvTpb / 32;
   double part = 0.0;
-#pragma unroll
-  for (int d = 0; d < B; ++d) {
-    S.q[(size_t)i * B + d] = y[d];
-    part += S.p[(size_t)i * B + d] * y[d];
+  for (int r = row0 + warp * RPW; r < row1; r += nw * RPW) {
+    const int i = r + g;
+    const bool valid = g < RPW && i < row1;
+    const double y = row_mv_warp<double, B>(valid ? i : -1, sub, S.rowptr, S.colind, S.diag, S.offd, S.p);
+    if (valid && writer) {
+      S.q[(size_t)i * B + comp] = y;
+      part += S.p[(size_t)i * B + comp] * y;
+    }
   }
   return part;
 }
 
-// rd_i = b_i - (A x)_i; returns rd_i . rd_i
+// rd = b - A x over one chunk; returns this thread's share of rd.rd
 template <int B>
-__device__ __forceinline__ double row_true_res(const SrvSlot& S, int i) {
-  double y[B];
-  row_mv<double, double, B>(i, S.rowptr, S.colind, S.diag, S.offd, S.x, y);
+__device__ __forceinline__ double chunk_true_res(const SrvSlot& S, int row0, int row1) {
+  constexpr int RPW = RowLanes<B>::RPW;
+  int g, sub;
+  row_lane<B>(threadIdx.x & 31, g, sub);
+  bool writer;
+  const int comp = row_comp<B>(sub, writer);
+  const int warp = threadIdx.x >> 5, nw = kSrvTpb / 32;
   double part = 0.0;
-#pragma unroll
-  for (int d = 0; d < B; ++d) {
-    const double r = S.rhs[(size_t)i * B + d] - y[d];
-    S.rd[(size_t)i * B + d] = r;
-    part += r * r;
+  for (int r = row0 + warp * RPW; r < row1; r += nw * RPW) {
+    const int i = r + g;
+    const bool valid = g < RPW && i < row1;
+    const double y = row_mv_warp<double, B>(valid ? i : -1, sub, S.rowptr, S.colind, S.diag, S.offd, S.x);
+    if (valid && writer) {
+      const double rv = S.rhs[(size_t)i * B + comp] - y;
+      S.rd[(size_t)i * B + comp] = rv;
+      part += rv * rv;
+    }
   }
   return part;
+}
+
+__device__ __forceinline__ void chunk_rows(const SrvSlot& S, int c, int& row0, int& row1) {
+  row0 = (c - S.chunk0) * kSrvRows;
+  row1 = min(row0 + kSrvRows, S.n);
 }
 
 // rz_new = r.z; beta = rz_new / rz (0 in the first iteration)
@@ -161,9 +186,10 @@ __global__ void __launch_bounds__(kSrvTpb) k_srv_spmv_pap(const SrvTable* T, dou
   for (int c = blockIdx.x; c < nch; c += gridDim.x) {
     const SrvSlot S = T->slot[find_slot(T, c)];
     if (ld_relaxed_int(&S.st->done) != 0) continue;
-    const int i = (c - S.chunk0) * kSrvRows + threadIdx.x;
-    double part = 0.0;
-    if (i < S.n) part = S.b == 1 ? row_q_pap<1>(S, i) : S.b == 2 ? row_q_pap<2>(S, i) : row_q_pap<3>(S, i);
+    int row0, row1;
+    chunk_rows(S, c, row0, row1);
+    const double part = S.b == 1 ? chunk_q_pap<1>(S, row0, row1)
+                        : S.b == 2 ? chunk_q_pap<2>(S, row0, row1) : chunk_q_pap<3>(S, row0, row1);
     double tot;
     if (slot_sum(part, c, S, partials, &tot) && threadIdx.x == 0) {
       S.st->pap = tot;
@@ -229,9 +255,10 @@ __global__ void __launch_bounds__(kSrvTpb) k_srv_check_true(const SrvTable* T, d
   for (int c = blockIdx.x; c < nch; c += gridDim.x) {
     const SrvSlot S = T->slot[find_slot(T, c)];
     if (ld_relaxed_int(&S.st->done) != 1 || ld_relaxed_int(&S.st->verified) != 0) continue;
-    const int i = (c - S.chunk0) * kSrvRows + threadIdx.x;
-    double part = 0.0;
-    if (i < S.n) part = S.b == 1 ? row_true_res<1>(S, i) : S.b == 2 ? row_true_res<2>(S, i) : row_true_res<3>(S, i);
+    int row0, row1;
+    chunk_rows(S, c, row0, row1);
+    const double part = S.b == 1 ? chunk_true_res<1>(S, row0, row1)
+                        : S.b == 2 ? chunk_true_res<2>(S, row0, row1) : chunk_true_res<3>(S, row0, row1);
     double tot;
     if (slot_sum(part, c, S, partials, &tot) && threadIdx.x == 0) {
       PcgState* st = S.st;

@@ -7,9 +7,9 @@
 
 namespace dfg {
 
-constexpr int kSrvRows = 256;       // rows per chunk (one thread per block row)
+constexpr int kSrvRows = 2048;      // block rows per chunk
 constexpr int kSrvMaxSlots = 256;   // in-flight solves per server
-constexpr int kSrvTpb = kSrvRows;
+constexpr int kSrvTpb = 256;        // threads per block of the batched kernels
 
 // One in-flight solve.  Its rows are cut into chunks of kSrvRows; chunk k of
 // the slot is chunk chunk0 + k of the launch's chunk space.  Reductions sum a

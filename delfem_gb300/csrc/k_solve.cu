@@ -66,20 +66,29 @@ __device__ bool grid_sum(double v, Red red, double* total) {
 
 // ------------------------------------------------------------------- SpMV
 
-// q = A p and pAp = p.q; the last block sets alpha = rz / pAp
+// q = A p and pAp = p.q; the last block sets alpha = rz / pAp.  Rows are
+// taken by lane groups (row_mv_warp), RowLanes<B>::RPW rows per warp.
 template <typename T, int B>
-__global__ void k_spmv_pap(MatView Am, const T* __restrict__ p, T* __restrict__ q, PcgState* st, Red red) {
+__global__ void __launch_bounds__(kSpmvTpb, 2) k_spmv_pap(MatView Am, const T* __restrict__ p, T* __restrict__ q,
+                                                      PcgState* st, Red red) {
   if (st->done) return;
   const T* diag = reinterpret_cast<const T*>(Am.diag);
   const T* offd = reinterpret_cast<const T*>(Am.offd);
+  constexpr int RPW = RowLanes<B>::RPW;
+  int g, sub;
+  row_lane<B>(threadIdx.x & 31, g, sub);
+  bool writer;
+  const int comp = row_comp<B>(sub, writer);
+  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nwarp = ((long long)gridDim.x * blockDim.x) >> 5;
   double part = 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < Am.n; i += gridDim.x * blockDim.x) {
-    T y[B];
-    row_mv<T, T, B>(i, Am.rowptr, Am.colind, diag, offd, p, y);
-#pragma unroll
-    for (int d = 0; d < B; ++d) {
-      q[(size_t)i * B + d] = y[d];
-      part += (double)p[(size_t)i * B + d] * (double)y[d];
+  for (long long r0 = warp * RPW; r0 < Am.n; r0 += nwarp * RPW) {
+    const long long i = r0 + g;
+    const bool valid = g < RPW && i < Am.n;
+    const T y = row_mv_warp<T, B>(valid ? (int)i : -1, sub, Am.rowptr, Am.colind, diag, offd, p);
+    if (valid && writer) {
+      q[(size_t)i * B + comp] = y;
+      part += (double)p[(size_t)i * B + comp] * (double)y;
     }
   }
   double tot;
@@ -404,9 +413,9 @@ cudaError_t pcg_after_precond0(const PcgVecs& v, PcgState* st, Red red, bool fp3
 }
 cudaError_t pcg_spmv_pap(const MatView& A, const PcgVecs& v, PcgState* st, Red red, cudaStream_t s) {
   switch (A.b) {
-    case 1: k_spmv_pap<double, 1> RED_LAUNCH(A, v.p, v.q, st, red); break;
-    case 2: k_spmv_pap<double, 2> RED_LAUNCH(A, v.p, v.q, st, red); break;
-    case 3: k_spmv_pap<double, 3> RED_LAUNCH(A, v.p, v.q, st, red); break;
+    case 1: k_spmv_pap<double, 1><<<kRedGrid, kSpmvTpb, 0, s>>>(A, v.p, v.q, st, red); break;
+    case 2: k_spmv_pap<double, 2><<<kRedGrid, kSpmvTpb, 0, s>>>(A, v.p, v.q, st, red); break;
+    case 3: k_spmv_pap<double, 3><<<kRedGrid, kSpmvTpb, 0, s>>>(A, v.p, v.q, st, red); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -464,9 +473,9 @@ cudaError_t mix_after_precond0(const MixVecs& v, PcgState* st, Red red, cudaStre
 }
 cudaError_t mix_spmv_pap(const MatView& A32, const MixVecs& v, PcgState* st, Red red, cudaStream_t s) {
   switch (A32.b) {
-    case 1: k_spmv_pap<float, 1> RED_LAUNCH(A32, v.p, v.q, st, red); break;
-    case 2: k_spmv_pap<float, 2> RED_LAUNCH(A32, v.p, v.q, st, red); break;
-    case 3: k_spmv_pap<float, 3> RED_LAUNCH(A32, v.p, v.q, st, red); break;
+    case 1: k_spmv_pap<float, 1><<<kRedGrid, kSpmvTpb, 0, s>>>(A32, v.p, v.q, st, red); break;
+    case 2: k_spmv_pap<float, 2><<<kRedGrid, kSpmvTpb, 0, s>>>(A32, v.p, v.q, st, red); break;
+    case 3: k_spmv_pap<float, 3><<<kRedGrid, kSpmvTpb, 0, s>>>(A32, v.p, v.q, st, red); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

@@ -29,6 +29,7 @@ struct Red {
 };
 constexpr int kRedGrid = 304;   // 2 x 152 SMs
 constexpr int kRedTpb = 256;
+constexpr int kSpmvTpb = 512;   // SpMV blocks: 16 warps, two blocks per SM at the reduction grid
 
 struct MatView {
   int n, b;

@@ -73,17 +73,39 @@ __device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, unsigned parity) {
       : "memory");
   return ok != 0;
 }
-// bounded wait; returns false (and records a timeout) when it gives up
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int* err) {
+// First failure of a launch: err[0] = code, err[1..3] = where it happened
+// (wait site, slot, range or row); later failures leave the record alone.
+__device__ __forceinline__ void record_fail(int* err, int code, int site, int a, int b) {
+  if (atomicCAS(err, 0, code) == 0) {
+    err[1] = site;
+    err[2] = a;
+    err[3] = b;
+    __threadfence();
+  }
+}
+
+// Bounded wait for a copy known to be in flight (no failure record).
+__device__ __forceinline__ void mbar_drain(uint64_t* bar, unsigned parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity) && clock64() - t0 < kDrainCycles) {
+  }
+}
+
+// Bounded wait: false when another waiter of the launch has already failed
+// (checked every 32 polls) or after kWaitCycles, when it records a timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int* err, int site, int slot, int range) {
   if (mbar_test_wait(bar, parity)) return true;
-  long long n = 0;
-  while (!mbar_try_wait(bar, parity)) {
-    if (++n > kSpinLimit) {
-      atomicExch(err, kErrTimeout);
-      return false;
+  const long long t0 = clock64();
+  for (unsigned n = 1;; ++n) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((n & 31) == 0) {
+      if (ld_relaxed_int(err) != 0) return false;
+      if (clock64() - t0 > kWaitCycles) {
+        record_fail(err, kErrTimeout, site, slot, range);
+        return false;
+      }
     }
   }
-  return true;
 }
 __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
   asm volatile(
@@ -101,14 +123,18 @@ __device__ __forceinline__ void named_sync(int id, int nthreads) {
 // Rare path: a gathered window still held the sentinel (its producer wrote
 // after the copy); poll those values from global memory, bounded.
 template <typename T>
-__device__ __noinline__ T poll_value(const T* p, const int* err, int* abort) {
-  long long spins = 0;
+__device__ __noinline__ T poll_value(const T* p, int* err, int* abort, int slot, int row) {
   T x = ld_relaxed(p);
-  while (is_sentinel(x)) {
+  const long long t0 = clock64();
+  for (unsigned n = 1; is_sentinel(x); ++n) {
     x = ld_relaxed(p);
-    if ((++spins & 1023) == 0) {
-      if (ld_relaxed_int(err) != 0 || spins > kSpinLimit) {
-        if (spins > kSpinLimit) atomicExch(const_cast<int*>(err), kErrTimeout);
+    if ((n & 255) == 0) {
+      if (ld_relaxed_int(err) != 0) {
+        *abort = 1;
+        break;
+      }
+      if (clock64() - t0 > kWaitCycles) {
+        record_fail(err, kErrTimeout, kSitePoll, slot, row);
         *abort = 1;
         break;
       }
@@ -131,7 +157,7 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
   unsigned char* rstage = smem + (((size_t)3 * NS * 8 + 127) / 128) * 128;
   unsigned char* vstage = rstage + (size_t)NS * a.rec_stage;
   unsigned char* ringreg = vstage + (size_t)NS * a.val_stage;  // 32 zero bytes, then the ring
-  __shared__ int s_range, s_slot;
+  __shared__ int s_range, s_slot, s_stop;
 
   if (a.done && *a.done) return;
   if (threadIdx.x == 0) {
@@ -187,11 +213,17 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
       // ------------------------------------------------------------ loader
       // stage / phase of pipeline position g+i, advanced incrementally
       int rs_st = g_st, rs_ph = g_ph;     // next record to issue
+      int n_issued = 0, n_waited = 0;     // record copies of this range issued / waited for
       int vl_st = g_st, vl_ph = g_ph;     // next step to gather for
       auto issue_rec = [&](int i) {       // step s0+i into stage rs_st
-        if (g + i >= NS) {
-          if (!mbar_wait(&empty[rs_st], (unsigned)(rs_ph ^ 1), a.err)) abort = true;
+        if (g + i >= NS && !abort) {
+          if (!mbar_wait(&empty[rs_st], (unsigned)(rs_ph ^ 1), a.err, kSiteEmpty, jslot, r)) abort = true;
         }
+        if (abort) {  // no new copies once the launch is failing
+          if (++rs_st == NS) { rs_st = 0; rs_ph ^= 1; }
+          return;
+        }
+        ++n_issued;
         if (lane == 0) {
           const long long o0 = rec_off[s0 + i], o1 = rec_off[s0 + i + 1];
           mbar_expect_tx(&rec_full[rs_st], (unsigned)(o1 - o0));
@@ -204,7 +236,10 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
       for (int i = 0; i < nst; ++i) {
         if (i + LA < nst) issue_rec(i + LA);
         const int st = vl_st;
-        if (!mbar_wait(&rec_full[st], (unsigned)vl_ph, a.err)) abort = true;
+        if (!abort) {
+          if (mbar_wait(&rec_full[st], (unsigned)vl_ph, a.err, kSiteRecLoad, jslot, r)) ++n_waited;
+          else abort = true;
+        }
         if (++vl_st == NS) { vl_st = 0; vl_ph ^= 1; }
         const unsigned char* rec = rstage + (size_t)st * a.rec_stage;
         unsigned char* val = vstage + (size_t)st * a.val_stage;
@@ -232,12 +267,20 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
         }
         cp_async_arrive_noinc(&full[st]);
       }
+      // after a failure, record copies already issued land before the CTA
+      // moves on (bounded): lane 0 issued them
+      if (abort && lane == 0) {
+        for (int k = n_waited; k < n_issued; ++k) {
+          const long long pos = g + k;
+          mbar_drain(&rec_full[pos % NS], (unsigned)((pos / NS) & 1));
+        }
+      }
     } else {
       // ----------------------------------------------------------- compute
       int st = g_st, ph = g_ph, rs = 0;
       for (int i = 0; i < nst; ++i) {
-        if (!mbar_wait(&rec_full[st], (unsigned)ph, a.err)) abort = true;
-        if (!mbar_wait(&full[st], (unsigned)ph, a.err)) abort = true;
+        if (!abort && !mbar_wait(&rec_full[st], (unsigned)ph, a.err, kSiteRecCompute, jslot, r)) abort = true;
+        if (!abort && !mbar_wait(&full[st], (unsigned)ph, a.err, kSiteFull, jslot, r)) abort = true;
         const unsigned char* rec = rstage + (size_t)st * a.rec_stage;
         const unsigned char* val = vstage + (size_t)st * a.val_stage;
         const int nent = reinterpret_cast<const int*>(rec)[0];
@@ -274,7 +317,8 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
 #pragma unroll
                 for (int d = 0; d < B; ++d)
                   if (e < nent && is_sentinel(v[e][d]))
-                    v[e][d] = poll_value<T>(&out[(size_t)grow[e * 32 + lane] * B + d], a.err, &ab);
+                    v[e][d] = poll_value<T>(&out[(size_t)grow[e * 32 + lane] * B + d], a.err, &ab, jslot,
+                                            grow[e * 32 + lane]);
               abort |= ab != 0;
             }
 #pragma unroll
@@ -305,7 +349,9 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
                 int ab = 0;
 #pragma unroll
                 for (int d = 0; d < B; ++d)
-                  if (is_sentinel(v[d])) v[d] = poll_value<T>(&out[(size_t)grow[e * 32 + lane] * B + d], a.err, &ab);
+                  if (is_sentinel(v[d]))
+                    v[d] = poll_value<T>(&out[(size_t)grow[e * 32 + lane] * B + d], a.err, &ab, jslot,
+                                         grow[e * 32 + lane]);
                 abort |= ab != 0;
               }
 #pragma unroll
@@ -348,10 +394,14 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
     g_st = (int)(g % NS);  // once per range
     g_ph = (int)((g / NS) & 1);
     if (__any_sync(0xffffffffu, abort)) {
-      if (lane == 0) atomicExch(a.err, a.err[0] ? a.err[0] : kErrTimeout);
+      if (lane == 0) record_fail(a.err, kErrTimeout, kSiteRange, jslot, r);
     }
+    // one read of the error word decides for both warps: a warp that left on
+    // its own read while the other went on would strand it at the next bar.sync
     named_sync(1, 64);
-    if (ld_relaxed_int(a.err) != 0) break;
+    if (threadIdx.x == 0) s_stop = ld_relaxed_int(a.err) != 0;
+    named_sync(1, 64);
+    if (s_stop) break;
   }
   cp_async_wait_all();
 }

@@ -573,6 +573,13 @@ void admission_thread(dfg_server_s* S) {
     std::lock_guard<std::mutex> lk(S->mu);
     S->arena.release(r->tbase, r->T.total);
     r->have_t = false;
+    if (S->fatal != DFG_OK) {  // the serving loop has stopped
+      r->status = S->fatal;
+      r->error = S->fatal_msg;
+      release_locked(S, r);
+      finish_locked(S, r);
+      continue;
+    }
     if (nsing > 10) {
       r->status = DFG_SINGULAR_PIVOT;
       r->error = "ILU(0): " + std::to_string(nsing) + " singular pivots (more than 10)";
@@ -671,10 +678,23 @@ SweepArgs class_args(dfg_server_s* S, int k, int dir) {
 // first iteration (and the stop checks) with timing events.
 cudaGraphExec_t capture_graph(dfg_server_s* S, int mask, bool prof) {
   cudaGraph_t g = nullptr;
+  struct EndOnThrow {  // a failed launch must not leave the stream capturing
+    cudaStream_t st;
+    bool armed = true;
+    ~EndOnThrow() {
+      if (armed) {
+        cudaGraph_t dead = nullptr;
+        cudaStreamEndCapture(st, &dead);
+        if (dead) cudaGraphDestroy(dead);
+        cudaGetLastError();
+      }
+    }
+  };
   auto mark = [&](int k, int edge, cudaStream_t st) {
     if (prof) SCK(cudaEventRecordWithFlags(S->ev_prof[2 * k + edge], st, cudaEventRecordExternal));
   };
   SCK(cudaStreamBeginCapture(S->s_iter, cudaStreamCaptureModeThreadLocal));
+  EndOnThrow guard{S->s_iter};
   const int grid = S->vec_grid;
   for (int it = 0; it < S->chunk; ++it) {
     const bool pf = prof && it == 0;
@@ -716,6 +736,7 @@ cudaGraphExec_t capture_graph(dfg_server_s* S, int mask, bool prof) {
   SCK(srv_collect(S->d_tab, reinterpret_cast<SrvStatus*>(S->d_stat), S->s_iter));
   SCK(cudaMemcpyAsync(S->h_stat, S->d_stat, sizeof(SrvStatus) * kSrvMaxSlots + 16, cudaMemcpyDeviceToHost,
                       S->s_iter));
+  guard.armed = false;
   SCK(cudaStreamEndCapture(S->s_iter, &g));
   cudaGraphExec_t exec = nullptr;
   const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
@@ -813,7 +834,8 @@ void loop_thread(dfg_server_s* S) {
         SCK(cudaStreamSynchronize(S->s_iter));
         S->busy_s += std::chrono::duration<double>(Clock::now() - tb).count();
         if (prof) account_profile(S, act);
-        const int err = *reinterpret_cast<int*>(S->h_stat + sizeof(SrvStatus) * kSrvMaxSlots);
+        const int* errw = reinterpret_cast<const int*>(S->h_stat + sizeof(SrvStatus) * kSrvMaxSlots);
+        const int err = errw[0];
         const SrvStatus* stv = reinterpret_cast<const SrvStatus*>(S->h_stat);
         std::vector<Req*> keep;
         for (int i = 0; i < (int)act.size(); ++i) {
@@ -829,7 +851,8 @@ void loop_thread(dfg_server_s* S) {
           r->rel_true = s.rel_true;
           if (err != 0) {
             r->status = DFG_TIMEOUT;
-            r->error = "a triangular-sweep wait timed out";
+            r->error = "a triangular-sweep wait gave up (site " + std::to_string(errw[1]) + ", table slot " +
+                       std::to_string(errw[2]) + ", range/row " + std::to_string(errw[3]) + ")";
           } else if (s.done == 1) {
             r->status = DFG_OK;
           } else if (s.done == 3) {
@@ -867,9 +890,19 @@ void loop_thread(dfg_server_s* S) {
     std::lock_guard<std::mutex> lk(S->mu);
     S->fatal = DFG_CUDA_ERROR;
     S->fatal_msg = std::string("serving loop: ") + cudaGetErrorString(f.e) + " at " + f.what;
-    for (Req* r : act) { r->status = S->fatal; r->error = S->fatal_msg; finish_locked(S, r); }
-    for (Req* r : retiring) { r->status = S->fatal; r->error = S->fatal_msg; finish_locked(S, r); }
-    for (Req* r : S->activated) { r->status = S->fatal; r->error = S->fatal_msg; finish_locked(S, r); }
+    for (std::vector<Req*>* lst : {&act, &retiring})
+      for (Req* r : *lst) {
+        r->status = S->fatal;
+        r->error = S->fatal_msg;
+        release_locked(S, r);
+        finish_locked(S, r);
+      }
+    for (Req* r : S->activated) {
+      r->status = S->fatal;
+      r->error = S->fatal_msg;
+      release_locked(S, r);
+      finish_locked(S, r);
+    }
     S->activated.clear();
     S->cv_adm.notify_all();
   }
