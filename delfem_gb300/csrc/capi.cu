@@ -133,7 +133,25 @@ double* vec_ptr(dfg_ctx ctx_, dfg_system s, int iv) {
 }
 
 MatView view64(dfg_system s) {
-  return MatView{s->n, s->b, s->rowptr.as<int>(), s->colind.as<int>(), s->diag.p, s->offd.p};
+  return MatView{s->n, s->b, s->rowptr.as<int>(), s->colind.as<int>(), s->diag.p, s->offd.p,
+                 s->s_ptr.as<long long>(), s->s_width.as<int>(), s->s_col.as<int>(), s->s_val64.p};
+}
+MatView view32(dfg_system s) {
+  return MatView{s->n, s->b, s->rowptr.as<int>(), s->colind.as<int>(), s->diag32.p, s->offd32.p,
+                 s->s_ptr.as<long long>(), s->s_width.as<int>(), s->s_col.as<int>(), s->s_val32.p};
+}
+
+// Packs the sliced-ELL values of the current matrix (FP64 or FP32) if the
+// matrix changed since the last pack.
+void ensure_sell(dfg_ctx ctx_, dfg_system s, bool fp32) {
+  long long& ver = fp32 ? s->sell32_version : s->sell64_version;
+  if (ver == s->mat_version) return;
+  DBuf& out = fp32 ? s->s_val32 : s->s_val64;
+  dalloc(ctx_, out, (size_t)std::max<long long>(s->sell_blocks, 1) * s->b * s->b * (fp32 ? 4 : 8) + 64);
+  CK(sell_pack(s->sell_nslices, s->b, s->s_ptr.as<long long>(), s->s_src.as<int>(), s->diag.as<double>(),
+               s->offd.as<double>(), out.p, fp32, ctx_->stream));
+  ctx_->launches += 1;
+  ver = s->mat_version;
 }
 
 size_t vec_bytes(dfg_system s, size_t elem) { return (size_t)s->n * s->b * elem + 64; }
@@ -158,6 +176,14 @@ void system_alloc(dfg_ctx ctx_, dfg_system s) {
   upload(ctx_, s->rowptr, s->h_rowptr.data(), s->h_rowptr.size());
   upload(ctx_, s->colind, s->h_colind.data(), s->h_colind.size());
   upload(ctx_, s->diaind, s->h_diaind.data(), s->h_diaind.size());
+  const SellMap M = build_sell(s->n, s->h_rowptr.data(), s->h_colind.data());
+  s->sell_nslices = M.nslices;
+  s->sell_blocks = M.ptr.back();
+  upload(ctx_, s->s_ptr, M.ptr.data(), M.ptr.size());
+  upload(ctx_, s->s_width, M.width.data(), std::max<size_t>(M.width.size(), 1));
+  upload(ctx_, s->s_col, M.col.data(), std::max<size_t>(M.col.size(), 1));
+  upload(ctx_, s->s_src, M.src.data(), std::max<size_t>(M.src.size(), 1));
+  CK(cudaStreamSynchronize(ctx_->stream));  // the host map is about to go away
 }
 
 void check_pattern(dfg_ctx ctx_, int n, const int* rowptr, const int* colind) {
@@ -427,6 +453,7 @@ extern "C" int dfg_initialize_marge(dfg_system sys) {
     CK(cudaMemsetAsync(sys->res.p, 0, sys->res.bytes, ctx->stream));
     CK(cudaMemsetAsync(sys->upd.p, 0, sys->upd.bytes, ctx->stream));
     sys->mat32_valid = false;
+    ++sys->mat_version;
     sys->rhs0_valid = false;
     return DFG_OK;
   });
@@ -471,6 +498,7 @@ static int assemble(dfg_system sys, int kind, int need_b, int need_ndim, const d
     CK(launch_gather(g, ctx->stream));
     launched(ctx, 3);
     sys->mat32_valid = false;
+    ++sys->mat_version;
     return DFG_OK;
   });
 }
@@ -553,6 +581,7 @@ extern "C" int dfg_finalize_marge(dfg_system sys, double* norm_res) {
     CK(cudaMemcpyAsync(sys->rhs0.p, sys->res.p, m * 8, cudaMemcpyDeviceToDevice, ctx->stream));
     sys->rhs0_valid = true;
     sys->mat32_valid = false;
+    ++sys->mat_version;
     Red r = red_of(ctx, 0);
     CK(api_dot((long long)m, sys->res.as<double>(), sys->res.as<double>(), r, ctx->stream));
     launched(ctx);
@@ -587,6 +616,7 @@ extern "C" int dfg_set_matrix(dfg_system sys, const double* diag, const double* 
     if (offd && sys->nnz) CK(cudaMemcpyAsync(sys->offd.p, offd, (size_t)sys->nnz * bs * 8, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     sys->mat32_valid = false;
+    ++sys->mat_version;
     return DFG_OK;
   });
 }
@@ -1052,6 +1082,7 @@ static int solve_pcg_f64vec(dfg_system sys, dfg_precond prec, bool fp32z, bool t
     read_state(ctx, st, h);
     // iterations: a graph of `chunk` iterations, replayed until done
     const int chunk = m < 200000 ? 8 : 32;
+    ensure_sell(ctx, sys, false);
     const MatView A = view64(sys);
     Chunk g;
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
@@ -1162,8 +1193,9 @@ extern "C" int dfg_solve_pcg_mixed(dfg_system sys, dfg_precond prec, double* con
     MixVecs v{sys->rhs0.as<double>(), sys->upd.as<double>(), sys->w_rd.as<double>(), sys->w_d.as<double>(),
               sys->w_r32.as<float>(), sys->w_p32.as<float>(), sys->w_q32.as<float>(), prec->ybuf32.as<float>(),
               sys->w_z32.as<float>(), m};
+    ensure_sell(ctx, sys, true);
     const MatView A64 = view64(sys);
-    const MatView A32{sys->n, sys->b, sys->rowptr.as<int>(), sys->colind.as<int>(), sys->diag32.p, sys->offd32.p};
+    const MatView A32 = view32(sys);
     const int* done = reinterpret_cast<const int*>(reinterpret_cast<const char*>(st) + offsetof(PcgState, done));
     SweepLaunch F = sweep_launch(ctx, prec, prec->fwd, true, v.r, v.y, sc.tickets, done);
     SweepLaunch B = sweep_launch(ctx, prec, prec->bwd, true, v.y, v.z, sc.tickets + 1, done);
@@ -1316,8 +1348,9 @@ extern "C" int dfg_profile_kernels(dfg_system sys, dfg_precond prec, int mode, i
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     double acc[6] = {0, 0, 0, 0, 0, 0};
+    ensure_sell(ctx, sys, mixed);
     const MatView A64 = view64(sys);
-    const MatView A32{sys->n, sys->b, sys->rowptr.as<int>(), sys->colind.as<int>(), sys->diag32.p, sys->offd32.p};
+    const MatView A32 = view32(sys);
     // the update kernels run on copies, so the caller's residual, solution and
     // direction stay as the last solve left them
     DBuf tr, tx, tp, td, tr32;

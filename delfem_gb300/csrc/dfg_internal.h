@@ -112,6 +112,24 @@ struct GatherMap {
 bool build_gather_map(int n, const int* rowptr, const int* colind, int nelem, int nnoel,
                       const int* conn, GatherMap& out, std::string& err);
 
+// Sliced-ELL copy of the block matrix for the PCG products: slice s holds
+// rows [32s, 32s+32) and W_s block columns (the longest row of the slice, its
+// off-diagonal blocks in CRS order then the diagonal block, then padding).
+// Block position k = ptr[s] + w*32 + lane holds row 32s+lane's w-th block;
+// col[k] is its column (the row itself for padding) and src[k] its source:
+// >= 0 an off-diagonal CRS slot, -1 padding (zero), <= -2 the diagonal block
+// of row -src-2.  Values are stored entry-major per position group:
+// value (k, e) at (ptr[s]*bs + (w*bs + e)*32 + lane), so 32 lanes reading
+// entry e of their w-th block touch 32 consecutive words.
+struct SellMap {
+  int nslices = 0;
+  std::vector<long long> ptr;  // nslices+1, in blocks
+  std::vector<int> width;      // nslices
+  std::vector<int> col;        // ptr[nslices]
+  std::vector<int> src;        // ptr[nslices]
+};
+SellMap build_sell(int n, const int* rowptr, const int* colind);
+
 // --------------------------------------------------------------- handles
 
 struct Ctx;
@@ -152,6 +170,12 @@ struct dfg_system_s {
   dfg::DBuf diag, offd;            // FP64 matrix, reference layout
   dfg::DBuf diag32, offd32;        // FP32 copy (mixed precision)
   bool mat32_valid = false;
+  // sliced-ELL copies for the PCG products (SellMap), repacked when the
+  // matrix changed (mat_version) since the last pack
+  int sell_nslices = 0;
+  long long sell_blocks = 0;
+  dfg::DBuf s_ptr, s_width, s_col, s_src, s_val64, s_val32;
+  long long mat_version = 0, sell64_version = -1, sell32_version = -1;
   dfg::DBuf res, upd, rhs0;        // slots -1, -2 and the finalized right-hand side
   bool rhs0_valid = false;
   std::vector<dfg::DBuf> tmp;      // slots >= 0

@@ -3,8 +3,8 @@
 //
 // Each launch walks a global chunk space: chunk c belongs to the slot s with
 // chunk_start[s] <= c < chunk_start[s+1] and covers kSrvRows block rows of
-// it (vector kernels: a thread per element; SpMV: lane groups per row, see
-// row_mv_warp).  Blocks loop over chunks (fixed grid), so a launch's shape does not
+// it (vector kernels: a thread per element; products: a thread per block
+// row over the slot's sliced-ELL matrix).  Blocks loop over chunks (fixed grid), so a launch's shape does not
 // depend on the slots in flight and one captured graph serves every mix.
 // A slot whose state says `done` is skipped.
 //
@@ -91,24 +91,18 @@ __device__ __forceinline__ void chunk_elems(const SrvSlot& S, int c, long long& 
   e1 = row1 * S.b;
 }
 
-// q = A p over rows [row0, row1) of one chunk (warp-cooperative rows);
+// q = A p over rows [row0, row1) of one chunk (thread per row, sliced ELL);
 // returns this thread's share of p.q
 template <int B>
 __device__ __forceinline__ double chunk_q_pap(const SrvSlot& S, int row0, int row1) {
-  constexpr int RPW = RowLanes<B>::RPW;
-  int g, sub;
-  row_lane<B>(threadIdx.x & 31, g, sub);
-  bool writer;
-  const int comp = row_comp<B>(sub, writer);
-  const int warp = threadIdx.x >> 5, nw = kSrvTpb / 32;
   double part = 0.0;
-  for (int r = row0 + warp * RPW; r < row1; r += nw * RPW) {
-    const int i = r + g;
-    const bool valid = g < RPW && i < row1;
-    const double y = row_mv_warp<double, B>(valid ? i : -1, sub, S.rowptr, S.colind, S.diag, S.offd, S.p);
-    if (valid && writer) {
-      S.q[(size_t)i * B + comp] = y;
-      part += S.p[(size_t)i * B + comp] * y;
+  for (int i = row0 + threadIdx.x; i < row1; i += kSrvTpb) {
+    double y[B];
+    sell_row_mv<double, B>(i, S.sptr, S.swidth, S.scol, S.sval, S.p, y);
+#pragma unroll
+    for (int d = 0; d < B; ++d) {
+      S.q[(size_t)i * B + d] = y[d];
+      part += S.p[(size_t)i * B + d] * y[d];
     }
   }
   return part;
@@ -117,20 +111,14 @@ __device__ __forceinline__ double chunk_q_pap(const SrvSlot& S, int row0, int ro
 // rd = b - A x over one chunk; returns this thread's share of rd.rd
 template <int B>
 __device__ __forceinline__ double chunk_true_res(const SrvSlot& S, int row0, int row1) {
-  constexpr int RPW = RowLanes<B>::RPW;
-  int g, sub;
-  row_lane<B>(threadIdx.x & 31, g, sub);
-  bool writer;
-  const int comp = row_comp<B>(sub, writer);
-  const int warp = threadIdx.x >> 5, nw = kSrvTpb / 32;
   double part = 0.0;
-  for (int r = row0 + warp * RPW; r < row1; r += nw * RPW) {
-    const int i = r + g;
-    const bool valid = g < RPW && i < row1;
-    const double y = row_mv_warp<double, B>(valid ? i : -1, sub, S.rowptr, S.colind, S.diag, S.offd, S.x);
-    if (valid && writer) {
-      const double rv = S.rhs[(size_t)i * B + comp] - y;
-      S.rd[(size_t)i * B + comp] = rv;
+  for (int i = row0 + threadIdx.x; i < row1; i += kSrvTpb) {
+    double y[B];
+    sell_row_mv<double, B>(i, S.sptr, S.swidth, S.scol, S.sval, S.x, y);
+#pragma unroll
+    for (int d = 0; d < B; ++d) {
+      const double rv = S.rhs[(size_t)i * B + d] - y[d];
+      S.rd[(size_t)i * B + d] = rv;
       part += rv * rv;
     }
   }

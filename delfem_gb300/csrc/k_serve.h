@@ -18,10 +18,10 @@ constexpr int kSrvTpb = 256;        // threads per block of the batched kernels
 struct SrvSlot {
   int n, b;
   int chunk0, nchunks;
-  const int* rowptr;
-  const int* colind;
-  const double* diag;   // FP64 matrix, reference layout
-  const double* offd;
+  const long long* sptr;  // FP64 matrix, sliced-ELL copy (SellMap layout)
+  const int* swidth;
+  const int* scol;
+  const double* sval;
   const double* rhs;    // finalized right-hand side
   double* r;            // recursive residual
   double* x;            // solution

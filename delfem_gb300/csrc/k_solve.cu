@@ -66,29 +66,21 @@ __device__ bool grid_sum(double v, Red red, double* total) {
 
 // ------------------------------------------------------------------- SpMV
 
-// q = A p and pAp = p.q; the last block sets alpha = rz / pAp.  Rows are
-// taken by lane groups (row_mv_warp), RowLanes<B>::RPW rows per warp.
+// q = A p and pAp = p.q; the last block sets alpha = rz / pAp.  Thread per
+// block row over the sliced-ELL copy (coalesced value loads).
 template <typename T, int B>
 __global__ void __launch_bounds__(kSpmvTpb, 2) k_spmv_pap(MatView Am, const T* __restrict__ p, T* __restrict__ q,
-                                                      PcgState* st, Red red) {
+                                                         PcgState* st, Red red) {
   if (st->done) return;
-  const T* diag = reinterpret_cast<const T*>(Am.diag);
-  const T* offd = reinterpret_cast<const T*>(Am.offd);
-  constexpr int RPW = RowLanes<B>::RPW;
-  int g, sub;
-  row_lane<B>(threadIdx.x & 31, g, sub);
-  bool writer;
-  const int comp = row_comp<B>(sub, writer);
-  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const long long nwarp = ((long long)gridDim.x * blockDim.x) >> 5;
+  const T* sval = reinterpret_cast<const T*>(Am.sval);
   double part = 0.0;
-  for (long long r0 = warp * RPW; r0 < Am.n; r0 += nwarp * RPW) {
-    const long long i = r0 + g;
-    const bool valid = g < RPW && i < Am.n;
-    const T y = row_mv_warp<T, B>(valid ? (int)i : -1, sub, Am.rowptr, Am.colind, diag, offd, p);
-    if (valid && writer) {
-      q[(size_t)i * B + comp] = y;
-      part += (double)p[(size_t)i * B + comp] * (double)y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < Am.n; i += gridDim.x * blockDim.x) {
+    T y[B];
+    sell_row_mv<T, B>(i, Am.sptr, Am.swidth, Am.scol, sval, p, y);
+#pragma unroll
+    for (int d = 0; d < B; ++d) {
+      q[(size_t)i * B + d] = y[d];
+      part += (double)p[(size_t)i * B + d] * (double)y[d];
     }
   }
   double tot;
@@ -96,6 +88,38 @@ __global__ void __launch_bounds__(kSpmvTpb, 2) k_spmv_pap(MatView Am, const T* _
     st->pap = tot;
     st->alpha = st->rz / tot;
   }
+}
+
+// one block per slice: value (w, e) of lane l from the block named by src
+template <typename T, int B>
+__global__ void k_sell_pack(const long long* __restrict__ ptr, const int* __restrict__ src,
+                            const double* __restrict__ diag, const double* __restrict__ offd, T* __restrict__ out) {
+  constexpr int BS = B * B;
+  const int s = blockIdx.x;
+  const long long k0 = ptr[s];
+  const int nval = (int)(ptr[s + 1] - k0) * BS;
+  for (int o = threadIdx.x; o < nval; o += blockDim.x) {
+    const int lane = o & 31, e = (o >> 5) % BS, w = (o >> 5) / BS;
+    const int v = src[k0 + w * 32 + lane];
+    const double a = v >= 0 ? offd[(size_t)v * BS + e] : v == -1 ? 0.0 : diag[(size_t)(-v - 2) * BS + e];
+    out[k0 * BS + o] = (T)a;
+  }
+}
+
+cudaError_t sell_pack(int nslices, int b, const long long* ptr, const int* src, const double* diag,
+                      const double* offd, void* out, bool fp32, cudaStream_t s) {
+  if (nslices == 0) return cudaSuccess;
+#define DFG_SELL(B)                                                                                        \
+  if (fp32) k_sell_pack<float, B><<<nslices, 256, 0, s>>>(ptr, src, diag, offd, static_cast<float*>(out)); \
+  else k_sell_pack<double, B><<<nslices, 256, 0, s>>>(ptr, src, diag, offd, static_cast<double*>(out));
+  switch (b) {
+    case 1: DFG_SELL(1) break;
+    case 2: DFG_SELL(2) break;
+    case 3: DFG_SELL(3) break;
+    default: return cudaErrorInvalidValue;
+  }
+#undef DFG_SELL
+  return cudaGetLastError();
 }
 
 // ------------------------------------------------------------- FP64 PCG

@@ -37,7 +37,18 @@ struct MatView {
   const int* colind;
   const void* diag;   // double or float
   const void* offd;
+  // sliced-ELL copy of the same matrix (SellMap layout), used by the PCG
+  // products; values of the same type as diag/offd
+  const long long* sptr;
+  const int* swidth;
+  const int* scol;
+  const void* sval;
 };
+
+// Packs a block matrix (reference layout) into its sliced-ELL value array,
+// converting to FP32 when fp32 is set.
+cudaError_t sell_pack(int nslices, int b, const long long* ptr, const int* src, const double* diag,
+                      const double* offd, void* out, bool fp32, cudaStream_t s);
 
 // ---- FP64 PCG (plain path) -------------------------------------------------
 struct PcgVecs {

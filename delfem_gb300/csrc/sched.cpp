@@ -348,4 +348,43 @@ bool build_gather_map(int n, const int* rowptr, const int* colind, int nelem, in
   return true;
 }
 
+SellMap build_sell(int n, const int* rowptr, const int* colind) {
+  SellMap M;
+  M.nslices = (n + 31) / 32;
+  M.ptr.assign(M.nslices + 1, 0);
+  M.width.assign(M.nslices, 0);
+  for (int s = 0; s < M.nslices; ++s) {
+    int w = 0;
+    for (int i = 32 * s; i < std::min(n, 32 * s + 32); ++i) w = std::max(w, rowptr[i + 1] - rowptr[i] + 1);
+    M.width[s] = w;
+    M.ptr[s + 1] = M.ptr[s] + 32LL * w;
+  }
+  M.col.assign(M.ptr[M.nslices], 0);
+  M.src.assign(M.ptr[M.nslices], -1);
+  for (int s = 0; s < M.nslices; ++s)
+    for (int lane = 0; lane < 32; ++lane) {
+      const int i = 32 * s + lane;
+      const long long base = M.ptr[s] + lane;
+      if (i >= n) {
+        for (int w = 0; w < M.width[s]; ++w) M.col[base + 32LL * w] = 0;  // padding rows read x[0] * 0
+        continue;
+      }
+      const int nb = rowptr[i + 1] - rowptr[i];
+      for (int w = 0; w < M.width[s]; ++w) {
+        const long long k = base + 32LL * w;
+        if (w < nb) {
+          M.col[k] = colind[rowptr[i] + w];
+          M.src[k] = rowptr[i] + w;
+        } else if (w == nb) {
+          M.col[k] = i;
+          M.src[k] = -2 - i;
+        } else {
+          M.col[k] = i;
+          M.src[k] = -1;
+        }
+      }
+    }
+  return M;
+}
+
 }  // namespace dfg

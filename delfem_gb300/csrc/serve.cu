@@ -141,6 +141,7 @@ struct Req {
   std::vector<int> rowptr, colind, diaind;
   long long nnz = 0;
   GatherMap gm;
+  SellMap sell;
   Levels lev;
   SweepPlan pf, pb;
   std::vector<unsigned char> hf, hb;
@@ -152,8 +153,9 @@ struct Req {
   double alg[6] = {};
   // device memory plan (offsets into the persistent / transient blocks)
   Layout P, T;
-  size_t o_rowptr, o_colind, o_diag, o_offd, o_rhs, o_r, o_x, o_p, o_q, o_rd, o_y, o_z, o_r32;
+  size_t o_sptr, o_swidth, o_scol, o_sval, o_rhs, o_r, o_x, o_p, o_q, o_rd, o_y, o_z, o_r32;
   size_t o_recf, o_offf, o_rsf, o_recb, o_offb, o_rsb, o_st, o_cnt;
+  size_t t_rowptr, t_colind, t_diag, t_offd, t_ssrc;
   size_t t_coords, t_conn, t_coef, t_bc, t_load, t_em, t_er, t_sp, t_ss, t_rp, t_rs, t_dia, t_lev, t_fd, t_fo;
   size_t t_eof, t_esf, t_srf, t_eob, t_esb, t_srb;
   size_t pbase = 0, tbase = 0;
@@ -255,6 +257,7 @@ bool symbolic(dfg_server_s* S, Req* r) {
     return false;
   }
   r->lev = build_levels(n, r->rowptr.data(), r->colind.data(), r->diaind.data(), true);
+  r->sell = build_sell(n, r->rowptr.data(), r->colind.data());
   const int elem = S->fp32 ? 4 : 8;
   r->pf = choose_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), true, kRingSteps, elem);
   r->pb = choose_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), false, kRingSteps, elem);
@@ -272,16 +275,17 @@ bool symbolic(dfg_server_s* S, Req* r) {
     const double dm = (double)m, mat = (n + 1) * 4.0 + r->nnz * 4.0 + ((double)n + r->nnz) * bs * 8.0;
     r->alg[0] = dm * (8 + elem);
     r->alg[1] = dm * (16 + elem);
-    r->alg[2] = mat + dm * 16;
+    r->alg[2] = mat + dm * 16;  // values + CRS-equivalent indices + p read + q write
     r->alg[3] = dm * (16 + 8 + 16 + 8 + 2 * elem + (S->fp32 ? 4 : 0));
     r->alg[4] = (double)r->hf.size() + dm * 2 * elem;
     r->alg[5] = (double)r->hb.size() + dm * 2 * elem;
   }
   Layout& P = r->P;
-  r->o_rowptr = P.add((n + 1) * 4);
-  r->o_colind = P.add(Z * 4);
-  r->o_diag = P.add(n * bs * 8);
-  r->o_offd = P.add(Z * bs * 8);
+  const size_t sblk = (size_t)std::max<long long>(r->sell.ptr.back(), 1);
+  r->o_sptr = P.add(r->sell.ptr.size() * 8);
+  r->o_swidth = P.add(std::max<size_t>(r->sell.width.size(), 1) * 4);
+  r->o_scol = P.add(sblk * 4);
+  r->o_sval = P.add(sblk * bs * 8);
   r->o_rhs = P.add(m * 8);
   r->o_r = P.add(m * 8);
   r->o_x = P.add(m * 8);
@@ -301,6 +305,11 @@ bool symbolic(dfg_server_s* S, Req* r) {
   r->o_cnt = P.add(16);
   Layout& T = r->T;
   const size_t k = r->nnoel;
+  r->t_rowptr = T.add((n + 1) * 4);
+  r->t_colind = T.add(Z * 4);
+  r->t_diag = T.add(n * bs * 8);
+  r->t_offd = T.add(Z * bs * 8);
+  r->t_ssrc = T.add(sblk * 4);
   r->t_coords = T.add(r->coords.size() * 8);
   r->t_conn = T.add(r->conn.size() * 4);
   r->t_coef = T.add(std::max<size_t>(r->coef.size(), 1) * 8);
@@ -344,8 +353,12 @@ int admit_device(dfg_server_s* S, Req* r) {
   const long long m = (long long)n * b;
   const size_t bs = (size_t)b * b;
   cudaStream_t st = S->s_adm;
-  up(S, pb, r->o_rowptr, r->rowptr);
-  up(S, pb, r->o_colind, r->colind);
+  up(S, tb, r->t_rowptr, r->rowptr);
+  up(S, tb, r->t_colind, r->colind);
+  up(S, pb, r->o_sptr, r->sell.ptr);
+  up(S, pb, r->o_swidth, r->sell.width);
+  up(S, pb, r->o_scol, r->sell.col);
+  up(S, tb, r->t_ssrc, r->sell.src);
   up(S, tb, r->t_coords, r->coords);
   up(S, tb, r->t_conn, r->conn);
   up(S, tb, r->t_coef, r->coef);
@@ -369,8 +382,8 @@ int admit_device(dfg_server_s* S, Req* r) {
   up(S, tb, r->t_eob, r->pb.ent_off);
   up(S, tb, r->t_esb, r->pb.ent_slot);
   up(S, tb, r->t_srb, r->pb.step_rows);
-  double* diag = at<double>(S, pb, r->o_diag);
-  double* offd = at<double>(S, pb, r->o_offd);
+  double* diag = at<double>(S, tb, r->t_diag);
+  double* offd = at<double>(S, tb, r->t_offd);
   double* rhs = at<double>(S, pb, r->o_rhs);
   SCK(cudaMemsetAsync(diag, 0, n * bs * 8, st));
   SCK(cudaMemsetAsync(offd, 0, std::max<long long>(r->nnz, 1) * bs * 8, st));
@@ -411,8 +424,8 @@ int admit_device(dfg_server_s* S, Req* r) {
   bc.n = n;
   bc.nnz = r->nnz;
   bc.b = b;
-  bc.rowptr = at<int>(S, pb, r->o_rowptr);
-  bc.colind = at<int>(S, pb, r->o_colind);
+  bc.rowptr = at<int>(S, tb, r->t_rowptr);
+  bc.colind = at<int>(S, tb, r->t_colind);
   bc.flag = at<int>(S, tb, r->t_bc);
   bc.diag = diag;
   bc.offd = offd;
@@ -431,6 +444,10 @@ int admit_device(dfg_server_s* S, Req* r) {
     SCK(launch_ilu_level(b, at<int>(S, tb, r->t_lev) + r->lev.ptr[l], r->lev.ptr[l + 1] - r->lev.ptr[l],
                          bc.rowptr, bc.colind, at<int>(S, tb, r->t_dia), fd, fo, nsing, st));
   nl += nlev;
+  // the matrix into its sliced-ELL copy (the only copy that stays resident)
+  SCK(sell_pack(r->sell.nslices, b, at<long long>(S, pb, r->o_sptr), at<int>(S, tb, r->t_ssrc), diag, offd,
+                at<void>(S, pb, r->o_sval), false, st));
+  ++nl;
   // the factor into the step records
   for (int dir = 0; dir < 2; ++dir) {
     const SweepPlan& pl = dir == 0 ? r->pf : r->pb;
@@ -469,7 +486,7 @@ void finish_locked(dfg_server_s* S, Req* r) {
   // host set-up data is no longer needed
   r->coords = {}; r->coef = {}; r->load = {}; r->conn = {}; r->bcflag = {};
   r->rowptr = {}; r->colind = {}; r->diaind = {};
-  r->gm = GatherMap{}; r->lev = Levels{}; r->pf = SweepPlan{}; r->pb = SweepPlan{};
+  r->gm = GatherMap{}; r->sell = SellMap{}; r->lev = Levels{}; r->pf = SweepPlan{}; r->pb = SweepPlan{};
   r->hf = {}; r->hb = {}; r->of = {}; r->ob = {};
   ++S->n_finished;
   S->cv_done.notify_all();
@@ -597,10 +614,10 @@ SrvSlot slot_of(dfg_server_s* S, Req* r) {
   SrvSlot s{};
   s.n = r->n;
   s.b = r->b;
-  s.rowptr = at<int>(S, pb, r->o_rowptr);
-  s.colind = at<int>(S, pb, r->o_colind);
-  s.diag = at<double>(S, pb, r->o_diag);
-  s.offd = at<double>(S, pb, r->o_offd);
+  s.sptr = at<long long>(S, pb, r->o_sptr);
+  s.swidth = at<int>(S, pb, r->o_swidth);
+  s.scol = at<int>(S, pb, r->o_scol);
+  s.sval = at<double>(S, pb, r->o_sval);
   s.rhs = at<double>(S, pb, r->o_rhs);
   s.r = at<double>(S, pb, r->o_r);
   s.x = at<double>(S, pb, r->o_x);

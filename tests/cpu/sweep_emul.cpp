@@ -153,3 +153,57 @@ extern "C" int emul_sweep(int n, int b, const int* rowptr, const int* colind, in
   }
   return 0;
 }
+
+// Sliced-ELL map (build_sell) and value layout: emulates the packing kernel
+// (k_sell_pack) and the thread-per-row product (sell_row_mv) sequentially and
+// compares with the row-order CRS product (off-diagonal blocks in CRS order,
+// then the diagonal block): the same operation sequence, so the results must
+// be bitwise equal.  Returns 0 on success.
+extern "C" int emul_sell(int n, int b, const int* rowptr, const int* colind, const double* diag, const double* offd,
+                         const double* x, double* y_sell, double* y_crs, long long* info) {
+  const SellMap M = build_sell(n, rowptr, colind);
+  const int bs = b * b;
+  info[0] = M.nslices;
+  info[1] = M.ptr.back();
+  // packing
+  std::vector<double> val((size_t)M.ptr.back() * bs, 0.0);
+  for (int s = 0; s < M.nslices; ++s) {
+    const long long k0 = M.ptr[s];
+    const int nval = (int)(M.ptr[s + 1] - k0) * bs;
+    for (int o = 0; o < nval; ++o) {
+      const int lane = o & 31, e = (o >> 5) % bs, w = (o >> 5) / bs;
+      const int v = M.src[k0 + w * 32 + lane];
+      val[k0 * bs + o] = v >= 0 ? offd[(size_t)v * bs + e] : v == -1 ? 0.0 : diag[(size_t)(-v - 2) * bs + e];
+    }
+  }
+  // coverage: every CRS slot and every diagonal block exactly once
+  std::vector<int> seen_off(rowptr[n], 0), seen_dia(n, 0);
+  for (long long k = 0; k < M.ptr.back(); ++k) {
+    const int v = M.src[k];
+    if (v >= 0) seen_off[v]++;
+    else if (v <= -2) seen_dia[-v - 2]++;
+  }
+  for (int c = 0; c < rowptr[n]; ++c) if (seen_off[c] != 1) return 1;
+  for (int i = 0; i < n; ++i) if (seen_dia[i] != 1) return 2;
+  for (int i = 0; i < n; ++i) {
+    // SELL thread-per-row
+    const int s = i >> 5, lane = i & 31;
+    const long long k0 = M.ptr[s];
+    double acc[3] = {0, 0, 0};
+    for (int w = 0; w < M.width[s]; ++w) {
+      const int j = M.col[k0 + w * 32 + lane];
+      for (int p = 0; p < b; ++p)
+        for (int q = 0; q < b; ++q) acc[p] += val[k0 * bs + (w * bs + p * b + q) * 32 + lane] * x[(size_t)j * b + q];
+    }
+    for (int p = 0; p < b; ++p) y_sell[(size_t)i * b + p] = acc[p];
+    // CRS row order
+    double ref[3] = {0, 0, 0};
+    for (int c = rowptr[i]; c < rowptr[i + 1]; ++c)
+      for (int p = 0; p < b; ++p)
+        for (int q = 0; q < b; ++q) ref[p] += offd[(size_t)c * bs + p * b + q] * x[(size_t)colind[c] * b + q];
+    for (int p = 0; p < b; ++p)
+      for (int q = 0; q < b; ++q) ref[p] += diag[(size_t)i * bs + p * b + q] * x[(size_t)i * b + q];
+    for (int p = 0; p < b; ++p) y_crs[(size_t)i * b + p] = ref[p];
+  }
+  return 0;
+}

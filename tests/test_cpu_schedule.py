@@ -60,3 +60,27 @@ def test_sweep_schedule(emul, oracle_lib, idx, range_rows, R):
     assert rc == 0, f"backward schedule check failed with code {rc}"
     ref = oracle_lib.precond(n, b, out["rowptr"], out["colind"], out["diaind"], out["fdiag"], out["foffd"], rhs)
     np.testing.assert_allclose(z, ref, rtol=1e-11, atol=1e-12 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("idx", range(4))
+def test_sell_layout_matches_crs_product(emul, oracle_lib, idx):
+    """The sliced-ELL copy covers every block once and its thread-per-row
+    product repeats the CRS row-order sum bit for bit (g++ without FMA
+    contraction on both sides)."""
+    from conftest import bits
+    p = _problems()[idx]
+    out = oracle_lib.solve(p, stop_after_ilu=True)
+    n, b = out["n"], out["b"]
+    x = np.random.default_rng(10 + idx).standard_normal(n * b)
+    ys, yc = np.zeros(n * b), np.zeros(n * b)
+    info = np.zeros(4, dtype=np.int64)
+    P = ctypes.c_void_p
+    emul.emul_sell.argtypes = [ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P]
+    od = out["offd"] if out["offd"].size else np.zeros(1)
+    rc = emul.emul_sell(n, b, _p(out["rowptr"]), _p(out["colind"]), _p(out["diag"]), _p(od), _p(x), _p(ys), _p(yc),
+                        _p(info))
+    assert rc == 0
+    assert info[0] == (n + 31) // 32
+    assert np.array_equal(bits(ys), bits(yc))
+    xr = oracle_lib.matvec(n, b, out["rowptr"], out["colind"], out["diag"], out["offd"], x)
+    np.testing.assert_allclose(ys, xr, rtol=1e-12, atol=1e-14 * np.abs(xr).max())
