@@ -318,8 +318,10 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
+def ncu_traffic(kernel: str, algorithmic_bytes: float | None = None):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary
+    (profiles/ncu_traffic.txt), scaled to `algorithmic_bytes` when the
+    captured launch's algorithmic bytes are recorded; None without an entry."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     if not os.path.exists(path):
         return None
@@ -327,9 +329,13 @@ def ncu_traffic(kernel: str):
         parts = line.split()
         if len(parts) >= 2 and parts[0] == kernel:
             try:
-                return float(parts[1])
+                dram = float(parts[1])
+                cap = float(parts[2]) if len(parts) >= 3 else None
             except ValueError:
                 return None
+            if cap and algorithmic_bytes:
+                return round(dram * algorithmic_bytes / cap)
+            return round(dram)
     return None
 
 
@@ -344,7 +350,7 @@ def compose_line(args, world, p, results, prof, e2e, head):
             return None
         achieved = b / (ms[name] * 1e-3) / 1e9
         return dict(bound="hbm", achieved=round(achieved, 1), peak=hbm_peak, unit="GB/s",
-                    frac=round(achieved / hbm_peak, 4), traffic=ncu_traffic(name), peak_source=peak_kind,
+                    frac=round(achieved / hbm_peak, 4), traffic=ncu_traffic(name, b), peak_source=peak_kind,
                     kernel=name, ms_per_launch=round(ms[name], 4), algorithmic_bytes=int(b))
 
     def arm_summary(arm):
@@ -611,7 +617,7 @@ def compose_serve_line(args, world, cfg, items, timed_items, timed_probs, result
         v = swept[dom]
         achieved = v["bytes"] / (v["ms"] * 1e-3) / 1e9
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
-                "frac": round(achieved / hbm_peak, 4), "traffic": ncu_traffic(dom), "peak_source": peak_kind,
+                "frac": round(achieved / hbm_peak, 4), "traffic": ncu_traffic(dom, v["bytes"]), "peak_source": peak_kind,
                 "kernel": dom, "ms_per_launch": round(v["ms"], 4), "algorithmic_bytes": int(v["bytes"]),
                 "launches_timed": int(v["n"])}
     value = arms[head]["value"]
