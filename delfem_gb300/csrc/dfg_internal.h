@@ -90,6 +90,10 @@ SweepPlan build_sweep_plan(int n, int b, const int* rowptr, const int* colind, c
                            bool forward, int range_rows, int R);
 SweepPlan choose_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind,
                             bool forward, int R, int elem_size);
+// the plan with the fullest steps among ranges of 8, 16 and 32 typical
+// dependency distances (batched launches)
+SweepPlan fullest_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind, bool forward,
+                             int R);
 // the `keep` plans with the lowest model makespan over range sizes 256, 512, ... rows
 std::vector<SweepPlan> candidate_sweep_plans(int n, int b, const int* rowptr, const int* colind, const int* diaind,
                                              bool forward, int R, int keep);

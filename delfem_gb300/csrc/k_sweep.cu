@@ -15,7 +15,9 @@
 //     sides and of the 16-byte-aligned windows holding dependencies produced
 //     by other ranges; each lane's gathers arrive on the stage's `full`
 //     mbarrier when they complete (cp.async.mbarrier.arrive.noinc);
-//   * compute warp -- waits for `full`, evaluates the rows (dependency values
+//   * compute warp -- waits for `full` (which also covers the record: each
+//     loader lane arrives on it with release semantics after acquiring the
+//     record's barrier), evaluates the rows (dependency values
 //     come from a ring of its own recent results or from the gathered
 //     windows, selected without branching), writes results to the ring and to
 //     global memory, and releases the stage on its `empty` mbarrier.
@@ -163,7 +165,7 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
   if (threadIdx.x == 0) {
     for (int s = 0; s < NS; ++s) {
       mbar_init(&rec_full[s], 1);
-      mbar_init(&full[s], 32);
+      mbar_init(&full[s], 64);  // 32 copy-completion arrivals + 32 loader arrivals
       mbar_init(&empty[s], 1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -266,6 +268,11 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
           }
         }
         cp_async_arrive_noinc(&full[st]);
+        // release: the record this lane waited for is visible to whoever
+        // acquires `full`, so the compute warp waits on one barrier per step.
+        // A failing lane does not arrive: the compute warp then gives up on
+        // the error word instead of reading a record that may not have landed.
+        if (!abort) mbar_arrive(&full[st]);
       }
       // after a failure, record copies already issued land before the CTA
       // moves on (bounded): lane 0 issued them
@@ -279,7 +286,6 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
       // ----------------------------------------------------------- compute
       int st = g_st, ph = g_ph, rs = 0;
       for (int i = 0; i < nst; ++i) {
-        if (!abort && !mbar_wait(&rec_full[st], (unsigned)ph, a.err, kSiteRecCompute, jslot, r)) abort = true;
         if (!abort && !mbar_wait(&full[st], (unsigned)ph, a.err, kSiteFull, jslot, r)) abort = true;
         const unsigned char* rec = rstage + (size_t)st * a.rec_stage;
         const unsigned char* val = vstage + (size_t)st * a.val_stage;

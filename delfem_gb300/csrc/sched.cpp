@@ -348,6 +348,44 @@ bool build_gather_map(int n, const int* rowptr, const int* colind, int nelem, in
   return true;
 }
 
+// Schedule for batched launches, where many solves fill the device and a
+// CTA's steps are the scarce resource: the fullest steps (rows per step)
+// rather than the shortest single-solve makespan.  Candidate ranges hold
+// 8, 16 or 32 times the median distance from a row to its farthest dependency
+// (a grid line of a structured mesh), so a range spans up to 32 lines and a
+// step up to 32 rows; a larger range is taken only when its steps are at
+// least 10 % fuller (it also makes the solve's own critical path longer).
+SweepPlan fullest_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind, bool forward,
+                             int R) {
+  std::vector<int> dist;
+  dist.reserve(n);
+  for (int i = 0; i < n; ++i) {
+    if (forward) {
+      if (diaind[i] > rowptr[i]) dist.push_back(i - colind[rowptr[i]]);
+    } else {
+      if (rowptr[i + 1] > diaind[i]) dist.push_back(colind[rowptr[i + 1] - 1] - i);
+    }
+  }
+  long long D = 1;
+  if (!dist.empty()) {
+    std::nth_element(dist.begin(), dist.begin() + dist.size() / 2, dist.end());
+    D = std::max(1, dist[dist.size() / 2]);
+  }
+  SweepPlan best;
+  double best_fill = -1.0;
+  for (int mult : {8, 16, 32}) {
+    const int range_rows = (int)std::min<long long>(std::max<long long>(256, mult * D), std::max(n, 1));
+    SweepPlan P = build_sweep_plan(n, b, rowptr, colind, diaind, forward, range_rows, R);
+    const double fill = P.nsteps ? (double)n / P.nsteps : 0.0;
+    if (fill > best_fill * 1.10) {
+      best_fill = fill;
+      best = std::move(P);
+    }
+    if (range_rows >= n) break;
+  }
+  return best;
+}
+
 SellMap build_sell(int n, const int* rowptr, const int* colind) {
   SellMap M;
   M.nslices = (n + 31) / 32;

@@ -259,8 +259,8 @@ bool symbolic(dfg_server_s* S, Req* r) {
   r->lev = build_levels(n, r->rowptr.data(), r->colind.data(), r->diaind.data(), true);
   r->sell = build_sell(n, r->rowptr.data(), r->colind.data());
   const int elem = S->fp32 ? 4 : 8;
-  r->pf = choose_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), true, kRingSteps, elem);
-  r->pb = choose_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), false, kRingSteps, elem);
+  r->pf = fullest_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), true, kRingSteps);
+  r->pb = fullest_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), false, kRingSteps);
   r->maxe = std::max(r->pf.max_nent, r->pb.max_nent);
   if (r->maxe > 16) {
     r->error = "a row has more than 16 lower or upper neighbours; the serving sweeps take at most 16";

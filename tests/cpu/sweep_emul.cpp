@@ -28,8 +28,9 @@ extern "C" int emul_sweep(int n, int b, const int* rowptr, const int* colind, in
       if (colind[c] > i) { d = c; break; }
     diaind[i] = d;
   }
-  SweepPlan P = range_rows > 0 ? build_sweep_plan(n, b, rowptr, colind, diaind.data(), forward != 0, range_rows, R)
-                               : choose_sweep_plan(n, b, rowptr, colind, diaind.data(), forward != 0, R, 8);
+  SweepPlan P = range_rows > 0    ? build_sweep_plan(n, b, rowptr, colind, diaind.data(), forward != 0, range_rows, R)
+                : range_rows == 0 ? choose_sweep_plan(n, b, rowptr, colind, diaind.data(), forward != 0, R, 8)
+                                  : fullest_sweep_plan(n, b, rowptr, colind, diaind.data(), forward != 0, R);
   const int bs = b * b;
   info[0] = P.nranges;
   info[1] = P.nsteps;

@@ -40,7 +40,7 @@ def _problems():
 
 
 @pytest.mark.parametrize("idx", range(4))
-@pytest.mark.parametrize("range_rows", [0, 1, 37, 256, 100000])
+@pytest.mark.parametrize("range_rows", [-1, 0, 1, 37, 256, 100000])
 @pytest.mark.parametrize("R", [2, 8, 32])
 def test_sweep_schedule(emul, oracle_lib, idx, range_rows, R):
     p = _problems()[idx]
@@ -84,3 +84,23 @@ def test_sell_layout_matches_crs_product(emul, oracle_lib, idx):
     assert np.array_equal(bits(ys), bits(yc))
     xr = oracle_lib.matvec(n, b, out["rowptr"], out["colind"], out["diag"], out["offd"], x)
     np.testing.assert_allclose(ys, xr, rtol=1e-12, atol=1e-14 * np.abs(xr).max())
+
+
+def test_serving_schedule_has_fuller_steps(emul, oracle_lib):
+    """The batched-launch schedule (range_rows -1: fullest steps) packs more
+    rows per step than the single-solve choice on serving-like meshes."""
+    from delfem_gb300 import meshgen as mg
+    for p in (mg.rect_problem_2d(mg.SOLID2D, 20000, seed=3), mg.rect_problem_2d(mg.POISSON2D, 30000, seed=4)):
+        out = oracle_lib.solve(p, stop_after_ilu=True)
+        n, b = out["n"], out["b"]
+        rhs = np.ones(n * b)
+        fo = out["foffd"] if out["foffd"].size else np.zeros(1)
+        fill = {}
+        for rr in (-1, 0):
+            y = np.full(n * b, np.nan)
+            info = np.zeros(8, dtype=np.int64)
+            assert emul.emul_sweep(n, b, _p(out["rowptr"]), _p(out["colind"]), 1, rr, 32, _p(out["fdiag"]), _p(fo),
+                                   _p(rhs), _p(y), _p(info)) == 0
+            fill[rr] = n / info[1]
+        assert fill[-1] >= fill[0], fill
+        assert fill[-1] > 20, fill
