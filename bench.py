@@ -45,7 +45,7 @@ METRIC = "PCG solves/s at 1e-8 rel. residual, served mixed vs plain FP64 GPU; p5
 CONFIGS = {
     # name -> (meshgen factory kwargs, description)
     "serve2d": dict(kind="serve", dim=2, nreq=2000, seed=4, rate=50.0, budget=0),
-    "serve3d": dict(kind="serve", dim=3, nreq=500, seed=5, rate=10.0, budget=120 * 10**9),
+    "serve3d": dict(kind="serve", dim=3, nreq=500, seed=5, rate=30.0, budget=120 * 10**9),
     "solid2d_1000x500": dict(kind="solid2d", nx=1000, ny=500),
     "poisson2d_128": dict(kind="poisson2d", n=128),
     "solid3d_96": dict(kind="solid3d", n=96),
