@@ -486,7 +486,7 @@ def run_serve(args, rank, world, local):
     x_plain = {}
     for arm, mode in arms_run:
         with Server(ctx, mode=mode, budget_bytes=cfg["budget"], profile_every=16,
-                    max_inflight=args.max_inflight) as S:
+                    max_inflight=args.max_inflight, size_groups=args.size_groups) as S:
             wids = serve_segment(S, warm_items, warm_probs, 0.0)
             for i in wids:
                 S.wait(i)
@@ -646,7 +646,7 @@ def compose_serve_line(args, world, cfg, items, timed_items, timed_probs, result
                    "stop": "true relative residual <= tol (every request, both arms)",
                    "timing": "host clock around the timed stream, device synchronised at both ends",
                    "l2": "in-flight working set (GBs of matrices, factors, vectors) far above the 129 MB L2; no flush",
-                   "parallelism": f"one server per GPU, x{world}", "max_inflight": args.max_inflight,
+                   "parallelism": f"one server per GPU, x{world}", "max_inflight": args.max_inflight, "size_groups": args.size_groups,
                    "generation_s": round(t_gen, 1)},
         "p50_ms": arms[head]["p50_ms"],
         "p99_ms": arms[head]["p99_ms"],
@@ -744,6 +744,7 @@ def main():
     ap.add_argument("--cpu-serve-requests", type=int, default=12,
                     help="requests the one-core CPU baseline solves (serving configs)")
     ap.add_argument("--max-inflight", type=int, default=128, help="serving: solves resident at once (<= 256)")
+    ap.add_argument("--size-groups", type=int, default=0, help="serving: 1 table, 2-3 size groups, 0 = server default (3)")
     ap.add_argument("--ref-requests-per-core", type=int, default=2,
                     help="requests per host core per step of --impl reference (serving configs)")
     ap.add_argument("--arms", default=",".join(sorted({a for a, _ in ARMS + SERVE_ARMS})),

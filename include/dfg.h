@@ -283,6 +283,8 @@ typedef struct {
   int chunk_iters;        /* PCG iterations per graph replay, <= 64; 0 = 8 */
   int host_threads;       /* symbolic set-up threads; 0 = hardware threads - 2 */
   int profile_every;      /* every n-th replay times its first iteration per kernel; 0 = never */
+  int size_groups;        /* solves grouped by size, each group iterating at its own pace on its own
+                             streams: 1 = one table for all, 2-3 groups; 0 = 3 */
 } dfg_server_config;
 
 /* kind: 1 Poisson 2D (P1 triangles), 2 Poisson 3D (P1 tetrahedra),

@@ -72,6 +72,16 @@ def test_serve_budget_queues_and_rejects(gpu_ctx):
     assert stats["peak_inflight"] < len(probs)
 
 
+def test_serve_size_groups_same_results(gpu_ctx):
+    """Grouping solves by size changes when they iterate, not what they compute."""
+    probs = _stream(8, seed=14, nmin=300, nmax=60000)
+    one, _ = _serve(gpu_ctx, probs, mode="fp32f", size_groups=1)
+    three, st = _serve(gpu_ctx, probs, mode="fp32f", size_groups=3)
+    for a, b in zip(one, three):
+        assert a["status"] == 0 and b["status"] == 0
+        assert np.array_equal(bits(a["x"]), bits(b["x"])) and a["iterations"] == b["iterations"]
+
+
 def test_serve_3d_kinds(gpu_ctx, oracle_lib):
     from delfem_gb300 import meshgen as mg
     probs = [mg.box_problem_3d(mg.POISSON3D, 6, 7, 8, seed=1), mg.box_problem_3d(mg.SOLID3D, 5, 6, 7, seed=2),
