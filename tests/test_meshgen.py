@@ -71,3 +71,35 @@ def test_lognormal_coefficients(sigma):
     p = mg.solid3d_cube(6, coef_sigma=sigma)
     lg = np.log(p.coef)
     assert abs(lg.std() - sigma) < 0.05 and abs(lg.mean()) < 0.05
+
+
+def test_serving_streams_match_their_distributions():
+    from delfem_gb300 import meshgen as mg
+    st = mg.serve_stream_2d(rate=50.0)
+    assert len(st) == 2000
+    t = np.array([it.arrival for it in st])
+    assert np.all(np.diff(t) > 0) and 36 < t[-1] < 44           # Poisson arrivals at 50/s
+    sizes = np.array([it.size[0] for it in st])
+    assert sizes.min() >= 2000 and sizes.max() <= 400000
+    kinds = np.array([it.kind for it in st])
+    assert set(kinds) == {mg.POISSON2D, mg.SOLID2D} and 0.45 < np.mean(kinds == mg.POISSON2D) < 0.55
+    again = mg.serve_stream_2d(rate=50.0)
+    assert [(a.seed, a.size, a.kind) for a in again[:50]] == [(b.seed, b.size, b.kind) for b in st[:50]]
+    s3 = mg.serve_stream_3d()
+    assert len(s3) == 500 and all(16 <= e <= 80 for it in s3 for e in it.size)
+
+
+def test_serving_requests_are_well_posed():
+    from delfem_gb300 import meshgen as mg
+    for it in mg.serve_stream_2d(nreq=12, seed=3, nmin=300, nmax=5000):
+        p = it.problem()
+        assert abs(p.nnode - it.size[0]) <= 0.25 * it.size[0] + 20
+        assert p.bcflag.any()                                    # at least one Dirichlet side
+        assert p.load is not None and not np.any(p.load[p.bcflag != 0])
+        assert p.coef is not None and np.all(p.coef > 0)
+        e1 = p.coords[p.conn[:, 1]] - p.coords[p.conn[:, 0]]
+        e2 = p.coords[p.conn[:, 2]] - p.coords[p.conn[:, 0]]
+        assert np.all(e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0] > 0)   # counter-clockwise, non-degenerate
+    for it in mg.serve_stream_3d(nreq=3, seed=4, emin=3, emax=5):
+        p = it.problem()
+        assert p.bcflag.any() and p.nnode == np.prod([e + 1 for e in it.size])
