@@ -81,6 +81,24 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(v: float, world: int, device=None) -> float:
+    """Max of a per-rank value over the process group (NCCL on the GPU path,
+    any backend with CPU tensors); the value itself at N = 1."""
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device if device is not None else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, wall_per_rank: float, world: int, device=None) -> float:
+    """Units processed by all ranks (each rank serves its own replica of the
+    workload) over the slowest rank's time."""
+    return units_per_rank * world / max_over_ranks(wall_per_rank, world, device)
+
+
 # ------------------------------------------------------------------- clocks
 
 class ClockSampler:
@@ -283,11 +301,7 @@ def run_gpu(args, rank, world, local):
 
     # max over ranks
     def gmax(v):
-        if world > 1:
-            t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{local}")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            return float(t.item())
-        return v
+        return max_over_ranks(v, world, f"cuda:{local}")
 
     for mode in results:
         results[mode]["total_ms"] = gmax(results[mode]["total_ms"])
@@ -536,11 +550,7 @@ def run_serve(args, rank, world, local):
             dof_iters=sum(p.ndof * (r["iterations"] + 1) for p, r in zip(timed_probs, res)))
 
     def gmax(v):
-        if world > 1:
-            t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{local}")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            return float(t.item())
-        return v
+        return max_over_ranks(v, world, f"cuda:{local}")
 
     for arm in results:
         results[arm]["wall"] = gmax(results[arm]["wall"])
