@@ -818,12 +818,19 @@ void run_sweep(dfg_ctx ctx_, bool forward, int b, bool fp32, const SweepLaunch& 
   launched(ctx_);
 }
 
-// Schedule choice: the cost model keeps a few candidate range sizes and each
-// is timed on the device with one FP32 sweep of the real structure (values
-// do not change the timing); the fastest wins.
+// Schedule choice: the cost model keeps a few candidate range sizes, the
+// fullest-step plan joins them, and each is timed on the device with one FP32
+// sweep of the real structure (values do not change the timing); the fastest
+// wins.
 void setup_sweep(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, const dfg_system sys, bool forward) {
   std::vector<SweepPlan> cands = candidate_sweep_plans(sys->n, sys->b, sys->h_rowptr.data(), sys->h_colind.data(),
                                                        sys->h_diaind.data(), forward, 32, 4);
+  // and the fullest-step plan (ranges of up to 32 grid lines), if it differs
+  SweepPlan full = fullest_sweep_plan(sys->n, sys->b, sys->h_rowptr.data(), sys->h_colind.data(),
+                                      sys->h_diaind.data(), forward, 32);
+  bool seen = false;
+  for (const SweepPlan& c : cands) seen |= (c.nranges == full.nranges && c.nsteps == full.nsteps);
+  if (!seen) cands.push_back(std::move(full));
   size_t best = 0;
   if (cands.size() > 1) {
     const long long m = (long long)sys->n * sys->b;
