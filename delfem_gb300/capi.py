@@ -97,6 +97,7 @@ SIGNATURES = {
     "dfg_server_stats": (_I, [_P, _P]),
     "dfg_server_destroy": (_I, [_P]),
     "dfg_server_profile": (_I, [_P, _P]),
+    "dfg_selftest_wait_timeout": (_I, [_P, _PI]),
 }
 
 

@@ -1031,14 +1031,39 @@ struct Chunk {
   }
 };
 
+// Reads and clears the error word (code, wait site, slot, range or row) and
+// reports the timeout; the context stays usable.
 int timeout_status(dfg_ctx ctx_) {
-  CK(cudaMemsetAsync(ctx_->err_word.p, 0, sizeof(int), ctx_->stream));
+  int w[4] = {0, 0, 0, 0};
+  CK(cudaMemcpyAsync(w, ctx_->err_word.p, sizeof(w), cudaMemcpyDeviceToHost, ctx_->stream));
+  CK(cudaMemsetAsync(ctx_->err_word.p, 0, sizeof(w), ctx_->stream));
   CK(cudaStreamSynchronize(ctx_->stream));
-  set_err(ctx_, "a triangular-sweep wait timed out");
+  set_err(ctx_, "a triangular-sweep wait timed out (site " + std::to_string(w[1]) + ", slot " +
+                    std::to_string(w[2]) + ", range/row " + std::to_string(w[3]) + ")");
+  ctx_->last_timeout_site = w[1];
   return DFG_TIMEOUT;
 }
 
 }  // namespace
+
+extern "C" int dfg_selftest_wait_timeout(dfg_ctx ctx, int* site) {
+  if (!ctx) return DFG_INVALID_ARGUMENT;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    DBuf never;
+    dalloc(ctx, never, 64);
+    CK(fill_sentinel(1, never.p, false, ctx->stream));
+    CK(launch_wait_selftest(never.as<double>(), ctx->err_word.as<int>(), ctx->stream));
+    launched(ctx);
+    if (read_err(ctx) == 0) {
+      set_err(ctx, "the wait self-test did not time out");
+      return DFG_CUDA_ERROR;
+    }
+    const int st = timeout_status(ctx);
+    if (site) *site = ctx->last_timeout_site;
+    return st;
+  });
+}
 
 // FP64-vector PCG with an FP64 or FP32 factor (dfg_solve_pcg / _ex).
 static int solve_pcg_f64vec(dfg_system sys, dfg_precond prec, bool fp32z, bool target_true, double* conv_ratio,

@@ -163,6 +163,7 @@ struct dfg_ctx_s {
   dfg::DBuf err_word;     // int, device error word (dfg::kErr*)
   dfg::DBuf scratch;      // reduction partials + scalars
   int* h_pinned = nullptr;  // small pinned host area for status reads
+  int last_timeout_site = 0;  // wait site of the last reported timeout
 };
 
 struct dfg_system_s {

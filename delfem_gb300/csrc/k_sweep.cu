@@ -476,6 +476,20 @@ static cudaError_t set_attr(size_t max_smem) {
   return e;
 }
 
+// Self-test of the bounded waits: one poll, with the sweep's own poll, of a
+// value nothing writes (it holds the sentinel).  It gives up after the wait
+// budget, records the failure in the error word and returns.
+__global__ void k_wait_selftest(const double* never, int* err) {
+  if (threadIdx.x != 0) return;
+  int abort = 0;
+  (void)poll_value<double>(never, err, &abort, -1, 0);
+}
+
+cudaError_t launch_wait_selftest(const double* never, int* err, cudaStream_t st) {
+  k_wait_selftest<<<1, 32, 0, st>>>(never, err);
+  return cudaGetLastError();
+}
+
 cudaError_t sweep_set_smem_limits(size_t max_smem) {
   cudaError_t e = cudaSuccess;
 #define DFG_ATTR(T, B)                                        \

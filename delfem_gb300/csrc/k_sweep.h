@@ -57,6 +57,8 @@ inline int sweep_val_stage(int max_nent, int B, int elem) { return sweep_rhs_byt
 cudaError_t launch_sweep(bool forward, bool fp32, int B, const SweepArgs& a, int grid, size_t smem,
                          cudaStream_t st);
 cudaError_t sweep_set_smem_limits(size_t max_smem);
+// one bounded wait on a value nothing writes (`never` holds the sentinel)
+cudaError_t launch_wait_selftest(const double* never, int* err, cudaStream_t st);
 
 // packing the factor into step records (k_sweep.cu)
 struct PackArgs {

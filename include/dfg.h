@@ -253,6 +253,15 @@ int dfg_solve_pcg_mixed(dfg_system sys, dfg_precond prec, double* conv_ratio,
  * bytes[0..2] = algorithmic bytes of one SpMV, forward and backward sweep. */
 int dfg_profile_kernels(dfg_system sys, dfg_precond prec, int mode, int reps, double* ms, double* bytes);
 
+/* Self-test of the device-side bounded waits (no counterpart in the
+ * reference): launches one wait, with the sweep kernels' own poll, on a value
+ * that nothing writes.  The wait gives up after its budget (about 2 s of SM
+ * clock), records the failure in the context's error word and returns; this
+ * call then reads and clears the record and returns DFG_TIMEOUT with the
+ * recorded wait site in *site (3 = poll of a dependency value).  Nothing
+ * faults, traps or hangs, and the context stays usable afterwards. */
+int dfg_selftest_wait_timeout(dfg_ctx ctx, int* site);
+
 /* ||b - A x||_2 / ||b||_2 in FP64 for the system's current matrix, with
  * b = the given host right-hand side and x = the update slot. */
 int dfg_true_residual(dfg_system sys, const double* b, double* rel);

@@ -222,3 +222,23 @@ def test_fp64_true_residual_target(gpu_ctx, oracle_lib):
     r = s.run("fp64", target_true=True)
     assert r["converged"] and r["conv"] <= 1e-8 and s.ls.true_residual() <= 1e-8
     s.close()
+
+
+def test_bounded_wait_times_out_and_context_stays_usable(gpu_ctx):
+    """A device wait on a value nothing writes gives up after its budget,
+    reports DFG_TIMEOUT with the wait site, and the context keeps working."""
+    import ctypes
+    import time
+    from delfem_gb300 import capi
+    from delfem_gb300 import meshgen as mg
+    site = ctypes.c_int(0)
+    t0 = time.perf_counter()
+    st = capi.lib().dfg_selftest_wait_timeout(gpu_ctx.h, ctypes.byref(site))
+    waited = time.perf_counter() - t0
+    assert st == capi.DFG_TIMEOUT and site.value == 3
+    assert 0.5 < waited < 30.0
+    assert b"timed out" in capi.lib().dfg_last_error(gpu_ctx.h)
+    s = _solver(gpu_ctx, mg.poisson2d_square(8, seed=3))
+    r = s.run("fp64")
+    assert r["converged"]
+    s.close()
