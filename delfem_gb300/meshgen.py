@@ -395,7 +395,7 @@ def serve_stream_3d(nreq: int = 500, seed: int = 5, rate: float = 50.0, emin: in
 # --------------------------------------------------------------------------
 
 PROBLEM_MAGIC = 0x44464731
-RESULT_MAGIC = 0x44464732
+RESULT_MAGIC = 0x44464733
 
 
 def write_problem(p: Problem, path: str) -> None:
@@ -442,8 +442,11 @@ def read_result(path: str) -> dict:
     out["rhs"] = take("<f8", n * b)
     (out["norm_res"],) = take("<d")
     out["ilu_ok"], out["prec_ok"] = take("<2i")
+    out["fill_level"], nnz_f = take("<2i")
+    out["rowptr_f"] = take("<i4", n + 1)
+    out["colind_f"] = take("<i4", nnz_f)
     out["fdiag"] = take("<f8", n * bs)
-    out["foffd"] = take("<f8", nnz * bs)
+    out["foffd"] = take("<f8", nnz_f * bs)
     out["converged"], out["iter"] = take("<2i")
     (out["conv"],) = take("<d")
     out["x"] = take("<f8", n * b)

@@ -86,6 +86,115 @@ void dfo_diaind(int n, const int* rowptr, const int* colind, int* diaind) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* ILU(k) fill pattern -- CMatDiaFrac_BlkCrs::AddFracPtn                      */
+/* (matvec/matdiafrac_blkcrs.cpp:1254-1382) as CPreconditioner_ILU calls it   */
+/* for one segment (ls/preconditioner.cpp:96-157)                             */
+/* ------------------------------------------------------------------------ */
+
+/* Row i starts as the sorted columns of A's row i, all at level 0.  Its
+ * entries k < i are visited in ascending order, fill entries found on the way
+ * included; an entry of level L >= lev_fill (any level when lev_fill == -1
+ * is allowed) spawns nothing.  Entry k spawns, for every entry (k, j), j > k,
+ * of the finished row k whose level M is below the limit, the entry (i, j) at
+ * level max(L, M) + 1 unless (i, j) is already in the row (its level then
+ * stays as it is) or j == i.  Unchanged pattern for lev_fill == 0, an empty
+ * off-diagonal pattern, or a full one.  Returns nnz of the factor; when it
+ * exceeds cap nothing is written and the caller retries with that capacity. */
+long dfo_ilu_pattern(int n, const int* rowptr, const int* colind, int lev_fill,
+                     int* rowptr_f, int* colind_f, long cap) {
+  const long nnz = rowptr[n];
+  if (lev_fill == 0 || nnz == 0 || nnz == (long)n * (n - 1)) {
+    if (nnz > cap) return nnz;
+    memcpy(rowptr_f, rowptr, sizeof(int) * (size_t)(n + 1));
+    memcpy(colind_f, colind, sizeof(int) * (size_t)nnz);
+    return nnz;
+  }
+  const int END = n;                     /* list terminator */
+  int* nxt = (int*)malloc(sizeof(int) * (size_t)(n + 1));  /* nxt[n] = head */
+  int* lv = (int*)malloc(sizeof(int) * (size_t)n);
+  int* mark = (int*)malloc(sizeof(int) * (size_t)n);
+  int* dia = (int*)malloc(sizeof(int) * (size_t)n);
+  long fcap = nnz * 2 + 16, fz = 0;
+  int* fcol = (int*)malloc(sizeof(int) * (size_t)fcap);
+  int* flev = (int*)malloc(sizeof(int) * (size_t)fcap);
+  long* fptr = (long*)malloc(sizeof(long) * (size_t)(n + 1));
+  for (int i = 0; i < n; ++i) mark[i] = -1;
+  fptr[0] = 0;
+  for (int i = 0; i < n; ++i) {
+    /* the row as a sorted linked list; nxt[END] is its first column */
+    int last = END;
+    for (int c = rowptr[i]; c < rowptr[i + 1]; ++c) {
+      const int j = colind[c];
+      nxt[last] = j;
+      lv[j] = 0;
+      mark[j] = i;
+      last = j;
+    }
+    nxt[last] = END;
+    for (int k = nxt[END]; k != END; k = nxt[k]) {
+      const int lik = lv[k];
+      if (lev_fill != -1 && lik + 1 > lev_fill) continue;
+      if (k >= i) break;
+      int pos = k; /* insertion point search starts at k: every new column is > k */
+      for (long kj = dia[k]; kj < fptr[k + 1]; ++kj) {
+        const int lkj = flev[kj];
+        if (lev_fill != -1 && lkj + 1 > lev_fill) continue;
+        const int j = fcol[kj];
+        if (j == i || mark[j] == i) continue;
+        while (nxt[pos] != END && nxt[pos] < j) pos = nxt[pos];
+        nxt[j] = nxt[pos];
+        nxt[pos] = j;
+        lv[j] = (lik > lkj ? lik : lkj) + 1;
+        mark[j] = i;
+        pos = j;
+      }
+    }
+    /* emit the row */
+    int cnt = 0;
+    for (int j = nxt[END]; j != END; j = nxt[j]) ++cnt;
+    if (fz + cnt > fcap) {
+      while (fz + cnt > fcap) fcap *= 2;
+      fcol = (int*)realloc(fcol, sizeof(int) * (size_t)fcap);
+      flev = (int*)realloc(flev, sizeof(int) * (size_t)fcap);
+    }
+    dia[i] = -1;
+    for (int j = nxt[END]; j != END; j = nxt[j]) {
+      if (dia[i] < 0 && j > i) dia[i] = (int)fz;
+      fcol[fz] = j;
+      flev[fz] = lv[j];
+      ++fz;
+    }
+    if (dia[i] < 0) dia[i] = (int)fz;
+    fptr[i + 1] = fz;
+  }
+  if (fz <= cap) {
+    for (int i = 0; i <= n; ++i) rowptr_f[i] = (int)fptr[i];
+    memcpy(colind_f, fcol, sizeof(int) * (size_t)fz);
+  }
+  free(nxt); free(lv); free(mark); free(dia); free(fcol); free(flev); free(fptr);
+  return fz;
+}
+
+/* SetValue_Initialize (matvec/matdiafrac_blkcrs.h:90-96): the factor storage
+ * is zeroed, then A's diagonal and off-diagonal blocks are copied into the
+ * slots of the same columns (A's pattern is a subset of the factor's). */
+int dfo_ilu_init(int n, int b, const int* rowptr, const int* colind, const double* diag, const double* offd,
+                 const int* rowptr_f, const int* colind_f, double* fdiag, double* foffd) {
+  const int bs = b * b;
+  memcpy(fdiag, diag, sizeof(double) * (size_t)n * bs);
+  memset(foffd, 0, sizeof(double) * (size_t)rowptr_f[n] * bs);
+  for (int i = 0; i < n; ++i) {
+    int cf = rowptr_f[i];
+    for (int c = rowptr[i]; c < rowptr[i + 1]; ++c) {
+      while (cf < rowptr_f[i + 1] && colind_f[cf] < colind[c]) ++cf;
+      if (cf == rowptr_f[i + 1] || colind_f[cf] != colind[c]) return -1;
+      memcpy(foffd + (size_t)cf * bs, offd + (size_t)c * bs, sizeof(double) * bs);
+    }
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Scatter (Mearge) -- matvec/matdia_blkcrs.cpp:165-258                      */
 /* ------------------------------------------------------------------------ */
 
@@ -722,6 +831,14 @@ int dfo_pcg(int n, int b, const int* rowptr, const int* colind, const int* diain
             const double* diag, const double* offd,
             const double* fdiag, const double* foffd,
             double* r, double* x, double* conv, unsigned* iter, double* work) {
+  return dfo_pcg_f(n, b, rowptr, colind, diag, offd, rowptr, colind, diaind, fdiag, foffd, r, x, conv, iter,
+                   work);
+}
+
+int dfo_pcg_f(int n, int b, const int* rowptr, const int* colind, const double* diag, const double* offd,
+              const int* rowptr_f, const int* colind_f, const int* diaind_f,
+              const double* fdiag, const double* foffd,
+              double* r, double* x, double* conv, unsigned* iter, double* work) {
   const long m = (long)n * b;
   const double tol = *conv;
   const unsigned mx_iter = *iter;
@@ -735,8 +852,8 @@ int dfo_pcg(int n, int b, const int* rowptr, const int* colind, const int* diain
     sq_inv_norm_res0 = 1.0 / s0;
   }
   memcpy(z, r, sizeof(double) * (size_t)m);
-  dfo_forward(n, b, rowptr, colind, diaind, fdiag, foffd, z);
-  dfo_backward(n, b, rowptr, colind, diaind, foffd, z);
+  dfo_forward(n, b, rowptr_f, colind_f, diaind_f, fdiag, foffd, z);
+  dfo_backward(n, b, rowptr_f, colind_f, diaind_f, foffd, z);
   memcpy(p, z, sizeof(double) * (size_t)m);
   double rz = vdot(m, r, z);
   for (unsigned it = 0; it < mx_iter; ++it) {
@@ -754,8 +871,8 @@ int dfo_pcg(int n, int b, const int* rowptr, const int* colind, const int* diain
       }
     }
     memcpy(z, r, sizeof(double) * (size_t)m);
-    dfo_forward(n, b, rowptr, colind, diaind, fdiag, foffd, z);
-    dfo_backward(n, b, rowptr, colind, diaind, foffd, z);
+    dfo_forward(n, b, rowptr_f, colind_f, diaind_f, fdiag, foffd, z);
+    dfo_backward(n, b, rowptr_f, colind_f, diaind_f, foffd, z);
     const double rz_new = vdot(m, r, z);
     const double beta = rz_new / rz;
     rz = rz_new;

@@ -1,5 +1,5 @@
 /*
- * dfg_oracle.h -- CPU oracle for the DelFEM assembly + ILU(0)-PCG path.
+ * dfg_oracle.h -- CPU oracle for the DelFEM assembly + ILU-PCG path.
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
  * algorithm, used by tests/, __graft_entry__.smoke() and bench.py's CPU
@@ -34,6 +34,19 @@ long dfo_pattern(int nnode, int nelem, int nnoel, const int* conn,
 /* ILU(0) split index: first CRS slot of row i whose column is > i
  * (matvec/matdiafrac_blkcrs.cpp:203-218). */
 void dfo_diaind(int n, const int* rowptr, const int* colind, int* diaind);
+
+/* Block pattern of the ILU(lev_fill) factor, without the diagonal, columns
+ * ascending per row (CMatDiaFrac_BlkCrs::AddFracPtn, matvec/matdiafrac_blkcrs.cpp:
+ * 1254-1382; lev_fill -1 = no level limit).  Returns the factor's nnz; when it
+ * exceeds cap nothing is written. */
+long dfo_ilu_pattern(int n, const int* rowptr, const int* colind, int lev_fill,
+                     int* rowptr_f, int* colind_f, long cap);
+
+/* A's values into the factor pattern, zero elsewhere (SetValue_Initialize,
+ * matvec/matdiafrac_blkcrs.h:90-96).  Returns -1 when A's pattern is not a
+ * subset of the factor's. */
+int dfo_ilu_init(int n, int b, const int* rowptr, const int* colind, const double* diag, const double* offd,
+                 const int* rowptr_f, const int* colind_f, double* fdiag, double* foffd);
 
 /* Element assembly (scatter follows CMatDia_BlkCrs::Mearge,
  * matvec/matdia_blkcrs.cpp:165-258, in element order).
@@ -92,6 +105,12 @@ int dfo_pcg(int n, int b, const int* rowptr, const int* colind, const int* diain
             const double* diag, const double* offd,
             const double* fdiag, const double* foffd,
             double* r, double* x, double* conv, unsigned* iter, double* work);
+
+/* dfo_pcg with the factor in its own pattern (ILU(k), k != 0). */
+int dfo_pcg_f(int n, int b, const int* rowptr, const int* colind, const double* diag, const double* offd,
+              const int* rowptr_f, const int* colind_f, const int* diaind_f,
+              const double* fdiag, const double* foffd,
+              double* r, double* x, double* conv, unsigned* iter, double* work);
 
 /* Wall-time helpers for the CPU baseline. */
 double dfo_now(void);

@@ -3,7 +3,7 @@
 Loads oracle/_build/libdfg_oracle.so (the C restatement in dfg_oracle.c,
 built by ``make -C oracle port``) and runs the whole hot path of the
 reference on a ``delfem_gb300.meshgen.Problem``: pattern, assembly,
-extra loads, Dirichlet finalize, ILU(0), PCG.  Only tests/, the smoke test
+extra loads, Dirichlet finalize, ILU(k) (k = 0 by default), PCG.  Only tests/, the smoke test
 and bench.py's CPU-baseline leg import this module; the product never does.
 
 ``run_reference_harness`` executes the reference itself (oracle/_ref,
@@ -56,6 +56,11 @@ def lib():
         L.dfo_matvec.argtypes = [_I, _I, _P, _P, _P, _P, _D, _P, _D, _P]
         L.dfo_pcg.argtypes = [_I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                               ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_uint), _P]
+        L.dfo_pcg_f.argtypes = [_I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_uint), _P]
+        L.dfo_ilu_pattern.restype = ctypes.c_long
+        L.dfo_ilu_pattern.argtypes = [_I, _P, _P, _I, _P, _P, ctypes.c_long]
+        L.dfo_ilu_init.argtypes = [_I, _I, _P, _P, _P, _P, _P, _P, _P, _P]
         L.dfo_now.restype = _D
         _lib = L
     return _lib
@@ -82,6 +87,21 @@ def diaind(rowptr, colind):
     d = np.zeros(n, dtype=np.int32)
     lib().dfo_diaind(n, _p(rowptr), _p(colind), _p(d))
     return d
+
+
+def ilu_pattern(rowptr, colind, fill_level: int):
+    """Block pattern (rowptr_f, colind_f) of the ILU(fill_level) factor."""
+    n = rowptr.size - 1
+    rowptr = np.ascontiguousarray(rowptr, dtype=np.int32)
+    colind = np.ascontiguousarray(colind if colind.size else np.zeros(1, np.int32), dtype=np.int32)
+    cap = max(2 * int(rowptr[-1]), 1)
+    while True:
+        rp = np.zeros(n + 1, dtype=np.int32)
+        ci = np.zeros(cap, dtype=np.int32)
+        nz = lib().dfo_ilu_pattern(n, _p(rowptr), _p(colind), fill_level, _p(rp), _p(ci), cap)
+        if nz <= cap:
+            return rp, ci[:nz]
+        cap = nz
 
 
 def assemble(p, rowptr, colind):
@@ -120,8 +140,9 @@ def assemble(p, rowptr, colind):
     return diag, offd[: colind.size * bs], res
 
 
-def solve(p, tol=None, maxit=None, stop_after_ilu=False) -> dict:
-    """The reference's whole path on the CPU; returns every intermediate."""
+def solve(p, tol=None, maxit=None, stop_after_ilu=False, fill_level: int = 0) -> dict:
+    """The reference's whole path on the CPU with an ILU(fill_level)
+    preconditioner; returns every intermediate."""
     L = lib()
     t0 = L.dfo_now()
     rowptr, colind = pattern(p.nnode, p.conn)
@@ -137,14 +158,28 @@ def solve(p, tol=None, maxit=None, stop_after_ilu=False) -> dict:
     offd = offd_c[: colind.size * bs]
     rhs = res.copy()
     dind = diaind(rowptr, colind)
-    fdiag = diag.copy()
-    foffd = offd.copy() if offd.size else np.zeros(1)
     t2 = L.dfo_now()
-    ilu_rc = L.dfo_ilu0(n, b, _p(rowptr), _p(colind), _p(dind), _p(fdiag), _p(foffd))
+    if fill_level == 0:
+        rowptr_f, colind_f, dind_f = rowptr, colind, dind
+        fdiag = diag.copy()
+        foffd = offd.copy() if offd.size else np.zeros(1)
+    else:
+        rowptr_f, colind_f = ilu_pattern(rowptr, colind, fill_level)
+        dind_f = diaind(rowptr_f, colind_f)
+        fdiag = np.zeros(n * bs)
+        foffd = np.zeros(max(colind_f.size, 1) * bs)
+        offd_a = offd if offd.size else np.zeros(1)
+        cf = colind_f if colind_f.size else np.zeros(1, np.int32)
+        if L.dfo_ilu_init(n, b, _p(rowptr), _p(colind), _p(diag), _p(offd_a), _p(rowptr_f), _p(cf),
+                          _p(fdiag), _p(foffd)) != 0:
+            raise ValueError("A's pattern is not inside the factor's")
+    cf = colind_f if colind_f.size else np.zeros(1, np.int32)
+    ilu_rc = L.dfo_ilu0(n, b, _p(rowptr_f), _p(cf), _p(dind_f), _p(fdiag), _p(foffd))
     t3 = L.dfo_now()
     out = dict(n=n, b=b, nnz=colind.size, rowptr=rowptr, colind=colind, diaind=dind,
-               diag=diag, offd=offd, rhs=rhs, norm_res=norm_res, ilu_rc=ilu_rc,
-               fdiag=fdiag, foffd=foffd[: colind.size * bs], t_assemble=t1 - t0, t_ilu=t3 - t2)
+               diag=diag, offd=offd, rhs=rhs, norm_res=norm_res, ilu_rc=ilu_rc, fill_level=fill_level,
+               rowptr_f=rowptr_f, colind_f=colind_f, diaind_f=dind_f,
+               fdiag=fdiag, foffd=foffd[: colind_f.size * bs], t_assemble=t1 - t0, t_ilu=t3 - t2)
     if stop_after_ilu:
         return out
     r = rhs.copy()
@@ -154,8 +189,8 @@ def solve(p, tol=None, maxit=None, stop_after_ilu=False) -> dict:
     it = ctypes.c_uint(p.maxit if maxit is None else maxit)
     offd_a = offd if offd.size else np.zeros(1)
     t4 = L.dfo_now()
-    ok = L.dfo_pcg(n, b, _p(rowptr), _p(colind), _p(dind), _p(diag), _p(offd_a), _p(fdiag), _p(foffd),
-                   _p(r), _p(x), ctypes.byref(conv), ctypes.byref(it), _p(work))
+    ok = L.dfo_pcg_f(n, b, _p(rowptr), _p(colind), _p(diag), _p(offd_a), _p(rowptr_f), _p(cf), _p(dind_f),
+                     _p(fdiag), _p(foffd), _p(r), _p(x), ctypes.byref(conv), ctypes.byref(it), _p(work))
     t5 = L.dfo_now()
     out.update(x=x, conv=conv.value, iter=it.value, converged=bool(ok), t_pcg=t5 - t4)
     return out
@@ -187,11 +222,12 @@ def harness_available() -> bool:
     return os.path.exists(HARNESS)
 
 
-def run_reference_harness(p) -> dict:
-    """Runs the reference code itself (oracle/_ref/ref_harness) on ``p``."""
+def run_reference_harness(p, fill_level: int = 0) -> dict:
+    """Runs the reference code itself (oracle/_ref/ref_harness) on ``p`` with
+    an ILU preconditioner of the given fill level."""
     from delfem_gb300 import meshgen as mg
     with tempfile.TemporaryDirectory() as td:
         fi, fo = os.path.join(td, "p.bin"), os.path.join(td, "r.bin")
         mg.write_problem(p, fi)
-        subprocess.run([HARNESS, fi, fo], check=True, stdout=subprocess.DEVNULL)
+        subprocess.run([HARNESS, fi, fo, str(fill_level)], check=True, stdout=subprocess.DEVNULL)
         return mg.read_result(fo)

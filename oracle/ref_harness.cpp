@@ -8,8 +8,9 @@
 //   CLinearSystem_Field::AddPattern_Field -> BC flags -> InitializeMarge ->
 //   AddLinSys_* (or the per-element-coefficient restatement feeding the
 //   reference's own Mearge) -> extra loads -> FinalizeMarge ->
-//   CPreconditioner_ILU(fill 0) -> LsSol::Solve_PCG.
+//   CPreconditioner_ILU(fill level, 0 by default) -> LsSol::Solve_PCG.
 //
+// Usage: ref_harness problem.bin out.bin [fill_level]
 // Input / output formats are described in tests/golden/make_golden.py.
 #include <cassert>
 #include <cmath>
@@ -208,8 +209,9 @@ static void wr(FILE* f, const void* p, size_t n) { if (n) fwrite(p, 1, n, f); }
 static void wri(FILE* f, int v) { wr(f, &v, 4); }
 
 int main(int argc, char** argv) {
-  if (argc != 3) { fprintf(stderr, "usage: %s problem.bin out.bin\n", argv[0]); return 2; }
+  if (argc != 3 && argc != 4) { fprintf(stderr, "usage: %s problem.bin out.bin [fill_level]\n", argv[0]); return 2; }
   Problem p = load(argv[1]);
+  const int fill_level = argc == 4 ? atoi(argv[3]) : 0;
   const int b = p.b;
   CFieldWorld world;
   GridMesh mesh(p);
@@ -234,7 +236,7 @@ int main(int argc, char** argv) {
         if (p.bcflag[(size_t)i * b + d]) bc.SetBC(i, d);
   }
   LsSol::CPreconditioner_ILU prec;
-  prec.SetFillInLevel(0);
+  prec.SetFillInLevel(fill_level);
   prec.SetLinearSystem(ls.m_ls);
 
   ls.InitializeMarge();
@@ -274,17 +276,31 @@ int main(int argc, char** argv) {
     for (int q = 0; q < bs; ++q) diag[(size_t)i * bs + q] = dv[q];
     for (int d = 0; d < b; ++d) rhs[(size_t)i * b + d] = res.GetValue(i, d);
   }
-  // ILU(0) factor, computed through the same calls the preconditioner makes
-  // (SetValue_Initialize + DoILUDecomp; preconditioner.cpp:229-272).
+  // ILU factor, computed through the same calls the preconditioner makes for
+  // one segment: the level-0 copy of the pattern, then for a non-zero level
+  // AddFracPtn + MakePatternFinalize (preconditioner.cpp:96-157), then
+  // SetValue_Initialize + DoILUDecomp (preconditioner.cpp:229-272).
   MatVec::CMatDiaFrac_BlkCrs frac(0, A);
+  if (fill_level != 0) {
+    frac.AddFracPtn(fill_level);
+    frac.MakePatternFinalize();
+  }
   frac.SetValue_Initialize(A);
   const bool ilu_ok = frac.DoILUDecomp();
-  std::vector<double> fdiag((size_t)n * bs), foffd((size_t)rowptr[n] * bs);
+  std::vector<int> rowptr_f(n + 1, 0), colind_f;
+  for (int i = 0; i < n; ++i) {
+    unsigned int np = 0;
+    const unsigned int* ci = frac.GetPtrIndPSuP(i, np);
+    for (unsigned k = 0; k < np; ++k) colind_f.push_back((int)ci[k]);
+    rowptr_f[i + 1] = (int)colind_f.size();
+  }
+  const int nnz_f = rowptr_f[n];
+  std::vector<double> fdiag((size_t)n * bs), foffd((size_t)nnz_f * bs);
   for (int i = 0; i < n; ++i) {
     const double* dv = frac.GetValDiaPtr(i);
     for (int q = 0; q < bs; ++q) fdiag[(size_t)i * bs + q] = dv[q];
   }
-  for (int c = 0; c < rowptr[n]; ++c) {
+  for (int c = 0; c < nnz_f; ++c) {
     const double* cv = frac.GetValCrsPtr(c);
     for (int q = 0; q < bs; ++q) foffd[(size_t)c * bs + q] = cv[q];
   }
@@ -303,7 +319,7 @@ int main(int argc, char** argv) {
 
   FILE* f = fopen(argv[2], "wb");
   if (!f) { perror(argv[2]); return 2; }
-  wri(f, 0x44464732); wri(f, n); wri(f, b); wri(f, rowptr[n]);
+  wri(f, 0x44464733); wri(f, n); wri(f, b); wri(f, rowptr[n]);
   wr(f, rowptr.data(), rowptr.size() * 4);
   wr(f, colind.data(), colind.size() * 4);
   wr(f, diag.data(), diag.size() * 8);
@@ -311,6 +327,9 @@ int main(int argc, char** argv) {
   wr(f, rhs.data(), rhs.size() * 8);
   wr(f, &norm_res, 8);
   wri(f, ilu_ok ? 1 : 0); wri(f, prec_ok ? 1 : 0);
+  wri(f, fill_level); wri(f, nnz_f);
+  wr(f, rowptr_f.data(), rowptr_f.size() * 4);
+  wr(f, colind_f.data(), colind_f.size() * 4);
   wr(f, fdiag.data(), fdiag.size() * 8);
   wr(f, foffd.data(), foffd.size() * 8);
   wri(f, converged ? 1 : 0); wri(f, (int)iter); wr(f, &conv, 8);

@@ -25,6 +25,11 @@ def golden_files():
     return sorted(glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
 
 
+def golden_iluk_files():
+    """Fixtures with an ILU fill level other than 0 (ref_fill_level)."""
+    return sorted(glob.glob(os.path.join(GOLDEN_DIR, "iluk", "*.npz")))
+
+
 def load_golden(path):
     """Returns (problem, reference outputs) of one committed fixture."""
     from delfem_gb300 import meshgen as mg

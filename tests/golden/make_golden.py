@@ -4,8 +4,11 @@ itself (the DelFEM sources compiled headless into oracle/_ref/ref_harness by
 
 Each fixture <name>.npz holds the problem (mesh, coefficients, loads,
 Dirichlet flags, parameters) and the reference's outputs: the block pattern,
-the assembled matrix and right-hand side after FinalizeMarge, the ILU(0)
+the assembled matrix and right-hand side after FinalizeMarge, the ILU
 factor, and the result of LsSol::Solve_PCG (iterations, ratio, solution).
+The fixtures in this directory use ILU(0); those in iluk/ use other fill
+levels (CPreconditioner_ILU::SetFillInLevel) and add the factor's own block
+pattern (ref_rowptr_f, ref_colind_f) and ref_fill_level.
 
 Harness problem file (little-endian): int32 magic 0x44464731, kind, nnode,
 ndim, nelem, nnoel, b; f64 coords[nnode*ndim]; i32 conn[nelem*nnoel];
@@ -13,7 +16,7 @@ i32 has_coef (+ f64 coef[nelem]); f64 params[8]; i32 bcflag[nnode*b];
 i32 has_load (+ f64 load[nnode*b]); i32 has_u (+ f64 u); i32 has_v (+ f64 v);
 f64 tol; i32 maxit.  The result file layout is read by meshgen.read_result.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [ilu0|iluk|all]
 """
 from __future__ import annotations
 
@@ -44,30 +47,60 @@ def cases():
     ]
 
 
-def fixture_name(p: mg.Problem, k: int) -> str:
+def iluk_cases():
+    """(problem, fill level): the solid default ILU(1) of CEqnSystem_Solid2D
+    (eqnsys_solid.cpp:640), higher levels, a level whose pattern is smaller
+    than the level below it, and the unlimited level -1 (complete LU)."""
+    return [
+        (mg.solid2d_cantilever(10, 5, seed=13, coef_sigma=0.5), 1),
+        (mg.poisson2d_square(12, seed=12, coef_sigma=0.5), 2),
+        (mg.poisson2d_square(8, seed=11), 3),
+        (mg.solid3d_cube(3, seed=15, coef_sigma=1.0), 1),
+        (mg.poisson3d_cube(5, seed=18, coef_sigma=1.0), 2),
+        (mg.solid2d_cantilever(6, 3, seed=14, coef_sigma=0.0), -1),
+        (mg.diffusion2d_square(6, seed=19), 1),
+    ]
+
+
+def fixture_name(p: mg.Problem, k: int, fill_level: int = 0) -> str:
     tag = "coef" if p.coef is not None else "uniform"
-    return f"{k:02d}_{p.name.replace('^', 'c')}_{tag}"
+    lev = "" if fill_level == 0 else (f"_ilu{fill_level}" if fill_level > 0 else "_ilufull")
+    return f"{k:02d}_{p.name.replace('^', 'c')}_{tag}{lev}"
+
+
+def write_fixture(path: str, p: mg.Problem, fill_level: int) -> None:
+    R = O.run_reference_harness(p, fill_level)
+    d = dict(kind=p.kind, coords=p.coords, conn=p.conn, params=p.params, bcflag=p.bcflag, tol=p.tol,
+             maxit=p.maxit)
+    for nm in ("coef", "load", "u", "v"):
+        a = getattr(p, nm)
+        if a is not None:
+            d[nm] = a
+    for nm in ("rowptr", "colind", "diag", "offd", "rhs", "fdiag", "foffd", "x"):
+        d["ref_" + nm] = R[nm]
+    for nm in ("norm_res", "ilu_ok", "converged", "iter", "conv"):
+        d["ref_" + nm] = np.array(R[nm])
+    if fill_level != 0:
+        d["ref_fill_level"] = np.array(fill_level)
+        d["ref_rowptr_f"] = R["rowptr_f"]
+        d["ref_colind_f"] = R["colind_f"]
+    np.savez_compressed(path, **d)
+    print(f"{path}: n={R['n']} b={R['b']} nnz={R['nnz']} nnz_f={R['colind_f'].size} iter={R['iter']} "
+          f"conv={R['conv']:.3e}")
 
 
 def main():
     if not O.harness_available():
         raise SystemExit("oracle/_ref/ref_harness is missing: run `make -C oracle ref` where the reference exists")
+    which = sys.argv[1] if len(sys.argv) > 1 else "all"
     here = os.path.dirname(os.path.abspath(__file__))
-    for k, p in enumerate(cases()):
-        R = O.run_reference_harness(p)
-        d = dict(kind=p.kind, coords=p.coords, conn=p.conn, params=p.params, bcflag=p.bcflag, tol=p.tol,
-                 maxit=p.maxit)
-        for nm in ("coef", "load", "u", "v"):
-            a = getattr(p, nm)
-            if a is not None:
-                d[nm] = a
-        for nm in ("rowptr", "colind", "diag", "offd", "rhs", "fdiag", "foffd", "x"):
-            d["ref_" + nm] = R[nm]
-        for nm in ("norm_res", "ilu_ok", "converged", "iter", "conv"):
-            d["ref_" + nm] = np.array(R[nm])
-        path = os.path.join(here, fixture_name(p, k) + ".npz")
-        np.savez_compressed(path, **d)
-        print(f"{path}: n={R['n']} b={R['b']} nnz={R['nnz']} iter={R['iter']} conv={R['conv']:.3e}")
+    if which in ("ilu0", "all"):
+        for k, p in enumerate(cases()):
+            write_fixture(os.path.join(here, fixture_name(p, k) + ".npz"), p, 0)
+    if which in ("iluk", "all"):
+        os.makedirs(os.path.join(here, "iluk"), exist_ok=True)
+        for k, (p, lev) in enumerate(iluk_cases()):
+            write_fixture(os.path.join(here, "iluk", fixture_name(p, k, lev) + ".npz"), p, lev)
 
 
 if __name__ == "__main__":

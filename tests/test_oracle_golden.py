@@ -4,7 +4,7 @@ ILU(0) factor and the PCG result must be bit-identical."""
 import numpy as np
 import pytest
 
-from conftest import bits, golden_files, load_golden
+from conftest import bits, golden_files, golden_iluk_files, load_golden
 
 
 @pytest.mark.parametrize("path", golden_files(), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
@@ -31,3 +31,52 @@ def test_reference_solution_meets_tolerance(path, oracle_lib):
     out = oracle_lib.solve(p, stop_after_ilu=True)
     rel = oracle_lib.true_residual(out, ref["x"])
     assert rel < 1e-7
+
+
+@pytest.mark.parametrize("path", golden_iluk_files(), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
+def test_oracle_iluk_matches_reference(path, oracle_lib):
+    """ILU(k): the fill pattern (AddFracPtn), the factor on it and the PCG
+    result are bit-identical to the reference's at the fixture's level."""
+    p, ref = load_golden(path)
+    lev = int(ref["fill_level"])
+    out = oracle_lib.solve(p, fill_level=lev)
+    assert np.array_equal(out["rowptr_f"], ref["rowptr_f"])
+    assert np.array_equal(out["colind_f"], ref["colind_f"])
+    for k in ("diag", "offd", "rhs", "fdiag", "foffd", "x"):
+        assert np.array_equal(bits(out[k]), bits(ref[k])), k
+    assert out["iter"] == int(ref["iter"]) and out["conv"] == float(ref["conv"])
+
+
+def test_iluk_fixtures_cover_levels():
+    levs = sorted(int(load_golden(f)[1]["fill_level"]) for f in golden_iluk_files())
+    assert levs[0] == -1 and 1 in levs and 2 in levs and 3 in levs
+
+
+def test_iluk_pattern_properties(oracle_lib):
+    """Level 0 leaves the pattern as it is; every level keeps A's pattern;
+    the unlimited level gives the complete fill of natural-order LU."""
+    from delfem_gb300 import meshgen as mg
+    p = mg.poisson2d_square(9, seed=3)
+    rp, ci = oracle_lib.pattern(p.nnode, p.conn)
+    r0, c0 = oracle_lib.ilu_pattern(rp, ci, 0)
+    assert np.array_equal(r0, rp) and np.array_equal(c0, ci)
+    n = rp.size - 1
+    for lev in (1, 2, 5, -1):
+        rf, cf = oracle_lib.ilu_pattern(rp, ci, lev)
+        for i in range(n):
+            assert set(ci[rp[i]:rp[i + 1]]) <= set(cf[rf[i]:rf[i + 1]])
+            assert np.all(np.diff(cf[rf[i]:rf[i + 1]]) > 0) and i not in set(cf[rf[i]:rf[i + 1]])
+    # complete LU fill of the structurally symmetric pattern: row i holds every
+    # column j > i up to its last original neighbour's reach (the profile)
+    rf, cf = oracle_lib.ilu_pattern(rp, ci, -1)
+    dense = np.zeros((n, n), bool)
+    for i in range(n):
+        dense[i, ci[rp[i]:rp[i + 1]]] = True
+    for k in range(n):  # symbolic Gaussian elimination
+        lower = np.nonzero(dense[k + 1:, k])[0] + k + 1
+        upper = np.nonzero(dense[k, k + 1:])[0] + k + 1
+        for i in lower:
+            dense[i, upper] = True
+    np.fill_diagonal(dense, False)
+    for i in range(n):
+        assert np.array_equal(cf[rf[i]:rf[i + 1]], np.nonzero(dense[i])[0]), i
