@@ -52,10 +52,10 @@ CONFIGS = {
     "solid3d_48": dict(kind="solid3d", n=48),
     "solid2d_200x100": dict(kind="solid2d", nx=200, ny=100),
 }
-# PCG iterations of the full FP64 solve of the default workload, measured with
-# the reference's own algorithm (bit-exact CPU restatement, 1e-8); used to
-# extrapolate the bounded CPU samples to whole solves.
-REF_ITERS = {"solid2d_1000x500": 2540, "poisson2d_128": 132, "solid2d_200x100": None}
+# PCG iterations of the full FP64 solve of a workload at an ILU fill level,
+# measured with the reference's own algorithm (bit-exact CPU restatement,
+# 1e-8); used to extrapolate the bounded CPU samples to whole solves.
+REF_ITERS = {("solid2d_1000x500", 0): 2540, ("poisson2d_128", 0): 132}
 
 
 # (name in the JSON line, solver mode)
@@ -158,19 +158,19 @@ class ClockSampler:
 
 def _cpu_sample(args):
     """Bounded CPU sample of one solve (runs in a spawned process): assembly +
-    Dirichlet + ILU(0) of the full problem and `iters` PCG iterations."""
-    name, iters = args
+    Dirichlet + ILU(k) of the full problem and `iters` PCG iterations."""
+    name, iters, fill_level = args
     sys.path.insert(0, ROOT)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     p = make_problem(name)
     t0 = time.perf_counter()
-    out = O.solve(p, tol=1e-30, maxit=iters)
+    out = O.solve(p, tol=1e-30, maxit=iters, fill_level=fill_level)
     t = time.perf_counter() - t0
     return dict(t_assemble=out["t_assemble"], t_ilu=out["t_ilu"], t_pcg=out["t_pcg"], iters=iters, wall=t)
 
 
-def cpu_rate(name, iters_full, procs, sample_iters):
+def cpu_rate(name, iters_full, procs, sample_iters, fill_level=0):
     """Solves/s of the reference algorithm on `procs` host cores (independent
     solves, one per core), extrapolated from bounded samples."""
     import multiprocessing as mp
@@ -179,7 +179,7 @@ def cpu_rate(name, iters_full, procs, sample_iters):
     O.build()
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs) as pool:
-        res = pool.map(_cpu_sample, [(name, sample_iters)] * procs)
+        res = pool.map(_cpu_sample, [(name, sample_iters, fill_level)] * procs)
     per = []
     for r in res:
         t_it = r["t_pcg"] / max(r["iters"], 1)
@@ -209,7 +209,7 @@ def run_gpu(args, rank, world, local):
 
     p = make_problem(args.config)
     ctx = L.Context(local)
-    s = FESolve(ctx, p)
+    s = FESolve(ctx, p, fill_level=args.fill_level)
     stream = ctx.stream
 
     def ev():
@@ -398,6 +398,7 @@ def compose_line(args, world, p, results, prof, e2e, head):
         "dtype": "f32" if head == "mixed_fp32_all" else "f32 factor/sweeps, f64 SpMV/vectors",
         "data": "synthetic (seeded jittered mesh, log-normal coefficients)",
         "config": {"workload": args.config, "nodes": p.nnode, "dof": p.ndof, "elements": p.nelem,
+                   "preconditioner": f"ILU({args.fill_level})" if args.fill_level >= 0 else "ILU(no level limit)",
                    "tol": 1e-8, "stop": "true relative residual <= tol (all arms)", "mixed_form": head,
                    "parallelism": f"replicas x{world} (independent solves per GPU)",
                    "l2": "working set (matrix 112 MB + factor records + vectors) larger than the 129 MB L2; no flush"},
@@ -419,11 +420,12 @@ def compose_line(args, world, p, results, prof, e2e, head):
         line["e2e"] = {"value": round(e2e["value"], 4), "unit": "solves/s", "h2d_bytes_per_step": int(e2e["h2d"]),
                        "d2h_bytes_per_step": int(e2e["d2h"])}
     if not args.no_cpu_baseline:
-        iters_full = REF_ITERS.get(args.config) or results[("plain_fp64" if "plain_fp64" in results else head)]["iters"][-1]
+        iters_full = REF_ITERS.get((args.config, args.fill_level)) or \
+            results[("plain_fp64" if "plain_fp64" in results else head)]["iters"][-1]
         sample_iters = args.cpu_sample_iters
-        rate, t_solve, res = cpu_rate(args.config, iters_full, 1, sample_iters)
+        rate, t_solve, res = cpu_rate(args.config, iters_full, 1, sample_iters, args.fill_level)
         line["cpu_baseline"] = {"value": round(rate, 6), "unit": "solves/s", "cores": 1, "kind": "port",
-                                "sample": f"assembly + Dirichlet + ILU(0) of the full workload and {sample_iters} "
+                                "sample": f"assembly + Dirichlet + ILU({args.fill_level}) of the full workload and {sample_iters} "
                                           f"PCG iterations on one host core, extrapolated to {iters_full + 1} "
                                           f"iterations ({t_solve:.1f} s per solve)"}
     return line
@@ -688,13 +690,13 @@ def run_reference(args, rank, world):
     procs = os.cpu_count() or 1
     if CONFIGS[args.config]["kind"] == "serve":
         return run_reference_serve(args, world, procs)
-    iters_full = REF_ITERS.get(args.config)
+    iters_full = REF_ITERS.get((args.config, args.fill_level))
     if iters_full is None:
         iters_full = 3000
     rates = []
     t_all0 = time.perf_counter()
     for i in range(args.warmup + args.steps):
-        rate, t_solve, res = cpu_rate(args.config, iters_full, procs, args.cpu_sample_iters)
+        rate, t_solve, res = cpu_rate(args.config, iters_full, procs, args.cpu_sample_iters, args.fill_level)
         if i >= args.warmup:
             rates.append(rate)
     value = statistics.median(rates)
@@ -702,11 +704,11 @@ def run_reference(args, rank, world):
         "metric": METRIC, "impl": "reference", "value": round(value, 6), "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered mesh, log-normal coefficients)",
-        "config": {"workload": args.config, "tol": 1e-8,
+        "config": {"workload": args.config, "tol": 1e-8, "preconditioner": f"ILU({args.fill_level})",
                    "parallelism": f"{procs} independent single-threaded solves (one per host core)"},
         "ms_per_step": round(1e3 * procs / value, 1),
         "cpu_baseline": {"value": round(value, 6), "unit": "solves/s", "cores": procs, "kind": "port",
-                         "sample": f"per core: assembly + Dirichlet + ILU(0) of the full workload and "
+                         "sample": f"per core: assembly + Dirichlet + ILU({args.fill_level}) of the full workload and "
                                    f"{args.cpu_sample_iters} PCG iterations, extrapolated to {iters_full + 1} "
                                    f"iterations; the reference algorithm's bit-exact C restatement"},
         "e2e": {"value": round(value, 6), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -753,6 +755,8 @@ def main():
     ap.add_argument("--cpu-sample-iters", type=int, default=60)
     ap.add_argument("--cpu-serve-requests", type=int, default=12,
                     help="requests the one-core CPU baseline solves (serving configs)")
+    ap.add_argument("--fill-level", type=int, default=0,
+                    help="single-solve workloads: ILU fill level (CPreconditioner_ILU::SetFillInLevel; -1 = no limit)")
     ap.add_argument("--max-inflight", type=int, default=128, help="serving: solves resident at once (<= 256)")
     ap.add_argument("--size-groups", type=int, default=0, help="serving: 1 table, 2-3 size groups, 0 = server default (3)")
     ap.add_argument("--ref-requests-per-core", type=int, default=2,

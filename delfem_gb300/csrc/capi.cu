@@ -818,16 +818,30 @@ void run_sweep(dfg_ctx ctx_, bool forward, int b, bool fp32, const SweepLaunch& 
   launched(ctx_);
 }
 
+// The factor's block pattern: the system's for ILU(0), the preconditioner's
+// own when fill-in changed it.
+struct FactorPattern {
+  const int *rowptr, *colind, *diaind;        // host
+  const int *d_rowptr, *d_colind, *d_diaind;  // device
+};
+FactorPattern factor_pattern(dfg_precond pr) {
+  if (pr->own_pattern)
+    return {pr->h_rowptr.data(), pr->h_colind.data(), pr->h_diaind.data(),
+            pr->rowptr.as<int>(), pr->colind.as<int>(), pr->diaind.as<int>()};
+  const dfg_system s = pr->sys;
+  return {s->h_rowptr.data(), s->h_colind.data(), s->h_diaind.data(),
+          s->rowptr.as<int>(), s->colind.as<int>(), s->diaind.as<int>()};
+}
+
 // Schedule choice: the cost model keeps a few candidate range sizes, the
 // fullest-step plan joins them, and each is timed on the device with one FP32
 // sweep of the real structure (values do not change the timing); the fastest
 // wins.
 void setup_sweep(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, const dfg_system sys, bool forward) {
-  std::vector<SweepPlan> cands = candidate_sweep_plans(sys->n, sys->b, sys->h_rowptr.data(), sys->h_colind.data(),
-                                                       sys->h_diaind.data(), forward, 32, 4);
+  const FactorPattern F = factor_pattern(pr);
+  std::vector<SweepPlan> cands = candidate_sweep_plans(sys->n, sys->b, F.rowptr, F.colind, F.diaind, forward, 32, 4);
   // and the fullest-step plan (ranges of up to 32 grid lines), if it differs
-  SweepPlan full = fullest_sweep_plan(sys->n, sys->b, sys->h_rowptr.data(), sys->h_colind.data(),
-                                      sys->h_diaind.data(), forward, 32);
+  SweepPlan full = fullest_sweep_plan(sys->n, sys->b, F.rowptr, F.colind, F.diaind, forward, 32);
   bool seen = false;
   for (const SweepPlan& c : cands) seen |= (c.nranges == full.nranges && c.nsteps == full.nsteps);
   if (!seen) cands.push_back(std::move(full));
@@ -899,8 +913,8 @@ extern "C" int dfg_precond_destroy(dfg_precond prec) {
 
 extern "C" int dfg_precond_set_fill_level(dfg_precond prec, int lev) {
   if (!prec) return DFG_INVALID_ARGUMENT;
-  if (lev != 0) {
-    prec->ctx->last_error = "only fill-in level 0 is implemented";
+  if (lev < -1) {
+    prec->ctx->last_error = "fill-in level must be >= -1 (-1: no limit)";
     return DFG_INVALID_ARGUMENT;
   }
   prec->lev = lev;
@@ -916,11 +930,41 @@ extern "C" int dfg_precond_set_linear_system(dfg_precond prec, dfg_system sys) {
     prec->sys = sys;
     prec->n = sys->n;
     prec->b = sys->b;
-    prec->nnz = sys->nnz;
+    prec->symbolic = prec->numeric = prec->numeric32 = false;
+    // fill-in (CPreconditioner_ILU::SetLinearSystem -> AddFracPtn)
+    prec->own_pattern = false;
+    prec->h_rowptr.clear(); prec->h_colind.clear(); prec->h_diaind.clear();
+    prec->rowptr.release(); prec->colind.release(); prec->diaind.release(); prec->a2f.release();
+    if (prec->lev != 0) {
+      std::vector<int> rp, ci;
+      REQUIRE(ilu_fill_pattern(sys->n, sys->h_rowptr.data(), sys->h_colind.data(), prec->lev, rp, ci, INT32_MAX - 1),
+              DFG_INVALID_ARGUMENT, "the ILU fill-in pattern exceeds 2^31 blocks");
+      if ((long long)ci.size() != sys->nnz) {
+        std::vector<int> a2f;
+        REQUIRE(factor_slot_map(sys->n, sys->h_rowptr.data(), sys->h_colind.data(), rp.data(), ci.data(), a2f),
+                DFG_INVALID_ARGUMENT, "the fill-in pattern does not contain the matrix pattern");
+        prec->h_diaind.resize(sys->n);
+        for (int i = 0; i < sys->n; ++i) {
+          int d = rp[i + 1];
+          for (int c = rp[i]; c < rp[i + 1]; ++c)
+            if (ci[c] > i) { d = c; break; }
+          prec->h_diaind[i] = d;
+        }
+        prec->h_rowptr = std::move(rp);
+        prec->h_colind = std::move(ci);
+        upload(ctx, prec->rowptr, prec->h_rowptr.data(), prec->h_rowptr.size());
+        upload(ctx, prec->colind, prec->h_colind.data(), std::max<size_t>(prec->h_colind.size(), 1));
+        upload(ctx, prec->diaind, prec->h_diaind.data(), prec->h_diaind.size());
+        upload(ctx, prec->a2f, a2f.data(), std::max<size_t>(a2f.size(), 1));
+        prec->own_pattern = true;
+      }
+    }
+    const FactorPattern F = factor_pattern(prec);
+    prec->nnz = F.rowptr[sys->n];
     const size_t bs = (size_t)sys->b * sys->b;
     dalloc(ctx, prec->fdiag, (size_t)sys->n * bs * 8);
-    dalloc(ctx, prec->foffd, (size_t)std::max<long long>(sys->nnz, 1) * bs * 8);
-    prec->lev_fwd = build_levels(sys->n, sys->h_rowptr.data(), sys->h_colind.data(), sys->h_diaind.data(), true);
+    dalloc(ctx, prec->foffd, (size_t)std::max<long long>(prec->nnz, 1) * bs * 8);
+    prec->lev_fwd = build_levels(sys->n, F.rowptr, F.colind, F.diaind, true);
     upload(ctx, prec->lev_rows, prec->lev_fwd.rows.data(), std::max<size_t>(prec->lev_fwd.rows.size(), 1));
     setup_sweep(ctx, prec, prec->fwd, sys, true);
     setup_sweep(ctx, prec, prec->bwd, sys, false);
@@ -940,19 +984,26 @@ extern "C" int dfg_precond_set_value(dfg_precond prec, dfg_system sys) {
     dfg_ctx ctx_ = ctx;
     REQUIRE(prec->symbolic && prec->sys == sys, DFG_NOT_READY, "dfg_precond_set_linear_system must come first");
     const size_t bs = (size_t)sys->b * sys->b;
-    // SetValue_Initialize: copy A into the factor storage
+    // SetValue_Initialize: copy A into the factor storage (zero at fill-in)
     CK(cudaMemcpyAsync(prec->fdiag.p, sys->diag.p, (size_t)sys->n * bs * 8, cudaMemcpyDeviceToDevice, ctx->stream));
-    if (sys->nnz)
+    if (prec->own_pattern) {
+      CK(cudaMemsetAsync(prec->foffd.p, 0, (size_t)prec->nnz * bs * 8, ctx->stream));
+      CK(launch_factor_init(sys->b, sys->nnz, prec->a2f.as<int>(), sys->offd.as<double>(), prec->foffd.as<double>(),
+                            ctx->stream));
+      launched(ctx);
+    } else if (sys->nnz) {
       CK(cudaMemcpyAsync(prec->foffd.p, sys->offd.p, (size_t)sys->nnz * bs * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    const FactorPattern F = factor_pattern(prec);
     Scratch sc = scratch_of(ctx);
     int* nsing = sc.tickets + 8;
     CK(cudaMemsetAsync(nsing, 0, sizeof(int), ctx->stream));
     const Levels& L = prec->lev_fwd;
     const int nl = (int)L.ptr.size() - 1;
     for (int l = 0; l < nl; ++l)
-      CK(launch_ilu_level(sys->b, prec->lev_rows.as<int>() + L.ptr[l], L.ptr[l + 1] - L.ptr[l], sys->rowptr.as<int>(),
-                          sys->colind.as<int>(), sys->diaind.as<int>(), prec->fdiag.as<double>(),
-                          prec->foffd.as<double>(), nsing, ctx->stream));
+      CK(launch_ilu_level(sys->b, prec->lev_rows.as<int>() + L.ptr[l], L.ptr[l + 1] - L.ptr[l], F.d_rowptr,
+                          F.d_colind, F.d_diaind, prec->fdiag.as<double>(), prec->foffd.as<double>(), nsing,
+                          ctx->stream));
     launched(ctx, nl);
     int h_nsing = 0;
     CK(cudaMemcpyAsync(&h_nsing, nsing, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -962,7 +1013,7 @@ extern "C" int dfg_precond_set_value(dfg_precond prec, dfg_system sys) {
     prec->numeric = true;
     prec->numeric32 = false;
     if (h_nsing > 10) {
-      set_err(ctx, "ILU(0): " + std::to_string(h_nsing) + " singular pivots (more than 10)");
+      set_err(ctx, "ILU: " + std::to_string(h_nsing) + " singular pivots (more than 10)");
       return DFG_SINGULAR_PIVOT;
     }
     return DFG_OK;
@@ -1002,6 +1053,19 @@ extern "C" int dfg_precond_solve(dfg_precond prec, dfg_system sys, int iv) {
     }
     return DFG_OK;
   });
+}
+
+extern "C" int dfg_precond_get_pattern(dfg_precond prec, long long* nnz, int* rowptr, int* colind) {
+  if (!prec) return DFG_INVALID_ARGUMENT;
+  if (!prec->symbolic) {
+    prec->ctx->last_error = "dfg_precond_set_linear_system must come first";
+    return DFG_NOT_READY;
+  }
+  const FactorPattern F = factor_pattern(prec);
+  if (nnz) *nnz = prec->nnz;
+  if (rowptr) std::memcpy(rowptr, F.rowptr, sizeof(int) * (size_t)(prec->n + 1));
+  if (colind) std::memcpy(colind, F.colind, sizeof(int) * (size_t)prec->nnz);
+  return DFG_OK;
 }
 
 extern "C" int dfg_precond_get_factor(dfg_precond prec, double* fdiag, double* foffd) {
@@ -1450,9 +1514,10 @@ extern "C" int dfg_profile_kernels(dfg_system sys, dfg_precond prec, int mode, i
     if (bytes) {
       const double spmv_sz = mixed ? 4.0 : 8.0, sw_sz = fp32z ? 4.0 : 8.0;
       const double bs = (double)sys->b * sys->b, N = sys->n, Z = (double)sys->nnz;
+      const FactorPattern F = factor_pattern(prec);  // the sweeps read the factor's blocks
       long long zl = 0;
-      for (int i = 0; i < sys->n; ++i) zl += sys->h_diaind[i] - sys->h_rowptr[i];
-      const double Zl = (double)zl, Zu = Z - Zl;
+      for (int i = 0; i < sys->n; ++i) zl += F.diaind[i] - F.rowptr[i];
+      const double Zl = (double)zl, Zu = (double)prec->nnz - Zl;
       bytes[0] = (Z + N) * bs * spmv_sz + 4.0 * (Z + N + 1) + 2.0 * N * sys->b * spmv_sz;   // values, indices, x, y
       bytes[1] = (Zl + N) * bs * sw_sz + 4.0 * (Zl + N + 1) + 2.0 * N * sys->b * sw_sz;       // L, D^-1, indices, in, out
       bytes[2] = Zu * bs * sw_sz + 4.0 * (Zu + N + 1) + 2.0 * N * sys->b * sw_sz;             // U', indices, in, out

@@ -86,6 +86,12 @@ struct Levels {
 };
 
 Levels build_levels(int n, const int* rowptr, const int* colind, const int* diaind, bool forward);
+// ILU(lev_fill) factor pattern (AddFracPtn); false beyond max_nnz entries
+bool ilu_fill_pattern(int n, const int* rowptr, const int* colind, int lev_fill, std::vector<int>& rowptr_f,
+                      std::vector<int>& colind_f, long long max_nnz);
+// A's CRS slot -> factor slot of the same block
+bool factor_slot_map(int n, const int* rowptr, const int* colind, const int* rowptr_f, const int* colind_f,
+                     std::vector<int>& a2f);
 SweepPlan build_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind,
                            bool forward, int range_rows, int R);
 SweepPlan choose_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind,
@@ -205,7 +211,11 @@ struct dfg_precond_s {
   dfg_system sys = nullptr;        // system of the symbolic set-up
   bool symbolic = false, numeric = false, numeric32 = false;
   int n = 0, b = 1;
-  long long nnz = 0;
+  long long nnz = 0;               // off-diagonal blocks of the factor
+  // Factor pattern: the system's (own_pattern false) unless fill-in changed it
+  bool own_pattern = false;
+  std::vector<int> h_rowptr, h_colind, h_diaind;
+  dfg::DBuf rowptr, colind, diaind, a2f;  // a2f: A's CRS slot -> factor slot
   dfg::DBuf fdiag, foffd;          // factor, reference layout (FP64)
   dfg::Levels lev_fwd;
   dfg::DBuf lev_rows;

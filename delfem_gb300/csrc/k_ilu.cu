@@ -1,7 +1,8 @@
-// k_ilu.cu -- numeric block ILU(0) factorisation, level-scheduled.
+// k_ilu.cu -- numeric block ILU factorisation, level-scheduled.
 //
 // Restates CMatDiaFrac_BlkCrs::DoILUDecomp (src/matvec/matdiafrac_blkcrs.cpp:
-// 774-1107) for 1x1, 2x2 and 3x3 blocks.  Row i only reads rows k < i that
+// 774-1107) for 1x1, 2x2 and 3x3 blocks, on the factor's own pattern (A's
+// for ILU(0), with fill-in for ILU(k)).  Row i only reads rows k < i that
 // are finished (they sit in earlier levels of the forward dependency DAG)
 // and only writes its own row, so all rows of one level run in parallel, one
 // thread each.  This file is compiled with -fmad=false and every expression
@@ -133,6 +134,26 @@ __global__ void k_ilu_level(const int* __restrict__ rows, int cnt, const int* __
       }
     }
   }
+}
+
+// SetValue_Initialize for a factor with fill-in (matvec/matdiafrac_blkcrs.h:
+// 90-96): the factor storage was zeroed; every block of A goes to the slot of
+// the same column in the factor pattern.  One thread per value.
+__global__ void k_factor_init(long long nval, int bs, const int* __restrict__ a2f, const double* __restrict__ offd,
+                              double* __restrict__ foffd) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nval) return;
+  const long long c = t / bs;
+  foffd[(size_t)a2f[c] * bs + (t - c * bs)] = offd[t];
+}
+
+cudaError_t launch_factor_init(int B, long long nnz_a, const int* a2f, const double* offd, double* foffd,
+                               cudaStream_t st) {
+  const long long nval = nnz_a * B * B;
+  if (nval <= 0) return cudaSuccess;
+  const int tpb = 256;
+  k_factor_init<<<(unsigned)((nval + tpb - 1) / tpb), tpb, 0, st>>>(nval, B * B, a2f, offd, foffd);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_ilu_level(int B, const int* rows, int cnt, const int* rowptr, const int* colind,

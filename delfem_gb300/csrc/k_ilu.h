@@ -1,4 +1,4 @@
-// k_ilu.h -- launch interface of the ILU(0) numeric factorisation.
+// k_ilu.h -- launch interface of the numeric block ILU factorisation.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -6,4 +6,7 @@ namespace dfg {
 // factorises the rows of one level (rows[0..cnt)) in place
 cudaError_t launch_ilu_level(int B, const int* rows, int cnt, const int* rowptr, const int* colind,
                              const int* diaind, double* fdiag, double* foffd, int* nsing, cudaStream_t st);
+// scatters A's off-diagonal blocks into a zeroed factor with fill-in
+cudaError_t launch_factor_init(int B, long long nnz_a, const int* a2f, const double* offd, double* foffd,
+                               cudaStream_t st);
 }  // namespace dfg

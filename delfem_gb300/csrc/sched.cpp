@@ -44,6 +44,88 @@ void pattern_from_elements(int nnode, int nelem, int nnoel, const int* conn,
   }
 }
 
+// Block pattern of the ILU(lev_fill) factor: CMatDiaFrac_BlkCrs::AddFracPtn
+// (src/matvec/matdiafrac_blkcrs.cpp:1254-1382) as CPreconditioner_ILU::
+// SetLinearSystem calls it for one segment (src/ls/preconditioner.cpp:96-157).
+// Row i starts as A's row at level 0.  Its entries k < i are taken in
+// ascending column order, fill found on the way included; an entry of level
+// L spawns only while L + 1 <= lev_fill (always for lev_fill == -1): every
+// entry (k, j), j > k, of the finished factor row k whose level M passes the
+// same test adds (i, j) at level max(L, M) + 1, unless j == i or (i, j) is
+// already present (its level then stays).  Level 0, an empty off-diagonal
+// pattern and a full one leave the pattern as it is.  False when the factor
+// would exceed `max_nnz` entries.
+bool ilu_fill_pattern(int n, const int* rowptr, const int* colind, int lev_fill, std::vector<int>& rowptr_f,
+                      std::vector<int>& colind_f, long long max_nnz) {
+  const long long nnz = rowptr[n];
+  if (lev_fill == 0 || nnz == 0 || nnz == (long long)n * (n - 1)) {
+    rowptr_f.assign(rowptr, rowptr + n + 1);
+    colind_f.assign(colind, colind + nnz);
+    return true;
+  }
+  const auto spawns = [lev_fill](int l) { return lev_fill < 0 || l + 1 <= lev_fill; };
+  constexpr int kEnd = -1;
+  std::vector<int> succ(n + 1), lev(n), seen(n, -1), upper(n);  // succ[n]: first column of the row
+  std::vector<int> flev;
+  rowptr_f.assign(n + 1, 0);
+  colind_f.clear();
+  colind_f.reserve((size_t)nnz * 2);
+  flev.reserve((size_t)nnz * 2);
+  for (int i = 0; i < n; ++i) {
+    int last = n;
+    for (int c = rowptr[i]; c < rowptr[i + 1]; ++c) {
+      const int j = colind[c];
+      succ[last] = j;
+      last = j;
+      lev[j] = 0;
+      seen[j] = i;
+    }
+    succ[last] = kEnd;
+    for (int k = succ[n]; k != kEnd; k = succ[k]) {
+      if (!spawns(lev[k])) continue;
+      if (k >= i) break;
+      int at = k;  // new columns are > k and ascend with the loop below
+      for (int q = upper[k]; q < rowptr_f[k + 1]; ++q) {
+        if (!spawns(flev[q])) continue;
+        const int j = colind_f[q];
+        if (j == i || seen[j] == i) continue;
+        while (succ[at] != kEnd && succ[at] < j) at = succ[at];
+        succ[j] = succ[at];
+        succ[at] = j;
+        lev[j] = std::max(lev[k], flev[q]) + 1;
+        seen[j] = i;
+        at = j;
+      }
+    }
+    upper[i] = -1;
+    for (int j = succ[n]; j != kEnd; j = succ[j]) {
+      if (upper[i] < 0 && j > i) upper[i] = (int)colind_f.size();
+      colind_f.push_back(j);
+      flev.push_back(lev[j]);
+    }
+    if ((long long)colind_f.size() > max_nnz) return false;
+    if (upper[i] < 0) upper[i] = (int)colind_f.size();
+    rowptr_f[i + 1] = (int)colind_f.size();
+  }
+  return true;
+}
+
+// For every CRS slot of A, the slot of the same block in the factor pattern
+// (which contains A's); false if some block is missing.
+bool factor_slot_map(int n, const int* rowptr, const int* colind, const int* rowptr_f, const int* colind_f,
+                     std::vector<int>& a2f) {
+  a2f.assign((size_t)rowptr[n], -1);
+  for (int i = 0; i < n; ++i) {
+    int q = rowptr_f[i];
+    for (int c = rowptr[i]; c < rowptr[i + 1]; ++c) {
+      while (q < rowptr_f[i + 1] && colind_f[q] < colind[c]) ++q;
+      if (q == rowptr_f[i + 1] || colind_f[q] != colind[c]) return false;
+      a2f[c] = q;
+    }
+  }
+  return true;
+}
+
 static inline void deps_of(int row, bool forward, const int* rowptr, const int* diaind, int& c0, int& c1) {
   if (forward) { c0 = rowptr[row]; c1 = diaind[row]; }
   else { c0 = diaind[row]; c1 = rowptr[row + 1]; }

@@ -214,7 +214,9 @@ class LinearSystemField:
 
 
 class PreconditionerILU:
-    """LsSol::CPreconditioner_ILU (include/delfem/ls/preconditioner.h:59-108), fill level 0."""
+    """LsSol::CPreconditioner_ILU (include/delfem/ls/preconditioner.h:59-108):
+    ILU(0) by default; SetFillInLevel(k) before SetLinearSystem gives the
+    reference's level-of-fill ILU(k) (-1: no level limit)."""
 
     def __init__(self, ctx: Context):
         self.ctx = ctx
@@ -241,13 +243,27 @@ class PreconditionerILU:
         check(self.ctx.h, lib().dfg_precond_solve(self.h, ls.h, iv), "dfg_precond_solve")
         return True
 
+    def GetPattern(self):
+        """(rowptr, colind) of the factor: A's pattern plus fill-in."""
+        nnz = ctypes.c_longlong()
+        check(self.ctx.h, lib().dfg_precond_get_pattern(self.h, ctypes.byref(nnz), None, None),
+              "dfg_precond_get_pattern")
+        rowptr = np.zeros(self.ls.n + 1, dtype=np.int32)
+        colind = np.zeros(max(nnz.value, 1), dtype=np.int32)
+        check(self.ctx.h, lib().dfg_precond_get_pattern(self.h, None, _p(rowptr), _p(colind)),
+              "dfg_precond_get_pattern")
+        return rowptr, colind[: nnz.value]
+
     def GetFactor(self):
         ls = self.ls
         bs = ls.b * ls.b
+        nnz = ctypes.c_longlong()
+        check(self.ctx.h, lib().dfg_precond_get_pattern(self.h, ctypes.byref(nnz), None, None),
+              "dfg_precond_get_pattern")
         fdiag = np.zeros(ls.n * bs)
-        foffd = np.zeros(max(ls.nnz, 1) * bs)
+        foffd = np.zeros(max(nnz.value, 1) * bs)
         check(self.ctx.h, lib().dfg_precond_get_factor(self.h, _p(fdiag), _p(foffd)), "dfg_precond_get_factor")
-        return fdiag, foffd[: ls.nnz * bs]
+        return fdiag, foffd[: nnz.value * bs]
 
     def close(self):
         if getattr(self, "h", None):

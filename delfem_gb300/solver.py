@@ -1,6 +1,7 @@
 """Whole-path driver for a ``meshgen.Problem``: pattern, mesh upload,
-Dirichlet flags, symbolic ILU set-up, then per solve InitializeMarge ->
-AddLinSys_* -> extra loads -> FinalizeMarge -> ILU(0) numeric -> PCG.
+Dirichlet flags, symbolic ILU set-up (fill level 0 unless asked), then per
+solve InitializeMarge -> AddLinSys_* -> extra loads -> FinalizeMarge -> ILU
+numeric -> PCG.
 
 This is the sequence of the reference's low-level drivers
 (test_glut_lowlev/solid2d/main.cpp:186-298) expressed through the drop-in
@@ -17,7 +18,7 @@ from . import meshgen as mg
 
 
 class FESolve:
-    def __init__(self, ctx: L.Context, p: mg.Problem):
+    def __init__(self, ctx: L.Context, p: mg.Problem, fill_level: int = 0):
         self.ctx, self.p = ctx, p
         self.ls = L.LinearSystemField(ctx, p.nnode, p.b, conn=p.conn)
         self.ls.set_mesh(p.coords, p.conn)
@@ -29,7 +30,7 @@ class FESolve:
         if p.load is not None:
             self.ls.SetLoad(p.load)
         self.prec = L.PreconditionerILU(ctx)
-        self.prec.SetFillInLevel(0)
+        self.prec.SetFillInLevel(fill_level)
         self.prec.SetLinearSystem(self.ls)
 
     def assemble(self) -> float:

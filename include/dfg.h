@@ -195,17 +195,25 @@ int dfg_axpy(dfg_system sys, double alpha, int iv1, int iv2);
  * src/matvec/matdia_blkcrs.cpp:921-1094) */
 int dfg_matvec(dfg_system sys, double alpha, int iv1, double beta, int iv2);
 
-/* ------------------------------------------------------- ILU(0) preconditioner */
+/* ---------------------------------------------------------- ILU preconditioner */
 
 /* LsSol::CPreconditioner_ILU (include/delfem/ls/preconditioner.h:59-108). */
 int dfg_precond_create(dfg_ctx ctx, dfg_precond* out);
 int dfg_precond_destroy(dfg_precond prec);
-/* SetFillInLevel (preconditioner.h:77-84); only level 0 is implemented. */
+/* SetFillInLevel (preconditioner.h:77): 0 (the default) = ILU(0), k > 0 =
+ * level-of-fill ILU(k), -1 = no level limit (complete LU in natural order).
+ * Takes effect at the next dfg_precond_set_linear_system; < -1 is rejected. */
 int dfg_precond_set_fill_level(dfg_precond prec, int lev);
-/* Symbolic set-up: pattern copy, split index, level sets and sweep schedules
+/* Symbolic set-up: the factor's block pattern (A's for level 0; with the
+ * fill-in of CMatDiaFrac_BlkCrs::AddFracPtn, src/matvec/matdiafrac_blkcrs.cpp:
+ * 1254-1382, otherwise), split index, level sets and sweep schedules
  * (CPreconditioner_ILU::SetLinearSystem, src/ls/preconditioner.cpp:57-211;
  * CMatDiaFrac_BlkCrs(0,A), src/matvec/matdiafrac_blkcrs.cpp:171-225). */
 int dfg_precond_set_linear_system(dfg_precond prec, dfg_system sys);
+/* The factor's block pattern after the symbolic set-up: *nnz off-diagonal
+ * blocks; rowptr (n+1) and colind (nnz) in the layout of
+ * dfg_system_get_pattern, each written when non-NULL. */
+int dfg_precond_get_pattern(dfg_precond prec, long long* nnz, int* rowptr, int* colind);
 /* Numeric factorisation of the system's current matrix
  * (CPreconditioner_ILU::SetValue, src/ls/preconditioner.cpp:217-297 ->
  * DoILUDecomp, src/matvec/matdiafrac_blkcrs.cpp:774-1107).  Returns
@@ -213,7 +221,8 @@ int dfg_precond_set_linear_system(dfg_precond prec, dfg_system sys);
 int dfg_precond_set_value(dfg_precond prec, dfg_system sys);
 /* {iv} := (LU)^-1 {iv} (CPreconditioner_ILU::SolvePrecond, src/ls/preconditioner.cpp:301-335). */
 int dfg_precond_solve(dfg_precond prec, dfg_system sys, int iv);
-/* Host copy of the factor in the reference layout. */
+/* Host copy of the factor in the reference layout: fdiag n*b*b, foffd
+ * nnz*b*b with nnz and the block order of dfg_precond_get_pattern. */
 int dfg_precond_get_factor(dfg_precond prec, double* fdiag, double* foffd);
 
 /* ------------------------------------------------------------------- solvers */

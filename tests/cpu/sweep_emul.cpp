@@ -208,3 +208,16 @@ extern "C" int emul_sell(int n, int b, const int* rowptr, const int* colind, con
   }
   return 0;
 }
+
+// The library's ILU(k) fill pattern (sched.cpp ilu_fill_pattern) for the CPU
+// tests: returns the factor's nnz, writing rowptr_f/colind_f when it fits cap.
+extern "C" long long emul_ilu_pattern(int n, const int* rowptr, const int* colind, int lev, int* rowptr_f,
+                                      int* colind_f, long long cap) {
+  std::vector<int> rp, ci;
+  if (!ilu_fill_pattern(n, rowptr, colind, lev, rp, ci, (long long)1 << 40)) return -1;
+  if ((long long)ci.size() <= cap) {
+    std::memcpy(rowptr_f, rp.data(), sizeof(int) * rp.size());
+    if (!ci.empty()) std::memcpy(colind_f, ci.data(), sizeof(int) * ci.size());
+  }
+  return (long long)ci.size();
+}

@@ -26,7 +26,19 @@ def emul():
     L = ctypes.CDLL(EMUL_SO)
     P = ctypes.c_void_p
     L.emul_sweep.argtypes = [ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P, P]
+    L.emul_ilu_pattern.restype = ctypes.c_longlong
+    L.emul_ilu_pattern.argtypes = [ctypes.c_int, P, P, ctypes.c_int, P, P, ctypes.c_longlong]
     return L
+
+
+def _lib_ilu_pattern(emul, rowptr, colind, lev):
+    n = rowptr.size - 1
+    ci0 = colind if colind.size else np.zeros(1, np.int32)
+    nz = emul.emul_ilu_pattern(n, _p(rowptr), _p(ci0), lev, None, None, -1)
+    rp = np.zeros(n + 1, np.int32)
+    ci = np.zeros(max(nz, 1), np.int32)
+    assert emul.emul_ilu_pattern(n, _p(rowptr), _p(ci0), lev, _p(rp), _p(ci), nz) == nz
+    return rp, ci[:nz]
 
 
 def _p(a):
@@ -104,3 +116,49 @@ def test_serving_schedule_has_fuller_steps(emul, oracle_lib):
             fill[rr] = n / info[1]
         assert fill[-1] >= fill[0], fill
         assert fill[-1] > 20, fill
+
+
+def test_library_fill_pattern_matches_reference(emul):
+    """The library's host ILU(k) pattern builder equals the reference's
+    AddFracPtn output on every fixture of tests/golden/iluk/."""
+    from conftest import golden_iluk_files, load_golden
+    files = golden_iluk_files()
+    assert files
+    for f in files:
+        _, ref = load_golden(f)
+        rp, ci = _lib_ilu_pattern(emul, ref["rowptr"].astype(np.int32), ref["colind"].astype(np.int32),
+                                  int(ref["fill_level"]))
+        assert np.array_equal(rp, ref["rowptr_f"]) and np.array_equal(ci, ref["colind_f"]), f
+
+
+@pytest.mark.parametrize("lev", [0, 1, 2, 3, -1])
+def test_library_fill_pattern_matches_oracle(emul, oracle_lib, lev):
+    from delfem_gb300 import meshgen as mg
+    for p in (mg.poisson2d_square(15, seed=7), mg.solid2d_cantilever(12, 6, seed=8), mg.poisson3d_cube(4, seed=9)):
+        rp, ci = oracle_lib.pattern(p.nnode, p.conn)
+        a = _lib_ilu_pattern(emul, rp, ci, lev)
+        b = oracle_lib.ilu_pattern(rp, ci, lev)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), (p.name, lev)
+
+
+@pytest.mark.parametrize("lev", [1, 2, -1])
+@pytest.mark.parametrize("range_rows", [-1, 0, 37])
+def test_sweep_schedule_on_fill_pattern(emul, oracle_lib, lev, range_rows):
+    """Sweep schedules built on an ILU(k) factor pattern pass the same checks
+    and reproduce the oracle's ILU(k) substitutions."""
+    from delfem_gb300 import meshgen as mg
+    p = mg.solid2d_cantilever(16, 7, seed=21, coef_sigma=0.5)
+    out = oracle_lib.solve(p, stop_after_ilu=True, fill_level=lev)
+    n, b = out["n"], out["b"]
+    rp, ci, di = out["rowptr_f"], out["colind_f"], out["diaind_f"]
+    rhs = np.random.default_rng(lev + 5).standard_normal(n * b)
+    fo = out["foffd"] if out["foffd"].size else np.zeros(1)
+    info = np.zeros(8, dtype=np.int64)
+    y = np.full(n * b, np.nan)
+    assert emul.emul_sweep(n, b, _p(rp), _p(ci), 1, range_rows, 8, _p(out["fdiag"]), _p(fo), _p(rhs), _p(y),
+                           _p(info)) == 0
+    z = np.full(n * b, np.nan)
+    assert emul.emul_sweep(n, b, _p(rp), _p(ci), 0, range_rows, 8, _p(out["fdiag"]), _p(fo), _p(y), _p(z),
+                           _p(info)) == 0
+    ref = oracle_lib.precond(n, b, rp, ci, di, out["fdiag"], out["foffd"], rhs)
+    np.testing.assert_allclose(z, ref, rtol=1e-11, atol=1e-12 * np.abs(ref).max())

@@ -173,11 +173,14 @@ def test_singular_pivots_reported(gpu_ctx):
     s.close()
 
 
-def test_fill_level_other_than_zero_rejected(gpu_ctx):
+def test_fill_level_below_minus_one_rejected(gpu_ctx):
+    """Levels >= -1 are the reference's (ILU(k), -1 = no limit); below is an error."""
     from delfem_gb300 import capi, linsys as L
     prec = L.PreconditionerILU(gpu_ctx)
+    for lev in (0, 1, 7, -1):
+        prec.SetFillInLevel(lev)
     with pytest.raises(capi.DfgError) as e:
-        prec.SetFillInLevel(1)
+        prec.SetFillInLevel(-3)
     assert e.value.status == capi.DFG_INVALID_ARGUMENT
 
 
