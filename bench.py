@@ -55,7 +55,8 @@ CONFIGS = {
 # PCG iterations of the full FP64 solve of a workload at an ILU fill level,
 # measured with the reference's own algorithm (bit-exact CPU restatement,
 # 1e-8); used to extrapolate the bounded CPU samples to whole solves.
-REF_ITERS = {("solid2d_1000x500", 0): 2540, ("poisson2d_128", 0): 132}
+REF_ITERS = {("solid2d_1000x500", 0): 2540, ("solid2d_1000x500", 1): 1389, ("poisson2d_128", 0): 132,
+             ("solid2d_200x100", 0): 496, ("solid2d_200x100", 1): 270}
 
 
 # (name in the JSON line, solver mode)
