@@ -885,3 +885,77 @@ int dfo_pcg_f(int n, int b, const int* rowptr, const int* colind, const double* 
   }
   return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Preconditioned BiCGSTAB -- LsSol::Solve_PBiCGSTAB                          */
+/* (ls/solver_ls_iter.cpp:291-408), one COPY / DOT / AXPY / SCAL / MATVEC /   */
+/* SolvePrecond per call of the reference, in its order                       */
+/* ------------------------------------------------------------------------ */
+
+int dfo_bicgstab(int n, int b, const int* rowptr, const int* colind, const double* diag, const double* offd,
+                 const int* rowptr_f, const int* colind_f, const int* diaind_f,
+                 const double* fdiag, const double* foffd,
+                 double* r, double* x, double* conv, unsigned* iter, double* work) {
+  const long m = (long)n * b;
+  const size_t vb = sizeof(double) * (size_t)m;
+  const double tol = *conv;
+  const unsigned mx_iter = *iter;
+  double* s = work;
+  double* ms = work + m;
+  double* ams = work + 2 * m;
+  double* p = work + 3 * m;
+  double* mp = work + 4 * m;
+  double* amp = work + 5 * m;
+  double* r2 = work + 6 * m;
+  double sq_inv_norm_res_ini;
+  {
+    const double sq = vdot(m, r, r);
+    if (sq < 1.0e-60) { /* x is left as it is */
+      *conv = sqrt(sq);
+      *iter = 0;
+      return 1;
+    }
+    sq_inv_norm_res_ini = 1.0 / sq;
+  }
+  vscal(m, 0.0, x);
+  memcpy(r2, r, vb);
+  memcpy(p, r, vb);
+  *iter = mx_iter;
+  for (unsigned it = 1; it < mx_iter; ++it) {
+    memcpy(mp, p, vb);
+    dfo_forward(n, b, rowptr_f, colind_f, diaind_f, fdiag, foffd, mp);
+    dfo_backward(n, b, rowptr_f, colind_f, diaind_f, foffd, mp);
+    const double r_r2 = vdot(m, r, r2);
+    dfo_matvec(n, b, rowptr, colind, diag, offd, 1.0, mp, 0.0, amp);
+    const double alpha = r_r2 / vdot(m, amp, r2);
+    memcpy(s, r, vb);
+    vaxpy(m, -alpha, amp, s);
+    memcpy(ms, s, vb);
+    dfo_forward(n, b, rowptr_f, colind_f, diaind_f, fdiag, foffd, ms);
+    dfo_backward(n, b, rowptr_f, colind_f, diaind_f, foffd, ms);
+    dfo_matvec(n, b, rowptr, colind, diag, offd, 1.0, ms, 0.0, ams);
+    double omega;
+    {
+      const double den = vdot(m, ams, ams);
+      const double num = vdot(m, s, ams);
+      omega = num / den;
+    }
+    vaxpy(m, alpha, mp, x);
+    vaxpy(m, omega, ms, x);
+    memcpy(r, s, vb);
+    vaxpy(m, -omega, ams, r);
+    {
+      const double sq = vdot(m, r, r);
+      if (sq * sq_inv_norm_res_ini < tol * tol) {
+        *conv = sqrt(sq * sq_inv_norm_res_ini);
+        *iter = it;
+        return 1;
+      }
+    }
+    const double beta = vdot(m, r, r2) * alpha / (r_r2 * omega);
+    vscal(m, beta, p);
+    vaxpy(m, 1.0, r, p);
+    vaxpy(m, -beta * omega, amp, p);
+  }
+  return 0; /* the reference returns true here too, with *conv untouched */
+}

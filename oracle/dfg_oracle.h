@@ -112,6 +112,19 @@ int dfo_pcg_f(int n, int b, const int* rowptr, const int* colind, const double* 
               const double* fdiag, const double* foffd,
               double* r, double* x, double* conv, unsigned* iter, double* work);
 
+/* LsSol::Solve_PBiCGSTAB (ls/solver_ls_iter.cpp:291-408) with the ILU factor
+ * in its own pattern.  r: residual in, residual out; x: solution out.  *conv
+ * in = tolerance, out = achieved ratio when converged (untouched otherwise,
+ * as in the reference); *iter in = max iterations, out = the 1-based
+ * iteration of convergence (max iterations otherwise).  A residual with
+ * ||r||^2 < 1e-60 returns at once with *conv = ||r|| and x untouched.
+ * Returns 1 when converged (the reference returns true in both cases).
+ * work: 7*n*b doubles. */
+int dfo_bicgstab(int n, int b, const int* rowptr, const int* colind, const double* diag, const double* offd,
+                 const int* rowptr_f, const int* colind_f, const int* diaind_f,
+                 const double* fdiag, const double* foffd,
+                 double* r, double* x, double* conv, unsigned* iter, double* work);
+
 /* Wall-time helpers for the CPU baseline. */
 double dfo_now(void);
 

@@ -58,6 +58,7 @@ def lib():
                               ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_uint), _P]
         L.dfo_pcg_f.argtypes = [_I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                 ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_uint), _P]
+        L.dfo_bicgstab.argtypes = L.dfo_pcg_f.argtypes
         L.dfo_ilu_pattern.restype = ctypes.c_long
         L.dfo_ilu_pattern.argtypes = [_I, _P, _P, _I, _P, _P, ctypes.c_long]
         L.dfo_ilu_init.argtypes = [_I, _I, _P, _P, _P, _P, _P, _P, _P, _P]
@@ -140,9 +141,10 @@ def assemble(p, rowptr, colind):
     return diag, offd[: colind.size * bs], res
 
 
-def solve(p, tol=None, maxit=None, stop_after_ilu=False, fill_level: int = 0) -> dict:
+def solve(p, tol=None, maxit=None, stop_after_ilu=False, fill_level: int = 0, solver: str = "pcg") -> dict:
     """The reference's whole path on the CPU with an ILU(fill_level)
-    preconditioner; returns every intermediate."""
+    preconditioner and Solve_PCG or Solve_PBiCGSTAB; returns every
+    intermediate."""
     L = lib()
     t0 = L.dfo_now()
     rowptr, colind = pattern(p.nnode, p.conn)
@@ -182,6 +184,10 @@ def solve(p, tol=None, maxit=None, stop_after_ilu=False, fill_level: int = 0) ->
                fdiag=fdiag, foffd=foffd[: colind_f.size * bs], t_assemble=t1 - t0, t_ilu=t3 - t2)
     if stop_after_ilu:
         return out
+    out.update(bicgstab(out, p.tol if tol is None else tol, p.maxit if maxit is None else maxit)
+               if solver == "bicgstab" else {})
+    if solver == "bicgstab":
+        return out
     r = rhs.copy()
     x = np.zeros(n * b)
     work = np.zeros(2 * n * b)
@@ -194,6 +200,46 @@ def solve(p, tol=None, maxit=None, stop_after_ilu=False, fill_level: int = 0) ->
     t5 = L.dfo_now()
     out.update(x=x, conv=conv.value, iter=it.value, converged=bool(ok), t_pcg=t5 - t4)
     return out
+
+
+def bicgstab(out: dict, tol: float, maxit: int, rhs=None, diag=None, offd=None, x0=None) -> dict:
+    """Solve_PBiCGSTAB on the system and factor in ``out`` (a ``solve(...,
+    stop_after_ilu=True)`` result); the matrix and right-hand side may be
+    replaced (e.g. by a non-symmetric one with the same pattern, factorised
+    by the caller into out["fdiag"] / out["foffd"])."""
+    L = lib()
+    n, b = out["n"], out["b"]
+    diag = out["diag"] if diag is None else diag
+    offd = out["offd"] if offd is None else offd
+    r = np.array(out["rhs"] if rhs is None else rhs, dtype=np.float64, copy=True)
+    x = np.zeros(n * b) if x0 is None else np.array(x0, dtype=np.float64, copy=True)
+    work = np.zeros(7 * n * b)
+    conv = ctypes.c_double(tol)
+    it = ctypes.c_uint(maxit)
+    offd_a = offd if offd.size else np.zeros(1)
+    cf = out["colind_f"] if out["colind_f"].size else np.zeros(1, np.int32)
+    fo = out["foffd"] if out["foffd"].size else np.zeros(1)
+    t0 = L.dfo_now()
+    ok = L.dfo_bicgstab(n, b, _p(out["rowptr"]), _p(out["colind"]), _p(diag), _p(offd_a), _p(out["rowptr_f"]),
+                        _p(cf), _p(out["diaind_f"]), _p(out["fdiag"]), _p(fo), _p(r), _p(x), ctypes.byref(conv),
+                        ctypes.byref(it), _p(work))
+    return dict(x=x, conv=conv.value, iter=it.value, converged=bool(ok), t_solve=L.dfo_now() - t0, r=r)
+
+
+def factor(out: dict, diag, offd):
+    """ILU factor of another matrix on the pattern of ``out`` (same fill)."""
+    L = lib()
+    n, b = out["n"], out["b"]
+    bs = b * b
+    fdiag = np.zeros(n * bs)
+    foffd = np.zeros(max(out["colind_f"].size, 1) * bs)
+    cf = out["colind_f"] if out["colind_f"].size else np.zeros(1, np.int32)
+    offd_a = offd if offd.size else np.zeros(1)
+    if L.dfo_ilu_init(n, b, _p(out["rowptr"]), _p(out["colind"] if out["colind"].size else np.zeros(1, np.int32)),
+                      _p(diag), _p(offd_a), _p(out["rowptr_f"]), _p(cf), _p(fdiag), _p(foffd)) != 0:
+        raise ValueError("pattern mismatch")
+    rc = L.dfo_ilu0(n, b, _p(out["rowptr_f"]), _p(cf), _p(out["diaind_f"]), _p(fdiag), _p(foffd))
+    return fdiag, foffd[: out["colind_f"].size * bs], rc
 
 
 def matvec(n, b, rowptr, colind, diag, offd, x, alpha=1.0, beta=0.0, y=None):
@@ -222,12 +268,13 @@ def harness_available() -> bool:
     return os.path.exists(HARNESS)
 
 
-def run_reference_harness(p, fill_level: int = 0) -> dict:
+def run_reference_harness(p, fill_level: int = 0, solver: str = "pcg") -> dict:
     """Runs the reference code itself (oracle/_ref/ref_harness) on ``p`` with
-    an ILU preconditioner of the given fill level."""
+    an ILU preconditioner of the given fill level and Solve_PCG ("pcg") or
+    Solve_PBiCGSTAB ("bicgstab")."""
     from delfem_gb300 import meshgen as mg
     with tempfile.TemporaryDirectory() as td:
         fi, fo = os.path.join(td, "p.bin"), os.path.join(td, "r.bin")
         mg.write_problem(p, fi)
-        subprocess.run([HARNESS, fi, fo, str(fill_level)], check=True, stdout=subprocess.DEVNULL)
+        subprocess.run([HARNESS, fi, fo, str(fill_level), solver], check=True, stdout=subprocess.DEVNULL)
         return mg.read_result(fo)

@@ -10,7 +10,8 @@
 //   reference's own Mearge) -> extra loads -> FinalizeMarge ->
 //   CPreconditioner_ILU(fill level, 0 by default) -> LsSol::Solve_PCG.
 //
-// Usage: ref_harness problem.bin out.bin [fill_level]
+// Usage: ref_harness problem.bin out.bin [fill_level [pcg|bicgstab]]
+// (the solver is LsSol::Solve_PCG by default, LsSol::Solve_PBiCGSTAB on request)
 // Input / output formats are described in tests/golden/make_golden.py.
 #include <cassert>
 #include <cmath>
@@ -209,9 +210,13 @@ static void wr(FILE* f, const void* p, size_t n) { if (n) fwrite(p, 1, n, f); }
 static void wri(FILE* f, int v) { wr(f, &v, 4); }
 
 int main(int argc, char** argv) {
-  if (argc != 3 && argc != 4) { fprintf(stderr, "usage: %s problem.bin out.bin [fill_level]\n", argv[0]); return 2; }
+  if (argc < 3 || argc > 5) {
+    fprintf(stderr, "usage: %s problem.bin out.bin [fill_level [pcg|bicgstab]]\n", argv[0]);
+    return 2;
+  }
   Problem p = load(argv[1]);
-  const int fill_level = argc == 4 ? atoi(argv[3]) : 0;
+  const int fill_level = argc >= 4 ? atoi(argv[3]) : 0;
+  const bool bicgstab = argc == 5 && strcmp(argv[4], "bicgstab") == 0;
   const int b = p.b;
   CFieldWorld world;
   GridMesh mesh(p);
@@ -311,7 +316,7 @@ int main(int argc, char** argv) {
   bool converged = false;
   {
     LsSol::CLinearSystemPreconditioner lsp(ls.m_ls, prec);
-    converged = LsSol::Solve_PCG(conv, iter, lsp);
+    converged = bicgstab ? LsSol::Solve_PBiCGSTAB(conv, iter, lsp) : LsSol::Solve_PCG(conv, iter, lsp);
   }
   MatVec::CVector_Blk& upd = ls.GetUpdate(id_field, CORNER, world);
   std::vector<double> x((size_t)n * b);

@@ -30,6 +30,11 @@ def golden_iluk_files():
     return sorted(glob.glob(os.path.join(GOLDEN_DIR, "iluk", "*.npz")))
 
 
+def golden_bicgstab_files():
+    """Fixtures solved by Solve_PBiCGSTAB (ref_solver), ILU(ref_fill_level)."""
+    return sorted(glob.glob(os.path.join(GOLDEN_DIR, "bicgstab", "*.npz")))
+
+
 def load_golden(path):
     """Returns (problem, reference outputs) of one committed fixture."""
     from delfem_gb300 import meshgen as mg

@@ -8,7 +8,8 @@ the assembled matrix and right-hand side after FinalizeMarge, the ILU
 factor, and the result of LsSol::Solve_PCG (iterations, ratio, solution).
 The fixtures in this directory use ILU(0); those in iluk/ use other fill
 levels (CPreconditioner_ILU::SetFillInLevel) and add the factor's own block
-pattern (ref_rowptr_f, ref_colind_f) and ref_fill_level.
+pattern (ref_rowptr_f, ref_colind_f) and ref_fill_level; those in bicgstab/
+hold the result of LsSol::Solve_PBiCGSTAB instead of Solve_PCG (ref_solver).
 
 Harness problem file (little-endian): int32 magic 0x44464731, kind, nnode,
 ndim, nelem, nnoel, b; f64 coords[nnode*ndim]; i32 conn[nelem*nnoel];
@@ -16,7 +17,7 @@ i32 has_coef (+ f64 coef[nelem]); f64 params[8]; i32 bcflag[nnode*b];
 i32 has_load (+ f64 load[nnode*b]); i32 has_u (+ f64 u); i32 has_v (+ f64 v);
 f64 tol; i32 maxit.  The result file layout is read by meshgen.read_result.
 
-Run from the repository root:  python tests/golden/make_golden.py [ilu0|iluk|all]
+Run from the repository root:  python tests/golden/make_golden.py [ilu0|iluk|bicgstab|all]
 """
 from __future__ import annotations
 
@@ -62,14 +63,38 @@ def iluk_cases():
     ]
 
 
+def bicgstab_cases():
+    """(problem, fill level): Solve_PBiCGSTAB on ILU(0) and ILU(1), an
+    iteration limit that stops it early (the reference then returns true with
+    the ratio untouched) and a zero right-hand side (immediate return)."""
+    zero = mg.poisson2d_square(6, seed=23)
+    zero.params = zero.params.copy()
+    zero.params[1] = 0.0
+    zero.load = None
+    zero.name = "poisson2d_6x6_zero"
+    short = mg.solid2d_cantilever(10, 5, seed=24, coef_sigma=0.5)
+    short.maxit = 5
+    short.name = "solid2d_10x5_maxit5"
+    return [
+        (mg.poisson2d_square(12, seed=12, coef_sigma=0.5), 0),
+        (mg.solid2d_cantilever(10, 5, seed=13, coef_sigma=0.5), 0),
+        (mg.solid2d_cantilever(10, 5, seed=13, coef_sigma=0.5), 1),
+        (mg.solid3d_cube(3, seed=15, coef_sigma=1.0), 0),
+        (mg.poisson3d_cube(5, seed=18, coef_sigma=1.0), 1),
+        (mg.diffusion2d_square(6, seed=19), 0),
+        (short, 0),
+        (zero, 0),
+    ]
+
+
 def fixture_name(p: mg.Problem, k: int, fill_level: int = 0) -> str:
     tag = "coef" if p.coef is not None else "uniform"
     lev = "" if fill_level == 0 else (f"_ilu{fill_level}" if fill_level > 0 else "_ilufull")
     return f"{k:02d}_{p.name.replace('^', 'c')}_{tag}{lev}"
 
 
-def write_fixture(path: str, p: mg.Problem, fill_level: int) -> None:
-    R = O.run_reference_harness(p, fill_level)
+def write_fixture(path: str, p: mg.Problem, fill_level: int, solver: str = "pcg") -> None:
+    R = O.run_reference_harness(p, fill_level, solver)
     d = dict(kind=p.kind, coords=p.coords, conn=p.conn, params=p.params, bcflag=p.bcflag, tol=p.tol,
              maxit=p.maxit)
     for nm in ("coef", "load", "u", "v"):
@@ -80,7 +105,9 @@ def write_fixture(path: str, p: mg.Problem, fill_level: int) -> None:
         d["ref_" + nm] = R[nm]
     for nm in ("norm_res", "ilu_ok", "converged", "iter", "conv"):
         d["ref_" + nm] = np.array(R[nm])
-    if fill_level != 0:
+    if solver != "pcg":
+        d["ref_solver"] = np.array(solver)
+    if fill_level != 0 or solver != "pcg":
         d["ref_fill_level"] = np.array(fill_level)
         d["ref_rowptr_f"] = R["rowptr_f"]
         d["ref_colind_f"] = R["colind_f"]
@@ -101,6 +128,10 @@ def main():
         os.makedirs(os.path.join(here, "iluk"), exist_ok=True)
         for k, (p, lev) in enumerate(iluk_cases()):
             write_fixture(os.path.join(here, "iluk", fixture_name(p, k, lev) + ".npz"), p, lev)
+    if which in ("bicgstab", "all"):
+        os.makedirs(os.path.join(here, "bicgstab"), exist_ok=True)
+        for k, (p, lev) in enumerate(bicgstab_cases()):
+            write_fixture(os.path.join(here, "bicgstab", fixture_name(p, k, lev) + ".npz"), p, lev, "bicgstab")
 
 
 if __name__ == "__main__":

@@ -4,7 +4,7 @@ ILU(0) factor and the PCG result must be bit-identical."""
 import numpy as np
 import pytest
 
-from conftest import bits, golden_files, golden_iluk_files, load_golden
+from conftest import bits, golden_bicgstab_files, golden_files, golden_iluk_files, load_golden
 
 
 @pytest.mark.parametrize("path", golden_files(), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
@@ -80,3 +80,26 @@ def test_iluk_pattern_properties(oracle_lib):
     np.fill_diagonal(dense, False)
     for i in range(n):
         assert np.array_equal(cf[rf[i]:rf[i + 1]], np.nonzero(dense[i])[0]), i
+
+
+@pytest.mark.parametrize("path", golden_bicgstab_files(), ids=lambda p: p.rsplit("/", 1)[-1][:-4])
+def test_oracle_bicgstab_matches_reference(path, oracle_lib):
+    """Solve_PBiCGSTAB: solution, ratio and iteration count bit-identical to
+    the reference's, including its early return on a zero right-hand side and
+    its untouched ratio when the iteration limit is reached."""
+    p, ref = load_golden(path)
+    assert str(ref["solver"]) == "bicgstab"
+    out = oracle_lib.solve(p, fill_level=int(ref["fill_level"]), solver="bicgstab")
+    assert np.array_equal(bits(out["x"]), bits(ref["x"]))
+    assert out["iter"] == int(ref["iter"]) and out["conv"] == float(ref["conv"])
+    if out["iter"] == p.maxit:
+        assert not out["converged"] and out["conv"] == p.tol  # the reference returns true here
+    else:
+        assert out["converged"]
+
+
+def test_bicgstab_fixtures_cover_quirks():
+    refs = [load_golden(f) for f in golden_bicgstab_files()]
+    assert any(int(r["iter"]) == 0 and float(r["conv"]) == 0.0 for _, r in refs)
+    assert any(int(r["iter"]) == p.maxit for p, r in refs)
+    assert any(int(r["fill_level"]) == 1 for _, r in refs)
