@@ -160,18 +160,19 @@ class ClockSampler:
 def _cpu_sample(args):
     """Bounded CPU sample of one solve (runs in a spawned process): assembly +
     Dirichlet + ILU(k) of the full problem and `iters` PCG iterations."""
-    name, iters, fill_level = args
+    name, iters, fill_level, solver = args
     sys.path.insert(0, ROOT)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     p = make_problem(name)
     t0 = time.perf_counter()
-    out = O.solve(p, tol=1e-30, maxit=iters, fill_level=fill_level)
+    out = O.solve(p, tol=1e-30, maxit=iters, fill_level=fill_level, solver=solver)
     t = time.perf_counter() - t0
-    return dict(t_assemble=out["t_assemble"], t_ilu=out["t_ilu"], t_pcg=out["t_pcg"], iters=iters, wall=t)
+    t_it = out["t_pcg"] if solver == "pcg" else out["t_solve"]
+    return dict(t_assemble=out["t_assemble"], t_ilu=out["t_ilu"], t_pcg=t_it, iters=iters, wall=t)
 
 
-def cpu_rate(name, iters_full, procs, sample_iters, fill_level=0):
+def cpu_rate(name, iters_full, procs, sample_iters, fill_level=0, solver="pcg"):
     """Solves/s of the reference algorithm on `procs` host cores (independent
     solves, one per core), extrapolated from bounded samples."""
     import multiprocessing as mp
@@ -180,7 +181,7 @@ def cpu_rate(name, iters_full, procs, sample_iters, fill_level=0):
     O.build()
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs) as pool:
-        res = pool.map(_cpu_sample, [(name, sample_iters, fill_level)] * procs)
+        res = pool.map(_cpu_sample, [(name, sample_iters, fill_level, solver)] * procs)
     per = []
     for r in res:
         t_it = r["t_pcg"] / max(r["iters"], 1)
@@ -228,7 +229,7 @@ def run_gpu(args, rank, world, local):
     def step(mode):
         s.assemble()
         ok = s.factor()
-        r = s.solve(mode, target_true=True)
+        r = s.solve(mode, target_true=True, solver=args.solver)
         return ok, r
 
     arms_run = [(a, m) for a, m in ARMS if a in args.arms.split(",")]
@@ -400,7 +401,10 @@ def compose_line(args, world, p, results, prof, e2e, head):
         "data": "synthetic (seeded jittered mesh, log-normal coefficients)",
         "config": {"workload": args.config, "nodes": p.nnode, "dof": p.ndof, "elements": p.nelem,
                    "preconditioner": f"ILU({args.fill_level})" if args.fill_level >= 0 else "ILU(no level limit)",
-                   "tol": 1e-8, "stop": "true relative residual <= tol (all arms)", "mixed_form": head,
+                   "solver": "LsSol::Solve_PCG" if args.solver == "pcg" else "LsSol::Solve_PBiCGSTAB",
+                   "tol": 1e-8, "mixed_form": head,
+                   "stop": ("true relative residual <= tol (all arms)" if args.solver == "pcg" else
+                            "recursive relative residual <= tol (the reference's test); true one reported"),
                    "parallelism": f"replicas x{world} (independent solves per GPU)",
                    "l2": "working set (matrix 112 MB + factor records + vectors) larger than the 129 MB L2; no flush"},
         "p50_ms": arms[head]["p50_ms"],
@@ -421,13 +425,13 @@ def compose_line(args, world, p, results, prof, e2e, head):
         line["e2e"] = {"value": round(e2e["value"], 4), "unit": "solves/s", "h2d_bytes_per_step": int(e2e["h2d"]),
                        "d2h_bytes_per_step": int(e2e["d2h"])}
     if not args.no_cpu_baseline:
-        iters_full = REF_ITERS.get((args.config, args.fill_level)) or \
+        iters_full = (REF_ITERS.get((args.config, args.fill_level)) if args.solver == "pcg" else None) or \
             results[("plain_fp64" if "plain_fp64" in results else head)]["iters"][-1]
         sample_iters = args.cpu_sample_iters
-        rate, t_solve, res = cpu_rate(args.config, iters_full, 1, sample_iters, args.fill_level)
+        rate, t_solve, res = cpu_rate(args.config, iters_full, 1, sample_iters, args.fill_level, args.solver)
         line["cpu_baseline"] = {"value": round(rate, 6), "unit": "solves/s", "cores": 1, "kind": "port",
                                 "sample": f"assembly + Dirichlet + ILU({args.fill_level}) of the full workload and {sample_iters} "
-                                          f"PCG iterations on one host core, extrapolated to {iters_full + 1} "
+                                          f"{args.solver.upper()} iterations on one host core, extrapolated to {iters_full + 1} "
                                           f"iterations ({t_solve:.1f} s per solve)"}
     return line
 
@@ -481,6 +485,8 @@ def run_serve(args, rank, world, local):
 
     cfg = CONFIGS[args.config]
     items = serve_stream(args.config)
+    if args.serve_requests:
+        items = items[: args.serve_requests]  # a prefix of the stream (profiling runs)
     nseg = args.warmup + args.steps
     seg = [items[(len(items) * k) // nseg:(len(items) * (k + 1)) // nseg] for k in range(nseg)]
     warm_items = [it for sg in seg[:args.warmup] for it in sg]
@@ -502,7 +508,7 @@ def run_serve(args, rank, world, local):
     results = {}
     x_plain = {}
     for arm, mode in arms_run:
-        with Server(ctx, mode=mode, budget_bytes=cfg["budget"], profile_every=16,
+        with Server(ctx, mode=mode, budget_bytes=int(args.serve_budget) or cfg["budget"], profile_every=16,
                     max_inflight=args.max_inflight, size_groups=args.size_groups) as S:
             wids = serve_segment(S, warm_items, warm_probs, 0.0)
             for i in wids:
@@ -756,6 +762,12 @@ def main():
     ap.add_argument("--cpu-sample-iters", type=int, default=60)
     ap.add_argument("--cpu-serve-requests", type=int, default=12,
                     help="requests the one-core CPU baseline solves (serving configs)")
+    ap.add_argument("--serve-requests", type=int, default=0,
+                    help="serving: serve only the first N requests of the stream (0 = all; for profiling runs)")
+    ap.add_argument("--serve-budget", type=float, default=0,
+                    help="serving: admission budget in bytes (0 = the workload's; small for ncu replays)")
+    ap.add_argument("--solver", default="pcg", choices=["pcg", "bicgstab"],
+                    help="single-solve workloads: Solve_PCG or Solve_PBiCGSTAB (arms plain_fp64, mixed_fp32_factor)")
     ap.add_argument("--fill-level", type=int, default=0,
                     help="single-solve workloads: ILU fill level (CPreconditioner_ILU::SetFillInLevel; -1 = no limit)")
     ap.add_argument("--max-inflight", type=int, default=128, help="serving: solves resident at once (<= 256)")

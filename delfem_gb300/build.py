@@ -27,6 +27,7 @@ SOURCES = {
     "sched.cpp": [],
     "k_sweep.cu": [],
     "k_solve.cu": [],
+    "k_bicg.cu": [],
     "k_assemble.cu": ["-fmad=false"],
     "k_ilu.cu": ["-fmad=false"],
     "k_api.cu": ["-fmad=false"],

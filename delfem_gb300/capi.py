@@ -86,6 +86,7 @@ SIGNATURES = {
     "dfg_solve_pcg": (_I, [_P, _P, _PD, _PU]),
     "dfg_solve_pcg_mixed": (_I, [_P, _P, _PD, _PU, _PU]),
     "dfg_solve_pcg_ex": (_I, [_P, _P, _I, _I, _PD, _PU, _PU]),
+    "dfg_solve_pbicgstab": (_I, [_P, _P, _I, _PD, _PU]),
     "dfg_true_residual": (_I, [_P, _P, _PD]),
     "dfg_ctx_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
     "dfg_profile_kernels": (_I, [_P, _P, _I, _I, _P, _P]),

@@ -203,6 +203,7 @@ struct dfg_system_s {
   // solver workspace (allocated on first solve)
   dfg::DBuf w_p, w_q, w_z, w_state;          // FP64 PCG
   dfg::DBuf w_rd, w_d, w_r32, w_p32, w_q32, w_z32;  // mixed
+  dfg::DBuf w_bicg;                           // BiCGSTAB vectors, state, paired-sum scratch
 };
 
 struct dfg_precond_s {

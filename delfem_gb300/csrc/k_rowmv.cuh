@@ -41,11 +41,12 @@ namespace dfg {
 // (block w, entry e) is one coalesced 32-word access, and the width W_s is
 // uniform across the warp.  The row's blocks come in CRS order, then the
 // diagonal block, then zero padding: the same accumulation sequence as
-// row_mv.
-template <typename T, int B>
+// row_mv.  x may be stored narrower than the values (X = float with T =
+// double: a vector from FP32 sweeps); it is widened on load.
+template <typename T, int B, typename X = T>
 __device__ __forceinline__ void sell_row_mv(int i, const long long* __restrict__ ptr, const int* __restrict__ width,
                                             const int* __restrict__ col, const T* __restrict__ val,
-                                            const T* __restrict__ x, T y[B]) {
+                                            const X* __restrict__ x, T y[B]) {
   constexpr int BS = B * B;
   const int s = i >> 5, lane = i & 31;
   const long long k0 = ptr[s];
@@ -59,7 +60,7 @@ __device__ __forceinline__ void sell_row_mv(int i, const long long* __restrict__
     const int j = c[w * 32];
     T xv[B];
 #pragma unroll
-    for (int q = 0; q < B; ++q) xv[q] = x[(size_t)j * B + q];
+    for (int q = 0; q < B; ++q) xv[q] = (T)x[(size_t)j * B + q];
 #pragma unroll
     for (int p = 0; p < B; ++p)
 #pragma unroll

@@ -12,57 +12,11 @@
 #include <cmath>
 
 #include "dfg_common.cuh"
-#include "k_solve.h"
+#include "k_reduce.cuh"
 #include "k_rowmv.cuh"
+#include "k_solve.h"
 
 namespace dfg {
-
-// ------------------------------------------------------------- reductions
-
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// sum over the block (fixed order); result valid in every thread
-__device__ double block_sum(double v) {
-  __shared__ double ws[32];
-  v = warp_sum(v);
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  __syncthreads();
-  if (l == 0) ws[w] = v;
-  __syncthreads();
-  const int nw = (blockDim.x + 31) >> 5;
-  double t = (threadIdx.x < nw) ? ws[threadIdx.x] : 0.0;
-  if (w == 0) t = warp_sum(t);
-  __syncthreads();
-  if (threadIdx.x == 0) ws[0] = t;
-  __syncthreads();
-  return ws[0];
-}
-
-// Publishes this block's partial; returns true (in every thread) in the
-// last block, which then holds the grid total in *total.
-__device__ bool grid_sum(double v, Red red, double* total) {
-  __shared__ bool last;
-  const double bs = block_sum(v);
-  if (threadIdx.x == 0) {
-    red.partials[blockIdx.x] = bs;
-    __threadfence();
-    const unsigned prev = atomicAdd(red.counter, 1u);
-    last = (prev == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (!last) return false;
-  __threadfence();
-  double t = 0.0;
-  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) t += ld_relaxed(&red.partials[i]);
-  t = block_sum(t);
-  if (threadIdx.x == 0) *red.counter = 0u;
-  *total = t;
-  return true;
-}
 
 // ------------------------------------------------------------------- SpMV
 

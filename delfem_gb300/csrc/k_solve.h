@@ -104,6 +104,40 @@ cudaError_t mix_accumulate(const MixVecs& v, cudaStream_t s);
 cudaError_t mix_clear_done(PcgState* st, cudaStream_t s);
 cudaError_t to_fp32(long long m, const double* a, float* b, cudaStream_t s);
 
+// ---- preconditioned BiCGSTAB (k_bicg.cu) ----------------------------------
+struct BicgState {
+  double rho;            // (r, r2) of the current iteration
+  double alpha, omega, beta;
+  double rr, rr0, inv_rr0, tol2, conv;
+  int it;                // current iteration, 1-based as the reference counts
+  int maxit, done, iter_out;
+};
+// done codes: 0 running, 1 converged, 2 iteration limit, 3 NaN,
+//             4 residual below 1e-60 at the start (nothing touched)
+struct BicgVecs {
+  double* r;   // residual slot
+  double* x;   // update slot
+  double* r2;  // shadow residual (the initial r)
+  double* p;
+  double* amp; // A M^-1 p
+  double* s;
+  double* ams; // A M^-1 s
+  void* mp;    // M^-1 p (sweep output type)
+  void* ms;    // M^-1 s
+  void* y;     // forward-sweep output
+  float* p32;  // FP32 sweep inputs (FP32 factor only)
+  float* s32;
+  long long m;
+};
+// red2: partials for 2 x kRedGrid values and its own counter
+cudaError_t bicg_init(const BicgVecs& v, BicgState* st, Red red, double tol, int maxit, int* tickets, bool fp32z,
+                      cudaStream_t s);
+cudaError_t bicg_amp(const MatView& A, const BicgVecs& v, BicgState* st, Red red, bool fp32z, cudaStream_t s);
+cudaError_t bicg_s(const BicgVecs& v, BicgState* st, int* tickets, bool fp32z, cudaStream_t s);
+cudaError_t bicg_ams(const MatView& A, const BicgVecs& v, BicgState* st, Red red2, bool fp32z, cudaStream_t s);
+cudaError_t bicg_update(const BicgVecs& v, BicgState* st, Red red2, bool fp32z, cudaStream_t s);
+cudaError_t bicg_p(const BicgVecs& v, BicgState* st, int* tickets, bool fp32z, cudaStream_t s);
+
 // ---- strict drop-in BLAS (k_api.cu, bit-exact elementwise ops) ------------
 cudaError_t api_matvec(const MatView& A, double alpha, const double* x, double beta, double* y, cudaStream_t s);
 cudaError_t api_axpy(long long m, double alpha, const double* x, double* y, cudaStream_t s);

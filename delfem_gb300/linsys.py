@@ -369,6 +369,62 @@ def Solve_PCG_ex(conv_ratio: float, iteration: int, ls: LinearSystemField, prec:
     return st == capi.DFG_OK, c.value, it.value, refin.value
 
 
+def Solve_PBiCGSTAB(conv_ratio: float, iteration: int, ls: LinearSystemField, prec: PreconditionerILU,
+                    mode: str = "fp64"):
+    """LsSol::Solve_PBiCGSTAB (src/ls/solver_ls_iter.cpp:291-408), device-resident
+    (mode "fp64" or "fp32f").  Returns (converged, ratio, 1-based iteration);
+    when not converged the ratio is the tolerance given, as in the reference."""
+    c = ctypes.c_double(conv_ratio)
+    it = ctypes.c_uint(iteration)
+    st = lib().dfg_solve_pbicgstab(ls.h, prec.h, capi.MODES[mode], ctypes.byref(c), ctypes.byref(it))
+    if st not in (capi.DFG_OK, capi.DFG_NOT_CONVERGED):
+        check(ls.ctx.h, st, "dfg_solve_pbicgstab")
+    return st == capi.DFG_OK, c.value, it.value
+
+
+def Solve_PBiCGSTAB_reference_loop(conv_ratio: float, iteration: int, lsp: LinearSystemPreconditioner):
+    """The reference's Solve_PBiCGSTAB control flow (solver_ls_iter.cpp:291-408)
+    over the ILinearSystemPreconditioner_Sol virtuals (the strict drop-in).
+    Returns (the reference's return value, ratio, iteration)."""
+    tol, mx = conv_ratio, iteration
+    if lsp.GetTmpVectorArySize() < 7:
+        lsp.ReSizeTmpVecSolver(7)
+    ix, ir = -2, -1
+    i_s, iMs, iAMs, ip, iMp, iAMp, ir2 = 0, 1, 2, 3, 4, 5, 6
+    sq0 = lsp.DOT(ir, ir)
+    if sq0 < 1.0e-60:
+        return True, float(np.sqrt(sq0)), 0
+    inv0 = 1.0 / sq0
+    lsp.SCAL(0.0, ix)
+    lsp.COPY(ir, ir2)
+    lsp.COPY(ir, ip)
+    for it in range(1, mx):
+        lsp.COPY(ip, iMp)
+        lsp.SolvePrecond(iMp)
+        r_r2 = lsp.DOT(ir, ir2)
+        lsp.MATVEC(1.0, iMp, 0.0, iAMp)
+        alpha = r_r2 / lsp.DOT(iAMp, ir2)
+        lsp.COPY(ir, i_s)
+        lsp.AXPY(-alpha, iAMp, i_s)
+        lsp.COPY(i_s, iMs)
+        lsp.SolvePrecond(iMs)
+        lsp.MATVEC(1.0, iMs, 0.0, iAMs)
+        den = lsp.DOT(iAMs, iAMs)
+        omega = lsp.DOT(i_s, iAMs) / den
+        lsp.AXPY(alpha, iMp, ix)
+        lsp.AXPY(omega, iMs, ix)
+        lsp.COPY(i_s, ir)
+        lsp.AXPY(-omega, iAMs, ir)
+        sq = lsp.DOT(ir, ir)
+        if sq * inv0 < tol * tol:
+            return True, float(np.sqrt(sq * inv0)), it
+        beta = lsp.DOT(ir, ir2) * alpha / (r_r2 * omega)
+        lsp.SCAL(beta, ip)
+        lsp.AXPY(1.0, ir, ip)
+        lsp.AXPY(-beta * omega, iAMp, ip)
+    return True, tol, mx
+
+
 def Solve_PCG_reference_loop(conv_ratio: float, iteration: int, lsp: LinearSystemPreconditioner):
     """The reference's Solve_PCG control flow (solver_ls_iter.cpp:100-172)
     written against the ILinearSystemPreconditioner_Sol virtuals: this is how

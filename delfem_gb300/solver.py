@@ -51,12 +51,17 @@ class FESolve:
         return self.prec.SetValue(self.ls)
 
     def solve(self, mode: str = "fp64", tol: float | None = None, maxit: int | None = None,
-              target_true: bool = False) -> dict:
+              target_true: bool = False, solver: str = "pcg") -> dict:
         """mode: "fp64" (LsSol::Solve_PCG semantics unless target_true), "mixed"
         (FP32 factor/sweeps/SpMV/vectors + FP64 refinement, always on the true
-        residual) or "fp32f" (FP32 factor and sweeps only)."""
+        residual) or "fp32f" (FP32 factor and sweeps only).  solver "bicgstab"
+        runs LsSol::Solve_PBiCGSTAB instead (modes fp64 / fp32f; its stop test
+        is the recursive residual, target_true does not apply)."""
         tol = self.p.tol if tol is None else tol
         maxit = self.p.maxit if maxit is None else maxit
+        if solver == "bicgstab":
+            ok, conv, it = L.Solve_PBiCGSTAB(tol, maxit, self.ls, self.prec, mode)
+            return dict(converged=ok, conv=conv, iter=it, refinements=0)
         if mode == "fp64" and not target_true:
             ok, conv, it = L.Solve_PCG(tol, maxit, self.ls, self.prec)
             return dict(converged=ok, conv=conv, iter=it, refinements=0)
@@ -67,7 +72,7 @@ class FESolve:
         return dict(converged=ok, conv=conv, iter=it, refinements=refin)
 
     def run(self, mode: str = "fp64", tol: float | None = None, maxit: int | None = None,
-            target_true: bool = False) -> dict:
+            target_true: bool = False, solver: str = "pcg") -> dict:
         t0 = time.perf_counter()
         norm_res = self.assemble()
         self.ctx.synchronize()
@@ -75,7 +80,7 @@ class FESolve:
         ok = self.factor()
         self.ctx.synchronize()
         t2 = time.perf_counter()
-        out = self.solve(mode, tol, maxit, target_true)
+        out = self.solve(mode, tol, maxit, target_true, solver)
         t3 = time.perf_counter()
         out.update(norm_res=norm_res, ilu_ok=ok, t_assemble=t1 - t0, t_ilu=t2 - t1, t_solve=t3 - t2)
         return out

@@ -245,6 +245,18 @@ int dfg_solve_pcg(dfg_system sys, dfg_precond prec, double* conv_ratio, unsigned
 int dfg_solve_pcg_ex(dfg_system sys, dfg_precond prec, int mode, int target_true, double* conv_ratio,
                      unsigned* iteration, unsigned* refinements);
 
+/* LsSol::Solve_PBiCGSTAB (src/ls/solver_ls_iter.cpp:291-408) run
+ * device-resident, for non-symmetric systems (SPD ones too); the same slots
+ * as dfg_solve_pcg.  mode: DFG_PREC_FP64, or DFG_PREC_FP32_FACTOR (factor and
+ * sweeps in FP32, everything else FP64).  *conv_ratio: tolerance in, achieved
+ * ||r||/||r0|| out when converged (left as given otherwise, as the reference
+ * does); *iteration: maximum in, 1-based iteration of convergence out (the
+ * maximum when it did not converge).  A residual with ||r||^2 < 1e-60 returns
+ * at once with *conv_ratio = ||r||, *iteration = 0 and the update slot
+ * untouched.  Returns DFG_OK when converged and DFG_NOT_CONVERGED when the
+ * limit was reached (the reference returns true in both cases). */
+int dfg_solve_pbicgstab(dfg_system sys, dfg_precond prec, int mode, double* conv_ratio, unsigned* iteration);
+
 /* Mixed-precision form of the same solve: FP32 factor, sweeps and SpMV
  * inside FP64 iterative refinement (FP64 outer residual r = b - A x, FP64
  * alpha/beta reductions and FP64 solution accumulation).  *conv_ratio: target

@@ -14,8 +14,9 @@
 //  * the AddLinSys_* overloads take the GPU system with the reference's
 //    parameter lists (eqn_poisson.h:71-76, eqn_diffusion.h:68-73,
 //    eqn_linear_solid2d.h:68-72, eqn_linear_solid3d.h:59-64);
-//  * DfgDelFEM::Solve_PCG is the device-resident fast path with the
-//    in/out semantics of LsSol::Solve_PCG (solver_ls_iter.h:38-39).
+//  * DfgDelFEM::Solve_PCG and DfgDelFEM::Solve_PBiCGSTAB are the
+//    device-resident fast paths with the in/out semantics of LsSol::Solve_PCG
+//    and LsSol::Solve_PBiCGSTAB (solver_ls_iter.h:38-45).
 #ifndef DFG_DELFEM_HPP
 #define DFG_DELFEM_HPP
 
@@ -175,6 +176,14 @@ inline bool Solve_PCG(double& conv_ratio, unsigned int& iteration, CLinearSystem
 inline bool Solve_PCG_Mixed(double& conv_ratio, unsigned int& iteration, CLinearSystem_FieldGPU& ls) {
   unsigned int outer = 0;
   return dfg_solve_pcg_mixed(ls.system(), ls.preconditioner(), &conv_ratio, &iteration, &outer) == DFG_OK;
+}
+
+// ---- device-resident LsSol::Solve_PBiCGSTAB (solver_ls_iter.cpp:291-408);
+// like the reference it returns true at the iteration limit too, with
+// num_iter = the limit and conv_ratio left as given
+inline bool Solve_PBiCGSTAB(double& conv_ratio, unsigned int& num_iter, CLinearSystem_FieldGPU& ls) {
+  const int st = dfg_solve_pbicgstab(ls.system(), ls.preconditioner(), DFG_PREC_FP64, &conv_ratio, &num_iter);
+  return st == DFG_OK || st == DFG_NOT_CONVERGED;
 }
 
 }  // namespace DfgDelFEM

@@ -1,8 +1,8 @@
 // integration_main.cpp -- TEST INFRASTRUCTURE: a DelFEM-side program that
 // uses include/dfg_delfem.hpp exactly as a maintainer would: mesh through
 // Msh::IMesh into CFieldWorld, the GPU linear system from the field, the
-// reference's own LsSol::Solve_PCG driving it through the virtual interface,
-// and the device-resident fast path.  Compiled (and, where a GPU exists, run)
+// reference's own LsSol::Solve_PCG and LsSol::Solve_PBiCGSTAB driving it
+// through the virtual interface, and the device-resident fast paths.  Compiled (and, where a GPU exists, run)
 // by tests/test_integration_adapter.py against the reference's headers.
 #include <cassert>
 #include <cstdio>
@@ -62,7 +62,24 @@ int main() {
   const bool ok_fast = DfgDelFEM::Solve_PCG(conv2, iter2, ls);
   std::printf("reference loop: %d iter %u conv %.3e; device loop: %d iter %u conv %.3e\n", ok_ref, iter, conv, ok_fast,
               iter2, conv2);
+  // BiCGSTAB, the reference's loop and the device one, on a fresh right-hand side each
+  ls.InitializeMarge();
+  DfgDelFEM::AddLinSys_Poisson(ls, 1.0, 1.0);
+  ls.FinalizeMarge();
+  double conv3 = 1e-8;
+  unsigned int iter3 = 1000;
+  const bool ok_ref_b = LsSol::Solve_PBiCGSTAB(conv3, iter3, ls);
+  ls.InitializeMarge();
+  DfgDelFEM::AddLinSys_Poisson(ls, 1.0, 1.0);
+  ls.FinalizeMarge();
+  double conv4 = 1e-8;
+  unsigned int iter4 = 1000;
+  const bool ok_fast_b = DfgDelFEM::Solve_PBiCGSTAB(conv4, iter4, ls);
+  std::printf("BiCGSTAB reference loop: %d iter %u conv %.3e; device loop: %d iter %u conv %.3e\n", ok_ref_b, iter3,
+              conv3, ok_fast_b, iter4, conv4);
   ls.UpdateValueOfField(id_field, world);
   dfg_ctx_destroy(ctx);
-  return (ok_ref && ok_fast && (iter > iter2 ? iter - iter2 : iter2 - iter) <= 2) ? 0 : 2;
+  const bool pcg_ok = ok_ref && ok_fast && (iter > iter2 ? iter - iter2 : iter2 - iter) <= 2;
+  const bool bicg_ok = ok_ref_b && ok_fast_b && iter3 < 1000 && (iter3 > iter4 ? iter3 - iter4 : iter4 - iter3) <= 2;
+  return (pcg_ok && bicg_ok) ? 0 : 2;
 }
