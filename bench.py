@@ -397,7 +397,7 @@ def compose_line(args, world, p, results, prof, e2e, head):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32" if head == "mixed_fp32_all" else "f32 factor/sweeps, f64 SpMV/vectors",
+        "dtype": {"mixed_fp32_all": "f32", "plain_fp64": "f64"}.get(head, "f32 factor/sweeps, f64 SpMV/vectors"),
         "data": "synthetic (seeded jittered mesh, log-normal coefficients)",
         "config": {"workload": args.config, "nodes": p.nnode, "dof": p.ndof, "elements": p.nelem,
                    "preconditioner": f"ILU({args.fill_level})" if args.fill_level >= 0 else "ILU(no level limit)",
@@ -767,7 +767,7 @@ def main():
     ap.add_argument("--serve-budget", type=float, default=0,
                     help="serving: admission budget in bytes (0 = the workload's; small for ncu replays)")
     ap.add_argument("--solver", default="pcg", choices=["pcg", "bicgstab"],
-                    help="single-solve workloads: Solve_PCG or Solve_PBiCGSTAB (arms plain_fp64, mixed_fp32_factor)")
+                    help="single-solve workloads: Solve_PCG or Solve_PBiCGSTAB (BiCGSTAB: arm plain_fp64 only)")
     ap.add_argument("--fill-level", type=int, default=0,
                     help="single-solve workloads: ILU fill level (CPreconditioner_ILU::SetFillInLevel; -1 = no limit)")
     ap.add_argument("--max-inflight", type=int, default=128, help="serving: solves resident at once (<= 256)")

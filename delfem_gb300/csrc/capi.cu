@@ -1373,42 +1373,29 @@ extern "C" int dfg_solve_pcg_mixed(dfg_system sys, dfg_precond prec, double* con
   });
 }
 
-// Preconditioned BiCGSTAB (LsSol::Solve_PBiCGSTAB) on the device: an FP64
-// or FP32 factor, FP64 vectors, SpMV and reductions; chunks of iterations
-// captured in a graph and replayed until the device state says done.
+// Preconditioned BiCGSTAB (LsSol::Solve_PBiCGSTAB) on the device, all FP64;
+// chunks of iterations captured in a graph and replayed until the device
+// state says done.
 extern "C" int dfg_solve_pbicgstab(dfg_system sys, dfg_precond prec, int mode, double* conv_ratio,
                                    unsigned* iteration) {
   if (!sys || !prec || !conv_ratio || !iteration) return DFG_INVALID_ARGUMENT;
   dfg_ctx ctx = sys->ctx;
   return guarded(ctx, [&]() -> int {
     dfg_ctx ctx_ = ctx;
-    REQUIRE(mode == DFG_PREC_FP64 || mode == DFG_PREC_FP32_FACTOR, DFG_INVALID_ARGUMENT,
-            "BiCGSTAB runs with mode DFG_PREC_FP64 or DFG_PREC_FP32_FACTOR");
+    REQUIRE(mode == DFG_PREC_FP64, DFG_INVALID_ARGUMENT,
+            "BiCGSTAB runs in DFG_PREC_FP64 only: with a preconditioner applied in FP32 its recurrences diverge "
+            "on ill-conditioned systems");
     REQUIRE(prec->numeric && prec->sys == sys, DFG_NOT_READY, "preconditioner value not set for this system");
-    const bool fp32z = mode == DFG_PREC_FP32_FACTOR;
     const long long m = (long long)sys->n * sys->b;
-    if (fp32z) ensure_numeric32(ctx, prec);
-    // workspace: 7 FP64 vectors, 2 sweep-typed ones, 2 FP32 inputs, state, paired partials
-    const size_t v8 = ((size_t)m * 8 + 255) / 256 * 256, vz = ((size_t)m * (fp32z ? 4 : 8) + 255) / 256 * 256;
-    const size_t v4 = fp32z ? ((size_t)m * 4 + 255) / 256 * 256 : 0;
-    const size_t off_z = 5 * v8, off_f = off_z + 2 * vz, off_st = off_f + 2 * v4;
-    const size_t off_red = off_st + 256, total = off_red + 2 * kRedGrid * 8 + 256;
+    // workspace: r2, p, AMp, s, AMs, Mp, Ms; state; paired-sum partials
+    const size_t v8 = ((size_t)m * 8 + 255) / 256 * 256;
+    const size_t off_st = 7 * v8, off_red = off_st + 256, total = off_red + 2 * kRedGrid * 8 + 256;
     dalloc(ctx, sys->w_bicg, total);
     char* w = sys->w_bicg.as<char>();
-    BicgVecs v{};
-    v.r = sys->res.as<double>();
-    v.x = sys->upd.as<double>();
-    v.r2 = reinterpret_cast<double*>(w);
-    v.p = reinterpret_cast<double*>(w + v8);
-    v.amp = reinterpret_cast<double*>(w + 2 * v8);
-    v.s = reinterpret_cast<double*>(w + 3 * v8);
-    v.ams = reinterpret_cast<double*>(w + 4 * v8);
-    v.mp = w + off_z;
-    v.ms = w + off_z + vz;
-    v.y = fp32z ? prec->ybuf32.p : prec->ybuf64.p;
-    v.p32 = fp32z ? reinterpret_cast<float*>(w + off_f) : nullptr;
-    v.s32 = fp32z ? reinterpret_cast<float*>(w + off_f + v4) : nullptr;
-    v.m = m;
+    double* vec[7];
+    for (int k = 0; k < 7; ++k) vec[k] = reinterpret_cast<double*>(w + k * v8);
+    BicgVecs v{sys->res.as<double>(), sys->upd.as<double>(), vec[0], vec[1], vec[2], vec[3], vec[4], vec[5], vec[6],
+               prec->ybuf64.as<double>(), m};
     BicgState* st = reinterpret_cast<BicgState*>(w + off_st);
     Red red2{reinterpret_cast<double*>(w + off_red), reinterpret_cast<unsigned*>(w + off_red + 2 * kRedGrid * 8),
              nullptr};
@@ -1416,15 +1403,13 @@ extern "C" int dfg_solve_pbicgstab(dfg_system sys, dfg_precond prec, int mode, d
     Scratch sc = scratch_of(ctx);
     Red red = red_of(ctx, 1);
     const int* done = reinterpret_cast<const int*>(reinterpret_cast<const char*>(st) + offsetof(BicgState, done));
-    const void* in_p = fp32z ? (const void*)v.p32 : (const void*)v.p;
-    const void* in_s = fp32z ? (const void*)v.s32 : (const void*)v.s;
-    SweepLaunch F1 = sweep_launch(ctx, prec, prec->fwd, fp32z, in_p, v.y, sc.tickets, done);
-    SweepLaunch B1 = sweep_launch(ctx, prec, prec->bwd, fp32z, v.y, v.mp, sc.tickets + 1, done);
-    SweepLaunch F2 = sweep_launch(ctx, prec, prec->fwd, fp32z, in_s, v.y, sc.tickets, done);
-    SweepLaunch B2 = sweep_launch(ctx, prec, prec->bwd, fp32z, v.y, v.ms, sc.tickets + 1, done);
+    SweepLaunch F1 = sweep_launch(ctx, prec, prec->fwd, false, v.p, v.y, sc.tickets, done);
+    SweepLaunch B1 = sweep_launch(ctx, prec, prec->bwd, false, v.y, v.mp, sc.tickets + 1, done);
+    SweepLaunch F2 = sweep_launch(ctx, prec, prec->fwd, false, v.s, v.y, sc.tickets, done);
+    SweepLaunch B2 = sweep_launch(ctx, prec, prec->bwd, false, v.y, v.ms, sc.tickets + 1, done);
     const int maxit = (int)std::min<unsigned>(*iteration, 0x7fffffffu);
     const double tol = *conv_ratio;
-    CK(bicg_init(v, st, red, tol, maxit, sc.tickets, fp32z, ctx->stream));
+    CK(bicg_init(v, st, red, tol, maxit, sc.tickets, ctx->stream));
     launched(ctx, 2);
     BicgState h{};
     CK(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1436,15 +1421,15 @@ extern "C" int dfg_solve_pbicgstab(dfg_system sys, dfg_precond prec, int mode, d
       Chunk g;
       CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
       for (int c = 0; c < chunk; ++c) {
-        launch_sweep(true, fp32z, sys->b, F1.args, F1.grid, F1.smem, ctx->stream);
-        launch_sweep(false, fp32z, sys->b, B1.args, B1.grid, B1.smem, ctx->stream);
-        bicg_amp(A, v, st, red, fp32z, ctx->stream);
-        bicg_s(v, st, sc.tickets, fp32z, ctx->stream);
-        launch_sweep(true, fp32z, sys->b, F2.args, F2.grid, F2.smem, ctx->stream);
-        launch_sweep(false, fp32z, sys->b, B2.args, B2.grid, B2.smem, ctx->stream);
-        bicg_ams(A, v, st, red2, fp32z, ctx->stream);
-        bicg_update(v, st, red2, fp32z, ctx->stream);
-        bicg_p(v, st, sc.tickets, fp32z, ctx->stream);
+        launch_sweep(true, false, sys->b, F1.args, F1.grid, F1.smem, ctx->stream);
+        launch_sweep(false, false, sys->b, B1.args, B1.grid, B1.smem, ctx->stream);
+        bicg_amp(A, v, st, red, ctx->stream);
+        bicg_s(v, st, sc.tickets, ctx->stream);
+        launch_sweep(true, false, sys->b, F2.args, F2.grid, F2.smem, ctx->stream);
+        launch_sweep(false, false, sys->b, B2.args, B2.grid, B2.smem, ctx->stream);
+        bicg_ams(A, v, st, red2, ctx->stream);
+        bicg_update(v, st, red2, ctx->stream);
+        bicg_p(v, st, sc.tickets, ctx->stream);
       }
       CK(cudaStreamEndCapture(ctx->stream, &g.graph));
       CK(cudaGraphInstantiate(&g.exec, g.graph, 0));

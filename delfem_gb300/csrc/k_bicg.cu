@@ -14,9 +14,11 @@
 // the beta numerator of the iteration before (r does not change in between),
 // so it is carried over in the state instead of being recomputed.  Vector
 // updates round like the reference's AXPY / SCAL (separate multiply and add,
-// AXPY skipped for a zero coefficient).  Z is the sweeps' output type: double
-// with an FP64 factor, float with an FP32 factor (then FP32 copies of p and
-// s feed the sweeps).
+// AXPY skipped for a zero coefficient).  Everything is FP64: BiCGSTAB's
+// shadow-residual recurrences do not survive a preconditioner applied in
+// FP32 (fresh rounding at every application makes it a different operator
+// each time; on a 200x100 cantilever that doubles the iterations, and with
+// the factor rounded too the iteration diverges), unlike CG's.
 #include <cmath>
 
 #include "dfg_common.cuh"
@@ -25,11 +27,6 @@
 #include "k_solve.h"
 
 namespace dfg {
-
-template <typename Z>
-__device__ __forceinline__ double zload(const void* z, long long k) {
-  return (double)reinterpret_cast<const Z*>(z)[k];
-}
 
 // y := y + a x, rounded as CVector_Blk's AXPY (no contraction)
 __device__ __forceinline__ double axpy1(double y, double a, double x) { return __dadd_rn(y, __dmul_rn(a, x)); }
@@ -64,7 +61,6 @@ __global__ void k_bicg_init0(BicgVecs v, BicgState* st, Red red, double tol, int
 }
 
 // x := 0 x; r2 = r; p = r; sweep outputs to the sentinel; tickets reset
-template <typename Z>
 __global__ void k_bicg_init1(BicgVecs v, BicgState* st, int* tickets) {
   if (st->done == 4) return;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < v.m; k += (long long)gridDim.x * blockDim.x) {
@@ -72,9 +68,8 @@ __global__ void k_bicg_init1(BicgVecs v, BicgState* st, int* tickets) {
     const double r = v.r[k];
     v.r2[k] = r;
     v.p[k] = r;
-    if constexpr (sizeof(Z) == 4) v.p32[k] = (float)r;
-    reinterpret_cast<Z*>(v.y)[k] = sentinel_value<Z>();
-    reinterpret_cast<Z*>(v.mp)[k] = sentinel_value<Z>();
+    v.y[k] = sentinel_value<double>();
+    v.mp[k] = sentinel_value<double>();
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     tickets[0] = 0;
@@ -83,15 +78,14 @@ __global__ void k_bicg_init1(BicgVecs v, BicgState* st, int* tickets) {
 }
 
 // AMp = A Mp; alpha = rho / (AMp, r2)
-template <typename Z, int B>
+template <int B>
 __global__ void __launch_bounds__(kSpmvTpb, 2) k_bicg_amp(MatView Am, BicgVecs v, BicgState* st, Red red) {
   if (st->done) return;
   const double* sval = reinterpret_cast<const double*>(Am.sval);
-  const Z* mp = reinterpret_cast<const Z*>(v.mp);
   double part = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < Am.n; i += gridDim.x * blockDim.x) {
     double y[B];
-    sell_row_mv<double, B, Z>(i, Am.sptr, Am.swidth, Am.scol, sval, mp, y);
+    sell_row_mv<double, B>(i, Am.sptr, Am.swidth, Am.scol, sval, v.mp, y);
 #pragma unroll
     for (int d = 0; d < B; ++d) {
       v.amp[(size_t)i * B + d] = y[d];
@@ -103,7 +97,6 @@ __global__ void __launch_bounds__(kSpmvTpb, 2) k_bicg_amp(MatView Am, BicgVecs v
 }
 
 // s = r; s += -alpha AMp; sweep outputs to the sentinel; tickets reset
-template <typename Z>
 __global__ void k_bicg_s(BicgVecs v, BicgState* st, int* tickets) {
   if (st->done) return;
   const double na = -st->alpha;
@@ -111,9 +104,8 @@ __global__ void k_bicg_s(BicgVecs v, BicgState* st, int* tickets) {
     double s = v.r[k];
     if (na != 0.0) s = axpy1(s, na, v.amp[k]);
     v.s[k] = s;
-    if constexpr (sizeof(Z) == 4) v.s32[k] = (float)s;
-    reinterpret_cast<Z*>(v.y)[k] = sentinel_value<Z>();
-    reinterpret_cast<Z*>(v.ms)[k] = sentinel_value<Z>();
+    v.y[k] = sentinel_value<double>();
+    v.ms[k] = sentinel_value<double>();
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     tickets[0] = 0;
@@ -122,15 +114,14 @@ __global__ void k_bicg_s(BicgVecs v, BicgState* st, int* tickets) {
 }
 
 // AMs = A Ms; omega = (s, AMs) / (AMs, AMs)
-template <typename Z, int B>
+template <int B>
 __global__ void __launch_bounds__(kSpmvTpb, 2) k_bicg_ams(MatView Am, BicgVecs v, BicgState* st, Red red) {
   if (st->done) return;
   const double* sval = reinterpret_cast<const double*>(Am.sval);
-  const Z* ms = reinterpret_cast<const Z*>(v.ms);
   double tt = 0.0, ts = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < Am.n; i += gridDim.x * blockDim.x) {
     double y[B];
-    sell_row_mv<double, B, Z>(i, Am.sptr, Am.swidth, Am.scol, sval, ms, y);
+    sell_row_mv<double, B>(i, Am.sptr, Am.swidth, Am.scol, sval, v.ms, y);
 #pragma unroll
     for (int d = 0; d < B; ++d) {
       v.ams[(size_t)i * B + d] = y[d];
@@ -144,15 +135,14 @@ __global__ void __launch_bounds__(kSpmvTpb, 2) k_bicg_ams(MatView Am, BicgVecs v
 
 // x += alpha Mp; x += omega Ms; r = s; r += -omega AMs; (r, r) -> stop test;
 // (r, r2) -> beta and the next rho
-template <typename Z>
 __global__ void k_bicg_update(BicgVecs v, BicgState* st, Red red) {
   if (st->done) return;
   const double alpha = st->alpha, omega = st->omega, no = -omega;
   double rr = 0.0, rr2 = 0.0;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < v.m; k += (long long)gridDim.x * blockDim.x) {
     double x = v.x[k];
-    if (alpha != 0.0) x = axpy1(x, alpha, zload<Z>(v.mp, k));
-    if (omega != 0.0) x = axpy1(x, omega, zload<Z>(v.ms, k));
+    if (alpha != 0.0) x = axpy1(x, alpha, v.mp[k]);
+    if (omega != 0.0) x = axpy1(x, omega, v.ms[k]);
     v.x[k] = x;
     double r = v.s[k];
     if (no != 0.0) r = axpy1(r, no, v.ams[k]);
@@ -183,7 +173,6 @@ __global__ void k_bicg_update(BicgVecs v, BicgState* st, Red red) {
 }
 
 // p := beta p; p += 1.0 r; p += -beta omega AMp; next iteration
-template <typename Z>
 __global__ void k_bicg_p(BicgVecs v, BicgState* st, int* tickets) {
   if (st->done) return;
   const double beta = st->beta, c = -beta * st->omega;
@@ -192,9 +181,8 @@ __global__ void k_bicg_p(BicgVecs v, BicgState* st, int* tickets) {
     p = __dadd_rn(p, v.r[k]);
     if (c != 0.0) p = axpy1(p, c, v.amp[k]);
     v.p[k] = p;
-    if constexpr (sizeof(Z) == 4) v.p32[k] = (float)p;
-    reinterpret_cast<Z*>(v.y)[k] = sentinel_value<Z>();
-    reinterpret_cast<Z*>(v.mp)[k] = sentinel_value<Z>();
+    v.y[k] = sentinel_value<double>();
+    v.mp[k] = sentinel_value<double>();
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     tickets[0] = 0;
@@ -203,53 +191,43 @@ __global__ void k_bicg_p(BicgVecs v, BicgState* st, int* tickets) {
   }
 }
 
-#define DFG_ZD(kern, ...)                                                          \
-  do {                                                                             \
-    if (fp32z) kern<float><<<kRedGrid, kRedTpb, 0, s>>>(__VA_ARGS__);              \
-    else kern<double><<<kRedGrid, kRedTpb, 0, s>>>(__VA_ARGS__);                   \
+#define DFG_BDISPATCH(kern, ...)                                                    \
+  do {                                                                              \
+    switch (A.b) {                                                                  \
+      case 1: kern<1><<<kRedGrid, kSpmvTpb, 0, s>>>(__VA_ARGS__); break;            \
+      case 2: kern<2><<<kRedGrid, kSpmvTpb, 0, s>>>(__VA_ARGS__); break;            \
+      case 3: kern<3><<<kRedGrid, kSpmvTpb, 0, s>>>(__VA_ARGS__); break;            \
+      default: return cudaErrorInvalidValue;                                        \
+    }                                                                               \
   } while (0)
 
-#define DFG_ZB(kern, ...)                                                                   \
-  do {                                                                                      \
-    switch (A.b) {                                                                          \
-      case 1: if (fp32z) kern<float, 1><<<kRedGrid, kSpmvTpb, 0, s>>>(__VA_ARGS__);         \
-              else kern<double, 1><<<kRedGrid, kSpmvTpb, 0, s>>>(__VA_ARGS__); break;       \
-      case 2: if (fp32z) kern<float, 2><<<kRedGrid, kSpmvTpb, 0, s>>>(__VA_ARGS__);         \
-              else kern<double, 2><<<kRedGrid, kSpmvTpb, 0, s>>>(__VA_ARGS__); break;       \
-      case 3: if (fp32z) kern<float, 3><<<kRedGrid, kSpmvTpb, 0, s>>>(__VA_ARGS__);         \
-              else kern<double, 3><<<kRedGrid, kSpmvTpb, 0, s>>>(__VA_ARGS__); break;       \
-      default: return cudaErrorInvalidValue;                                                \
-    }                                                                                       \
-  } while (0)
-
-cudaError_t bicg_init(const BicgVecs& v, BicgState* st, Red red, double tol, int maxit, int* tickets, bool fp32z,
+cudaError_t bicg_init(const BicgVecs& v, BicgState* st, Red red, double tol, int maxit, int* tickets,
                       cudaStream_t s) {
   k_bicg_init0<<<kRedGrid, kRedTpb, 0, s>>>(v, st, red, tol, maxit);
-  DFG_ZD(k_bicg_init1, v, st, tickets);
+  k_bicg_init1<<<kRedGrid, kRedTpb, 0, s>>>(v, st, tickets);
   return cudaGetLastError();
 }
-cudaError_t bicg_amp(const MatView& A, const BicgVecs& v, BicgState* st, Red red, bool fp32z, cudaStream_t s) {
-  DFG_ZB(k_bicg_amp, A, v, st, red);
+cudaError_t bicg_amp(const MatView& A, const BicgVecs& v, BicgState* st, Red red, cudaStream_t s) {
+  DFG_BDISPATCH(k_bicg_amp, A, v, st, red);
   return cudaGetLastError();
 }
-cudaError_t bicg_s(const BicgVecs& v, BicgState* st, int* tickets, bool fp32z, cudaStream_t s) {
-  DFG_ZD(k_bicg_s, v, st, tickets);
+cudaError_t bicg_s(const BicgVecs& v, BicgState* st, int* tickets, cudaStream_t s) {
+  k_bicg_s<<<kRedGrid, kRedTpb, 0, s>>>(v, st, tickets);
   return cudaGetLastError();
 }
-cudaError_t bicg_ams(const MatView& A, const BicgVecs& v, BicgState* st, Red red2, bool fp32z, cudaStream_t s) {
-  DFG_ZB(k_bicg_ams, A, v, st, red2);
+cudaError_t bicg_ams(const MatView& A, const BicgVecs& v, BicgState* st, Red red2, cudaStream_t s) {
+  DFG_BDISPATCH(k_bicg_ams, A, v, st, red2);
   return cudaGetLastError();
 }
-cudaError_t bicg_update(const BicgVecs& v, BicgState* st, Red red2, bool fp32z, cudaStream_t s) {
-  DFG_ZD(k_bicg_update, v, st, red2);
+cudaError_t bicg_update(const BicgVecs& v, BicgState* st, Red red2, cudaStream_t s) {
+  k_bicg_update<<<kRedGrid, kRedTpb, 0, s>>>(v, st, red2);
   return cudaGetLastError();
 }
-cudaError_t bicg_p(const BicgVecs& v, BicgState* st, int* tickets, bool fp32z, cudaStream_t s) {
-  DFG_ZD(k_bicg_p, v, st, tickets);
+cudaError_t bicg_p(const BicgVecs& v, BicgState* st, int* tickets, cudaStream_t s) {
+  k_bicg_p<<<kRedGrid, kRedTpb, 0, s>>>(v, st, tickets);
   return cudaGetLastError();
 }
 
-#undef DFG_ZD
-#undef DFG_ZB
+#undef DFG_BDISPATCH
 
 }  // namespace dfg

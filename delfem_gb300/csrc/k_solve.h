@@ -122,21 +122,18 @@ struct BicgVecs {
   double* amp; // A M^-1 p
   double* s;
   double* ams; // A M^-1 s
-  void* mp;    // M^-1 p (sweep output type)
-  void* ms;    // M^-1 s
-  void* y;     // forward-sweep output
-  float* p32;  // FP32 sweep inputs (FP32 factor only)
-  float* s32;
+  double* mp;  // M^-1 p
+  double* ms;  // M^-1 s
+  double* y;   // forward-sweep output
   long long m;
 };
 // red2: partials for 2 x kRedGrid values and its own counter
-cudaError_t bicg_init(const BicgVecs& v, BicgState* st, Red red, double tol, int maxit, int* tickets, bool fp32z,
-                      cudaStream_t s);
-cudaError_t bicg_amp(const MatView& A, const BicgVecs& v, BicgState* st, Red red, bool fp32z, cudaStream_t s);
-cudaError_t bicg_s(const BicgVecs& v, BicgState* st, int* tickets, bool fp32z, cudaStream_t s);
-cudaError_t bicg_ams(const MatView& A, const BicgVecs& v, BicgState* st, Red red2, bool fp32z, cudaStream_t s);
-cudaError_t bicg_update(const BicgVecs& v, BicgState* st, Red red2, bool fp32z, cudaStream_t s);
-cudaError_t bicg_p(const BicgVecs& v, BicgState* st, int* tickets, bool fp32z, cudaStream_t s);
+cudaError_t bicg_init(const BicgVecs& v, BicgState* st, Red red, double tol, int maxit, int* tickets, cudaStream_t s);
+cudaError_t bicg_amp(const MatView& A, const BicgVecs& v, BicgState* st, Red red, cudaStream_t s);
+cudaError_t bicg_s(const BicgVecs& v, BicgState* st, int* tickets, cudaStream_t s);
+cudaError_t bicg_ams(const MatView& A, const BicgVecs& v, BicgState* st, Red red2, cudaStream_t s);
+cudaError_t bicg_update(const BicgVecs& v, BicgState* st, Red red2, cudaStream_t s);
+cudaError_t bicg_p(const BicgVecs& v, BicgState* st, int* tickets, cudaStream_t s);
 
 // ---- strict drop-in BLAS (k_api.cu, bit-exact elementwise ops) ------------
 cudaError_t api_matvec(const MatView& A, double alpha, const double* x, double beta, double* y, cudaStream_t s);

@@ -371,9 +371,10 @@ def Solve_PCG_ex(conv_ratio: float, iteration: int, ls: LinearSystemField, prec:
 
 def Solve_PBiCGSTAB(conv_ratio: float, iteration: int, ls: LinearSystemField, prec: PreconditionerILU,
                     mode: str = "fp64"):
-    """LsSol::Solve_PBiCGSTAB (src/ls/solver_ls_iter.cpp:291-408), device-resident
-    (mode "fp64" or "fp32f").  Returns (converged, ratio, 1-based iteration);
-    when not converged the ratio is the tolerance given, as in the reference."""
+    """LsSol::Solve_PBiCGSTAB (src/ls/solver_ls_iter.cpp:291-408), device-resident,
+    FP64 (other modes are rejected).  Returns (converged, ratio, 1-based
+    iteration); when not converged the ratio is the tolerance given, as in the
+    reference."""
     c = ctypes.c_double(conv_ratio)
     it = ctypes.c_uint(iteration)
     st = lib().dfg_solve_pbicgstab(ls.h, prec.h, capi.MODES[mode], ctypes.byref(c), ctypes.byref(it))

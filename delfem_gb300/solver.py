@@ -55,8 +55,8 @@ class FESolve:
         """mode: "fp64" (LsSol::Solve_PCG semantics unless target_true), "mixed"
         (FP32 factor/sweeps/SpMV/vectors + FP64 refinement, always on the true
         residual) or "fp32f" (FP32 factor and sweeps only).  solver "bicgstab"
-        runs LsSol::Solve_PBiCGSTAB instead (modes fp64 / fp32f; its stop test
-        is the recursive residual, target_true does not apply)."""
+        runs LsSol::Solve_PBiCGSTAB instead (mode fp64 only; its stop test is
+        the recursive residual, target_true does not apply)."""
         tol = self.p.tol if tol is None else tol
         maxit = self.p.maxit if maxit is None else maxit
         if solver == "bicgstab":

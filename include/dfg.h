@@ -247,8 +247,10 @@ int dfg_solve_pcg_ex(dfg_system sys, dfg_precond prec, int mode, int target_true
 
 /* LsSol::Solve_PBiCGSTAB (src/ls/solver_ls_iter.cpp:291-408) run
  * device-resident, for non-symmetric systems (SPD ones too); the same slots
- * as dfg_solve_pcg.  mode: DFG_PREC_FP64, or DFG_PREC_FP32_FACTOR (factor and
- * sweeps in FP32, everything else FP64).  *conv_ratio: tolerance in, achieved
+ * as dfg_solve_pcg.  mode: DFG_PREC_FP64 (other modes are rejected with
+ * DFG_INVALID_ARGUMENT: BiCGSTAB does not tolerate a preconditioner applied
+ * in FP32, whose rounding differs at every application; on ill-conditioned
+ * systems its iteration then diverges).  *conv_ratio: tolerance in, achieved
  * ||r||/||r0|| out when converged (left as given otherwise, as the reference
  * does); *iteration: maximum in, 1-based iteration of convergence out (the
  * maximum when it did not converge).  A residual with ||r||^2 < 1e-60 returns

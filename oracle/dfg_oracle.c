@@ -896,6 +896,14 @@ int dfo_bicgstab(int n, int b, const int* rowptr, const int* colind, const doubl
                  const int* rowptr_f, const int* colind_f, const int* diaind_f,
                  const double* fdiag, const double* foffd,
                  double* r, double* x, double* conv, unsigned* iter, double* work) {
+  return dfo_bicgstab_hist(n, b, rowptr, colind, diag, offd, rowptr_f, colind_f, diaind_f, fdiag, foffd, r, x, conv,
+                           iter, work, NULL);
+}
+
+int dfo_bicgstab_hist(int n, int b, const int* rowptr, const int* colind, const double* diag, const double* offd,
+                      const int* rowptr_f, const int* colind_f, const int* diaind_f,
+                      const double* fdiag, const double* foffd,
+                      double* r, double* x, double* conv, unsigned* iter, double* work, double* hist) {
   const long m = (long)n * b;
   const size_t vb = sizeof(double) * (size_t)m;
   const double tol = *conv;
@@ -946,6 +954,7 @@ int dfo_bicgstab(int n, int b, const int* rowptr, const int* colind, const doubl
     vaxpy(m, -omega, ams, r);
     {
       const double sq = vdot(m, r, r);
+      if (hist) hist[it] = sq * sq_inv_norm_res_ini;
       if (sq * sq_inv_norm_res_ini < tol * tol) {
         *conv = sqrt(sq * sq_inv_norm_res_ini);
         *iter = it;

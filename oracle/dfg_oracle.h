@@ -124,6 +124,12 @@ int dfo_bicgstab(int n, int b, const int* rowptr, const int* colind, const doubl
                  const int* rowptr_f, const int* colind_f, const int* diaind_f,
                  const double* fdiag, const double* foffd,
                  double* r, double* x, double* conv, unsigned* iter, double* work);
+/* dfo_bicgstab recording hist[it] = ||r||^2 / ||r0||^2 after iteration it
+ * (hist: max iterations doubles). */
+int dfo_bicgstab_hist(int n, int b, const int* rowptr, const int* colind, const double* diag, const double* offd,
+                      const int* rowptr_f, const int* colind_f, const int* diaind_f,
+                      const double* fdiag, const double* foffd,
+                      double* r, double* x, double* conv, unsigned* iter, double* work, double* hist);
 
 /* Wall-time helpers for the CPU baseline. */
 double dfo_now(void);

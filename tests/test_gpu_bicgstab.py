@@ -27,25 +27,22 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
 
 
-@pytest.mark.parametrize("mode", ["fp64", "fp32f"])
 @pytest.mark.parametrize("path", golden_bicgstab_files(), ids=IDS)
-def test_bicgstab_matches_reference(gpu_ctx, path, mode):
+def test_bicgstab_matches_reference(gpu_ctx, path):
     from delfem_gb300 import linsys as L
     p, ref = load_golden(path)
     s = _setup(gpu_ctx, p, int(ref["fill_level"]))
     rhs = s.ls.GetResidual().copy()
-    ok, conv, it = L.Solve_PBiCGSTAB(p.tol, p.maxit, s.ls, s.prec, mode)
+    ok, conv, it = L.Solve_PBiCGSTAB(p.tol, p.maxit, s.ls, s.prec)
     x = s.solution()
     if int(ref["iter"]) == 0:  # zero right-hand side: immediate return, x untouched
         assert ok and it == 0 and conv == float(ref["conv"]) and not np.any(x)
     elif int(ref["iter"]) == p.maxit:  # limit reached: ratio as given, iteration = limit
         assert not ok and it == p.maxit and conv == p.tol
-        if mode == "fp64":
-            assert _rel(x, ref["x"]) <= 1e-6
+        assert _rel(x, ref["x"]) <= 1e-6
     else:
         assert ok and conv < p.tol
-        if mode == "fp64":
-            assert abs(it - int(ref["iter"])) <= 2, (it, int(ref["iter"]))
+        assert abs(it - int(ref["iter"])) <= 2, (it, int(ref["iter"]))
         assert _rel(x, ref["x"]) <= 1e-6
         assert s.ls.true_residual(rhs) <= 10 * p.tol
     s.close()
@@ -99,9 +96,8 @@ def _skew(out, c, seed):
     return offd.reshape(-1)
 
 
-@pytest.mark.parametrize("mode", ["fp64", "fp32f"])
 @pytest.mark.parametrize("kind,lev", [("poisson2d", 0), ("solid2d", 0), ("solid2d", 1), ("poisson3d", 0)])
-def test_bicgstab_nonsymmetric_vs_oracle(gpu_ctx, oracle_lib, kind, lev, mode):
+def test_bicgstab_nonsymmetric_vs_oracle(gpu_ctx, oracle_lib, kind, lev):
     from delfem_gb300 import linsys as L
     from delfem_gb300 import meshgen as mg
     p = {"poisson2d": lambda: mg.poisson2d_square(40, seed=41, coef_sigma=0.5),
@@ -118,12 +114,9 @@ def test_bicgstab_nonsymmetric_vs_oracle(gpu_ctx, oracle_lib, kind, lev, mode):
     assert s.factor()
     gd, go = s.prec.GetFactor()
     assert np.array_equal(bits(gd), bits(fdiag)) and np.array_equal(bits(go), bits(foffd))
-    ok, conv, it = L.Solve_PBiCGSTAB(1e-8, 5000, s.ls, s.prec, mode)
+    ok, conv, it = L.Solve_PBiCGSTAB(1e-8, 5000, s.ls, s.prec)
     assert ok and conv < 1e-8
-    if mode == "fp64":
-        assert abs(it - ref["iter"]) <= 2, (it, ref["iter"])
-    else:
-        assert it <= ref["iter"] * 1.5 + 5
+    assert abs(it - ref["iter"]) <= 2, (it, ref["iter"])
     x = s.solution()
     assert _rel(x, ref["x"]) <= 1e-6
     Ax = oracle_lib.matvec(out["n"], out["b"], out["rowptr"], out["colind"], out["diag"], offd_ns, x)
@@ -131,16 +124,17 @@ def test_bicgstab_nonsymmetric_vs_oracle(gpu_ctx, oracle_lib, kind, lev, mode):
     s.close()
 
 
-def test_bicgstab_rejects_mixed_mode_and_is_repeatable(gpu_ctx):
+def test_bicgstab_rejects_fp32_modes_and_is_repeatable(gpu_ctx):
     from delfem_gb300 import capi
     from delfem_gb300 import linsys as L
     from delfem_gb300 import meshgen as mg
     p = mg.solid2d_cantilever(30, 12, seed=45)
     s = _setup(gpu_ctx, p, 0)
     rhs = s.ls.GetResidual().copy()
-    with pytest.raises(capi.DfgError) as e:
-        L.Solve_PBiCGSTAB(1e-8, 100, s.ls, s.prec, "mixed")
-    assert e.value.status == capi.DFG_INVALID_ARGUMENT
+    for mode in ("mixed", "fp32f"):
+        with pytest.raises(capi.DfgError) as e:
+            L.Solve_PBiCGSTAB(1e-8, 100, s.ls, s.prec, mode)
+        assert e.value.status == capi.DFG_INVALID_ARGUMENT
     ok1, c1, it1 = L.Solve_PBiCGSTAB(1e-8, 1000, s.ls, s.prec)
     x1 = s.solution()
     s.ls.SetVector(-1, rhs)
