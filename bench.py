@@ -52,11 +52,14 @@ CONFIGS = {
     "solid3d_48": dict(kind="solid3d", n=48),
     "solid2d_200x100": dict(kind="solid2d", nx=200, ny=100),
 }
-# PCG iterations of the full FP64 solve of a workload at an ILU fill level,
-# measured with the reference's own algorithm (bit-exact CPU restatement,
-# 1e-8); used to extrapolate the bounded CPU samples to whole solves.
-REF_ITERS = {("solid2d_1000x500", 0): 2540, ("solid2d_1000x500", 1): 1389, ("poisson2d_128", 0): 132,
-             ("solid2d_200x100", 0): 496, ("solid2d_200x100", 1): 270}
+# Iterations of the full FP64 solve of a workload at an ILU fill level with
+# a solver, measured with the reference's own algorithm (bit-exact CPU
+# restatement, 1e-8); used to extrapolate the bounded CPU samples to whole
+# solves.
+REF_ITERS = {("solid2d_1000x500", 0, "pcg"): 2540, ("solid2d_1000x500", 1, "pcg"): 1389,
+             ("poisson2d_128", 0, "pcg"): 132, ("solid2d_200x100", 0, "pcg"): 496,
+             ("solid2d_200x100", 1, "pcg"): 270, ("solid2d_1000x500", 0, "bicgstab"): 2258,
+             ("solid2d_200x100", 0, "bicgstab"): 374}
 
 
 # (name in the JSON line, solver mode)
@@ -429,7 +432,7 @@ def compose_line(args, world, p, results, prof, e2e, head):
         line["e2e"] = {"value": round(e2e["value"], 4), "unit": "solves/s", "h2d_bytes_per_step": int(e2e["h2d"]),
                        "d2h_bytes_per_step": int(e2e["d2h"])}
     if not args.no_cpu_baseline:
-        iters_full = (REF_ITERS.get((args.config, args.fill_level)) if args.solver == "pcg" else None) or \
+        iters_full = REF_ITERS.get((args.config, args.fill_level, args.solver)) or \
             results[("plain_fp64" if "plain_fp64" in results else head)]["iters"][-1]
         sample_iters = args.cpu_sample_iters
         rate, t_solve, res = cpu_rate(args.config, iters_full, 1, sample_iters, args.fill_level, args.solver)
@@ -701,7 +704,7 @@ def run_reference(args, rank, world):
     procs = os.cpu_count() or 1
     if CONFIGS[args.config]["kind"] == "serve":
         return run_reference_serve(args, world, procs)
-    iters_full = REF_ITERS.get((args.config, args.fill_level))
+    iters_full = REF_ITERS.get((args.config, args.fill_level, args.solver))
     if iters_full is None:
         iters_full = 3000
     rates = []
