@@ -25,6 +25,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--expt-r
 SOURCES = {
     "capi.cu": [],
     "sched.cpp": [],
+    "meshio.cpp": ["-Xcompiler", "-ffp-contract=off"],
     "k_sweep.cu": [],
     "k_solve.cu": [],
     "k_bicg.cu": [],

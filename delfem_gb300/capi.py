@@ -55,6 +55,9 @@ SIGNATURES = {
     "dfg_system_set_mesh": (_I, [_P, _I, _P, _I, _I, _P]),
     "dfg_system_set_coef": (_I, [_P, _P]),
     "dfg_system_set_field": (_I, [_P, _P, _P]),
+    "dfg_system_update_field": (_I, [_P, _I]),
+    "dfg_system_get_field": (_I, [_P, _P, _P]),
+    "dfg_mesh_read_gid": (_I, [ctypes.c_char_p, _PI, _PI, _PI, _PI, _P, _P]),
     "dfg_set_bcflags": (_I, [_P, _P]),
     "dfg_initialize_marge": (_I, [_P]),
     "dfg_assemble_poisson": (_I, [_P, _D, _D]),

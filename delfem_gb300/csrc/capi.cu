@@ -423,6 +423,46 @@ extern "C" int dfg_system_set_field(dfg_system sys, const double* u, const doubl
   });
 }
 
+extern "C" int dfg_system_update_field(dfg_system sys, int fdt) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    REQUIRE(fdt == 0 || fdt == 1, DFG_INVALID_ARGUMENT, "fdt must be 0 (VALUE) or 1 (VELOCITY)");
+    const long long m = (long long)sys->n * sys->b;
+    DBuf& f = fdt == 0 ? sys->fu : sys->fv;
+    bool& has = fdt == 0 ? sys->has_u : sys->has_v;
+    if (!has) {
+      dalloc(ctx, f, (size_t)m * 8);
+      CK(cudaMemsetAsync(f.p, 0, (size_t)m * 8, ctx->stream));
+      has = true;
+    }
+    CK(api_axpy(m, 1.0, sys->upd.as<double>(), f.as<double>(), ctx->stream));  // AddValueToNodeSegment(.., 1.0)
+    launched(ctx);
+    CK(cudaStreamSynchronize(ctx->stream));
+    return DFG_OK;
+  });
+}
+
+extern "C" int dfg_system_get_field(dfg_system sys, double* u, double* v) {
+  if (!sys) return DFG_INVALID_ARGUMENT;
+  dfg_ctx ctx = sys->ctx;
+  return guarded(ctx, [&]() -> int {
+    dfg_ctx ctx_ = ctx;
+    const size_t bytes = (size_t)sys->n * sys->b * 8;
+    if (u) {
+      if (sys->has_u) CK(cudaMemcpyAsync(u, sys->fu.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+      else std::memset(u, 0, bytes);
+    }
+    if (v) {
+      if (sys->has_v) CK(cudaMemcpyAsync(v, sys->fv.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+      else std::memset(v, 0, bytes);
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return DFG_OK;
+  });
+}
+
 extern "C" int dfg_set_bcflags(dfg_system sys, const int* flags) {
   if (!sys) return DFG_INVALID_ARGUMENT;
   dfg_ctx ctx = sys->ctx;

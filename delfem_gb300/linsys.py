@@ -116,6 +116,18 @@ class LinearSystemField:
         v = None if v is None else _f64(v)
         check(self.ctx.h, lib().dfg_system_set_field(self.h, _p(u), _p(v)), "dfg_system_set_field")
 
+    def UpdateValueOfField(self, fdt: int = 0):
+        """CLinearSystem_Field::UpdateValueOfField on the resident field:
+        value (fdt 0) or velocity (fdt 1) += update, on the device."""
+        check(self.ctx.h, lib().dfg_system_update_field(self.h, fdt), "dfg_system_update_field")
+
+    def get_field(self):
+        """Host copies (u, v) of the resident field."""
+        u = np.zeros(self.n * self.b)
+        v = np.zeros(self.n * self.b)
+        check(self.ctx.h, lib().dfg_system_get_field(self.h, _p(u), _p(v)), "dfg_system_get_field")
+        return u, v
+
     def SetLoad(self, f):
         """Resident nodal load added at every FinalizeMarge (None clears it)."""
         ff = None if f is None else _f64(f)

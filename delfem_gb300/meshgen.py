@@ -451,3 +451,84 @@ def read_result(path: str) -> dict:
     (out["conv"],) = take("<d")
     out["x"] = take("<f8", n * b)
     return out
+
+
+# ------------------------------------------------------------ GiD mesh files
+
+def read_gid_msh(path: str):
+    """Nodes and elements of a GiD ".msh" file through the library's reader
+    (dfg_mesh_read_gid; no device needed): (coords (nnode, ndim), conn
+    (nelem, nnoel) 0-based), triangles in 2D or tetrahedra in 3D."""
+    import ctypes
+    from . import capi
+    L = capi.lib()
+    nd, nk, nn, ne = (ctypes.c_int() for _ in range(4))
+    st = L.dfg_mesh_read_gid(path.encode(), ctypes.byref(nd), ctypes.byref(nk), ctypes.byref(nn),
+                             ctypes.byref(ne), None, None)
+    if st != capi.DFG_OK:
+        raise capi.DfgError(st, "dfg_mesh_read_gid", L.dfg_last_error(None).decode(errors="replace"))
+    coords = np.zeros((nn.value, nd.value))
+    conn = np.zeros((ne.value, nk.value), dtype=np.int32)
+    st = L.dfg_mesh_read_gid(path.encode(), ctypes.byref(nd), ctypes.byref(nk), ctypes.byref(nn), ctypes.byref(ne),
+                             ctypes.c_void_p(coords.ctypes.data), ctypes.c_void_p(conn.ctypes.data))
+    if st != capi.DFG_OK:
+        raise capi.DfgError(st, "dfg_mesh_read_gid", L.dfg_last_error(None).decode(errors="replace"))
+    return coords, conn
+
+
+def write_gid_msh(path: str, coords: np.ndarray, conn: np.ndarray) -> None:
+    """Writes a GiD ".msh" file in the layout of the reference's input meshes
+    (three coordinates per node, 17 significant digits so that reading it
+    back gives the same doubles)."""
+    nnoel = conn.shape[1]
+    etype = {3: "Triangle", 4: "Tetrahedra"}[nnoel]
+    with open(path, "w") as f:
+        f.write(f"MESH    dimension 3 ElemType {etype}  Nnode {nnoel}\nCoordinates\n")
+        for i, c in enumerate(coords):
+            xyz = list(c) + [0.0] * (3 - len(c))
+            f.write(f"{i + 1:6d} {xyz[0]:.17g} {xyz[1]:.17g} {xyz[2]:.17g}\n")
+        f.write("end coordinates\n\nElements\n")
+        for e, v in enumerate(conn):
+            f.write(f"{e + 1:6d} " + " ".join(str(int(x) + 1) for x in v) + "\n")
+        f.write("end elements\n")
+
+
+def boundary_nodes(conn: np.ndarray) -> np.ndarray:
+    """Nodes on the boundary of a triangle or tetrahedron mesh: those of the
+    edges (faces) that belong to one element only."""
+    k = conn.shape[1]
+    faces = np.sort(np.concatenate([np.delete(conn, j, axis=1) for j in range(k)]), axis=1)
+    uniq, counts = np.unique(faces, axis=0, return_counts=True)
+    return np.unique(uniq[counts == 1].ravel())
+
+
+def mesh_problem(kind: int, coords: np.ndarray, conn: np.ndarray, seed: int = 0, coef_sigma: float = 0.0,
+                 tol: float = 1e-8, name: str = "mesh") -> Problem:
+    """A load case on a given mesh: Poisson kinds with alpha = source = 1 and
+    u = 0 on every boundary node; solid kinds clamped on the boundary nodes of
+    smallest x, under gravity -1e-3 along the last axis (E = 1, nu = 0.3)."""
+    rng = np.random.default_rng(seed)
+    coords = np.ascontiguousarray(coords, dtype=np.float64)
+    conn = np.ascontiguousarray(conn, dtype=np.int32)
+    b = BLOCK[kind]
+    bnd = boundary_nodes(conn)
+    bc = np.zeros(coords.shape[0] * b, dtype=np.int32)
+    prm = np.zeros(8)
+    if kind in (POISSON2D, POISSON3D):
+        bc[bnd] = 1
+        prm[0] = 1.0
+        prm[1] = 1.0
+    elif kind in (SOLID2D, SOLID3D):
+        xmin = coords[:, 0].min()
+        clamp = bnd[np.abs(coords[bnd, 0] - xmin) <= 1e-9 * max(1.0, abs(xmin))]
+        for d in range(b):
+            bc[clamp * b + d] = 1
+        lam, myu = lame(1.0, 0.3)
+        prm[0] = lam
+        prm[1] = myu
+        prm[2] = 1.0
+        prm[2 + b] = -1e-3  # g_y in 2D (params[4]), g_z in 3D (params[5])
+    else:
+        raise ValueError("mesh_problem covers the Poisson and solid kinds")
+    coef = _lognormal(rng, conn.shape[0], coef_sigma) if coef_sigma > 0 else None
+    return Problem(kind, coords, conn, prm, bc, coef=coef, tol=tol, name=name)

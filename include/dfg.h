@@ -104,6 +104,15 @@ int dfg_system_set_coef(dfg_system sys, const double* coef);
 /* Current field values u and velocities v (nblk*blklen doubles each, NULL = 0),
  * read by the element routines as the reference reads the field node segments. */
 int dfg_system_set_field(dfg_system sys, const double* u, const double* v);
+/* CLinearSystem_Field::UpdateValueOfField (src/femls/linearsystem_field.cpp:
+ * 716-794) on the resident field: field += 1.0 * update slot, for the
+ * field's value (fdt 0, VALUE) or velocity (fdt 1, VELOCITY), on the device
+ * -- the next assembly reads it without a host round trip.  A field not set
+ * before starts from zero, as a fresh reference field does. */
+int dfg_system_update_field(dfg_system sys, int fdt);
+/* Host copy of the resident field (u and/or v, nblk*blklen doubles each;
+ * NULL skips one; zeros for a field never set). */
+int dfg_system_get_field(dfg_system sys, double* u, double* v);
 /* Dirichlet flags, one int per DOF (1 = fixed).  Replaces
  * CLinearSystem_Field::SetFixedBoundaryCondition_Field -> CBCFlag::SetBC
  * (src/femls/linearsystem_field.cpp:618-710, include/delfem/matvec/bcflag_blk.h:153-164). */
@@ -224,6 +233,20 @@ int dfg_precond_solve(dfg_precond prec, dfg_system sys, int iv);
 /* Host copy of the factor in the reference layout: fdiag n*b*b, foffd
  * nnz*b*b with nnz and the block order of dfg_precond_get_pattern. */
 int dfg_precond_get_factor(dfg_precond prec, double* fdiag, double* foffd);
+
+/* ------------------------------------------------------------- mesh input */
+
+/* Reads a GiD mesh file (".msh", the format of the reference's input meshes,
+ * test_glut/input_file/) as Msh::CMesher2D::ReadFromFile_GiDMsh
+ * (src/msh/mesher2d.cpp:2463) reads triangles and Msh::CMesh3D::
+ * ReadFromFile_GiDMsh (src/msh/mesh3d.cpp:601) tetrahedra: *ndim = 2 with
+ * *nnoel = 3 (triangles; three-coordinate nodes in a coordinate plane are
+ * projected on it, dropping the axis of smallest variance) or *ndim = 3 with
+ * *nnoel = 4.  coords: nnode*ndim doubles, conn: nelem*nnoel 0-based node
+ * ids, in file order; call with both NULL to get the sizes first.  Needs no
+ * device.  Other element types and malformed files: DFG_INVALID_ARGUMENT,
+ * reason in dfg_last_error(NULL). */
+int dfg_mesh_read_gid(const char* path, int* ndim, int* nnoel, int* nnode, int* nelem, double* coords, int* conn);
 
 /* ------------------------------------------------------------------- solvers */
 

@@ -12,6 +12,10 @@
 //
 // Usage: ref_harness problem.bin out.bin [fill_level [pcg|bicgstab]]
 // (the solver is LsSol::Solve_PCG by default, LsSol::Solve_PBiCGSTAB on request)
+//        ref_harness --mesh2d|--mesh3d file.msh out.bin
+// (loads a GiD mesh file with the reference's reader, Msh::CMesher2D or
+// Msh::CMesh3D ::ReadFromFile_GiDMsh, and dumps the nodes and elements:
+// int32 magic 0x44464D31, ndim, nnoel, nnode, nelem; f64 coords; i32 conn)
 // Input / output formats are described in tests/golden/make_golden.py.
 #include <cassert>
 #include <cmath>
@@ -36,6 +40,8 @@
 #include "delfem/femeqn/eqn_linear_solid3d.h"
 #include "delfem/femeqn/ker_emat_tri.h"
 #include "delfem/femeqn/ker_emat_tet.h"
+#include "delfem/mesher2d.h"
+#include "delfem/mesh3d.h"
 
 using namespace Fem::Field;
 
@@ -209,7 +215,37 @@ static void assemble_coef(const Problem& p, MatVec::CMatDia_BlkCrs& A, MatVec::C
 static void wr(FILE* f, const void* p, size_t n) { if (n) fwrite(p, 1, n, f); }
 static void wri(FILE* f, int v) { wr(f, &v, 4); }
 
+static int dump_mesh(const char* kind, const char* in, const char* out) {
+  std::vector<double> co;
+  std::vector<int> cn;
+  int ndim = 0, nnoel = 0;
+  if (strcmp(kind, "--mesh2d") == 0) {
+    Msh::CMesher2D m;
+    if (!m.ReadFromFile_GiDMsh(in)) return 3;
+    for (const Com::CVector2D& v : m.GetVectorAry()) { co.push_back(v.x); co.push_back(v.y); }
+    for (const Msh::CTriAry2D& a : m.GetTriArySet())
+      for (const Msh::STri2D& t : a.m_aTri) for (int k = 0; k < 3; ++k) cn.push_back((int)t.v[k]);
+    ndim = 2; nnoel = 3;
+  } else {
+    Msh::CMesh3D m;
+    if (!m.ReadFromFile_GiDMsh(in)) return 3;
+    for (const Com::CVector3D& v : m.GetVectorAry()) { co.push_back(v.x); co.push_back(v.y); co.push_back(v.z); }
+    for (const Msh::CTetAry& a : m.GetTetArySet())
+      for (const Msh::STet& t : a.m_aTet) for (int k = 0; k < 4; ++k) cn.push_back((int)t.v[k]);
+    ndim = 3; nnoel = 4;
+  }
+  FILE* f = fopen(out, "wb");
+  if (!f) return 2;
+  const int hdr[5] = {0x44464D31, ndim, nnoel, (int)(co.size() / ndim), (int)(cn.size() / nnoel)};
+  fwrite(hdr, 4, 5, f);
+  fwrite(co.data(), 8, co.size(), f);
+  fwrite(cn.data(), 4, cn.size(), f);
+  fclose(f);
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc == 4 && strncmp(argv[1], "--mesh", 6) == 0) return dump_mesh(argv[1], argv[2], argv[3]);
   if (argc < 3 || argc > 5) {
     fprintf(stderr, "usage: %s problem.bin out.bin [fill_level [pcg|bicgstab]]\n", argv[0]);
     return 2;
