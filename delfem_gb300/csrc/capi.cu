@@ -15,6 +15,7 @@
 #include "dfg_internal.h"
 #include "k_assemble.h"
 #include "k_ilu.h"
+#include "k_pattern.h"
 #include "k_solve.h"
 #include "k_sweep.h"
 
@@ -326,6 +327,110 @@ extern "C" int dfg_system_create(dfg_ctx ctx, int nblk, int blklen, const int* r
   });
 }
 
+namespace {
+
+int read_flag(dfg_ctx ctx_, const int* d) {
+  int h = 0;
+  CK(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, ctx_->stream));
+  CK(cudaStreamSynchronize(ctx_->stream));
+  return h;
+}
+
+// Element incidences per node on the device (ptr: n+1 offsets, inc: e*k+i
+// sorted per node); returns the error flag (0, or kPatErrRange).
+int build_incidence(dfg_ctx ctx_, int n, long long nk, const int* d_conn, DBuf& ptr, DBuf& inc, DBuf& flag) {
+  DBuf cnt, bsum;
+  dalloc(ctx_, cnt, (size_t)std::max(n, 1) * 4);
+  dalloc(ctx_, flag, 16);
+  dalloc(ctx_, ptr, (size_t)(n + 1) * 8);
+  dalloc(ctx_, bsum, (size_t)std::max<long long>(scan_blocks(n), 1) * 8);
+  dalloc(ctx_, inc, (size_t)std::max<long long>(nk, 1) * 4);
+  CK(cudaMemsetAsync(cnt.p, 0, cnt.bytes, ctx_->stream));
+  CK(cudaMemsetAsync(flag.p, 0, flag.bytes, ctx_->stream));
+  CK(incidence_count(d_conn, nk, n, cnt.as<int>(), flag.as<int>(), ctx_->stream));
+  CK(exclusive_scan<long long>(cnt.as<int>(), n, ptr.as<long long>(), bsum.as<long long>(), ctx_->stream));
+  CK(cudaMemsetAsync(cnt.p, 0, cnt.bytes, ctx_->stream));  // now the placement cursors
+  CK(incidence_fill(d_conn, nk, n, ptr.as<long long>(), cnt.as<int>(), inc.as<int>(), ctx_->stream));
+  launched(ctx_, 6);
+  return read_flag(ctx_, flag.as<int>());
+}
+
+// The element pattern (MakePattern_FEM + AddPattern) built on the device and
+// copied to the host; false when a node's neighbour list overflows the
+// per-thread bound, and the caller builds on the host.
+bool device_pattern(dfg_ctx ctx_, int n, int nelem, int k, const int* conn, std::vector<int>& rp,
+                    std::vector<int>& ci) {
+  if ((long long)n * kPatCap > INT32_MAX) return false;  // int offsets
+  const long long nk = (long long)nelem * k;
+  DBuf dconn, ptr, inc, flag, rowcnt, rowptr, colind, bsum;
+  upload(ctx_, dconn, conn, (size_t)nk, 16);
+  REQUIRE(build_incidence(ctx_, n, nk, dconn.as<int>(), ptr, inc, flag) == 0, DFG_INVALID_ARGUMENT,
+          "connectivity index out of range");
+  dalloc(ctx_, rowcnt, (size_t)std::max(n, 1) * 4);
+  CK(pattern_count(n, k, dconn.as<int>(), ptr.as<long long>(), inc.as<int>(), rowcnt.as<int>(), flag.as<int>(),
+                   ctx_->stream));
+  launched(ctx_);
+  if (read_flag(ctx_, flag.as<int>()) != 0) return false;
+  dalloc(ctx_, rowptr, (size_t)(n + 1) * 4);
+  dalloc(ctx_, bsum, (size_t)std::max<long long>(scan_blocks(n), 1) * 4);
+  CK(exclusive_scan<int>(rowcnt.as<int>(), n, rowptr.as<int>(), bsum.as<int>(), ctx_->stream));
+  launched(ctx_, 3);
+  rp.assign(n + 1, 0);
+  CK(cudaMemcpyAsync(rp.data(), rowptr.p, (size_t)(n + 1) * 4, cudaMemcpyDeviceToHost, ctx_->stream));
+  CK(cudaStreamSynchronize(ctx_->stream));
+  const int nnz = rp[n];
+  dalloc(ctx_, colind, (size_t)std::max(nnz, 1) * 4);
+  CK(pattern_fill(n, k, dconn.as<int>(), ptr.as<long long>(), inc.as<int>(), rowptr.as<int>(), colind.as<int>(),
+                  ctx_->stream));
+  launched(ctx_);
+  ci.assign(nnz, 0);
+  if (nnz) CK(cudaMemcpyAsync(ci.data(), colind.p, (size_t)nnz * 4, cudaMemcpyDeviceToHost, ctx_->stream));
+  CK(cudaStreamSynchronize(ctx_->stream));
+  return true;
+}
+
+struct DeviceGather {
+  DBuf slot_ptr, slot_src, res_ptr, res_src;
+};
+
+// The assembly gather map (the element order of Mearge) built on the device
+// from the connectivity d_conn against the system's pattern; false when a
+// row is wider than the per-thread bound (build on the host).
+bool device_gather_map(dfg_ctx ctx_, dfg_system sys, int nelem, int k, const int* d_conn, DeviceGather& G) {
+  const int n = sys->n;
+  const long long nnz = sys->nnz, nk = (long long)nelem * k;
+  REQUIRE(nk * k <= INT32_MAX, DFG_INVALID_ARGUMENT, "mesh too large for 32-bit element-block indices");
+  DBuf ptr, inc, flag, slotcnt, bsum;
+  REQUIRE(build_incidence(ctx_, n, nk, d_conn, ptr, inc, flag) == 0, DFG_INVALID_ARGUMENT,
+          "connectivity index out of range");
+  const long long ns = n + nnz;
+  dalloc(ctx_, slotcnt, (size_t)std::max<long long>(ns, 1) * 4);
+  CK(cudaMemsetAsync(slotcnt.p, 0, slotcnt.bytes, ctx_->stream));
+  CK(slots_count(n, k, d_conn, ptr.as<long long>(), inc.as<int>(), sys->rowptr.as<int>(), sys->colind.as<int>(),
+                 slotcnt.as<int>(), flag.as<int>(), ctx_->stream));
+  launched(ctx_);
+  if (read_flag(ctx_, flag.as<int>()) != 0) return false;
+  dalloc(ctx_, G.slot_ptr, (size_t)(ns + 1) * 8);
+  dalloc(ctx_, bsum, (size_t)std::max<long long>(scan_blocks(ns), 1) * 8);
+  CK(exclusive_scan<long long>(slotcnt.as<int>(), ns, G.slot_ptr.as<long long>(), bsum.as<long long>(),
+                               ctx_->stream));
+  launched(ctx_, 3);
+  long long total = 0;
+  CK(cudaMemcpyAsync(&total, G.slot_ptr.as<long long>() + ns, 8, cudaMemcpyDeviceToHost, ctx_->stream));
+  CK(cudaStreamSynchronize(ctx_->stream));
+  REQUIRE(total <= INT32_MAX, DFG_INVALID_ARGUMENT, "mesh too large for 32-bit element-block indices");
+  dalloc(ctx_, G.slot_src, (size_t)std::max<long long>(total, 1) * 4);
+  CK(slots_fill(n, k, d_conn, ptr.as<long long>(), inc.as<int>(), sys->rowptr.as<int>(), sys->colind.as<int>(),
+                G.slot_ptr.as<long long>(), G.slot_src.as<int>(), ctx_->stream));
+  launched(ctx_);
+  G.res_ptr = std::move(ptr);
+  G.res_src = std::move(inc);
+  CK(cudaStreamSynchronize(ctx_->stream));
+  return true;
+}
+
+}  // namespace
+
 extern "C" int dfg_system_create_from_elements(dfg_ctx ctx, int nblk, int blklen, int nelem, int nnoel,
                                                const int* conn, dfg_system* out) {
   if (!ctx || !out) return DFG_INVALID_ARGUMENT;
@@ -336,7 +441,8 @@ extern "C" int dfg_system_create_from_elements(dfg_ctx ctx, int nblk, int blklen
     REQUIRE(nblk >= 0 && nelem >= 0 && nnoel >= 1 && (conn || nelem == 0), DFG_INVALID_ARGUMENT, "bad element arguments");
     for (long long k = 0; k < (long long)nelem * nnoel; ++k)
       REQUIRE(conn[k] >= 0 && conn[k] < nblk, DFG_INVALID_ARGUMENT, "connectivity index out of range");
-    pattern_from_elements(nblk, nelem, nnoel, conn, rp, ci);
+    // on the device; the host builder when a node has more neighbours than a thread's list holds
+    if (!device_pattern(ctx, nblk, nelem, nnoel, conn, rp, ci)) pattern_from_elements(nblk, nelem, nnoel, conn, rp, ci);
     return DFG_OK;
   });
   if (rc != DFG_OK) return rc;
@@ -376,20 +482,32 @@ extern "C" int dfg_system_set_mesh(dfg_system sys, int ndim, const double* coord
     REQUIRE((ndim == 2 && nnoel == 3) || (ndim == 3 && nnoel == 4), DFG_INVALID_ARGUMENT,
             "elements must be P1 triangles (2D) or P1 tetrahedra (3D)");
     REQUIRE(nelem >= 0 && coords && (conn || nelem == 0), DFG_INVALID_ARGUMENT, "bad mesh arguments");
-    GatherMap G;
-    std::string err;
-    REQUIRE(build_gather_map(sys->n, sys->h_rowptr.data(), sys->h_colind.data(), nelem, nnoel, conn, G, err),
-            DFG_INVALID_ARGUMENT, err);
+    // everything is built aside and replaces the system's mesh only once complete
+    DBuf dconn, dcoords;
+    DeviceGather D;
+    upload(ctx, dconn, conn, (size_t)nelem * nnoel, 16);
+    upload(ctx, dcoords, coords, (size_t)sys->n * ndim);
+    // gather map on the device; the host builder when a row is wider than a thread's list holds
+    if (!device_gather_map(ctx, sys, nelem, nnoel, dconn.as<int>(), D)) {
+      GatherMap G;
+      std::string err;
+      REQUIRE(build_gather_map(sys->n, sys->h_rowptr.data(), sys->h_colind.data(), nelem, nnoel, conn, G, err),
+              DFG_INVALID_ARGUMENT, err);
+      upload(ctx, D.slot_ptr, G.slot_ptr.data(), G.slot_ptr.size());
+      upload(ctx, D.slot_src, G.slot_src.data(), G.slot_src.size(), 16);
+      upload(ctx, D.res_ptr, G.res_ptr.data(), G.res_ptr.size());
+      upload(ctx, D.res_src, G.res_src.data(), G.res_src.size(), 16);
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    sys->conn = std::move(dconn);
+    sys->coords = std::move(dcoords);
+    sys->slot_ptr = std::move(D.slot_ptr);
+    sys->slot_src = std::move(D.slot_src);
+    sys->res_ptr = std::move(D.res_ptr);
+    sys->res_src = std::move(D.res_src);
     sys->ndim = ndim;
     sys->nelem = nelem;
     sys->nnoel = nnoel;
-    upload(ctx, sys->coords, coords, (size_t)sys->n * ndim);
-    upload(ctx, sys->conn, conn, (size_t)nelem * nnoel);
-    upload(ctx, sys->slot_ptr, G.slot_ptr.data(), G.slot_ptr.size());
-    upload(ctx, sys->slot_src, G.slot_src.data(), G.slot_src.size());
-    upload(ctx, sys->res_ptr, G.res_ptr.data(), G.res_ptr.size());
-    upload(ctx, sys->res_src, G.res_src.data(), G.res_src.size());
-    CK(cudaStreamSynchronize(ctx->stream));
     return DFG_OK;
   });
 }

@@ -17,6 +17,7 @@ Vector slots: -1 residual, -2 update, >= 0 work vectors
 from __future__ import annotations
 
 import ctypes
+import weakref
 
 import numpy as np
 
@@ -37,14 +38,22 @@ def _i32(a) -> np.ndarray:
 
 
 class Context:
-    """One CUDA device + stream (dfg_ctx)."""
+    """One CUDA device + stream (dfg_ctx).  Systems, preconditioners and
+    servers made on it register here; closing the context closes those still
+    open first (the C ABI wants them destroyed before their context)."""
 
     def __init__(self, device: int = 0):
+        self._children = weakref.WeakSet()
         h = ctypes.c_void_p()
         st = lib().dfg_ctx_create(device, ctypes.byref(h))
         if st != capi.DFG_OK:
             raise capi.DfgError(st, "dfg_ctx_create", lib().dfg_last_error(None).decode(errors="replace"))
         self.h = h
+
+    def adopt(self, obj) -> None:
+        """Registers an object with a native handle on this context; it must
+        have close() and a _close_order (lower closes first)."""
+        self._children.add(obj)
 
     def synchronize(self):
         check(self.h, lib().dfg_ctx_synchronize(self.h), "dfg_ctx_synchronize")
@@ -64,6 +73,8 @@ class Context:
 
     def close(self):
         if self.h:
+            for c in sorted(list(self._children), key=lambda o: o._close_order):
+                c.close()
             lib().dfg_ctx_destroy(self.h)
             self.h = None
 
@@ -91,6 +102,7 @@ class LinearSystemField:
             st = lib().dfg_system_create(ctx.h, self.n, self.b, _p(rowptr), _p(colind), ctypes.byref(h))
         check(ctx.h, st, "dfg_system_create")
         self.h = h
+        ctx.adopt(self)
         nnz = ctypes.c_longlong()
         lib().dfg_system_info(self.h, None, None, ctypes.byref(nnz))
         self.nnz = int(nnz.value)
@@ -213,9 +225,12 @@ class LinearSystemField:
         check(self.ctx.h, lib().dfg_true_residual(self.h, _p(bb), ctypes.byref(r)), "dfg_true_residual")
         return r.value
 
+    _close_order = 2
+
     def close(self):
         if getattr(self, "h", None):
-            lib().dfg_system_destroy(self.h)
+            if self.ctx.h:  # after its context the handle is only dropped
+                lib().dfg_system_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -235,6 +250,7 @@ class PreconditionerILU:
         h = ctypes.c_void_p()
         check(ctx.h, lib().dfg_precond_create(ctx.h, ctypes.byref(h)), "dfg_precond_create")
         self.h = h
+        ctx.adopt(self)
         self.ls = None
 
     def SetFillInLevel(self, lev: int):
@@ -277,9 +293,12 @@ class PreconditionerILU:
         check(self.ctx.h, lib().dfg_precond_get_factor(self.h, _p(fdiag), _p(foffd)), "dfg_precond_get_factor")
         return fdiag, foffd[: nnz.value * bs]
 
+    _close_order = 1
+
     def close(self):
         if getattr(self, "h", None):
-            lib().dfg_precond_destroy(self.h)
+            if self.ctx.h:
+                lib().dfg_precond_destroy(self.h)
             self.h = None
 
     def __del__(self):

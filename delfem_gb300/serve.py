@@ -34,6 +34,8 @@ class Server:
         h = ctypes.c_void_p()
         check(ctx.h, lib().dfg_server_create(ctx.h, ctypes.byref(cfg), ctypes.byref(h)), "dfg_server_create")
         self.h = h
+        if hasattr(ctx, "adopt"):
+            ctx.adopt(self)
         self.mode = mode
         self._out: dict[int, np.ndarray] = {}
 
@@ -93,9 +95,12 @@ class Server:
                 out[name] = {"n": n, "ms": ms, "bytes": by, "gbs": (by / (ms * 1e-3) / 1e9) if ms > 0 and by > 0 else None}
         return out
 
+    _close_order = 0
+
     def close(self) -> None:
-        if self.h:
-            lib().dfg_server_destroy(self.h)
+        if getattr(self, "h", None):
+            if self.ctx.h:  # after its context the handle is only dropped
+                lib().dfg_server_destroy(self.h)
             self.h = None
 
     def __enter__(self):

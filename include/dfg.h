@@ -56,6 +56,8 @@ typedef struct dfg_precond_s* dfg_precond;
 
 /* Creates a context on CUDA device `device` with its own stream. */
 int dfg_ctx_create(int device, dfg_ctx* out);
+/* Destroys the context; systems, preconditioners and servers made on it
+ * must be destroyed first (they use its stream and device). */
 int dfg_ctx_destroy(dfg_ctx ctx);
 /* Text of the last error raised through this context (never NULL); with
  * ctx == NULL, the reason the last dfg_ctx_create or dfg_dot_noalloc of this
