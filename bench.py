@@ -723,7 +723,7 @@ def run_reference(args, rank, world):
         "ms_per_step": round(1e3 * procs / value, 1),
         "cpu_baseline": {"value": round(value, 6), "unit": "solves/s", "cores": procs, "kind": "port",
                          "sample": f"per core: assembly + Dirichlet + ILU({args.fill_level}) of the full workload and "
-                                   f"{args.cpu_sample_iters} PCG iterations, extrapolated to {iters_full + 1} "
+                                   f"{args.cpu_sample_iters} {args.solver.upper()} iterations, extrapolated to {iters_full + 1} "
                                    f"iterations; the reference algorithm's bit-exact C restatement"},
         "e2e": {"value": round(value, 6), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": round(time.perf_counter() - t_all0, 1),
