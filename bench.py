@@ -115,7 +115,15 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{device}.csv")
+        # the raw samples go to DFG_CLOCKS_DIR when set (kept for inspection),
+        # else to a temporary file; the JSON line carries their summary
+        d = os.environ.get("DFG_CLOCKS_DIR")
+        if d:
+            self.path = os.path.join(d, f"clocks_rank{device}.csv")
+        else:
+            import tempfile
+            fd, self.path = tempfile.mkstemp(prefix=f"dfg_clocks{device}_", suffix=".csv")
+            os.close(fd)
 
     def __enter__(self):
         try:

@@ -2,9 +2,9 @@
  * dfg_oracle.h -- CPU oracle for the DelFEM assembly + ILU-PCG path.
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
- * algorithm, used by tests/, __graft_entry__.smoke() and bench.py's CPU
- * baseline as the checker.  The product library (libdfg) never links,
- * loads or calls it.
+ * algorithm; tests/ and __graft_entry__.smoke() check the library's results
+ * against it, and bench.py times it as the CPU baseline.  The product
+ * library (libdfg) never links, loads or calls it.
  *
  * Parity pin: every function here is checked bit-for-bit against the
  * reference code itself (compiled headless from its sources by
