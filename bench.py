@@ -118,6 +118,8 @@ class ClockSampler:
         # the raw samples go to DFG_CLOCKS_DIR when set (kept for inspection),
         # else to a temporary file; the JSON line carries their summary
         d = os.environ.get("DFG_CLOCKS_DIR")
+        self.temp = not d
+        self.cached = None
         if d:
             self.path = os.path.join(d, f"clocks_rank{device}.csv")
         else:
@@ -146,6 +148,13 @@ class ClockSampler:
             self.f.close()
 
     def summary(self):
+        if self.cached is None:
+            self.cached = self._read()
+            if self.temp and os.path.exists(self.path):
+                os.remove(self.path)
+        return self.cached
+
+    def _read(self):
         if self.proc is None or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         sm, smax, reasons = [], None, set()
