@@ -360,8 +360,8 @@ int build_incidence(dfg_ctx ctx_, int n, long long nk, const int* d_conn, DBuf& 
 // per-thread bound, and the caller builds on the host.
 bool device_pattern(dfg_ctx ctx_, int n, int nelem, int k, const int* conn, std::vector<int>& rp,
                     std::vector<int>& ci) {
-  if ((long long)n * kPatCap > INT32_MAX) return false;  // int offsets
   const long long nk = (long long)nelem * k;
+  if ((long long)n * kPatCap > INT32_MAX || nk > INT32_MAX) return false;  // int offsets and incidence ids
   DBuf dconn, ptr, inc, flag, rowcnt, rowptr, colind, bsum;
   upload(ctx_, dconn, conn, (size_t)nk, 16);
   REQUIRE(build_incidence(ctx_, n, nk, dconn.as<int>(), ptr, inc, flag) == 0, DFG_INVALID_ARGUMENT,
