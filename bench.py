@@ -48,6 +48,7 @@ CONFIGS = {
     "serve3d": dict(kind="serve", dim=3, nreq=500, seed=5, rate=30.0, budget=120 * 10**9),
     "solid2d_1000x500": dict(kind="solid2d", nx=1000, ny=500),
     "poisson2d_128": dict(kind="poisson2d", n=128),
+    "poisson2d_1000": dict(kind="poisson2d", n=1000),
     "solid3d_96": dict(kind="solid3d", n=96),
     "solid3d_48": dict(kind="solid3d", n=48),
     "solid2d_200x100": dict(kind="solid2d", nx=200, ny=100),
