@@ -399,6 +399,8 @@ def compose_line(args, world, p, results, prof, e2e, head):
         ms, by = prof[arm]
         return {"value": round(steps * world / (r["total_ms"] / 1e3), 4), "unit": "solves/s",
                 "p50_ms": round(_pct(r["lat"], 0.5), 3), "p99_ms": round(_pct(r["lat"], 0.99), 3),
+                "dof_iterations_per_s": round(sum(p.ndof * (it + 1) for it in r["iters"]) * world
+                                              / (r["total_ms"] / 1e3), 1),
                 "iterations": r["iters"][-1], "true_rel_residual": r["true_rel"],
                 "kernels_ms": {k: round(v, 4) for k, v in ms.items()},
                 "spmv_roofline": roof(ms, by, "spmv"), "gpu_launches": int(r["launches"])}
