@@ -532,3 +532,22 @@ def mesh_problem(kind: int, coords: np.ndarray, conn: np.ndarray, seed: int = 0,
         raise ValueError("mesh_problem covers the Poisson and solid kinds")
     coef = _lognormal(rng, conn.shape[0], coef_sigma) if coef_sigma > 0 else None
     return Problem(kind, coords, conn, prm, bc, coef=coef, tol=tol, name=name)
+
+
+def delaunay_mesh(npoints: int, dim: int, seed: int = 0):
+    """An unstructured P1 mesh: the Delaunay triangulation (dim 2) or
+    tetrahedralisation (dim 3) of seeded random points in the unit square or
+    cube plus its corners, elements oriented positively, nodes in the random
+    order they were drawn (irregular valences and bandwidth).  Needs scipy."""
+    from scipy.spatial import Delaunay
+    rng = np.random.default_rng(seed)
+    corners = np.array(list(itertools.product([0.0, 1.0], repeat=dim)))
+    pts = np.vstack([corners, rng.random((npoints, dim))])
+    conn = Delaunay(pts).simplices.astype(np.int32)
+    # orientation: positive area / volume
+    v = pts[conn[:, 1:]] - pts[conn[:, :1]]
+    det = np.linalg.det(v)
+    flip = det < 0
+    conn[flip, 0], conn[flip, 1] = conn[flip, 1].copy(), conn[flip, 0].copy()
+    keep = np.abs(det) > 1e-12  # drop slivers of zero measure
+    return pts, np.ascontiguousarray(conn[keep])

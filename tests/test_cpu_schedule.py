@@ -162,3 +162,15 @@ def test_sweep_schedule_on_fill_pattern(emul, oracle_lib, lev, range_rows):
                            _p(info)) == 0
     ref = oracle_lib.precond(n, b, rp, ci, di, out["fdiag"], out["foffd"], rhs)
     np.testing.assert_allclose(z, ref, rtol=1e-11, atol=1e-12 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("dim,lev", [(2, 1), (2, 2), (2, -1), (3, 1), (3, 2)])
+def test_library_fill_pattern_on_unstructured_meshes(emul, oracle_lib, dim, lev):
+    """Delaunay meshes in random node order (irregular valences and fill)."""
+    pytest.importorskip("scipy")
+    from delfem_gb300 import meshgen as mg
+    co, cn = mg.delaunay_mesh(400 if dim == 2 else 150, dim, seed=dim * 10 + lev)
+    rp, ci = oracle_lib.pattern(co.shape[0], cn)
+    a = _lib_ilu_pattern(emul, rp, ci, lev)
+    b = oracle_lib.ilu_pattern(rp, ci, lev)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])

@@ -140,3 +140,15 @@ def test_failed_set_mesh_keeps_previous_mesh(gpu_ctx, oracle_lib):
         assert np.array_equal(bits(gd), bits(diag)) and np.array_equal(bits(go), bits(offd))
     finally:
         ls.close()
+
+
+@pytest.mark.parametrize("dim,kind", [(2, "poisson2d"), (2, "solid2d"), (3, "poisson3d"), (3, "solid3d")])
+def test_device_build_on_unstructured_meshes(gpu_ctx, oracle_lib, dim, kind):
+    """Delaunay meshes with nodes in random order: irregular valences and
+    incidence counts for the device pattern and gather-map build."""
+    pytest.importorskip("scipy")
+    from delfem_gb300 import meshgen as mg
+    co, cn = mg.delaunay_mesh(6000 if dim == 2 else 2500, dim, seed=57 + dim)
+    k = {"poisson2d": mg.POISSON2D, "solid2d": mg.SOLID2D, "poisson3d": mg.POISSON3D, "solid3d": mg.SOLID3D}[kind]
+    p = mg.mesh_problem(k, co, cn, seed=8, coef_sigma=0.5)
+    _check_assembly(gpu_ctx, oracle_lib, p)
