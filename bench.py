@@ -233,6 +233,8 @@ def run_gpu(args, rank, world, local):
     p = make_problem(args.config)
     ctx = L.Context(local)
     s = FESolve(ctx, p, fill_level=args.fill_level)
+    sched = {1: "ranged", 2: "level-scheduled"}
+    sweeps = dict(zip(("forward", "backward"), (sched[k] for k in s.prec.GetSweepMode())))
     stream = ctx.stream
 
     def ev():
@@ -338,6 +340,7 @@ def run_gpu(args, rank, world, local):
     out = None
     if rank == 0:
         out = compose_line(args, world, p, results, prof, e2e, head)
+        out["config"]["sweep_schedule"] = sweeps
     s.close()
     ctx.close()
     if world > 1:

@@ -29,6 +29,7 @@ SOURCES = {
     "k_sweep.cu": [],
     "k_solve.cu": [],
     "k_bicg.cu": [],
+    "k_level.cu": [],
     "k_pattern.cu": [],
     "k_assemble.cu": ["-fmad=false"],
     "k_ilu.cu": ["-fmad=false"],

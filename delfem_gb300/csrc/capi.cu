@@ -920,6 +920,7 @@ void setup_sweep_plan(dfg_ctx ctx_, SweepDev& S) {
 }
 
 void pack_sweep(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, bool fp32) {
+  if (S.levels) return;  // the level-scheduled sweep reads the factor itself
   PackArgs a{};
   a.nsteps = S.plan.nsteps;
   a.rec = fp32 ? S.rec32.as<unsigned char>() : S.rec64.as<unsigned char>();
@@ -934,15 +935,48 @@ void pack_sweep(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, bool fp32) {
 }
 
 struct SweepLaunch {
+  bool forward = true, fp32 = false;
+  int b = 1;
+  // ranged
   SweepArgs args;
-  int grid;
-  size_t smem;
+  int grid = 0;
+  size_t smem = 0;
+  // level-scheduled
+  bool levels = false;
+  const Levels* lev = nullptr;
+  LevelSweepArgs la{};
 };
+
+// The factor's block pattern: the system's for ILU(0), the preconditioner's
+// own when fill-in changed it.
+struct FactorPattern {
+  const int *rowptr, *colind, *diaind;        // host
+  const int *d_rowptr, *d_colind, *d_diaind;  // device
+};
+FactorPattern factor_pattern(dfg_precond pr) {
+  if (pr->own_pattern)
+    return {pr->h_rowptr.data(), pr->h_colind.data(), pr->h_diaind.data(),
+            pr->rowptr.as<int>(), pr->colind.as<int>(), pr->diaind.as<int>()};
+  const dfg_system s = pr->sys;
+  return {s->h_rowptr.data(), s->h_colind.data(), s->h_diaind.data(),
+          s->rowptr.as<int>(), s->colind.as<int>(), s->diaind.as<int>()};
+}
 
 SweepLaunch sweep_launch(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, bool fp32, const void* in, void* out,
                          int* ticket, const int* done) {
   const int elem = fp32 ? 4 : 8;
   SweepLaunch L{};
+  L.forward = S.forward;
+  L.fp32 = fp32;
+  L.b = pr->b;
+  if (S.levels) {
+    const FactorPattern F = factor_pattern(pr);
+    L.levels = true;
+    L.lev = &S.lev;
+    L.la = LevelSweepArgs{S.lev_rows.as<int>(), F.d_rowptr, F.d_colind, F.d_diaind,
+                          fp32 ? pr->fdiag32.p : pr->fdiag.p, fp32 ? pr->foffd32.p : pr->foffd.p, in, out, done};
+    return L;
+  }
   SweepArgs& a = L.args;
   a.rec = fp32 ? S.rec32.as<unsigned char>() : S.rec64.as<unsigned char>();
   a.rec_off = fp32 ? S.rec_off32.as<long long>() : S.rec_off64.as<long long>();
@@ -971,79 +1005,144 @@ SweepLaunch sweep_launch(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, bool fp32, c
   return L;
 }
 
-void run_sweep(dfg_ctx ctx_, bool forward, int b, bool fp32, const SweepLaunch& L) {
-  CK(launch_sweep(forward, fp32, b, L.args, L.grid, L.smem, ctx_->stream));
-  launched(ctx_);
+// Launches one sweep on stream st (no error check and no launch count, so
+// that it can be captured into a graph); the ranged kernel or one launch per
+// level.
+cudaError_t enqueue_sweep(const SweepLaunch& L, cudaStream_t st) {
+  if (!L.levels) return launch_sweep(L.forward, L.fp32, L.b, L.args, L.grid, L.smem, st);
+  const Levels& V = *L.lev;
+  for (size_t l = 0; l + 1 < V.ptr.size(); ++l) {
+    const cudaError_t e = launch_sweep_level(L.forward, L.fp32, L.b, L.la, V.ptr[l], V.ptr[l + 1] - V.ptr[l], st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+long long launches_of(const SweepLaunch& L) { return L.levels ? (long long)L.lev->ptr.size() - 1 : 1; }
+
+void run_sweep(dfg_ctx ctx_, const SweepLaunch& L) {
+  CK(enqueue_sweep(L, ctx_->stream));
+  launched(ctx_, launches_of(L));
 }
 
-// The factor's block pattern: the system's for ILU(0), the preconditioner's
-// own when fill-in changed it.
-struct FactorPattern {
-  const int *rowptr, *colind, *diaind;        // host
-  const int *d_rowptr, *d_colind, *d_diaind;  // device
+struct GraphHolder {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ~GraphHolder() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+  }
 };
-FactorPattern factor_pattern(dfg_precond pr) {
-  if (pr->own_pattern)
-    return {pr->h_rowptr.data(), pr->h_colind.data(), pr->h_diaind.data(),
-            pr->rowptr.as<int>(), pr->colind.as<int>(), pr->diaind.as<int>()};
-  const dfg_system s = pr->sys;
-  return {s->h_rowptr.data(), s->h_colind.data(), s->h_diaind.data(),
-          s->rowptr.as<int>(), s->colind.as<int>(), s->diaind.as<int>()};
-}
 
-// Schedule choice: the cost model keeps a few candidate range sizes, the
-// fullest-step plan joins them, and each is timed on the device with one FP32
-// sweep of the real structure (values do not change the timing); the fastest
-// wins.
+// Schedule choice.  Ranged: the cost model keeps a few candidate range sizes
+// and the fullest-step plan joins them.  Level-scheduled: one launch per
+// dependency level.  Each candidate is timed on the device as one FP32 sweep
+// of the real structure (values do not change the timing; the level launches
+// as a graph, as the solvers replay them) and the fastest wins.  The
+// preconditioner's sweep mode can restrict the choice to one kind.
 void setup_sweep(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, const dfg_system sys, bool forward) {
   const FactorPattern F = factor_pattern(pr);
-  std::vector<SweepPlan> cands = candidate_sweep_plans(sys->n, sys->b, F.rowptr, F.colind, F.diaind, forward, 32, 4);
-  // and the fullest-step plan (ranges of up to 32 grid lines), if it differs
-  SweepPlan full = fullest_sweep_plan(sys->n, sys->b, F.rowptr, F.colind, F.diaind, forward, 32);
-  bool seen = false;
-  for (const SweepPlan& c : cands) seen |= (c.nranges == full.nranges && c.nsteps == full.nsteps);
-  if (!seen) cands.push_back(std::move(full));
-  size_t best = 0;
-  if (cands.size() > 1) {
-    const long long m = (long long)sys->n * sys->b;
-    DBuf vin, vout;
-    dalloc(ctx_, vin, (size_t)m * 4 + 64);
-    dalloc(ctx_, vout, (size_t)m * 4 + 64);
-    CK(cudaMemsetAsync(vin.p, 0, vin.bytes, ctx_->stream));
-    Scratch sc = scratch_of(ctx_);
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0));
-    CK(cudaEventCreate(&e1));
-    float best_ms = 1e30f;
-    for (size_t c = 0; c < cands.size(); ++c) {
-      SweepDev T;
-      T.plan = std::move(cands[c]);
-      build_records(ctx_, T, 4, T.rec32, T.rec_off32, T.rec_total32, T.max_rec32);
-      CK(cudaMemsetAsync(T.rec32.p, 0, T.rec32.bytes, ctx_->stream));  // factor values not packed: zeros
-      upload(ctx_, T.range_steps, T.plan.range_steps.data(), T.plan.range_steps.size());
-      SweepLaunch L = sweep_launch(ctx_, pr, T, true, vin.p, vout.p, sc.tickets + 2, nullptr);
-      float ms_min = 1e30f;
-      for (int rep = 0; rep < 2; ++rep) {
-        CK(fill_sentinel(m, vout.p, true, ctx_->stream));
-        CK(cudaMemsetAsync(sc.tickets + 2, 0, sizeof(int), ctx_->stream));
-        CK(cudaEventRecord(e0, ctx_->stream));
-        CK(launch_sweep(forward, true, sys->b, L.args, L.grid, L.smem, ctx_->stream));
-        CK(cudaEventRecord(e1, ctx_->stream));
-        CK(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, e0, e1));
-        ms_min = std::min(ms_min, ms);
-      }
-      launched(ctx_, 4);
-      if (ms_min < best_ms) { best_ms = ms_min; best = c; }
-      cands[c] = std::move(T.plan);
+  const int mode = pr->sweep_mode;
+  const long long m = (long long)sys->n * sys->b;
+  S.forward = forward;
+  S.levels = false;
+  DBuf vin, vout;
+  dalloc(ctx_, vin, (size_t)m * 4 + 64);
+  dalloc(ctx_, vout, (size_t)m * 4 + 64);
+  CK(cudaMemsetAsync(vin.p, 0, vin.bytes, ctx_->stream));
+  Scratch sc = scratch_of(ctx_);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  struct EventPair {
+    cudaEvent_t a, b;
+    ~EventPair() { cudaEventDestroy(a); cudaEventDestroy(b); }
+  } ev{e0, e1};
+  auto elapsed = [&](auto&& run) {
+    float best = 1e30f;
+    for (int rep = 0; rep < 2; ++rep) {
+      CK(cudaEventRecord(e0, ctx_->stream));
+      run();
+      CK(cudaEventRecord(e1, ctx_->stream));
+      CK(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      best = std::min(best, ms);
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (read_err(ctx_) != 0) {
-      CK(cudaMemsetAsync(ctx_->err_word.p, 0, sizeof(int), ctx_->stream));
-      set_err(ctx_, "a triangular-sweep wait timed out while choosing the schedule");
-      throw Fail{DFG_TIMEOUT};
+    return best;
+  };
+  // ranged candidates
+  std::vector<SweepPlan> cands;
+  size_t best = 0;
+  float best_ms = 1e30f;
+  if (mode != 2) {
+    cands = candidate_sweep_plans(sys->n, sys->b, F.rowptr, F.colind, F.diaind, forward, 32, 4);
+    // and the fullest-step plan (ranges of up to 32 grid lines), if it differs
+    SweepPlan full = fullest_sweep_plan(sys->n, sys->b, F.rowptr, F.colind, F.diaind, forward, 32);
+    bool seen = false;
+    for (const SweepPlan& c : cands) seen |= (c.nranges == full.nranges && c.nsteps == full.nsteps);
+    if (!seen) cands.push_back(std::move(full));
+    if (cands.size() > 1 || mode == 0) {
+      for (size_t c = 0; c < cands.size(); ++c) {
+        SweepDev T;
+        T.forward = forward;
+        T.plan = std::move(cands[c]);
+        build_records(ctx_, T, 4, T.rec32, T.rec_off32, T.rec_total32, T.max_rec32);
+        CK(cudaMemsetAsync(T.rec32.p, 0, T.rec32.bytes, ctx_->stream));  // factor values not packed: zeros
+        upload(ctx_, T.range_steps, T.plan.range_steps.data(), T.plan.range_steps.size());
+        SweepLaunch L = sweep_launch(ctx_, pr, T, true, vin.p, vout.p, sc.tickets + 2, nullptr);
+        const float ms = elapsed([&] {
+          CK(fill_sentinel(m, vout.p, true, ctx_->stream));
+          CK(cudaMemsetAsync(sc.tickets + 2, 0, sizeof(int), ctx_->stream));
+          CK(enqueue_sweep(L, ctx_->stream));
+        });
+        launched(ctx_, 4);
+        if (ms < best_ms) { best_ms = ms; best = c; }
+        cands[c] = std::move(T.plan);
+      }
+      if (read_err(ctx_) != 0) {
+        CK(cudaMemsetAsync(ctx_->err_word.p, 0, sizeof(int), ctx_->stream));
+        set_err(ctx_, "a triangular-sweep wait timed out while choosing the schedule");
+        throw Fail{DFG_TIMEOUT};
+      }
+    }
+  }
+  // level-scheduled candidate
+  if (mode != 1) {
+    Levels V = build_levels(sys->n, F.rowptr, F.colind, F.diaind, forward);
+    DBuf rows;
+    upload(ctx_, rows, V.rows.data(), std::max<size_t>(V.rows.size(), 1));
+    bool take = mode == 2;
+    if (!take) {
+      const size_t bs = (size_t)sys->b * sys->b;
+      DBuf zd, zo;
+      dalloc(ctx_, zd, (size_t)sys->n * bs * 4 + 64);
+      dalloc(ctx_, zo, (size_t)std::max<long long>(pr->nnz, 1) * bs * 4 + 64);
+      CK(cudaMemsetAsync(zd.p, 0, zd.bytes, ctx_->stream));
+      CK(cudaMemsetAsync(zo.p, 0, zo.bytes, ctx_->stream));
+      SweepLaunch L{};
+      L.forward = forward;
+      L.fp32 = true;
+      L.b = sys->b;
+      L.levels = true;
+      L.lev = &V;
+      L.la = LevelSweepArgs{rows.as<int>(), F.d_rowptr, F.d_colind, F.d_diaind, zd.p, zo.p, vin.p, vout.p, nullptr};
+      GraphHolder g;
+      CK(cudaStreamBeginCapture(ctx_->stream, cudaStreamCaptureModeThreadLocal));
+      const cudaError_t ce = enqueue_sweep(L, ctx_->stream);
+      CK(cudaStreamEndCapture(ctx_->stream, &g.graph));
+      CK(ce);
+      CK(cudaGraphInstantiate(&g.exec, g.graph, 0));
+      CK(cudaGraphLaunch(g.exec, ctx_->stream));  // first replay uploads the graph
+      const float ms = elapsed([&] { CK(cudaGraphLaunch(g.exec, ctx_->stream)); });
+      launched(ctx_, 3 * launches_of(L));
+      take = ms < best_ms;
+    }
+    if (take) {
+      S.levels = true;
+      S.lev = std::move(V);
+      S.lev_rows = std::move(rows);
+      S.plan = SweepPlan{};
+      return;
     }
   }
   S.plan = std::move(cands[best]);
@@ -1076,6 +1175,27 @@ extern "C" int dfg_precond_set_fill_level(dfg_precond prec, int lev) {
     return DFG_INVALID_ARGUMENT;
   }
   prec->lev = lev;
+  return DFG_OK;
+}
+
+extern "C" int dfg_precond_set_sweep_mode(dfg_precond prec, int mode) {
+  if (!prec) return DFG_INVALID_ARGUMENT;
+  if (mode < 0 || mode > 2) {
+    prec->ctx->last_error = "sweep mode must be 0 (timed choice), 1 (ranged) or 2 (level-scheduled)";
+    return DFG_INVALID_ARGUMENT;
+  }
+  prec->sweep_mode = mode;
+  return DFG_OK;
+}
+
+extern "C" int dfg_precond_get_sweep_mode(dfg_precond prec, int* fwd, int* bwd) {
+  if (!prec) return DFG_INVALID_ARGUMENT;
+  if (!prec->symbolic) {
+    prec->ctx->last_error = "dfg_precond_set_linear_system must come first";
+    return DFG_NOT_READY;
+  }
+  if (fwd) *fwd = prec->fwd.levels ? 2 : 1;
+  if (bwd) *bwd = prec->bwd.levels ? 2 : 1;
   return DFG_OK;
 }
 
@@ -1183,6 +1303,14 @@ void ensure_numeric32(dfg_ctx ctx_, dfg_precond prec) {
   if (prec->numeric32) return;
   pack_sweep(ctx_, prec, prec->fwd, true);
   pack_sweep(ctx_, prec, prec->bwd, true);
+  if (prec->fwd.levels || prec->bwd.levels) {  // the level-scheduled sweeps read the factor in CRS
+    const long long bs = (long long)prec->b * prec->b;
+    dalloc(ctx_, prec->fdiag32, (size_t)prec->n * bs * 4 + 64);
+    dalloc(ctx_, prec->foffd32, (size_t)std::max<long long>(prec->nnz, 1) * bs * 4 + 64);
+    CK(to_fp32((long long)prec->n * bs, prec->fdiag.as<double>(), prec->fdiag32.as<float>(), ctx_->stream));
+    CK(to_fp32(prec->nnz * bs, prec->foffd.as<double>(), prec->foffd32.as<float>(), ctx_->stream));
+    launched(ctx_, 2);
+  }
   prec->numeric32 = true;
 }
 }  // namespace
@@ -1199,10 +1327,10 @@ extern "C" int dfg_precond_solve(dfg_precond prec, dfg_system sys, int iv) {
     CK(cudaMemsetAsync(sc.tickets, 0, 2 * sizeof(int), ctx->stream));
     CK(fill_sentinel(m, prec->ybuf64.p, false, ctx->stream));
     SweepLaunch F = sweep_launch(ctx, prec, prec->fwd, false, v, prec->ybuf64.p, sc.tickets, nullptr);
-    run_sweep(ctx, true, sys->b, false, F);
+    run_sweep(ctx, F);
     CK(fill_sentinel(m, v, false, ctx->stream));
     SweepLaunch B = sweep_launch(ctx, prec, prec->bwd, false, prec->ybuf64.p, v, sc.tickets + 1, nullptr);
-    run_sweep(ctx, false, sys->b, false, B);
+    run_sweep(ctx, B);
     launched(ctx, 2);  // the two sentinel fills
     if (read_err(ctx) != 0) {
       CK(cudaMemsetAsync(ctx->err_word.p, 0, sizeof(int), ctx->stream));
@@ -1328,14 +1456,16 @@ static int solve_pcg_f64vec(dfg_system sys, dfg_precond prec, bool fp32z, bool t
     const double tol = *conv_ratio;
     // prologue (solver_ls_iter.cpp:106-128)
     CK(pcg_init(v, st, red, tol, maxit, sc.tickets, fp32z, ctx->stream));
-    run_sweep(ctx, true, sys->b, fp32z, F);
-    run_sweep(ctx, false, sys->b, fp32z, B);
+    run_sweep(ctx, F);
+    run_sweep(ctx, B);
     CK(pcg_after_precond0(v, st, red, fp32z, ctx->stream));
     launched(ctx, 2);
     PcgState h{};
     read_state(ctx, st, h);
     // iterations: a graph of `chunk` iterations, replayed until done
-    const int chunk = m < 200000 ? 8 : 32;
+    const long long per_it = 4 + launches_of(F) + launches_of(B);
+    // level-scheduled sweeps put one graph node per level: fewer iterations per graph
+    const int chunk = std::max(2, std::min(m < 200000 ? 8 : 32, (int)(4096 / per_it)));
     ensure_sell(ctx, sys, false);
     const MatView A = view64(sys);
     Chunk g;
@@ -1343,8 +1473,8 @@ static int solve_pcg_f64vec(dfg_system sys, dfg_precond prec, bool fp32z, bool t
     for (int c = 0; c < chunk; ++c) {
       pcg_spmv_pap(A, v, st, red, ctx->stream);
       pcg_update_rx(v, st, red, sc.tickets, fp32z, ctx->stream);
-      launch_sweep(true, fp32z, sys->b, F.args, F.grid, F.smem, ctx->stream);
-      launch_sweep(false, fp32z, sys->b, B.args, B.grid, B.smem, ctx->stream);
+      enqueue_sweep(F, ctx->stream);
+      enqueue_sweep(B, ctx->stream);
       pcg_rz_beta(v, st, red, fp32z, ctx->stream);
       pcg_update_p(v, st, fp32z, ctx->stream);
     }
@@ -1356,7 +1486,7 @@ static int solve_pcg_f64vec(dfg_system sys, dfg_precond prec, bool fp32z, bool t
     for (;;) {
       while (!h.done) {
         CK(cudaGraphLaunch(g.exec, ctx->stream));
-        launched(ctx, 6LL * chunk);
+        launched(ctx, per_it * chunk);
         read_state(ctx, st, h);
         if (read_err(ctx) != 0) return timeout_status(ctx);
         if (++guard > (long long)maxit / chunk + 64) break;
@@ -1381,8 +1511,8 @@ static int solve_pcg_f64vec(dfg_system sys, dfg_precond prec, bool fp32z, bool t
       }
       // continue from the true residual: finish this iteration and resume
       CK(pcg_replace(v, st, sc.tickets, fp32z, ctx->stream));
-      run_sweep(ctx, true, sys->b, fp32z, F);
-      run_sweep(ctx, false, sys->b, fp32z, B);
+      run_sweep(ctx, F);
+      run_sweep(ctx, B);
       CK(pcg_rz_beta(v, st, red, fp32z, ctx->stream));
       CK(pcg_update_p(v, st, fp32z, ctx->stream));
       launched(ctx, 3);
@@ -1472,18 +1602,19 @@ extern "C" int dfg_solve_pcg_mixed(dfg_system sys, dfg_precond prec, double* con
     // true residual of x = 0 is b; start the recursion from it
     CK(mix_true_residual(A64, v, st, red, ctx->stream));
     CK(mix_replace(v, st, sc.tickets, ctx->stream));
-    run_sweep(ctx, true, sys->b, true, F);
-    run_sweep(ctx, false, sys->b, true, B);
+    run_sweep(ctx, F);
+    run_sweep(ctx, B);
     CK(mix_after_precond0(v, st, red, ctx->stream));
     launched(ctx, 4);
-    const int chunk = m < 200000 ? 8 : 32;
+    const long long per_it = 4 + launches_of(F) + launches_of(B);
+    const int chunk = std::max(2, std::min(m < 200000 ? 8 : 32, (int)(4096 / per_it)));
     Chunk g;
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     for (int c = 0; c < chunk; ++c) {
       mix_spmv_pap(A32, v, st, red, ctx->stream);
       mix_update_rx(v, st, red, sc.tickets, ctx->stream);
-      launch_sweep(true, true, sys->b, F.args, F.grid, F.smem, ctx->stream);
-      launch_sweep(false, true, sys->b, B.args, B.grid, B.smem, ctx->stream);
+      enqueue_sweep(F, ctx->stream);
+      enqueue_sweep(B, ctx->stream);
       mix_rz_beta(v, st, red, ctx->stream);
       mix_update_p(v, st, ctx->stream);
     }
@@ -1496,7 +1627,7 @@ extern "C" int dfg_solve_pcg_mixed(dfg_system sys, dfg_precond prec, double* con
     long long guard = 0;
     for (;;) {
       CK(cudaGraphLaunch(g.exec, ctx->stream));
-      launched(ctx, 6LL * chunk);
+      launched(ctx, per_it * chunk);
       read_state(ctx, st, h);
       if (read_err(ctx) != 0) return timeout_status(ctx);
       if (h.done == 0) {
@@ -1518,8 +1649,8 @@ extern "C" int dfg_solve_pcg_mixed(dfg_system sys, dfg_precond prec, double* con
       // continue the recursion from the true residual: finish this iteration
       // (preconditioner, beta, direction) and resume the graph
       CK(mix_replace(v, st, sc.tickets, ctx->stream));
-      run_sweep(ctx, true, sys->b, true, F);
-      run_sweep(ctx, false, sys->b, true, B);
+      run_sweep(ctx, F);
+      run_sweep(ctx, B);
       CK(mix_rz_beta(v, st, red, ctx->stream));
       CK(mix_update_p(v, st, ctx->stream));
       launched(ctx, 3);
@@ -1575,16 +1706,17 @@ extern "C" int dfg_solve_pbicgstab(dfg_system sys, dfg_precond prec, int mode, d
     if (h.done == 0) {
       ensure_sell(ctx, sys, false);
       const MatView A = view64(sys);
-      const int chunk = m < 200000 ? 4 : 16;
+      const long long per_it = 5 + launches_of(F1) + launches_of(B1) + launches_of(F2) + launches_of(B2);
+      const int chunk = std::max(2, std::min(m < 200000 ? 4 : 16, (int)(4096 / per_it)));
       Chunk g;
       CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
       for (int c = 0; c < chunk; ++c) {
-        launch_sweep(true, false, sys->b, F1.args, F1.grid, F1.smem, ctx->stream);
-        launch_sweep(false, false, sys->b, B1.args, B1.grid, B1.smem, ctx->stream);
+        enqueue_sweep(F1, ctx->stream);
+        enqueue_sweep(B1, ctx->stream);
         bicg_amp(A, v, st, red, ctx->stream);
         bicg_s(v, st, sc.tickets, ctx->stream);
-        launch_sweep(true, false, sys->b, F2.args, F2.grid, F2.smem, ctx->stream);
-        launch_sweep(false, false, sys->b, B2.args, B2.grid, B2.smem, ctx->stream);
+        enqueue_sweep(F2, ctx->stream);
+        enqueue_sweep(B2, ctx->stream);
         bicg_ams(A, v, st, red2, ctx->stream);
         bicg_update(v, st, red2, ctx->stream);
         bicg_p(v, st, sc.tickets, ctx->stream);
@@ -1594,7 +1726,7 @@ extern "C" int dfg_solve_pbicgstab(dfg_system sys, dfg_precond prec, int mode, d
       long long guard = 0;
       while (!h.done) {
         CK(cudaGraphLaunch(g.exec, ctx->stream));
-        launched(ctx, 9LL * chunk);
+        launched(ctx, per_it * chunk);
         CK(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
         if (read_err(ctx) != 0) return timeout_status(ctx);
@@ -1738,11 +1870,11 @@ extern "C" int dfg_profile_kernels(dfg_system sys, dfg_precond prec, int mode, i
     timed(1, [&] {
         CK(fill_sentinel(m, ybuf, fp32z, ctx->stream));
         CK(cudaMemsetAsync(sc.tickets, 0, 2 * sizeof(int), ctx->stream));
-      }, [&] { run_sweep(ctx, true, sys->b, fp32z, F); });
+      }, [&] { run_sweep(ctx, F); });
     timed(2, [&] {
         CK(fill_sentinel(m, zbuf, fp32z, ctx->stream));
         CK(cudaMemsetAsync(sc.tickets, 0, 2 * sizeof(int), ctx->stream));
-      }, [&] { run_sweep(ctx, false, sys->b, fp32z, B); });
+      }, [&] { run_sweep(ctx, B); });
     if (mixed) {
       timed(3, nop, [&] { CK(mix_update_rx(w, st, red, sc.tickets, ctx->stream)); });
       timed(4, nop, [&] { CK(mix_rz_beta(w, st, red, ctx->stream)); });

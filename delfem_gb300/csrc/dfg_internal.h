@@ -147,7 +147,12 @@ struct Ctx;
 struct PcgState;  // device-side solver state (defined in solve.cu)
 
 struct SweepDev {
-  // one packed record buffer per precision
+  bool forward = true;
+  // level-scheduled (one launch per level, k_level.cu) instead of ranged
+  bool levels = false;
+  Levels lev;
+  DBuf lev_rows;
+  // ranged: one packed record buffer per precision
   DBuf rec64, rec32;
   DBuf rec_off64, rec_off32;       // long long per step (+1)
   DBuf step_nent, range_steps;
@@ -217,6 +222,8 @@ struct dfg_precond_s {
   bool own_pattern = false;
   std::vector<int> h_rowptr, h_colind, h_diaind;
   dfg::DBuf rowptr, colind, diaind, a2f;  // a2f: A's CRS slot -> factor slot
+  int sweep_mode = 0;                     // 0 timed choice, 1 ranged, 2 level-scheduled
+  dfg::DBuf fdiag32, foffd32;             // FP32 factor in CRS (level-scheduled FP32 sweeps)
   dfg::DBuf fdiag, foffd;          // factor, reference layout (FP64)
   dfg::Levels lev_fwd;
   dfg::DBuf lev_rows;

@@ -73,4 +73,20 @@ struct PackArgs {
 };
 cudaError_t launch_pack(bool forward, bool fp32, int B, const PackArgs& a, cudaStream_t st);
 
+// Level-scheduled sweep (k_level.cu): the factor in block CRS (values of
+// the sweep's type), rows listed level after level; one launch per level.
+struct LevelSweepArgs {
+  const int* rows;
+  const int* rowptr;
+  const int* colind;
+  const int* diaind;
+  const void* fdiag;   // D^-1 blocks (forward)
+  const void* foffd;   // L | D^-1 U blocks
+  const void* in;
+  void* out;
+  const int* done;     // nonzero: return at once
+};
+cudaError_t launch_sweep_level(bool forward, bool fp32, int b, const LevelSweepArgs& a, int first, int cnt,
+                               cudaStream_t s);
+
 }  // namespace dfg

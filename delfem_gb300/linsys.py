@@ -256,6 +256,17 @@ class PreconditionerILU:
     def SetFillInLevel(self, lev: int):
         check(self.ctx.h, lib().dfg_precond_set_fill_level(self.h, lev), "dfg_precond_set_fill_level")
 
+    def SetSweepMode(self, mode: int):
+        """0: timed choice (default), 1: ranged, 2: level-scheduled sweeps."""
+        check(self.ctx.h, lib().dfg_precond_set_sweep_mode(self.h, mode), "dfg_precond_set_sweep_mode")
+
+    def GetSweepMode(self):
+        """(forward, backward) kinds chosen at the symbolic set-up: 1 ranged, 2 level-scheduled."""
+        f, b = ctypes.c_int(), ctypes.c_int()
+        check(self.ctx.h, lib().dfg_precond_get_sweep_mode(self.h, ctypes.byref(f), ctypes.byref(b)),
+              "dfg_precond_get_sweep_mode")
+        return f.value, b.value
+
     def SetLinearSystem(self, ls: LinearSystemField):
         check(self.ctx.h, lib().dfg_precond_set_linear_system(self.h, ls.h), "dfg_precond_set_linear_system")
         self.ls = ls

@@ -18,7 +18,7 @@ from . import meshgen as mg
 
 
 class FESolve:
-    def __init__(self, ctx: L.Context, p: mg.Problem, fill_level: int = 0):
+    def __init__(self, ctx: L.Context, p: mg.Problem, fill_level: int = 0, sweep_mode: int = 0):
         self.ctx, self.p = ctx, p
         self.ls = L.LinearSystemField(ctx, p.nnode, p.b, conn=p.conn)
         self.ls.set_mesh(p.coords, p.conn)
@@ -31,6 +31,8 @@ class FESolve:
             self.ls.SetLoad(p.load)
         self.prec = L.PreconditionerILU(ctx)
         self.prec.SetFillInLevel(fill_level)
+        if sweep_mode:
+            self.prec.SetSweepMode(sweep_mode)
         self.prec.SetLinearSystem(self.ls)
 
     def assemble(self) -> float:

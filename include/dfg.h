@@ -221,6 +221,16 @@ int dfg_precond_set_fill_level(dfg_precond prec, int lev);
  * (CPreconditioner_ILU::SetLinearSystem, src/ls/preconditioner.cpp:57-211;
  * CMatDiaFrac_BlkCrs(0,A), src/matvec/matdiafrac_blkcrs.cpp:171-225). */
 int dfg_precond_set_linear_system(dfg_precond prec, dfg_system sys);
+/* How the triangular sweeps are scheduled (no counterpart in the reference,
+ * whose substitutions are sequential loops): 0 (default) times both kinds
+ * on the device at the symbolic set-up and keeps the faster per direction;
+ * 1 = ranged (contiguous row ranges pipelined across CTAs, good for the long
+ * thin wavefronts of 2D meshes); 2 = level-scheduled (one launch per
+ * dependency level, good for the wide levels of 3D meshes).  Takes effect at
+ * the next dfg_precond_set_linear_system; results agree to rounding. */
+int dfg_precond_set_sweep_mode(dfg_precond prec, int mode);
+/* The kind chosen per direction after the symbolic set-up (1 or 2). */
+int dfg_precond_get_sweep_mode(dfg_precond prec, int* fwd, int* bwd);
 /* The factor's block pattern after the symbolic set-up: *nnz off-diagonal
  * blocks; rowptr (n+1) and colind (nnz) in the layout of
  * dfg_system_get_pattern, each written when non-NULL. */

@@ -42,3 +42,12 @@ def test_context_creation_fails_cleanly_without_device(built):
     from delfem_gb300 import capi, linsys
     with pytest.raises(capi.DfgError):
         linsys.Context(0)
+
+
+def test_library_has_no_undefined_symbols_of_its_own(built):
+    """A source left out of the build links anyway (shared objects may carry
+    undefined symbols) and fails only at load time; catch it here."""
+    out = subprocess.run(["nm", "-D", "--undefined-only", "-C", built], capture_output=True, text=True,
+                         check=True).stdout
+    ours = [ln for ln in out.splitlines() if "dfg" in ln]
+    assert not ours, ours
