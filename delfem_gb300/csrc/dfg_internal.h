@@ -150,6 +150,7 @@ struct SweepDev {
   bool forward = true;
   // level-scheduled (one launch per level, k_level.cu) instead of ranged
   bool levels = false;
+  float t_ranged = -1.f, t_levels = -1.f;  // set-up timings of the two kinds (ms; -1 = not timed)
   Levels lev;
   DBuf lev_rows;
   // ranged: one packed record buffer per precision

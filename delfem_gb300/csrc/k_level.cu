@@ -14,22 +14,25 @@
 
 namespace dfg {
 
+// One warp per row: lane e takes the row's entries e, e+32, ..., so the
+// dependency and factor loads of a row are issued together; the partial sums
+// meet in a shuffle tree and lane 0 finishes the row.
 template <typename T, int B, bool FWD>
 __global__ void __launch_bounds__(128) k_sweep_level(LevelSweepArgs a, int first, int cnt) {
   if (a.done && *a.done) return;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= cnt) return;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= cnt) return;
   constexpr int BS = B * B;
   const T* __restrict__ in = reinterpret_cast<const T*>(a.in);
   T* out = reinterpret_cast<T*>(a.out);
   const T* __restrict__ fo = reinterpret_cast<const T*>(a.foffd);
-  const int i = a.rows[first + t];
-  T acc[B];
-#pragma unroll
-  for (int d = 0; d < B; ++d) acc[d] = in[(size_t)i * B + d];
+  const int i = a.rows[first + w];
   const int c0 = FWD ? a.rowptr[i] : a.diaind[i];
   const int c1 = FWD ? a.diaind[i] : a.rowptr[i + 1];
-  for (int c = c0; c < c1; ++c) {
+  T part[B];
+#pragma unroll
+  for (int p = 0; p < B; ++p) part[p] = 0;
+  for (int c = c0 + lane; c < c1; c += 32) {
     const int j = a.colind[c];
     const T* blk = fo + (size_t)c * BS;
     T x[B];
@@ -38,8 +41,16 @@ __global__ void __launch_bounds__(128) k_sweep_level(LevelSweepArgs a, int first
 #pragma unroll
     for (int p = 0; p < B; ++p)
 #pragma unroll
-      for (int q = 0; q < B; ++q) acc[p] -= blk[p * B + q] * x[q];
+      for (int q = 0; q < B; ++q) part[p] += blk[p * B + q] * x[q];
   }
+#pragma unroll
+  for (int p = 0; p < B; ++p)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part[p] += __shfl_xor_sync(0xffffffffu, part[p], o);
+  if (lane != 0) return;
+  T acc[B];
+#pragma unroll
+  for (int p = 0; p < B; ++p) acc[p] = in[(size_t)i * B + p] - part[p];
   if constexpr (FWD) {
     const T* dv = reinterpret_cast<const T*>(a.fdiag) + (size_t)i * BS;
 #pragma unroll
@@ -58,7 +69,7 @@ __global__ void __launch_bounds__(128) k_sweep_level(LevelSweepArgs a, int first
 cudaError_t launch_sweep_level(bool forward, bool fp32, int b, const LevelSweepArgs& a, int first, int cnt,
                                cudaStream_t s) {
   if (cnt <= 0) return cudaSuccess;
-  const unsigned grid = (unsigned)((cnt + 127) / 128);
+  const unsigned grid = (unsigned)((cnt + 3) / 4);  // four rows (warps) per block
 #define DFG_LVL(T, B)                                                                  \
   (forward ? (k_sweep_level<T, B, true><<<grid, 128, 0, s>>>(a, first, cnt), 0)       \
            : (k_sweep_level<T, B, false><<<grid, 128, 0, s>>>(a, first, cnt), 0))

@@ -267,6 +267,14 @@ class PreconditionerILU:
               "dfg_precond_get_sweep_mode")
         return f.value, b.value
 
+    def GetSweepTiming(self):
+        """Set-up timings (ms per FP32 sweep) behind the schedule choice:
+        forward ranged, forward level-scheduled, backward ranged, backward
+        level-scheduled (-1: not timed)."""
+        ms = np.zeros(4, dtype=np.float32)
+        check(self.ctx.h, lib().dfg_precond_get_sweep_timing(self.h, _p(ms)), "dfg_precond_get_sweep_timing")
+        return [float(x) for x in ms]
+
     def SetLinearSystem(self, ls: LinearSystemField):
         check(self.ctx.h, lib().dfg_precond_set_linear_system(self.h, ls.h), "dfg_precond_set_linear_system")
         self.ls = ls

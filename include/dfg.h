@@ -231,6 +231,10 @@ int dfg_precond_set_linear_system(dfg_precond prec, dfg_system sys);
 int dfg_precond_set_sweep_mode(dfg_precond prec, int mode);
 /* The kind chosen per direction after the symbolic set-up (1 or 2). */
 int dfg_precond_get_sweep_mode(dfg_precond prec, int* fwd, int* bwd);
+/* The set-up's timings behind that choice, ms per FP32 sweep: ms[0..3] =
+ * forward ranged, forward level-scheduled, backward ranged, backward
+ * level-scheduled (-1 where a kind was not timed). */
+int dfg_precond_get_sweep_timing(dfg_precond prec, float* ms);
 /* The factor's block pattern after the symbolic set-up: *nnz off-diagonal
  * blocks; rowptr (n+1) and colind (nnz) in the layout of
  * dfg_system_get_pattern, each written when non-NULL. */
