@@ -1114,7 +1114,7 @@ void setup_sweep(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, const dfg_system sys
     Levels V = build_levels(sys->n, F.rowptr, F.colind, F.diaind, forward);
     DBuf rows;
     upload(ctx_, rows, V.rows.data(), std::max<size_t>(V.rows.size(), 1));
-    bool take = mode == 2;
+    bool take = mode == 2 || V.ptr.size() <= 1;  // no rows: nothing to launch or time
     if (!take) {
       const size_t bs = (size_t)sys->b * sys->b;
       DBuf zd, zo;
