@@ -1,5 +1,5 @@
 // k_level.cu -- level-scheduled triangular sweeps: one launch per dependency
-// level, one thread per row of the level.
+// level, one warp per row of the level.
 //
 // CMatDiaFrac_BlkCrs::ForwardSubstitution / BackwardSubstitution
 // (src/matvec/matdiafrac_blkcrs.cpp:332-669) over the factor's block CRS,
