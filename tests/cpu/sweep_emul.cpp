@@ -9,7 +9,10 @@
 //   * a global reference points at a row that an earlier range (or an older
 //     step of the same range) has finished -- so ranges claimed in order
 //     can never wait on a range that has not started (no deadlock).
+// It also executes the level schedule of the level-scheduled sweep
+// (emul_level_sweep) with the same checks in their level form.
 // Built by tests/test_cpu_schedule.py with g++; never part of libdfg.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -220,4 +223,79 @@ extern "C" long long emul_ilu_pattern(int n, const int* rowptr, const int* colin
     if (!ci.empty()) std::memcpy(colind_f, ci.data(), sizeof(int) * ci.size());
   }
   return (long long)ci.size();
+}
+
+// The level schedule of the level-scheduled sweep (sched.cpp build_levels),
+// checked and executed level by level: rows form a permutation grouped by
+// level, every dependency of a row lies in an earlier level and a row's level
+// is one above its deepest dependency (the longest-path levels, so no launch
+// is wasted).  Each row is computed as k_sweep_level computes it: lane l of
+// the row's warp sums entries l, l+32, ... in order, the 32 partials meet in
+// the xor-butterfly, and lane 0 finishes the row.  Rows of later levels are
+// NaN until written, so a read ahead of the schedule shows in the result.
+// info[0] = number of levels, info[1] = widest level, info[2] = error code.
+extern "C" int emul_level_sweep(int n, int b, const int* rowptr, const int* colind, int forward, const double* fdiag,
+                                const double* foffd, const double* in, double* out, long long* info) {
+  std::vector<int> diaind(n);
+  for (int i = 0; i < n; ++i) {
+    int d = rowptr[i + 1];
+    for (int c = rowptr[i]; c < rowptr[i + 1]; ++c)
+      if (colind[c] > i) { d = c; break; }
+    diaind[i] = d;
+  }
+  const Levels V = build_levels(n, rowptr, colind, diaind.data(), forward != 0);
+  const int nl = (int)V.ptr.size() - 1;
+  info[0] = nl;
+  info[1] = 0;
+  info[2] = 0;
+  auto fail = [&](int code) { info[2] = code; return code; };
+  if (nl < 0 || V.ptr[0] != 0 || V.ptr[nl] != n || (int)V.rows.size() != n) return fail(1);
+  std::vector<int> seen(n, 0);
+  for (int l = 0; l < nl; ++l) {
+    if (V.ptr[l + 1] <= V.ptr[l]) return fail(2);  // an empty level is a wasted launch
+    info[1] = std::max<long long>(info[1], V.ptr[l + 1] - V.ptr[l]);
+    for (int k = V.ptr[l]; k < V.ptr[l + 1]; ++k) {
+      const int row = V.rows[k];
+      if (row < 0 || row >= n || seen[row]++ || V.level[row] != l) return fail(3);
+    }
+  }
+  const int bs = b * b;
+  for (int i = 0; i < n * b; ++i) out[i] = NAN;
+  for (int l = 0; l < nl; ++l) {
+    for (int k = V.ptr[l]; k < V.ptr[l + 1]; ++k) {
+      const int i = V.rows[k];
+      const int c0 = forward ? rowptr[i] : diaind[i];
+      const int c1 = forward ? diaind[i] : rowptr[i + 1];
+      int deepest = -1;
+      for (int c = c0; c < c1; ++c) deepest = std::max(deepest, V.level[colind[c]]);
+      if (deepest >= l || deepest + 1 != l) return fail(4);
+      double part[32][3] = {};
+      for (int lane = 0; lane < 32; ++lane)
+        for (int c = c0 + lane; c < c1; c += 32) {
+          const double* blk = foffd + (size_t)c * bs;
+          for (int p = 0; p < b; ++p)
+            for (int q = 0; q < b; ++q) part[lane][p] += blk[p * b + q] * out[(size_t)colind[c] * b + q];
+        }
+      for (int o = 16; o > 0; o >>= 1) {
+        double nxt[32][3];
+        for (int lane = 0; lane < 32; ++lane)
+          for (int p = 0; p < b; ++p) nxt[lane][p] = part[lane][p] + part[lane ^ o][p];
+        std::memcpy(part, nxt, sizeof(part));
+      }
+      double acc[3];
+      for (int p = 0; p < b; ++p) acc[p] = in[(size_t)i * b + p] - part[0][p];
+      for (int p = 0; p < b; ++p) {
+        double y = acc[p];
+        if (forward) {
+          const double* dv = fdiag + (size_t)i * bs;
+          y = dv[p * b] * acc[0];
+          for (int q = 1; q < b; ++q) y += dv[p * b + q] * acc[q];
+        }
+        out[(size_t)i * b + p] = y;
+      }
+    }
+  }
+  for (int i = 0; i < n * b; ++i)
+    if (std::isnan(out[i])) return fail(5);
+  return 0;
 }

@@ -2,7 +2,9 @@
 sequential CPU emulator of the GPU kernel's dependency decoding
 (tests/cpu/sweep_emul.cpp): complete coverage, valid ring references, no
 wait on a later range, and forward/backward results equal to the oracle's
-substitutions up to summation order."""
+substitutions up to summation order.  The level schedule of the
+level-scheduled sweep (build_levels) is executed the same way, in the level
+kernel's summation order."""
 import ctypes
 import os
 import subprocess
@@ -174,3 +176,70 @@ def test_library_fill_pattern_on_unstructured_meshes(emul, oracle_lib, dim, lev)
     a = _lib_ilu_pattern(emul, rp, ci, lev)
     b = oracle_lib.ilu_pattern(rp, ci, lev)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def _level_sweep(emul, n, b, rowptr, colind, forward, fdiag, foffd, vin):
+    P = ctypes.c_void_p
+    emul.emul_level_sweep.argtypes = [ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, P, P, P, P, P]
+    out = np.zeros(max(n * b, 1))
+    info = np.zeros(4, dtype=np.int64)
+    rc = emul.emul_level_sweep(n, b, _p(rowptr), _p(colind if colind.size else np.zeros(1, np.int32)), forward,
+                               _p(fdiag if fdiag.size else np.zeros(1)), _p(foffd if foffd.size else np.zeros(1)),
+                               _p(vin if vin.size else np.zeros(1)), _p(out), _p(info))
+    return rc, out[:n * b], info
+
+
+@pytest.mark.parametrize("idx", range(4))
+@pytest.mark.parametrize("lev", [0, 1])
+def test_level_schedule(emul, oracle_lib, idx, lev):
+    """The level schedule (sched.cpp build_levels) on ILU(0) and ILU(1)
+    factors: a permutation grouped by level, dependencies in earlier levels,
+    longest-path levels, and forward then backward substitution in the level
+    kernel's summation order equal to the oracle's preconditioner apply."""
+    p = _problems()[idx]
+    out = oracle_lib.solve(p, stop_after_ilu=True, fill_level=lev)
+    n, b = out["n"], out["b"]
+    rp, ci = out["rowptr_f"], out["colind_f"]
+    rhs = np.random.default_rng(40 + idx).standard_normal(n * b)
+    rc, y, info_f = _level_sweep(emul, n, b, rp, ci, 1, out["fdiag"], out["foffd"], rhs)
+    assert rc == 0, f"forward level schedule check failed with code {rc}"
+    rc, z, info_b = _level_sweep(emul, n, b, rp, ci, 0, out["fdiag"], out["foffd"], y)
+    assert rc == 0, f"backward level schedule check failed with code {rc}"
+    assert 1 <= info_f[0] <= n and 1 <= info_b[0] <= n
+    ref = oracle_lib.precond(n, b, rp, ci, out["diaind_f"], out["fdiag"], out["foffd"], rhs)
+    np.testing.assert_allclose(z, ref, rtol=1e-11, atol=1e-12 * np.abs(ref).max())
+
+
+def test_level_schedule_shapes(emul):
+    """Hand-made patterns: a chain (one row per level), a diagonal matrix
+    (one level), a long row (more than 32 dependencies, so several entries per
+    lane) and an empty system (no level)."""
+    def run(rows, n, b=1):
+        rp = np.zeros(n + 1, np.int32)
+        rp[1:] = np.cumsum([len(r) for r in rows])
+        ci = np.array([c for r in rows for c in sorted(r)], dtype=np.int32)
+        rng = np.random.default_rng(n)
+        fdiag = np.tile(np.eye(b).ravel(), n) * 0.5
+        foffd = rng.standard_normal(ci.size * b * b) * 0.01
+        vin = rng.standard_normal(n * b)
+        rc, y, info = _level_sweep(emul, n, b, rp, ci, 1, fdiag, foffd, vin)
+        assert rc == 0
+        # plain forward substitution (unit lower factor, then the diagonal inverse)
+        yr = np.zeros(n * b)
+        for i in range(n):
+            acc = vin[i * b:(i + 1) * b].copy()
+            for k in range(rp[i], rp[i + 1]):
+                j = ci[k]
+                if j < i:
+                    acc -= foffd[k * b * b:(k + 1) * b * b].reshape(b, b) @ yr[j * b:(j + 1) * b]
+            yr[i * b:(i + 1) * b] = fdiag[i * b * b:(i + 1) * b * b].reshape(b, b) @ acc
+        np.testing.assert_allclose(y, yr, rtol=1e-13, atol=1e-14)
+        return info
+    n = 50
+    chain = [[i - 1, i + 1] if 0 < i < n - 1 else ([1] if i == 0 else [n - 2]) for i in range(n)]
+    assert run(chain, n)[0] == n
+    assert run([[] for _ in range(n)], n)[:2].tolist() == [1, n]
+    wide = [[j for j in range(100) if j != i] if i == 99 else ([99] if i < 99 else []) for i in range(101)]
+    info = run(wide, 101, b=3)
+    assert info[0] == 2 and info[1] == 100
+    assert run([], 0)[0] == 0
