@@ -128,7 +128,10 @@ int dfg_initialize_marge(dfg_system sys);
 /* Fem::Eqn::AddLinSys_Poisson (src/femeqn/eqn_poisson.cpp:428-470): P1 triangle
  * (:49-125) or P1 tetrahedron (:249-323) according to the mesh. */
 int dfg_assemble_poisson(dfg_system sys, double alpha, double source);
-/* Fem::Eqn::AddLinSys_Diffusion (src/femeqn/eqn_diffusion.cpp:348-400), P1 triangle (:240-347). */
+/* Fem::Eqn::AddLinSys_Diffusion (src/femeqn/eqn_diffusion.cpp:348-400), P1 triangle (:240-347).
+ * The CLinearSystem_Field overload takes triangles only; a tetrahedral mesh is
+ * DFG_INVALID_ARGUMENT, where the reference prints "NotImplimented" and asserts.  (The 3D
+ * P1 routine at :662-768 serves the CLinearSystem_SaveDiaM_Newmark overload.) */
 int dfg_assemble_diffusion(dfg_system sys, double dt, double gamma,
                            double rho, double alpha, double source);
 /* Fem::Eqn::AddLinSys_LinearSolid2D_Static (src/femeqn/eqn_linear_solid2d.cpp:215-266),

@@ -191,6 +191,44 @@ def test_bad_pattern_rejected(gpu_ctx):
     assert e.value.status == capi.DFG_INVALID_ARGUMENT
 
 
+def test_equation_mesh_mismatch_rejected(gpu_ctx, oracle_lib):
+    """An equation on a mesh or block length it does not take is rejected
+    before anything is written, and the system stays usable: diffusion on
+    tetrahedra (the CLinearSystem_Field overload of AddLinSys_Diffusion takes
+    triangles only, src/femeqn/eqn_diffusion.cpp:348-398, and reports
+    anything else as not implemented), 2D elasticity on a scalar system, 3D
+    elasticity on a triangle mesh."""
+    from delfem_gb300 import capi, linsys as L, meshgen as mg
+    p = mg.poisson3d_cube(4, seed=81)
+    ls = L.LinearSystemField(gpu_ctx, p.nnode, 1, conn=p.conn)
+    try:
+        ls.set_mesh(p.coords, p.conn)
+        ls.InitializeMarge()
+        for call in (lambda: L.AddLinSys_Diffusion(0.1, 0.5, ls, 1.0, 1.0, 1.0),
+                     lambda: L.AddLinSys_LinearSolid2D_Static(ls, 1.0, 1.0, 0.0, 0.0, 0.0)):
+            with pytest.raises(capi.DfgError) as e:
+                call()
+            assert e.value.status == capi.DFG_INVALID_ARGUMENT
+        L.AddLinSys_Poisson(ls, float(p.params[0]), float(p.params[1]))
+        rp, ci = oracle_lib.pattern(p.nnode, p.conn)
+        diag, offd, res = oracle_lib.assemble(p, rp, ci)
+        gd, go = ls.GetMatrix()
+        assert np.array_equal(bits(gd), bits(diag)) and np.array_equal(bits(go), bits(offd))
+        assert np.array_equal(bits(ls.GetResidual()), bits(res))
+    finally:
+        ls.close()
+    q = mg.solid2d_cantilever(6, 3, seed=82)
+    ls = L.LinearSystemField(gpu_ctx, q.nnode, 3, conn=q.conn)
+    try:
+        ls.set_mesh(q.coords, q.conn)
+        ls.InitializeMarge()
+        with pytest.raises(capi.DfgError) as e:
+            L.AddLinSys_LinearSolid3D_Static(ls, 1.0, 1.0, 0.0, 0.0, 0.0, 0.0)
+        assert e.value.status == capi.DFG_INVALID_ARGUMENT
+    finally:
+        ls.close()
+
+
 def test_solution_is_deterministic(gpu_ctx):
     from delfem_gb300 import meshgen as mg
     p = mg.solid2d_cantilever(40, 20, seed=9)
