@@ -16,10 +16,14 @@
 //    eqn_linear_solid2d.h:68-72, eqn_linear_solid3d.h:59-64);
 //  * DfgDelFEM::Solve_PCG and DfgDelFEM::Solve_PBiCGSTAB are the
 //    device-resident fast paths with the in/out semantics of LsSol::Solve_PCG
-//    and LsSol::Solve_PBiCGSTAB (solver_ls_iter.h:38-45).
+//    and LsSol::Solve_PBiCGSTAB (solver_ls_iter.h:38-45);
+//  * CMatSolverGPU is the matrix-level MatVec::Sol::Solve_PCG
+//    (include/delfem/matvec/solver_mat_iter.h:47-51) over a host
+//    CMatDia_BlkCrs and CVector_Blk pair.
 #ifndef DFG_DELFEM_HPP
 #define DFG_DELFEM_HPP
 
+#include <algorithm>
 #include <cassert>
 #include <string>
 #include <vector>
@@ -29,6 +33,8 @@
 #include "delfem/field.h"
 #include "delfem/field_world.h"
 #include "delfem/ls/linearsystem_interface_solver.h"
+#include "delfem/matvec/matdia_blkcrs.h"
+#include "delfem/matvec/vector_blk.h"
 #include "delfem/node_ary.h"
 
 namespace DfgDelFEM {
@@ -185,6 +191,91 @@ inline bool Solve_PBiCGSTAB(double& conv_ratio, unsigned int& num_iter, CLinearS
   const int st = dfg_solve_pbicgstab(ls.system(), ls.preconditioner(), DFG_PREC_FP64, &conv_ratio, &num_iter);
   return st == DFG_OK || st == DFG_NOT_CONVERGED;
 }
+
+// ---- MatVec::Sol::Solve_PCG (src/matvec/solver_mat_iter.cpp:115-189), the
+// matrix-level PCG.  The reference passes the matrix, the residual and update
+// vectors, and a CPrecond_Blk with its factor matrix (a CMatDiaFrac_BlkCrs
+// made from the same matrix).  Here one object holds the matrix's device copy
+// and its ILU(fill_level) factor, so the call keeps the matrix and vector
+// arguments and the preconditioner pair becomes SetValue.  Same arithmetic as
+// LsSol::Solve_PCG; at the iteration limit it returns false with conv_ratio
+// left as given and iteration = the limit, as the matrix-level loop does.
+// The pattern must be the reference's own: columns sorted per row, no
+// diagonal (CMatDia_BlkCrs::AddPattern builds it so); block lengths 1-3.
+class CMatSolverGPU {
+ public:
+  // symbolic: the block pattern (GetPtrIndPSuP per row) and the factor's
+  CMatSolverGPU(dfg_ctx ctx, const MatVec::CMatDia_BlkCrs& mat, int fill_level = 0)
+      : n_((int)mat.NBlkMatCol()), b_(mat.LenBlkCol()) {
+    std::vector<int> rowptr(n_ + 1, 0);
+    for (int i = 0; i < n_; ++i) {
+      unsigned int np = 0;
+      const unsigned int* c = mat.GetPtrIndPSuP(i, np);
+      for (unsigned int k = 0; k < np; ++k) colind_.push_back((int)c[k]);
+      rowptr[i + 1] = (int)colind_.size();
+    }
+    const int* ci = colind_.empty() ? rowptr.data() : colind_.data();
+    ok_ = dfg_system_create(ctx, n_, b_, rowptr.data(), ci, &sys_) == DFG_OK &&
+          dfg_precond_create(ctx, &prec_) == DFG_OK && dfg_precond_set_fill_level(prec_, fill_level) == DFG_OK &&
+          dfg_precond_set_linear_system(prec_, sys_) == DFG_OK;
+  }
+  ~CMatSolverGPU() {
+    if (prec_) dfg_precond_destroy(prec_);
+    if (sys_) dfg_system_destroy(sys_);
+  }
+  CMatSolverGPU(const CMatSolverGPU&) = delete;
+  CMatSolverGPU& operator=(const CMatSolverGPU&) = delete;
+  bool IsValid() const { return ok_; }
+
+  // numeric: the matrix values (GetPtrValDia / GetPtrValPSuP) and the factor
+  // (CMatDiaFrac_BlkCrs::SetValue + DoILUDecomp); false on a singular pivot
+  bool SetValue(const MatVec::CMatDia_BlkCrs& mat) {
+    if (!ok_ || (int)mat.NBlkMatCol() != n_ || mat.LenBlkCol() != b_ || mat.NCrs() != colind_.size()) return false;
+    const size_t bs = (size_t)b_ * b_;
+    std::vector<double> diag(n_ * bs + 1), offd(colind_.size() * bs + 1);
+    size_t o = 0;
+    for (int i = 0; i < n_; ++i) {
+      const double* d = mat.GetPtrValDia(i);
+      std::copy(d, d + bs, diag.begin() + i * bs);
+      unsigned int np = 0;
+      const double* v = mat.GetPtrValPSuP(i, np);
+      std::copy(v, v + np * bs, offd.begin() + o);
+      o += np * bs;
+    }
+    return dfg_set_matrix(sys_, diag.data(), offd.data()) == DFG_OK && dfg_precond_set_value(prec_, sys_) == DFG_OK;
+  }
+
+  // r_vec: right-hand side in, recursive residual out; u_vec: solution out
+  bool Solve_PCG(double& conv_ratio, unsigned int& iteration, MatVec::CVector_Blk& r_vec, MatVec::CVector_Blk& u_vec) {
+    if (!ok_ || (int)r_vec.NBlk() != n_ || r_vec.Len() != b_ || (int)u_vec.NBlk() != n_ || u_vec.Len() != b_)
+      return false;
+    if (n_ == 0) {  // ||r||^2 = 0 < 1e-30: the reference's early return
+      conv_ratio = 0.0;
+      iteration = 0;
+      return true;
+    }
+    const double tol = conv_ratio;
+    const unsigned int mx = iteration;
+    if (dfg_set_vector(sys_, -1, r_vec.GetValuePtr(0)) != DFG_OK) return false;
+    const int st = dfg_solve_pcg(sys_, prec_, &conv_ratio, &iteration);
+    if ((st != DFG_OK && st != DFG_NOT_CONVERGED) || dfg_get_vector(sys_, -1, r_vec.GetValuePtr(0)) != DFG_OK ||
+        dfg_get_vector(sys_, -2, u_vec.GetValuePtr(0)) != DFG_OK)
+      return false;
+    if (st == DFG_NOT_CONVERGED) {
+      conv_ratio = tol;
+      iteration = mx;
+      return false;
+    }
+    return true;
+  }
+
+ private:
+  int n_, b_;
+  std::vector<int> colind_;
+  dfg_system sys_ = nullptr;
+  dfg_precond prec_ = nullptr;
+  bool ok_ = false;
+};
 
 }  // namespace DfgDelFEM
 

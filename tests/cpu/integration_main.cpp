@@ -2,15 +2,21 @@
 // uses include/dfg_delfem.hpp exactly as a maintainer would: mesh through
 // Msh::IMesh into CFieldWorld, the GPU linear system from the field, the
 // reference's own LsSol::Solve_PCG and LsSol::Solve_PBiCGSTAB driving it
-// through the virtual interface, and the device-resident fast paths.  Compiled (and, where a GPU exists, run)
-// by tests/test_integration_adapter.py against the reference's headers.
+// through the virtual interface, the device-resident fast paths, and the
+// matrix-level MatVec::Sol::Solve_PCG beside CMatSolverGPU on the same matrix.
+// Compiled (and, where a GPU exists, run) by tests/test_integration_adapter.py
+// against the reference's headers.
+#include <algorithm>
 #include <cassert>
+#include <cmath>
 #include <cstdio>
 #include <vector>
 
 #include "delfem/mesh_interface.h"
 #include "delfem/field_world.h"
 #include "delfem/ls/solver_ls_iter.h"
+#include "delfem/matvec/matdiafrac_blkcrs.h"
+#include "delfem/matvec/solver_mat_iter.h"
 #include "dfg_delfem.hpp"
 
 class Square : public Msh::IMesh {
@@ -36,6 +42,71 @@ class Square : public Msh::IMesh {
  private:
   int n_;
 };
+
+// The finalized system of `ls` as a reference CMatDia_BlkCrs; the reference's
+// matrix-level PCG with its ILU(0) CMatDiaFrac_BlkCrs against CMatSolverGPU:
+// both converge, iterations within 2, solutions within 1e-6 (relative L2).
+static int matrix_level_check(dfg_ctx ctx, DfgDelFEM::CLinearSystem_FieldGPU& ls) {
+  dfg_system sys = ls.system();
+  int n = 0, b = 0;
+  long long nnz = 0;
+  if (dfg_system_info(sys, &n, &b, &nnz) != DFG_OK) return 10;
+  const size_t bs = (size_t)b * b;
+  std::vector<int> rowptr(n + 1), colind(nnz > 0 ? nnz : 1);
+  std::vector<double> diag(n * bs), offd((nnz > 0 ? nnz : 1) * bs), rhs((size_t)n * b);
+  if (dfg_system_get_pattern(sys, rowptr.data(), colind.data()) != DFG_OK ||
+      dfg_get_matrix(sys, diag.data(), offd.data()) != DFG_OK || dfg_get_vector(sys, -1, rhs.data()) != DFG_OK)
+    return 11;
+  Com::CIndexedArray crs;
+  crs.InitializeSize(n);
+  for (int i = 0; i <= n; ++i) crs.index[i] = rowptr[i];
+  crs.array.assign(colind.begin(), colind.begin() + nnz);
+  MatVec::CMatDia_BlkCrs mat(n, b);
+  if (!mat.AddPattern(crs)) return 12;
+  for (int i = 0; i < n; ++i) {
+    std::copy(diag.begin() + i * bs, diag.begin() + (i + 1) * bs, mat.GetPtrValDia(i));
+    unsigned int np = 0;
+    const unsigned int* c = static_cast<const MatVec::CMatDia_BlkCrs&>(mat).GetPtrIndPSuP(i, np);
+    if ((int)np != rowptr[i + 1] - rowptr[i]) return 13;
+    for (unsigned int k = 0; k < np; ++k)
+      if ((int)c[k] != colind[rowptr[i] + k]) return 13;
+    double* v = mat.GetPtrValPSuP(i, np);
+    std::copy(offd.begin() + rowptr[i] * bs, offd.begin() + rowptr[i + 1] * bs, v);
+  }
+  MatVec::CVector_Blk r_ref(n, b), u_ref(n, b), r_gpu(n, b), u_gpu(n, b);
+  for (int i = 0; i < n; ++i)
+    for (int p = 0; p < b; ++p) {
+      r_ref.SetValue(i, p, rhs[(size_t)i * b + p]);
+      r_gpu.SetValue(i, p, rhs[(size_t)i * b + p]);
+    }
+  MatVec::CMatDiaFrac_BlkCrs frac(0, mat);
+  if (!frac.SetValue(mat)) return 14;
+  double conv_ref = 1e-8, conv_gpu = 1e-8;
+  unsigned int it_ref = 1000, it_gpu = 1000;
+  const bool ok_ref = MatVec::Sol::Solve_PCG(conv_ref, it_ref, mat, r_ref, u_ref, frac, mat);
+  DfgDelFEM::CMatSolverGPU solver(ctx, mat, 0);
+  if (!solver.IsValid() || !solver.SetValue(mat)) return 15;
+  const bool ok_gpu = solver.Solve_PCG(conv_gpu, it_gpu, r_gpu, u_gpu);
+  double d2 = 0.0, x2 = 0.0;
+  for (int i = 0; i < n; ++i)
+    for (int p = 0; p < b; ++p) {
+      const double d = u_gpu.GetValue(i, p) - u_ref.GetValue(i, p);
+      d2 += d * d;
+      x2 += u_ref.GetValue(i, p) * u_ref.GetValue(i, p);
+    }
+  std::printf("matrix-level PCG reference: %d iter %u conv %.3e; device: %d iter %u conv %.3e; |du|/|u| %.2e\n",
+              ok_ref, it_ref, conv_ref, ok_gpu, it_gpu, conv_gpu, x2 > 0 ? std::sqrt(d2 / x2) : std::sqrt(d2));
+  // the iteration limit: false, conv_ratio left as given, iteration = the limit
+  MatVec::CVector_Blk r_lim(n, b), u_lim(n, b);
+  for (int i = 0; i < n; ++i)
+    for (int p = 0; p < b; ++p) r_lim.SetValue(i, p, rhs[(size_t)i * b + p]);
+  double conv_lim = 1e-8;
+  unsigned int it_lim = 3;
+  const bool ok_lim = solver.Solve_PCG(conv_lim, it_lim, r_lim, u_lim);
+  if (ok_lim || conv_lim != 1e-8 || it_lim != 3) return 16;
+  const unsigned int di = it_ref > it_gpu ? it_ref - it_gpu : it_gpu - it_ref;
+  return (ok_ref && ok_gpu && di <= 2 && d2 <= 1e-12 * x2) ? 0 : 17;
+}
 
 int main() {
   dfg_ctx ctx = nullptr;
@@ -78,7 +149,12 @@ int main() {
   std::printf("BiCGSTAB reference loop: %d iter %u conv %.3e; device loop: %d iter %u conv %.3e\n", ok_ref_b, iter3,
               conv3, ok_fast_b, iter4, conv4);
   ls.UpdateValueOfField(id_field, world);
+  ls.InitializeMarge();
+  DfgDelFEM::AddLinSys_Poisson(ls, 1.0, 1.0);
+  ls.FinalizeMarge();
+  const int mat_rc = matrix_level_check(ctx, ls);
   dfg_ctx_destroy(ctx);
+  if (mat_rc != 0) return mat_rc;
   const bool pcg_ok = ok_ref && ok_fast && (iter > iter2 ? iter - iter2 : iter2 - iter) <= 2;
   const bool bicg_ok = ok_ref_b && ok_fast_b && iter3 < 1000 && (iter3 > iter4 ? iter3 - iter4 : iter4 - iter3) <= 2;
   return (pcg_ok && bicg_ok) ? 0 : 2;
