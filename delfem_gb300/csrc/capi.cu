@@ -1909,9 +1909,9 @@ extern "C" int dfg_profile_kernels(dfg_system sys, dfg_precond prec, int mode, i
     if (bytes) {
       const double spmv_sz = mixed ? 4.0 : 8.0, sw_sz = fp32z ? 4.0 : 8.0;
       const double bs = (double)sys->b * sys->b, N = sys->n, Z = (double)sys->nnz;
-      const FactorPattern F = factor_pattern(prec);  // the sweeps read the factor's blocks
+      const FactorPattern FP = factor_pattern(prec);  // the sweeps read the factor's blocks
       long long zl = 0;
-      for (int i = 0; i < sys->n; ++i) zl += F.diaind[i] - F.rowptr[i];
+      for (int i = 0; i < sys->n; ++i) zl += FP.diaind[i] - FP.rowptr[i];
       const double Zl = (double)zl, Zu = (double)prec->nnz - Zl;
       bytes[0] = (Z + N) * bs * spmv_sz + 4.0 * (Z + N + 1) + 2.0 * N * sys->b * spmv_sz;   // values, indices, x, y
       bytes[1] = (Zl + N) * bs * sw_sz + 4.0 * (Zl + N + 1) + 2.0 * N * sys->b * sw_sz;       // L, D^-1, indices, in, out

@@ -126,7 +126,6 @@ class Arena {
     }
   }
   size_t capacity() const { return cap_; }
-  size_t used() const { return used_; }
   size_t peak() const { return peak_; }
   static size_t round(size_t b) { return (std::max<size_t>(b, 1) + 255) / 256 * 256; }
 
