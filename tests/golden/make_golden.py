@@ -9,7 +9,8 @@ factor, and the result of LsSol::Solve_PCG (iterations, ratio, solution).
 The fixtures in this directory use ILU(0); those in iluk/ use other fill
 levels (CPreconditioner_ILU::SetFillInLevel) and add the factor's own block
 pattern (ref_rowptr_f, ref_colind_f) and ref_fill_level; those in bicgstab/
-hold the result of LsSol::Solve_PBiCGSTAB instead of Solve_PCG (ref_solver).
+hold the result of LsSol::Solve_PBiCGSTAB instead of Solve_PCG (ref_solver);
+those in known/ are problems with closed-form answers (known_cases).
 
 Harness problem file (little-endian): int32 magic 0x44464731, kind, nnode,
 ndim, nelem, nnoel, b; f64 coords[nnode*ndim]; i32 conn[nelem*nnoel];
@@ -17,7 +18,7 @@ i32 has_coef (+ f64 coef[nelem]); f64 params[8]; i32 bcflag[nnode*b];
 i32 has_load (+ f64 load[nnode*b]); i32 has_u (+ f64 u); i32 has_v (+ f64 v);
 f64 tol; i32 maxit.  The result file layout is read by meshgen.read_result.
 
-Run from the repository root:  python tests/golden/make_golden.py [ilu0|iluk|bicgstab|all]
+Run from the repository root:  python tests/golden/make_golden.py [ilu0|iluk|bicgstab|known|all]
 """
 from __future__ import annotations
 
@@ -87,6 +88,52 @@ def bicgstab_cases():
     ]
 
 
+def known_cases():
+    """Problems whose answers are known in closed form; the reference's own
+    run of each is committed beside it.
+    * A 2 x 2 Poisson grid without jitter, all sides fixed: its one free node
+      has the stencil 4 / -1 (axis neighbours) / 0 (along the split diagonal),
+      right-hand side source * h^2 = 0.25 and solution 0.0625.
+    * Linear fields, which P1 elements reproduce exactly, on jittered meshes
+      with uniform material and no source or body force.  The field is set on
+      the boundary (Dirichlet lifting: the field value enters the residual as
+      -K u), and field + update must equal it everywhere.  Cases: 2D Poisson,
+      2D elasticity (both displacement components) and 3D Poisson."""
+    out = []
+    coords, conn = mg.tri_grid(2, 2)
+    bc = np.ones(coords.shape[0], dtype=np.int32)
+    bc[4] = 0  # the centre node
+    prm = np.zeros(8); prm[0] = 1.0; prm[1] = 1.0
+    out.append(mg.Problem(mg.POISSON2D, coords, conn, prm, bc, tol=1e-12, name="poisson2d_2x2"))
+
+    def boundary_flags(conn, nnode, b):
+        f = np.zeros(nnode, dtype=np.int32)
+        f[mg.boundary_nodes(conn)] = 1
+        return np.repeat(f, b).astype(np.int32)
+
+    rng = np.random.default_rng(31)
+    coords, conn = mg.tri_grid(6, 5, 1.0, 1.0, 0.2, rng)
+    bc = boundary_flags(conn, coords.shape[0], 1)
+    g = 0.7 + 1.3 * coords[:, 0] - 0.4 * coords[:, 1]
+    prm = np.zeros(8); prm[0] = 1.0
+    out.append(mg.Problem(mg.POISSON2D, coords, conn, prm, bc, u=g * bc, tol=1e-12, name="poisson2d_linear"))
+
+    coords, conn = mg.tri_grid(7, 4, 2.0, 1.0, 0.2, rng)
+    bc = boundary_flags(conn, coords.shape[0], 2)
+    x, y = coords[:, 0], coords[:, 1]
+    g = np.stack([0.01 + 0.02 * x - 0.03 * y, -0.02 + 0.015 * x + 0.01 * y], axis=1).ravel()
+    E, nu = 1.0, 0.3
+    prm = np.zeros(8); prm[0] = E * nu / ((1 + nu) * (1 - 2 * nu)); prm[1] = E / (2 * (1 + nu))
+    out.append(mg.Problem(mg.SOLID2D, coords, conn, prm, bc, u=g * bc, tol=1e-12, name="solid2d_linear"))
+
+    coords, conn = mg.tet_grid(3, 3, 3, jitter=0.15, rng=rng)
+    bc = boundary_flags(conn, coords.shape[0], 1)
+    g = 0.5 + coords[:, 0] - 2.0 * coords[:, 1] + 0.25 * coords[:, 2]
+    prm = np.zeros(8); prm[0] = 1.0
+    out.append(mg.Problem(mg.POISSON3D, coords, conn, prm, bc, u=g * bc, tol=1e-12, name="poisson3d_linear"))
+    return out
+
+
 def fixture_name(p: mg.Problem, k: int, fill_level: int = 0) -> str:
     tag = "coef" if p.coef is not None else "uniform"
     lev = "" if fill_level == 0 else (f"_ilu{fill_level}" if fill_level > 0 else "_ilufull")
@@ -128,6 +175,10 @@ def main():
         os.makedirs(os.path.join(here, "iluk"), exist_ok=True)
         for k, (p, lev) in enumerate(iluk_cases()):
             write_fixture(os.path.join(here, "iluk", fixture_name(p, k, lev) + ".npz"), p, lev)
+    if which in ("known", "all"):
+        os.makedirs(os.path.join(here, "known"), exist_ok=True)
+        for k, p in enumerate(known_cases()):
+            write_fixture(os.path.join(here, "known", fixture_name(p, k) + ".npz"), p, 0)
     if which in ("bicgstab", "all"):
         os.makedirs(os.path.join(here, "bicgstab"), exist_ok=True)
         for k, (p, lev) in enumerate(bicgstab_cases()):
