@@ -1,0 +1,45 @@
+"""bench.py's JSON contract on the CPU.  The reference arm (the reference
+algorithm on every host core) prints one line carrying the base contract's
+keys and the `cpu_baseline` and zero-copy `e2e` objects.  The GPU arm
+without a GPU exits non-zero with the CUDA error: no CPU fallback exists."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+from conftest import ROOT
+
+
+def _run(*args, timeout=600):
+    return subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *args], cwd=ROOT, capture_output=True,
+                          text=True, timeout=timeout)
+
+
+def test_reference_arm_line():
+    r = _run("--impl", "reference", "--config", "poisson2d_128", "--steps", "1", "--warmup", "1")
+    assert r.returncode == 0, r.stderr[-3000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["n_gpus"] == 1 and d["steps"] == 1
+    assert d["warmup"] >= 3  # the contract's minimum, applied when fewer are asked for
+    assert d["unit"] == "solves/s" and d["higher_is_better"] is True and d["value"] > 0
+    assert d["config"]["workload"] == "poisson2d_128"
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["cores"] >= 1 and cb["kind"] in ("port", "reference") and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_gpu_arm_fails_loudly_without_a_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    r = _run("--config", "poisson2d_128", "--steps", "1", "--warmup", "3", timeout=300)
+    assert r.returncode != 0
+    assert not [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert "dfg_ctx_create" in r.stderr or "CUDA" in r.stderr
