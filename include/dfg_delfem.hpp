@@ -19,12 +19,16 @@
 //    and LsSol::Solve_PBiCGSTAB (solver_ls_iter.h:38-45);
 //  * CMatSolverGPU is the matrix-level MatVec::Sol::Solve_PCG
 //    (include/delfem/matvec/solver_mat_iter.h:47-51) over a host
-//    CMatDia_BlkCrs and CVector_Blk pair.
+//    CMatDia_BlkCrs and CVector_Blk pair;
+//  * CPreconditioner_ILU_GPU is an LsSol::CPreconditioner for the
+//    reference's own host CLinearSystem: only the ILU factor and its
+//    application move to the device.
 #ifndef DFG_DELFEM_HPP
 #define DFG_DELFEM_HPP
 
 #include <algorithm>
 #include <cassert>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -32,7 +36,9 @@
 #include "delfem/elem_ary.h"
 #include "delfem/field.h"
 #include "delfem/field_world.h"
+#include "delfem/ls/linearsystem.h"
 #include "delfem/ls/linearsystem_interface_solver.h"
+#include "delfem/ls/preconditioner.h"
 #include "delfem/matvec/matdia_blkcrs.h"
 #include "delfem/matvec/vector_blk.h"
 #include "delfem/node_ary.h"
@@ -245,6 +251,19 @@ class CMatSolverGPU {
     return dfg_set_matrix(sys_, diag.data(), offd.data()) == DFG_OK && dfg_precond_set_value(prec_, sys_) == DFG_OK;
   }
 
+  // vec := (LU)^-1 vec, the factor's forward and backward substitution
+  // (CMatDiaFrac_BlkCrs::ForwardSubstitution / BackwardSubstitution,
+  // src/matvec/matdiafrac_blkcrs.cpp:332-669) on the device
+  bool SolvePrecond(MatVec::CVector_Blk& vec) {
+    if (!ok_ || (int)vec.NBlk() != n_ || vec.Len() != b_) return false;
+    if (n_ == 0) return true;
+    unsigned ntmp = 0;
+    if (dfg_get_tmp_vector_size(sys_, &ntmp) != DFG_OK || (ntmp < 1 && dfg_resize_tmp_vec(sys_, 1) != DFG_OK))
+      return false;
+    return dfg_set_vector(sys_, 0, vec.GetValuePtr(0)) == DFG_OK && dfg_precond_solve(prec_, sys_, 0) == DFG_OK &&
+           dfg_get_vector(sys_, 0, vec.GetValuePtr(0)) == DFG_OK;
+  }
+
   // r_vec: right-hand side in, recursive residual out; u_vec: solution out
   bool Solve_PCG(double& conv_ratio, unsigned int& iteration, MatVec::CVector_Blk& r_vec, MatVec::CVector_Blk& u_vec) {
     if (!ok_ || (int)r_vec.NBlk() != n_ || r_vec.Len() != b_ || (int)u_vec.NBlk() != n_ || u_vec.Len() != b_)
@@ -275,6 +294,46 @@ class CMatSolverGPU {
   dfg_system sys_ = nullptr;
   dfg_precond prec_ = nullptr;
   bool ok_ = false;
+};
+
+// ---- LsSol::CPreconditioner_ILU (include/delfem/ls/preconditioner.h:55-97,
+// src/ls/preconditioner.cpp) for the reference's own host CLinearSystem: the
+// factor is built and applied on the device, everything else stays on the
+// host.  A DelFEM program swaps the one declaration
+//     LsSol::CPreconditioner_ILU prec;   ->   DfgDelFEM::CPreconditioner_ILU_GPU prec(ctx);
+// and keeps SetFillInLevel / SetLinearSystem(ls.m_ls) / SetValue(ls.m_ls),
+// LsSol::CLinearSystemPreconditioner lsp(ls.m_ls, prec) and the reference's
+// own LsSol::Solve_PCG.  One linear-system segment (one field), block length
+// 1-3; every apply copies the vector to the device and back.
+class CPreconditioner_ILU_GPU : public LsSol::CPreconditioner {
+ public:
+  explicit CPreconditioner_ILU_GPU(dfg_ctx ctx) : ctx_(ctx) {}
+  // CPreconditioner_ILU::SetFillInLevel (preconditioner.h:75): one segment,
+  // so ilss0 is -1 (all) or 0
+  void SetFillInLevel(int lev, int ilss0 = -1) {
+    if (ilss0 <= 0) lev_ = lev;
+  }
+  // symbolic: the segment's pattern and the factor's (preconditioner.cpp:57-211)
+  virtual void SetLinearSystem(const LsSol::CLinearSystem& ls) {
+    core_.reset();
+    if (ls.GetNLinSysSeg() != 1) return;
+    core_.reset(new CMatSolverGPU(ctx_, ls.GetMatrix(0), lev_));
+  }
+  // numeric factorisation (preconditioner.cpp:217-297); false on more than
+  // 10 singular pivots, as DoILUDecomp
+  virtual bool SetValue(const LsSol::CLinearSystem& ls) {
+    return core_ && core_->IsValid() && ls.GetNLinSysSeg() == 1 && core_->SetValue(ls.GetMatrix(0));
+  }
+  // forward then backward substitution of vector iv (preconditioner.cpp:301-335)
+  virtual bool SolvePrecond(LsSol::CLinearSystem& ls, unsigned int iv) {
+    return core_ && ls.GetNLinSysSeg() == 1 && core_->SolvePrecond(ls.GetVector((int)iv, 0));
+  }
+  bool IsValid() const { return core_ && core_->IsValid(); }
+
+ private:
+  dfg_ctx ctx_;
+  int lev_ = 0;
+  std::unique_ptr<CMatSolverGPU> core_;
 };
 
 }  // namespace DfgDelFEM

@@ -3,7 +3,8 @@
 // Msh::IMesh into CFieldWorld, the GPU linear system from the field, the
 // reference's own LsSol::Solve_PCG and LsSol::Solve_PBiCGSTAB driving it
 // through the virtual interface, the device-resident fast paths, and the
-// matrix-level MatVec::Sol::Solve_PCG beside CMatSolverGPU on the same matrix.
+// matrix-level MatVec::Sol::Solve_PCG beside CMatSolverGPU on the same matrix,
+// and the reference's host linear system with CPreconditioner_ILU_GPU.
 // Compiled (and, where a GPU exists, run) by tests/test_integration_adapter.py
 // against the reference's headers.
 #include <algorithm>
@@ -14,7 +15,11 @@
 
 #include "delfem/mesh_interface.h"
 #include "delfem/field_world.h"
+#include "delfem/femeqn/eqn_poisson.h"
+#include "delfem/femls/linearsystem_field.h"
+#include "delfem/ls/preconditioner.h"
 #include "delfem/ls/solver_ls_iter.h"
+#include "delfem/matvec/bcflag_blk.h"
 #include "delfem/matvec/matdiafrac_blkcrs.h"
 #include "delfem/matvec/solver_mat_iter.h"
 #include "dfg_delfem.hpp"
@@ -108,17 +113,73 @@ static int matrix_level_check(dfg_ctx ctx, DfgDelFEM::CLinearSystem_FieldGPU& ls
   return (ok_ref && ok_gpu && di <= 2 && d2 <= 1e-12 * x2) ? 0 : 17;
 }
 
+// The reference's own host CLinearSystem_Field, assembled by the reference's
+// AddLinSys_Poisson and solved by the reference's Solve_PCG twice: with its
+// CPreconditioner_ILU and with CPreconditioner_ILU_GPU swapped in.  Both
+// converge, iterations within 2, solutions within 1e-6 (relative L2).
+static int host_system_check(dfg_ctx ctx, Fem::Field::CFieldWorld& world, unsigned int id_field,
+                             const std::vector<int>& fixed) {
+  Fem::Ls::CLinearSystem_Field ls;
+  if (!ls.AddPattern_Field(id_field, world)) return 20;
+  MatVec::CBCFlag& bc = ls.m_ls.GetBCFlag(0);
+  for (size_t i = 0; i < fixed.size(); ++i)
+    if (fixed[i]) bc.SetBC((unsigned)i, 0);
+  LsSol::CPreconditioner_ILU prec_cpu;
+  prec_cpu.SetFillInLevel(0);
+  prec_cpu.SetLinearSystem(ls.m_ls);
+  DfgDelFEM::CPreconditioner_ILU_GPU prec_gpu(ctx);
+  prec_gpu.SetFillInLevel(0);
+  prec_gpu.SetLinearSystem(ls.m_ls);
+  if (!prec_gpu.IsValid()) return 21;
+  ls.InitializeMarge();
+  Fem::Eqn::AddLinSys_Poisson(ls, 1.0, 1.0, world, id_field);
+  ls.FinalizeMarge();
+  if (!prec_cpu.SetValue(ls.m_ls) || !prec_gpu.SetValue(ls.m_ls)) return 22;
+  const MatVec::CVector_Blk rhs = ls.m_ls.GetVector(-1, 0);
+  double conv[2] = {1e-8, 1e-8};
+  unsigned int it[2] = {1000, 1000};
+  std::vector<double> x[2];
+  for (int k = 0; k < 2; ++k) {
+    ls.m_ls.GetVector(-1, 0) = rhs;
+    LsSol::CPreconditioner& prec = k == 0 ? static_cast<LsSol::CPreconditioner&>(prec_cpu) : prec_gpu;
+    LsSol::CLinearSystemPreconditioner lsp(ls.m_ls, prec);
+    if (!LsSol::Solve_PCG(conv[k], it[k], lsp)) return 23 + k;
+    const MatVec::CVector_Blk& u = ls.m_ls.GetVector(-2, 0);
+    for (unsigned int i = 0; i < u.NBlk(); ++i) x[k].push_back(u.GetValue(i, 0));
+  }
+  double d2 = 0.0, x2 = 0.0;
+  for (size_t i = 0; i < x[0].size(); ++i) {
+    d2 += (x[1][i] - x[0][i]) * (x[1][i] - x[0][i]);
+    x2 += x[0][i] * x[0][i];
+  }
+  std::printf("host system, reference Solve_PCG: CPU ILU iter %u conv %.3e; GPU ILU iter %u conv %.3e; |du|/|u| %.2e\n",
+              it[0], conv[0], it[1], conv[1], std::sqrt(d2 / x2));
+  const unsigned int di = it[0] > it[1] ? it[0] - it[1] : it[1] - it[0];
+  return (di <= 2 && d2 <= 1e-12 * x2) ? 0 : 25;
+}
+
 int main() {
   dfg_ctx ctx = nullptr;
   if (dfg_ctx_create(0, &ctx) != DFG_OK) {
     std::printf("no CUDA device: adapter compiled and linked\n");
     return 0;
   }
+  const int nside = 16;
   Fem::Field::CFieldWorld world;
-  const unsigned int id_base = world.AddMesh(Square(16));
+  const unsigned int id_base = world.AddMesh(Square(nside));
   const unsigned int id_field = world.MakeField_FieldElemDim(id_base, 2, Fem::Field::SCALAR, Fem::Field::VALUE, Fem::Field::CORNER);
+  // u = 0 on the square's four sides (node j*(nside+1)+i at (i, j)/nside)
+  std::vector<int> fixed((nside + 1) * (nside + 1), 0);
+  for (int j = 0; j <= nside; ++j)
+    for (int i = 0; i <= nside; ++i) fixed[j * (nside + 1) + i] = i == 0 || j == 0 || i == nside || j == nside;
+  const int host_rc = host_system_check(ctx, world, id_field, fixed);
+  if (host_rc != 0) {
+    dfg_ctx_destroy(ctx);
+    return host_rc;
+  }
   DfgDelFEM::CLinearSystem_FieldGPU ls(ctx);
   if (!ls.AddPattern_Field(id_field, world)) return 1;
+  if (dfg_set_bcflags(ls.system(), fixed.data()) != DFG_OK) return 1;
   ls.SetFillInLevel(0);
   ls.SetPreconditionerLinearSystem();
   ls.InitializeMarge();
