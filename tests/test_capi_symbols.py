@@ -58,7 +58,8 @@ def test_header_is_plain_c_and_links(built, tmp_path):
     compiles as strict C99 without warnings, every declared entry point
     resolves when a C program links libdfg.so, and the calls that need no
     device (version, error text, the GiD reader's error path, context
-    creation without a GPU) behave from C as documented."""
+    creation without a GPU) behave from C as documented, and the server
+    structs' documented positional initializers still fill every field."""
     import os
     import shutil
     import torch
@@ -80,11 +81,15 @@ static const entry_fn entry_points[] = {{
 }};
 
 int main(void) {{
+  /* the positional initializers documented for the server */
+  dfg_server_config cfg = {{DFG_PREC_FP32_FACTOR, 1e-8, 20000, 0, 128, 8, 0, 0, 0}};
+  dfg_request q = {{4, 0, 0, NULL, NULL, NULL, NULL, 5, NULL, NULL, NULL}};
   size_t i;
   int nd = 0, nn = 0, nv = 0, ne = 0;
   dfg_ctx ctx = NULL;
   for (i = 0; i < sizeof entry_points / sizeof entry_points[0]; ++i)
     if (!entry_points[i]) return 10;
+  if (cfg.size_groups != 0 || q.nparams != 5 || q.x_out != NULL) return 16;
   if (strncmp(dfg_version(), "dfg", 3) != 0) return 11;
   if (dfg_last_error(NULL) == NULL) return 12;
   if (dfg_mesh_read_gid("{tmp_path}/missing.msh", &nd, &nn, &nv, &ne, NULL, NULL) != DFG_INVALID_ARGUMENT) return 13;
