@@ -167,6 +167,10 @@ int dfg_set_vector(dfg_system sys, int iv, const double* in);
 
 /* ---------------------------------------- solver interface (ILinearSystem_Sol) */
 
+/* Number of work vectors (slots >= 0) and resizing them
+ * (ILinearSystem_Sol::GetTmpVectorArySize / ReSizeTmpVecSolver,
+ * include/delfem/ls/linearsystem_interface_solver.h:71-73,
+ * src/ls/linearsystem.cpp:208-245); new slots start at zero. */
 int dfg_get_tmp_vector_size(dfg_system sys, unsigned* size);
 int dfg_resize_tmp_vec(dfg_system sys, unsigned size);
 /* *out = {v1}.{v2} (CLinearSystem::DOT, src/ls/linearsystem.cpp:335-360) */
@@ -425,7 +429,12 @@ int dfg_server_wait(dfg_server s, long long id, dfg_result* out);
 int dfg_server_error_text(dfg_server s, long long id, char* buf, int len);
 /* Blocks until every submitted request has completed. */
 int dfg_server_drain(dfg_server s);
+/* Counters since creation (dfg_server_counters): requests submitted and
+ * finished, replays, kernel launches, graph builds, peak solves in flight,
+ * device bytes reserved and at peak, bytes moved each way, busy time. */
 int dfg_server_stats(dfg_server s, dfg_server_counters* out);
+/* Per-kernel device time and algorithmic bytes summed over the profiled
+ * replays (dfg_server_config::profile_every). */
 int dfg_server_profile(dfg_server s, dfg_server_profile_t* out);
 /* Completes the requests in flight, then releases the server. */
 int dfg_server_destroy(dfg_server s);
