@@ -3,6 +3,8 @@
 // instead of a context's allocation, for callers that may not allocate
 // device memory.  Nothing here calls cudaMalloc, cudaFree or any allocating
 // library routine.
+#include <cuda.h>  // CUcontext / CUresult types only
+
 #include <mutex>
 #include <string>
 
@@ -85,21 +87,71 @@ __global__ void __launch_bounds__(kTpb) k_dot_noalloc(long long m, const double*
   }
 }
 
-// Device address of g_dot_scratch, looked up once per device with that device
-// current (the calling thread's current device).
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double* g_addr[kMaxDevices] = {};
+// Device address of g_dot_scratch, looked up once per CUDA context with that
+// context current.  A device's array lives in the module the context loaded,
+// so the address belongs to the context, not to the device ordinal: a device
+// reset (a new primary context) or a caller's own driver-API context gets a
+// lookup of its own.  Contexts are told apart by their unique ID
+// (cuCtxGetId, reached through the runtime's driver entry points: the
+// library does not link the driver API).
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
 
-cudaError_t scratch_address(int dev, double** out) {
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
-    double* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_dot_scratch);
+struct AddrEntry {
+  unsigned long long ctx_id;
+  double* addr;
+};
+constexpr int kMaxEntries = 64;
+std::mutex g_mu;
+AddrEntry g_addr[kMaxEntries] = {};
+int g_nentries = 0, g_next = 0;
+CtxGetCurrentFn g_get_current = nullptr;
+CtxGetIdFn g_get_id = nullptr;
+
+// ID of the calling thread's current context, 0 when none is current.
+cudaError_t current_context_id(unsigned long long* id) {
+  *id = 0;
+  if (!g_get_current || !g_get_id) {
+    cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = cudaDriverEntryPointSymbolNotFound;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", (void**)&g_get_current, 12000,
+                                                     cudaEnableDefault, &q1);
+    if (e == cudaSuccess)
+      e = cudaGetDriverEntryPointByVersion("cuCtxGetId", (void**)&g_get_id, 12000, cudaEnableDefault, &q2);
     if (e != cudaSuccess) return e;
-    g_addr[dev] = p;
+    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !g_get_current || !g_get_id) {
+      g_get_current = nullptr;
+      g_get_id = nullptr;
+      return cudaErrorNotSupported;
+    }
   }
-  *out = g_addr[dev];
+  CUcontext c = nullptr;
+  if (g_get_current(&c) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+  if (c && g_get_id(c, id) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+  return cudaSuccess;
+}
+
+cudaError_t scratch_address(double** out) {
+  std::lock_guard<std::mutex> lock(g_mu);
+  unsigned long long id = 0;
+  cudaError_t e = current_context_id(&id);
+  if (e != cudaSuccess) return e;
+  for (int k = 0; id != 0 && k < g_nentries; ++k)
+    if (g_addr[k].ctx_id == id) {
+      *out = g_addr[k].addr;
+      return cudaSuccess;
+    }
+  // first call in this context (the lookup also makes the device's primary
+  // context current on a thread that had none)
+  double* p = nullptr;
+  if ((e = cudaGetSymbolAddress((void**)&p, g_dot_scratch)) != cudaSuccess) return e;
+  if ((e = current_context_id(&id)) != cudaSuccess) return e;
+  if (id != 0) {
+    AddrEntry& slot = g_addr[g_nentries < kMaxEntries ? g_nentries++ : g_next];
+    if (g_nentries == kMaxEntries) g_next = (g_next + 1) % kMaxEntries;
+    slot.ctx_id = id;
+    slot.addr = p;
+  }
+  *out = p;
   return cudaSuccess;
 }
 
@@ -126,15 +178,9 @@ extern "C" int dfg_dot_noalloc(const double* x, const double* y, long long m, do
     *out = 0.0;
     return DFG_OK;
   }
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_fail("cudaGetDevice", e);
-  if (dev < 0 || dev >= kMaxDevices) {
-    set_noctx_error("dfg_dot_noalloc: device ordinal " + std::to_string(dev) + " beyond the supported 64");
-    return DFG_INVALID_ARGUMENT;
-  }
   double* scratch = nullptr;
-  if ((e = scratch_address(dev, &scratch)) != cudaSuccess) return cuda_fail("cudaGetSymbolAddress", e);
+  cudaError_t e = scratch_address(&scratch);
+  if (e != cudaSuccess) return cuda_fail("looking up the scratch array's address", e);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // the arrival counter must start at zero
   if ((e = cudaMemsetAsync(scratch + kCounter, 0, sizeof(unsigned), st)) != cudaSuccess)

@@ -196,9 +196,12 @@ int dfg_dot(dfg_system sys, int iv1, int iv2, double* out);
  * with DFG_INVALID_ARGUMENT (reason in dfg_last_error(NULL)).  The arrival
  * counter is cleared on `stream` before each launch.
  *
- * The first call on each device looks up the array's address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture begins.  All calls on one device share the one
+ * The first call in each CUDA context (the device's primary context, or a
+ * context the caller made current) looks up the array's address
+ * (cudaGetSymbolAddress) with that context current, and later calls in the
+ * same context reuse it; make that first call before any stream capture
+ * begins.  The address is kept per context ID, so after a device reset the
+ * next call looks it up again.  All calls on one device share the one
  * array: calls that overlap (several host threads, or several streams at
  * once) race, and the caller must serialise them. */
 #define DFG_DOT_NOALLOC_MAX_LEN 33554432LL /* 8192 blocks x 4096 elements */

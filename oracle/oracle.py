@@ -34,6 +34,16 @@ def build() -> None:
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
 
 
+def reference_dir() -> str:
+    """Where the reference checkout is looked for: DFG_REFERENCE_DIR when set,
+    else the default the Makefile holds (``make refdir``)."""
+    d = os.environ.get("DFG_REFERENCE_DIR")
+    if d:
+        return d
+    r = subprocess.run(["make", "-s", "--no-print-directory", "-C", HERE, "refdir"], capture_output=True, text=True)
+    return r.stdout.strip()
+
+
 def lib():
     global _lib
     if _lib is None:

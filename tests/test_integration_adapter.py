@@ -9,15 +9,16 @@ import subprocess
 import pytest
 
 from conftest import ROOT
+from oracle import reference_dir
 
-REF = "/root/reference"
+REF = reference_dir()
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "include", "delfem")), reason="reference headers absent")
 def test_adapter_compiles_and_links(tmp_path):
     from delfem_gb300 import build as B
     lib = B.build()
-    subprocess.run(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+    subprocess.run(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={REF}"], check=True)
     exe = str(tmp_path / "integration")
     cmd = ["g++", "-O1", "-std=c++17", "-w", "-include", "cassert", f"-I{REF}/include", f"-I{ROOT}/include",
            os.path.join(ROOT, "tests", "cpu", "integration_main.cpp"),

@@ -12,8 +12,9 @@ import numpy as np
 import pytest
 
 from conftest import bits
+from oracle import reference_dir
 
-REF_MESHES = "/root/reference/test_glut/input_file"
+REF_MESHES = os.path.join(reference_dir(), "test_glut", "input_file")
 TRI = ["rect_tri", "rect_tri2", "rect_tri3", "hexa_tri"]
 TET = ["cylinder_tet", "cylinder_tet2", "redtsolid_tet"]
 
