@@ -1,32 +1,38 @@
 #!/usr/bin/env python
 """Throughput benchmark of the FE assembly + ILU(0)-PCG hot path on GB300.
 
-Default workload (``--config serve2d``): the serving stream -- 2,000 solves
-arriving as a seeded Poisson process, 50/50 2D Poisson (1x1 blocks) and 2D
-plane-strain elasticity (2x2 blocks) on jittered triangulated rectangles,
-node counts log-uniform in [2k, 400k], log-normal (sigma 0.5) per-element
-coefficients, 1-3 random Dirichlet sides and one loaded side.  Every request
-runs AddLinSys_* -> FinalizeMarge -> ILU(0) -> PCG to a true relative residual
-<= 1e-8 inside the server (include/dfg.h, dfg_server_*), which admits requests
-by free device memory and iterates all in-flight solves together in batched
-launches replayed from one CUDA graph.  The W + K steps split the stream
-into equal consecutive segments: the first W are served as warm-up, the last
-K are served as one continuous timed stream (requests keep arriving while
-others run).  Arms: served FP32-factor mixed precision (``value``) and served
-plain FP64 (``plain_fp64``), on the same stream.  Requests come from host
-memory and solutions return to host memory, so ``value`` is end to end
-(``e2e`` repeats it with the bytes moved).  Timing is the host clock around
-the timed stream with the device synchronised at both ends (the server runs
-several streams and threads); per-kernel device times come from CUDA events
-inside profiled graph replays.
+Default workload (``--config serve2d``): the serving stream -- 2,000 solves,
+50/50 2D Poisson (1x1 blocks) and 2D plane-strain elasticity (2x2 blocks) on
+jittered triangulated rectangles, node counts log-uniform in [2k, 400k],
+log-normal (sigma 0.5) per-element coefficients, 1-3 random Dirichlet sides
+and one loaded side.  Every request runs AddLinSys_* -> FinalizeMarge ->
+ILU(0) -> PCG to a true relative residual <= 1e-8 inside the server
+(include/dfg.h, dfg_server_*), which admits requests by free device memory and
+iterates all in-flight solves together in batched launches replayed from
+captured CUDA graphs.  The W + K steps split the stream into equal
+consecutive segments: the first W are served as warm-up, the last K as one
+timed stream.  ``serve2d`` measures capacity: every timed request is
+submitted at t = 0 (the stream's seeded arrival times are ignored), so the
+server always has a queue (the line reports the fraction of the timed region
+with requests waiting for admission).  ``serve2d_latency`` serves the same
+stream at its seeded Poisson arrivals of 50 requests/s for p50/p99 latency at
+a fixed load.  Arms, on the same requests: served FP32-factor mixed precision
+(``value``), the benchmark spec's FP32-SpMV mixed form, and served plain FP64.
+Requests come from host memory and solutions return to host memory, so
+``value`` is end to end (``e2e`` repeats it with the bytes moved).  Timing is
+the host clock around the timed stream with the device synchronised at both
+ends (the server runs several streams and threads); per-kernel device times
+come from CUDA events inside profiled graph replays.
 
-``--config serve3d``: the 3D stream (500 solves, 3D Poisson / elasticity on
-hex grids of 16-80 cells per axis, sigma 1.0, admission budget 120 GB).
-Single-solve configurations (``solid2d_1000x500`` and smaller) time one
-complete solve per step with three precision arms.
+``--config serve3d`` / ``serve3d_latency``: the 3D stream (500 solves, 3D
+Poisson / elasticity on hex grids of 16-80 cells per axis, sigma 1.0,
+admission budget 120 GB).  Single-solve configurations (``solid2d_1000x500``
+and smaller) time one complete solve per step with three precision arms.
 
-``--impl reference`` times the reference's CPU algorithm (the oracle's
-bit-exact restatement) on all host cores instead.
+``--impl reference`` runs the reference's CPU algorithm (the oracle's
+bit-exact restatement) on all host cores: for the serving configurations it
+solves the same timed requests as the GPU arm, spread over the cores, timed
+by the wall clock.
 """
 from __future__ import annotations
 
@@ -44,8 +50,12 @@ sys.path.insert(0, ROOT)
 METRIC = "PCG solves/s at 1e-8 rel. residual, served mixed vs plain FP64 GPU; p50/p99 ms"
 CONFIGS = {
     # name -> (meshgen factory kwargs, description)
-    "serve2d": dict(kind="serve", dim=2, nreq=2000, seed=4, rate=50.0, budget=0),
-    "serve3d": dict(kind="serve", dim=3, nreq=500, seed=5, rate=30.0, budget=120 * 10**9),
+    # serving: `rate` is the seeded Poisson arrival rate of the stream;
+    # `saturate` submits every timed request at once (capacity)
+    "serve2d": dict(kind="serve", dim=2, nreq=2000, seed=4, rate=50.0, budget=0, saturate=True),
+    "serve2d_latency": dict(kind="serve", dim=2, nreq=2000, seed=4, rate=50.0, budget=0, saturate=False),
+    "serve3d": dict(kind="serve", dim=3, nreq=500, seed=5, rate=30.0, budget=120 * 10**9, saturate=True),
+    "serve3d_latency": dict(kind="serve", dim=3, nreq=500, seed=5, rate=30.0, budget=120 * 10**9, saturate=False),
     "solid2d_1000x500": dict(kind="solid2d", nx=1000, ny=500),
     "poisson2d_128": dict(kind="poisson2d", n=128),
     "poisson2d_1000": dict(kind="poisson2d", n=1000),
@@ -479,22 +489,45 @@ def serve_stream(name):
     return mg.serve_stream_3d(nreq=c["nreq"], seed=c["seed"], rate=c["rate"])
 
 
+def stream_segments(name, warmup, steps, serve_requests=0):
+    """The stream split into warmup + steps consecutive segments: (all items,
+    warm-up items, timed items) -- the same split in both arms."""
+    items = serve_stream(name)
+    if serve_requests:
+        items = items[:serve_requests]  # a prefix of the stream (profiling runs)
+    nseg = warmup + steps
+    seg = [items[(len(items) * k) // nseg:(len(items) * (k + 1)) // nseg] for k in range(nseg)]
+    return items, [it for sg in seg[:warmup] for it in sg], [it for sg in seg[warmup:] for it in sg]
+
+
+def serve_config(args, cfg, items, timed_items, timed_probs):
+    """The workload as both arms report it (identical dicts)."""
+    return {"workload": args.config, "requests": len(items), "requests_timed": len(timed_items),
+            "requests_per_step": round(len(timed_items) / args.steps, 1),
+            "arrivals": ("all timed requests submitted at t = 0 (capacity)" if cfg["saturate"]
+                         else f"seeded Poisson arrivals at {cfg['rate']:g} requests/s"),
+            "kinds": "2D Poisson / plane-strain elasticity 50:50" if cfg["dim"] == 2 else "3D Poisson / elasticity 50:50",
+            "tol": 1e-8, "stop": "true relative residual <= tol (every request, every arm)",
+            "l2": "in-flight working set (GBs of matrices, factors, vectors) far above the 129 MB L2; no flush"}
+
+
 def gen_problems(items, threads=8):
     from concurrent.futures import ThreadPoolExecutor
     with ThreadPoolExecutor(threads) as ex:
         return list(ex.map(lambda it: it.problem(), items))
 
 
-def serve_segment(S, items, probs, t_origin):
-    """Submits the requests at their arrival times (relative to the first),
-    returns the request ids in order."""
+def serve_segment(S, items, probs, saturate):
+    """Submits the requests, all at once (saturate) or at their seeded
+    arrival times relative to the first; returns the request ids in order."""
     ids = []
     a0 = items[0].arrival
     t0 = time.perf_counter()
     for it, p in zip(items, probs):
-        dt = (it.arrival - a0) - (time.perf_counter() - t0)
-        if dt > 0:
-            time.sleep(dt)
+        if not saturate:
+            dt = (it.arrival - a0) - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
         ids.append(S.submit(p))
     return ids
 
@@ -514,13 +547,7 @@ def run_serve(args, rank, world, local):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
     cfg = CONFIGS[args.config]
-    items = serve_stream(args.config)
-    if args.serve_requests:
-        items = items[: args.serve_requests]  # a prefix of the stream (profiling runs)
-    nseg = args.warmup + args.steps
-    seg = [items[(len(items) * k) // nseg:(len(items) * (k + 1)) // nseg] for k in range(nseg)]
-    warm_items = [it for sg in seg[:args.warmup] for it in sg]
-    timed_items = [it for sg in seg[args.warmup:] for it in sg]
+    items, warm_items, timed_items = stream_segments(args.config, args.warmup, args.steps, args.serve_requests)
     t_gen = time.perf_counter()
     warm_probs = gen_problems(warm_items)
     timed_probs = gen_problems(timed_items)
@@ -540,7 +567,7 @@ def run_serve(args, rank, world, local):
     for arm, mode in arms_run:
         with Server(ctx, mode=mode, budget_bytes=int(args.serve_budget) or cfg["budget"], profile_every=16,
                     max_inflight=args.max_inflight, size_groups=args.size_groups) as S:
-            wids = serve_segment(S, warm_items, warm_probs, 0.0)
+            wids = serve_segment(S, warm_items, warm_probs, cfg["saturate"])
             for i in wids:
                 S.wait(i)
                 S.release(i)
@@ -549,7 +576,7 @@ def run_serve(args, rank, world, local):
             barrier()
             with ClockSampler(local) as clk:
                 t0 = time.perf_counter()
-                ids = serve_segment(S, timed_items, timed_probs, t0)
+                ids = serve_segment(S, timed_items, timed_probs, cfg["saturate"])
                 S.drain()
                 barrier()
                 wall = time.perf_counter() - t0
@@ -583,6 +610,8 @@ def run_serve(args, rank, world, local):
             iters=[r["iterations"] for r in res], rel_true=max(r["rel_true"] for r in res),
             launches=st1["kernel_launches"] - st0["kernel_launches"], replays=st1["replays"] - st0["replays"],
             h2d=st1["h2d_bytes"] - st0["h2d_bytes"], d2h=st1["d2h_bytes"] - st0["d2h_bytes"],
+            backlog_frac=(st1["backlog_seconds"] - st0["backlog_seconds"]) / wall,
+            queued_frac=(st1["queued_seconds"] - st0["queued_seconds"]) / wall,
             peak_inflight=st1["peak_inflight"], peak_bytes=st1["peak_bytes"], budget=st1["budget_bytes"],
             busy=st1["busy_seconds"] - st0["busy_seconds"], prof=prof, clocks=clk.summary(),
             err_vs_plain=(max(err) if err else None),
@@ -620,8 +649,9 @@ def _cpu_serve_sample(args):
 
 
 def cpu_serve_rate(name, procs, per_proc, first=0):
-    """Solves/s of the reference algorithm on `procs` host cores, each solving
-    `per_proc` whole requests of the stream (requests first, first+1, ...)."""
+    """Solves/s of the reference algorithm on one host core over `per_proc`
+    whole requests of the stream (requests first, first+1, ...): requests
+    over summed solve seconds (the cpu_baseline leg of the GPU arm)."""
     import multiprocessing as mp
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
@@ -652,12 +682,15 @@ def compose_serve_line(args, world, cfg, items, timed_items, timed_probs, result
                 "max_true_rel_residual": r["rel_true"], "gpu_launches": int(r["launches"]),
                 "graph_replays": int(r["replays"]), "peak_inflight": int(r["peak_inflight"]),
                 "peak_device_bytes": int(r["peak_bytes"]),
+                "saturation": {"backlog_fraction": round(r["backlog_frac"], 4),
+                               "admission_queue_fraction": round(r["queued_frac"], 4)},
+                "error_vs_fp64_rel_l2_max": r["err_vs_plain"],
                 "kernels": {k: {"ms": round(v["ms"], 4), "gbs": round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1)
                                 if v["bytes"] > 0 and v["ms"] > 0 else None}
                             for k, v in sorted(r["prof"].items(), key=lambda kv: -kv[1]["ms"])}}
 
     arms = {arm: arm_summary(arm) for arm in results}
-    head = "mixed_fp32_factor" if "mixed_fp32_factor" in results else next(iter(results))
+    head = next((a for a in ("mixed_fp32_all", "mixed_fp32_factor") if a in results), next(iter(results)))
     hr = results[head]
     prof = hr["prof"]
     swept = {k: v for k, v in prof.items() if v["bytes"] > 0}
@@ -672,7 +705,6 @@ def compose_serve_line(args, world, cfg, items, timed_items, timed_probs, result
                 "launches_timed": int(v["n"])}
     value = arms[head]["value"]
     plain = arms.get("plain_fp64")
-    nreq = len(timed_items)
     line = {
         "metric": METRIC,
         "value": value,
@@ -684,24 +716,23 @@ def compose_serve_line(args, world, cfg, items, timed_items, timed_probs, result
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32 factor/sweeps, f64 SpMV/vectors/reductions",
+        "dtype": {"mixed_fp32_all": "f32 factor/sweeps/SpMV/Krylov vectors, f64 residual/dots/solution",
+                  "plain_fp64": "f64"}.get(head, "f32 factor/sweeps, f64 SpMV/vectors/reductions"),
         "data": "synthetic (seeded request stream: jittered meshes, log-normal coefficients)",
-        "config": {"workload": args.config, "requests": len(items), "requests_timed": nreq,
-                   "requests_per_step": round(nreq / steps, 1), "arrival_rate_per_s": cfg["rate"],
-                   "kinds": "2D Poisson / plane-strain elasticity 50:50" if cfg["dim"] == 2
-                   else "3D Poisson / elasticity 50:50",
-                   "dof_timed": int(sum(p.ndof for p in timed_probs)),
-                   "admission_budget_bytes": int(hr["budget"]), "tol": 1e-8,
-                   "stop": "true relative residual <= tol (every request, both arms)",
-                   "timing": "host clock around the timed stream, device synchronised at both ends",
-                   "l2": "in-flight working set (GBs of matrices, factors, vectors) far above the 129 MB L2; no flush",
-                   "parallelism": f"one server per GPU, x{world}", "max_inflight": args.max_inflight, "size_groups": args.size_groups,
-                   "generation_s": round(t_gen, 1)},
+        "config": serve_config(args, cfg, items, timed_items, timed_probs),
+        "serving": {"head_arm": head, "admission_budget_bytes": int(hr["budget"]),
+                    "timing": "host clock around the timed stream, device synchronised at both ends",
+                    "parallelism": f"one server per GPU, x{world}", "max_inflight": args.max_inflight,
+                    "size_groups": args.size_groups, "generation_s": round(t_gen, 1),
+                    "dof_timed": int(sum(p.ndof for p in timed_probs))},
         "p50_ms": arms[head]["p50_ms"],
         "p99_ms": arms[head]["p99_ms"],
         "plain_fp64": plain,
         "mixed_fp32_factor": arms.get("mixed_fp32_factor"),
+        "mixed_fp32_all": arms.get("mixed_fp32_all"),
         "mixed_over_plain": round(value / plain["value"], 3) if plain else None,
+        "mixed_over_plain_by_arm": {a: round(arms[a]["value"] / plain["value"], 3)
+                                    for a in arms if plain and a != "plain_fp64"},
         "error_vs_fp64_rel_l2_max": hr["err_vs_plain"],
         "roofline": roof,
         "gpu_launches": int(hr["launches"]),
@@ -753,31 +784,106 @@ def run_reference(args, rank, world):
     }
 
 
+def request_cost(it) -> float:
+    """Relative one-core cost of a stream request (for balancing the cores):
+    unknowns x block work x the ILU(0)-PCG iteration growth with size."""
+    from delfem_gb300 import meshgen as mg
+    if len(it.size) == 1:
+        n = float(it.size[0])
+        return n ** 1.5 * (3.5 if it.kind == mg.SOLID2D else 1.0)
+    n = float(it.size[0] * it.size[1] * it.size[2])
+    return n ** (4.0 / 3.0) * (9.0 if it.kind == mg.SOLID3D else 1.0)
+
+
+def lpt_assign(costs, procs):
+    """Longest-processing-time-first assignment of jobs to `procs` workers."""
+    import heapq
+    heap = [(0.0, j) for j in range(procs)]
+    out = [[] for _ in range(procs)]
+    for i in sorted(range(len(costs)), key=lambda i: -costs[i]):
+        load, j = heapq.heappop(heap)
+        out[j].append(i)
+        heapq.heappush(heap, (load + costs[i], j))
+    return out
+
+
+def _ref_serve_worker(name, warmup, steps, serve_requests, warm_idx, idx, barrier, q):
+    """One host core of the reference arm: builds its requests' problems
+    (untimed), solves one small warm-up request, meets the others at the
+    barrier, then solves its share of the timed requests whole."""
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    _, warm_items, timed_items = stream_segments(name, warmup, steps, serve_requests)
+    probs = [(i, timed_items[i].problem()) for i in idx]
+    for i in warm_idx:
+        O.solve(warm_items[i].problem())
+    barrier.wait()
+    out = []
+    for i, p in probs:
+        r = O.solve(p)
+        out.append((i, int(r["iter"]), bool(r["converged"]), time.perf_counter()))
+    q.put(out)
+
+
 def run_reference_serve(args, world, procs):
-    """The reference algorithm serving the stream's requests on all host
-    cores: each step, every core solves `--ref-requests-per-core` whole
-    requests (consecutive requests of the stream, a new set per step)."""
-    per = args.ref_requests_per_core
-    rates = []
+    """The reference algorithm serving the GPU arm's timed requests (the same
+    stream segments) on every host core: the requests are spread over the
+    cores by estimated cost (longest first), each core solves its share one
+    whole request after another (assembly, Dirichlet, ILU(0), PCG to 1e-8),
+    and the rate is requests over the wall clock from the moment all cores
+    start until the last finishes.  Problem generation happens before the
+    start."""
+    import multiprocessing as mp
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    cfg = CONFIGS[args.config]
+    items, warm_items, timed_items = stream_segments(args.config, args.warmup, args.steps, args.serve_requests)
+    if args.ref_sample_every > 1:
+        keep = list(range(0, len(timed_items), args.ref_sample_every))
+    else:
+        keep = list(range(len(timed_items)))
+    shares = lpt_assign([request_cost(timed_items[i]) for i in keep], procs)
+    shares = [[keep[k] for k in sh] for sh in shares]
+    smallest = sorted(range(len(warm_items)), key=lambda i: request_cost(warm_items[i]))
+    mpc = mp.get_context("spawn")
+    barrier = mpc.Barrier(procs + 1)
+    q = mpc.Queue()
     t_all0 = time.perf_counter()
-    for i in range(args.warmup + args.steps):
-        rate, times, wall = cpu_serve_rate(args.config, procs, per, first=i * procs * per)
-        if i >= args.warmup:
-            rates.append(rate)
-    value = statistics.median(rates)
+    ws = [mpc.Process(target=_ref_serve_worker,
+                      args=(args.config, args.warmup, args.steps, args.serve_requests,
+                            smallest[:1], shares[j], barrier, q))
+          for j in range(procs)]
+    for w in ws:
+        w.start()
+    barrier.wait()
+    t0 = time.perf_counter()
+    res = [q.get() for _ in ws]
+    for w in ws:
+        w.join()
+    done = [x for r in res for x in r]
+    t_end = max((x[3] for x in done), default=t0)
+    wall = max(t_end - t0, 1e-9)
+    if not all(x[2] for x in done):
+        raise RuntimeError("reference arm: a request did not converge")
+    n = len(done)
+    value = n / wall
     return {
         "metric": METRIC, "impl": "reference", "value": round(value, 4), "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded request stream)",
-        "config": {"workload": args.config, "tol": 1e-8,
-                   "parallelism": f"{procs} independent single-threaded solvers (one per host core)"},
-        "ms_per_step": round(1e3 * procs * per / value, 1),
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded request stream: jittered meshes, log-normal coefficients)",
+        "config": serve_config(args, cfg, items, timed_items, None),
+        "ms_per_step": round(1e3 * wall / args.steps, 1),
         "cpu_baseline": {"value": round(value, 4), "unit": "solves/s", "cores": procs, "kind": "port",
-                         "sample": f"per step {procs * per} whole requests of the stream ({per} per core), "
-                                   f"the reference algorithm's bit-exact C restatement; rate = cores x requests "
-                                   f"/ summed solve seconds"},
+                         "sample": (f"{n} of the {len(timed_items)} timed requests of the stream (every "
+                                    f"{max(args.ref_sample_every, 1)}), solved whole by the reference algorithm's "
+                                    f"bit-exact C restatement, {procs} cores (one single-threaded solver each, "
+                                    f"requests balanced by estimated cost); rate = requests / wall clock "
+                                    f"({wall:.1f} s)")},
         "e2e": {"value": round(value, 4), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": round(time.perf_counter() - t_all0, 1),
+        "iterations_median": int(_pct([x[1] for x in done], 0.5)) if done else None,
     }
 
 
@@ -802,8 +908,8 @@ def main():
                     help="single-solve workloads: ILU fill level (CPreconditioner_ILU::SetFillInLevel; -1 = no limit)")
     ap.add_argument("--max-inflight", type=int, default=128, help="serving: solves resident at once (<= 256)")
     ap.add_argument("--size-groups", type=int, default=0, help="serving: 1 table, 2-3 size groups, 0 = server default (3)")
-    ap.add_argument("--ref-requests-per-core", type=int, default=2,
-                    help="requests per host core per step of --impl reference (serving configs)")
+    ap.add_argument("--ref-sample-every", type=int, default=1,
+                    help="--impl reference, serving configs: solve every n-th timed request (1 = all of them)")
     ap.add_argument("--arms", default=",".join(sorted({a for a, _ in ARMS + SERVE_ARMS})),
                     help="comma-separated GPU arms to run (profiling runs pick one)")
     args = ap.parse_args()

@@ -131,7 +131,8 @@ class ServerCounters(ctypes.Structure):
     """dfg_server_counters"""
     _fields_ = [("submitted", _LL), ("finished", _LL), ("replays", _LL), ("kernel_launches", _LL),
                 ("graph_builds", _LL), ("peak_inflight", _LL), ("budget_bytes", _LL), ("peak_bytes", _LL),
-                ("h2d_bytes", _LL), ("d2h_bytes", _LL), ("busy_seconds", _D), ("now_seconds", _D)]
+                ("h2d_bytes", _LL), ("d2h_bytes", _LL), ("busy_seconds", _D), ("now_seconds", _D),
+                ("backlog_seconds", _D), ("queued_seconds", _D)]
 
 
 SERVER_NKERNELS = 24

@@ -256,8 +256,21 @@ struct dfg_server_s {
   // statistics
   long long replays = 0, launches = 0, peak_inflight = 0, graph_builds = 0;
   double busy_s = 0;
+  // occupancy of the queues ahead of the device, integrated over time (under mu):
+  // backlog = submitted and neither admitted nor finished; ready = set up and
+  // waiting for device memory or an in-flight slot
+  long long backlog = 0;
+  double t_acc = 0, backlog_s = 0, queued_s = 0;
 
   double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+  // brings the occupancy integrals up to now; called (under mu) before every
+  // change of `backlog` or `ready`
+  void account_locked() {
+    const double t = now();
+    if (backlog > 0) backlog_s += t - t_acc;
+    if (!ready.empty()) queued_s += t - t_acc;
+    t_acc = t;
+  }
 };
 
 namespace {
@@ -546,8 +559,10 @@ void symbolic_worker(dfg_server_s* S) {
       r->error = "host allocation failed during the symbolic set-up";
     }
     std::lock_guard<std::mutex> lk(S->mu);
+    S->account_locked();
     if (!ok) {
       r->status = DFG_INVALID_ARGUMENT;
+      --S->backlog;
       finish_locked(S, r);
       continue;
     }
@@ -555,10 +570,11 @@ void symbolic_worker(dfg_server_s* S) {
       r->status = DFG_OOM_REJECTED;
       r->error = "the request needs " + std::to_string(r->P.total + r->T.total) +
                  " device bytes, more than the whole admission budget";
+      --S->backlog;
       finish_locked(S, r);
       continue;
     }
-    S->ready[r->id] = r;
+    S->ready[r->id] = r;  // account_locked ran above, before this change
     S->cv_adm.notify_all();
   }
 }
@@ -572,6 +588,8 @@ void admission_thread(dfg_server_s* S) {
       for (;;) {
         if (S->fatal != DFG_OK) {
           // drain: everything not admitted fails with the fatal status
+          S->account_locked();
+          S->backlog -= (long long)S->ready.size();
           for (auto& kv : S->ready) {
             kv.second->status = S->fatal;
             kv.second->error = S->fatal_msg;
@@ -588,6 +606,8 @@ void admission_thread(dfg_server_s* S) {
               h->pbase = po;
               h->tbase = to;
               h->have_p = h->have_t = true;
+              S->account_locked();
+              --S->backlog;
               S->ready.erase(S->ready.begin());
               ++S->inflight;
               S->peak_inflight = std::max<long long>(S->peak_inflight, S->inflight);
@@ -1141,12 +1161,14 @@ extern "C" int dfg_server_submit(dfg_server s, const dfg_request* q, long long* 
   Req* raw = r.get();
   s->all[raw->id] = std::move(r);
   ++s->n_submitted;
+  s->account_locked();
   if (s->fatal != DFG_OK) {
     raw->status = s->fatal;
     raw->error = s->fatal_msg;
     finish_locked(s, raw);
     return DFG_OK;
   }
+  ++s->backlog;
   s->submitted.push_back(raw);
   s->cv_sym.notify_one();
   return DFG_OK;
@@ -1205,6 +1227,9 @@ extern "C" int dfg_server_stats(dfg_server s, dfg_server_counters* out) {
   out->h2d_bytes = s->h2d.load();
   out->d2h_bytes = s->d2h.load();
   out->busy_seconds = s->busy_s;
+  s->account_locked();
+  out->backlog_seconds = s->backlog_s;
+  out->queued_seconds = s->queued_s;
   out->now_seconds = s->now();
   return DFG_OK;
 }

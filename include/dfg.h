@@ -404,6 +404,9 @@ typedef struct {
   long long d2h_bytes;    /* solutions copied back */
   double busy_seconds;    /* loop-thread time with a replay in flight */
   double now_seconds;     /* on the clock of dfg_result's times */
+  double backlog_seconds; /* time with at least one request submitted and not yet admitted */
+  double queued_seconds;  /* time with at least one request set up and waiting for device
+                             memory or an in-flight slot (the device was full) */
 } dfg_server_counters;
 
 /* Per-kernel timing of profiled replays (dfg_server_config::profile_every):

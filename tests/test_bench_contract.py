@@ -35,6 +35,35 @@ def test_reference_arm_line():
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
 
 
+def test_reference_serving_arm_same_requests_wall_clock():
+    """The serving reference arm solves the GPU arm's timed requests (here a
+    4-request prefix of the stream: one timed request) and reports the same
+    workload config the GPU arm reports."""
+    r = _run("--impl", "reference", "--config", "serve2d", "--serve-requests", "4", "--steps", "1", "--warmup", "3")
+    assert r.returncode == 0, r.stderr[-3000:]
+    d = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][0])
+    assert d["impl"] == "reference" and d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 3
+    import bench
+    items, warm, timed = bench.stream_segments("serve2d", 3, 1, 4)
+    assert len(timed) == 1 and d["config"]["requests_timed"] == 1
+
+    class A:
+        config, steps = "serve2d", 1
+    ref_cfg = bench.serve_config(A, bench.CONFIGS["serve2d"], items, timed, None)
+    assert d["config"] == ref_cfg
+    assert "wall clock" in d["cpu_baseline"]["sample"] and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"]["value"] == d["value"]
+
+
+def test_lpt_assignment_balances():
+    import bench
+    costs = [10.0, 9.0, 8.0, 7.0, 6.0, 5.0, 4.0, 3.0, 2.0, 1.0]
+    shares = bench.lpt_assign(costs, 3)
+    assert sorted(i for sh in shares for i in sh) == list(range(10))
+    loads = [sum(costs[i] for i in sh) for sh in shares]
+    assert max(loads) - min(loads) <= max(costs)
+
+
 def test_gpu_arm_fails_loudly_without_a_gpu():
     import torch
     if torch.cuda.is_available():

@@ -31,7 +31,7 @@ def _rank(rank, world, port, q):
                rate=bench.whole_job_rate(100, wall, world))
 
     class Args:
-        config, steps, warmup, ref_requests_per_core, cpu_sample_iters = "serve2d", 1, 3, 1, 1
+        config, steps, warmup, ref_sample_every, serve_requests, cpu_sample_iters = "serve2d", 1, 3, 1, 4, 1
     if rank != 0:
         out["ref_line"] = bench.run_reference(Args, rank, world)   # rank > 0 does no work
     dist.barrier()
