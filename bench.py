@@ -478,7 +478,7 @@ def compose_line(args, world, p, results, prof, e2e, head):
 
 # ------------------------------------------------------------- serving arm
 
-SERVE_ARMS = [("plain_fp64", "fp64"), ("mixed_fp32_factor", "fp32f")]
+SERVE_ARMS = [("plain_fp64", "fp64"), ("mixed_fp32_factor", "fp32f"), ("mixed_fp32_all", "mixed")]
 
 
 def serve_stream(name):

@@ -27,6 +27,7 @@ SOURCES = {
     "sched.cpp": [],
     "meshio.cpp": ["-Xcompiler", "-ffp-contract=off"],
     "k_sweep.cu": [],
+    "k_solo.cu": [],
     "k_solve.cu": [],
     "k_bicg.cu": [],
     "k_level.cu": [],

@@ -112,7 +112,8 @@ SIGNATURES = {
 class ServerConfig(ctypes.Structure):
     """dfg_server_config"""
     _fields_ = [("mode", _I), ("tol", _D), ("maxit", _I), ("budget_bytes", _LL), ("max_inflight", _I),
-                ("chunk_iters", _I), ("host_threads", _I), ("profile_every", _I), ("size_groups", _I)]
+                ("chunk_iters", _I), ("host_threads", _I), ("profile_every", _I), ("size_groups", _I),
+                ("sweeps", _I)]
 
 
 class Request(ctypes.Structure):

@@ -973,8 +973,8 @@ SweepLaunch sweep_launch(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, bool fp32, c
     const FactorPattern F = factor_pattern(pr);
     L.levels = true;
     L.lev = &S.lev;
-    L.la = LevelSweepArgs{S.lev_rows.as<int>(), F.d_rowptr, F.d_colind, F.d_diaind,
-                          fp32 ? pr->fdiag32.p : pr->fdiag.p, fp32 ? pr->foffd32.p : pr->foffd.p, in, out, done};
+    L.la = LevelSweepArgs{S.lev_info.as<int4>(), F.d_colind, fp32 ? pr->fdiag32.p : pr->fdiag.p,
+                          fp32 ? pr->foffd32.p : pr->foffd.p, in, out, done, S.lev_G};
     return L;
   }
   SweepArgs& a = L.args;
@@ -1112,8 +1112,19 @@ void setup_sweep(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, const dfg_system sys
   // level-scheduled candidate
   if (mode != 1) {
     Levels V = build_levels(sys->n, F.rowptr, F.colind, F.diaind, forward);
+    // per position: the row and its entry range in this direction
+    std::vector<int4> info(std::max<size_t>(V.rows.size(), 1), make_int4(0, 0, 0, 0));
+    int widest = 0;
+    for (size_t k = 0; k < V.rows.size(); ++k) {
+      const int row = V.rows[k];
+      const int c0 = forward ? F.rowptr[row] : F.diaind[row];
+      const int c1 = forward ? F.diaind[row] : F.rowptr[row + 1];
+      info[k] = make_int4(row, c0, c1, 0);
+      widest = std::max(widest, c1 - c0);
+    }
+    const int G = level_group_lanes(widest);
     DBuf rows;
-    upload(ctx_, rows, V.rows.data(), std::max<size_t>(V.rows.size(), 1));
+    upload(ctx_, rows, info.data(), info.size());
     bool take = mode == 2 || V.ptr.size() <= 1;  // no rows: nothing to launch or time
     if (!take) {
       const size_t bs = (size_t)sys->b * sys->b;
@@ -1128,7 +1139,7 @@ void setup_sweep(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, const dfg_system sys
       L.b = sys->b;
       L.levels = true;
       L.lev = &V;
-      L.la = LevelSweepArgs{rows.as<int>(), F.d_rowptr, F.d_colind, F.d_diaind, zd.p, zo.p, vin.p, vout.p, nullptr};
+      L.la = LevelSweepArgs{rows.as<int4>(), F.d_colind, zd.p, zo.p, vin.p, vout.p, nullptr, G};
       GraphHolder g;
       CK(cudaStreamBeginCapture(ctx_->stream, cudaStreamCaptureModeThreadLocal));
       const cudaError_t ce = enqueue_sweep(L, ctx_->stream);
@@ -1144,7 +1155,8 @@ void setup_sweep(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, const dfg_system sys
     if (take) {
       S.levels = true;
       S.lev = std::move(V);
-      S.lev_rows = std::move(rows);
+      S.lev_info = std::move(rows);
+      S.lev_G = G;
       S.plan = SweepPlan{};
       return;
     }

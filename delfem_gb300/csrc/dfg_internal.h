@@ -78,6 +78,27 @@ inline long long rec_bytes(int nent, int bs, int sz, bool forward) {
 std::vector<unsigned char> pack_record_headers(const SweepPlan& P, int elem, std::vector<long long>& off,
                                                long long& max_rec);
 
+// Plan of one solve's sweep run by a single CTA (k_solo.cu): the SweepPlan
+// structure with one "range" per dependency level -- range_steps holds the
+// first step of each level, nranges the number of levels -- and steps of <= 32
+// rows of one level, in row order.  A dependency is a ring slot when its step
+// is among the R steps before the end of the consuming step's level (the
+// ring is never overwritten while that level runs), else a global row.
+SweepPlan solo_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind, bool forward,
+                          int R);
+
+// byte layout of one solo step record (k_solo.cu):
+//   [hdr 16][row 32*4][code nent*32*4][blk nent*32*bs*sz][dinv 32*bs*sz (forward only)]
+inline long long solo_rec_bytes(int nent, int bs, int sz, bool forward) {
+  return 16 + 128 + (long long)nent * 128 + (long long)nent * 32 * bs * sz + (forward ? 32LL * bs * sz : 0);
+}
+// Static parts of the solo step records (header, rows, codes) for element
+// size `elem`: code >= 0 is a byte offset into the CTA's ring region (0 = 32
+// zero bytes, for padding); code < 0 is -(row + 1) of a dependency read from
+// the output vector in global memory.
+std::vector<unsigned char> pack_solo_headers(const SweepPlan& P, int elem, std::vector<long long>& off,
+                                             long long& max_rec);
+
 // level sets of the triangular dependency DAG (rows sorted by level, then row)
 struct Levels {
   std::vector<int> level;   // per row
@@ -152,7 +173,8 @@ struct SweepDev {
   bool levels = false;
   float t_ranged = -1.f, t_levels = -1.f;  // set-up timings of the two kinds (ms; -1 = not timed)
   Levels lev;
-  DBuf lev_rows;
+  DBuf lev_info;   // level-scheduled: int4 {row, first entry, end entry, 0} per position
+  int lev_G = 4;   // level-scheduled: lanes per row
   // ranged: one packed record buffer per precision
   DBuf rec64, rec32;
   DBuf rec_off64, rec_off32;       // long long per step (+1)

@@ -1,5 +1,5 @@
 // k_level.cu -- level-scheduled triangular sweeps: one launch per dependency
-// level, one warp per row of the level.
+// level, a group of lanes per row of the level.
 //
 // CMatDiaFrac_BlkCrs::ForwardSubstitution / BackwardSubstitution
 // (src/matvec/matdiafrac_blkcrs.cpp:332-669) over the factor's block CRS,
@@ -14,25 +14,33 @@
 
 namespace dfg {
 
-// One warp per row: lane e takes the row's entries e, e+32, ..., so the
-// dependency and factor loads of a row are issued together; the partial sums
-// meet in a shuffle tree and lane 0 finishes the row.
+// G lanes per row (G a power of two, 4..32: the smallest that holds the
+// widest row of the sweep), 32/G rows per warp.  Lane k of a row's group
+// takes the row's entries k, k+G, ..., so the dependency and factor loads of
+// a row are issued together; the partial sums meet in an xor butterfly over
+// the group (every lane ends with the same totals) and lane p < B of the
+// group finishes component p of the row.  A row's position descriptor
+// {row, first entry, end entry} is one 16-byte load, so a row costs two
+// dependent loads (descriptor, then its entries' columns and blocks) before
+// the dependency values.
 template <typename T, int B, bool FWD>
 __global__ void __launch_bounds__(128) k_sweep_level(LevelSweepArgs a, int first, int cnt) {
   if (a.done && *a.done) return;
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (w >= cnt) return;
+  const int G = a.G;
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = gid / G, sub = gid & (G - 1);
+  const bool active = r < cnt;
   constexpr int BS = B * B;
   const T* __restrict__ in = reinterpret_cast<const T*>(a.in);
   T* out = reinterpret_cast<T*>(a.out);
   const T* __restrict__ fo = reinterpret_cast<const T*>(a.foffd);
-  const int i = a.rows[first + w];
-  const int c0 = FWD ? a.rowptr[i] : a.diaind[i];
-  const int c1 = FWD ? a.diaind[i] : a.rowptr[i + 1];
+  int4 inf = make_int4(0, 0, 0, 0);
+  if (active) inf = a.info[first + r];
+  const int i = inf.x, c0 = inf.y, c1 = inf.z;
   T part[B];
 #pragma unroll
   for (int p = 0; p < B; ++p) part[p] = 0;
-  for (int c = c0 + lane; c < c1; c += 32) {
+  for (int c = c0 + sub; c < c1; c += G) {
     const int j = a.colind[c];
     const T* blk = fo + (size_t)c * BS;
     T x[B];
@@ -43,33 +51,32 @@ __global__ void __launch_bounds__(128) k_sweep_level(LevelSweepArgs a, int first
 #pragma unroll
       for (int q = 0; q < B; ++q) part[p] += blk[p * B + q] * x[q];
   }
+  for (int o = G >> 1; o > 0; o >>= 1)
 #pragma unroll
-  for (int p = 0; p < B; ++p)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) part[p] += __shfl_xor_sync(0xffffffffu, part[p], o);
-  if (lane != 0) return;
+    for (int p = 0; p < B; ++p) part[p] += __shfl_xor_sync(0xffffffffu, part[p], o);
+  if (!active || sub >= B) return;
   T acc[B];
 #pragma unroll
   for (int p = 0; p < B; ++p) acc[p] = in[(size_t)i * B + p] - part[p];
+  T y = acc[0];
   if constexpr (FWD) {
-    const T* dv = reinterpret_cast<const T*>(a.fdiag) + (size_t)i * BS;
+    const T* dv = reinterpret_cast<const T*>(a.fdiag) + (size_t)i * BS + sub * B;
+    y = dv[0] * acc[0];
 #pragma unroll
-    for (int p = 0; p < B; ++p) {
-      T y = dv[p * B] * acc[0];
-#pragma unroll
-      for (int q = 1; q < B; ++q) y += dv[p * B + q] * acc[q];
-      out[(size_t)i * B + p] = y;
-    }
+    for (int q = 1; q < B; ++q) y += dv[q] * acc[q];
   } else {
 #pragma unroll
-    for (int p = 0; p < B; ++p) out[(size_t)i * B + p] = acc[p];
+    for (int p = 1; p < B; ++p)
+      if (sub == p) y = acc[p];
   }
+  out[(size_t)i * B + sub] = y;
 }
 
 cudaError_t launch_sweep_level(bool forward, bool fp32, int b, const LevelSweepArgs& a, int first, int cnt,
                                cudaStream_t s) {
   if (cnt <= 0) return cudaSuccess;
-  const unsigned grid = (unsigned)((cnt + 3) / 4);  // four rows (warps) per block
+  const long long lanes = (long long)cnt * a.G;
+  const unsigned grid = (unsigned)((lanes + 127) / 128);  // 128 threads per block
 #define DFG_LVL(T, B)                                                                  \
   (forward ? (k_sweep_level<T, B, true><<<grid, 128, 0, s>>>(a, first, cnt), 0)       \
            : (k_sweep_level<T, B, false><<<grid, 128, 0, s>>>(a, first, cnt), 0))

@@ -309,10 +309,226 @@ __global__ void k_srv_init_vectors(long long m, const double* rhs, double* r, do
   }
 }
 
-__global__ void k_srv_init_state(PcgState* st, const double* rr0p, double tol, int maxit) {
+// ------------------------------------------------------------ mixed form
+//
+// The loop of the single-solve mixed form (dfg_solve_pcg_mixed) on every
+// slot at once: FP32 recursion, FP64 reductions and correction, and reliable
+// updates (the FP64 true residual replaces the FP32 recursive one, the
+// search direction is kept) once the recursive residual has dropped by the
+// factor delta since the last update, or below the tolerance.  Updates fall
+// due inside a replay and are carried out at its end (srvm_fold,
+// srvm_refine); the stop is decided on the FP64 true residual only.
+
+__device__ __forceinline__ bool mixed_live(const PcgState* st) { return ld_relaxed_int(&st->done) == 0; }
+
+// rz_new = r.z (FP64 accumulation of FP32 products); beta = rz_new / rz
+__global__ void __launch_bounds__(kSrvTpb) k_srvm_rz_beta(const SrvTable* T, double* partials, int* tickets,
+                                                          int ntickets) {
+  if (blockIdx.x == 0 && threadIdx.x < ntickets) tickets[threadIdx.x] = 0;
+  const int nch = T->total_chunks;
+  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
+    const SrvSlot S = T->slot[find_slot(T, c)];
+    if (!mixed_live(S.st)) continue;
+    long long e0, e1;
+    chunk_elems(S, c, e0, e1);
+    const float* z = reinterpret_cast<const float*>(S.z);
+    double part = 0.0;
+    for (long long k = e0 + threadIdx.x; k < e1; k += kSrvTpb) part += (double)S.r32[k] * (double)z[k];
+    double tot;
+    if (slot_sum(part, c, S, partials, &tot) && threadIdx.x == 0) {
+      PcgState* st = S.st;
+      st->beta = (st->it == 0) ? 0.0 : tot / st->rz;
+      st->rz = tot;
+    }
+  }
+}
+
+// p := z in the first iteration, else p := z + beta p (FP32)
+__global__ void __launch_bounds__(kSrvTpb) k_srvm_update_p(const SrvTable* T) {
+  const int nch = T->total_chunks;
+  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
+    const SrvSlot S = T->slot[find_slot(T, c)];
+    if (!mixed_live(S.st)) continue;
+    long long e0, e1;
+    chunk_elems(S, c, e0, e1);
+    const bool first = S.st->it == 0;
+    const float beta = (float)S.st->beta;
+    const float* z = reinterpret_cast<const float*>(S.z);
+    for (long long k = e0 + threadIdx.x; k < e1; k += kSrvTpb) S.p32[k] = first ? z[k] : z[k] + beta * S.p32[k];
+  }
+}
+
+// q = A p on the FP32 values with FP32 accumulation; pAp in FP64; alpha
+template <int B>
+__device__ __forceinline__ double chunk_q_pap32(const SrvSlot& S, int row0, int row1) {
+  double part = 0.0;
+  for (int i = row0 + threadIdx.x; i < row1; i += kSrvTpb) {
+    float y[B];
+    sell_row_mv<float, B>(i, S.sptr, S.swidth, S.scol, S.sval32, S.p32, y);
+#pragma unroll
+    for (int d = 0; d < B; ++d) {
+      S.q32[(size_t)i * B + d] = y[d];
+      part += (double)S.p32[(size_t)i * B + d] * (double)y[d];
+    }
+  }
+  return part;
+}
+
+__global__ void __launch_bounds__(kSrvTpb) k_srvm_spmv_pap(const SrvTable* T, double* partials) {
+  const int nch = T->total_chunks;
+  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
+    const SrvSlot S = T->slot[find_slot(T, c)];
+    if (!mixed_live(S.st)) continue;
+    int row0, row1;
+    chunk_rows(S, c, row0, row1);
+    const double part = S.b == 1 ? chunk_q_pap32<1>(S, row0, row1)
+                        : S.b == 2 ? chunk_q_pap32<2>(S, row0, row1) : chunk_q_pap32<3>(S, row0, row1);
+    double tot;
+    if (slot_sum(part, c, S, partials, &tot) && threadIdx.x == 0) {
+      S.st->pap = tot;
+      S.st->alpha = S.st->rz / tot;
+    }
+  }
+}
+
+// r := r - alpha q (FP32); d := d + alpha p (FP64); rr = r.r (FP64); the
+// recursive stop (done 5: the true residual decides at the end of the replay),
+// the reliable-update trigger, the iteration limit; sweep outputs back to the
+// sentinel
+__global__ void __launch_bounds__(kSrvTpb) k_srvm_update_rx(const SrvTable* T, double* partials) {
+  const int nch = T->total_chunks;
+  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
+    const SrvSlot S = T->slot[find_slot(T, c)];
+    if (!mixed_live(S.st)) continue;
+    long long e0, e1;
+    chunk_elems(S, c, e0, e1);
+    const double alpha = S.st->alpha;
+    const float alpha32 = (float)alpha;
+    float* y = reinterpret_cast<float*>(S.y);
+    float* z = reinterpret_cast<float*>(S.z);
+    double part = 0.0;
+    for (long long k = e0 + threadIdx.x; k < e1; k += kSrvTpb) {
+      float r = S.r32[k];
+      if (alpha != 0.0) {
+        r = r - alpha32 * S.q32[k];
+        S.r32[k] = r;
+        S.d[k] = S.d[k] + alpha * (double)S.p32[k];
+      }
+      part += (double)r * (double)r;
+      y[k] = sentinel_value<float>();
+      z[k] = sentinel_value<float>();
+    }
+    double tot;
+    if (slot_sum(part, c, S, partials, &tot) && threadIdx.x == 0) {
+      PcgState* st = S.st;
+      st->rr = tot;
+      st->iter_out = st->it;
+      if (!(tot == tot)) {
+        st->done = 3;
+      } else if (tot * st->inv_rr0 < st->tol2) {
+        st->done = 5;
+      } else {
+        if (tot < st->delta2 * st->rr_ref) st->refine = 1;
+        if (st->it + 1 >= st->maxit) {
+          st->done = 2;
+          st->iter_out = st->maxit;
+        }
+      }
+      st->conv = sqrt(tot * st->inv_rr0);
+      st->it += 1;
+    }
+  }
+}
+
+__device__ __forceinline__ bool mixed_due(const PcgState* st) {
+  const int dn = ld_relaxed_int(&st->done);
+  return dn == 5 || (dn == 0 && ld_relaxed_int(&st->refine) != 0);
+}
+
+// x := x + d, d := 0 for slots due for a reliable update, stopped, or at
+// the end (limit, NaN)
+__global__ void __launch_bounds__(kSrvTpb) k_srvm_fold(const SrvTable* T) {
+  const int nch = T->total_chunks;
+  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
+    const SrvSlot S = T->slot[find_slot(T, c)];
+    const int dn = ld_relaxed_int(&S.st->done);
+    if (!(mixed_due(S.st) || dn == 2 || dn == 3)) continue;
+    long long e0, e1;
+    chunk_elems(S, c, e0, e1);
+    for (long long k = e0 + threadIdx.x; k < e1; k += kSrvTpb) {
+      S.x[k] = S.x[k] + S.d[k];
+      S.d[k] = 0.0;
+    }
+  }
+}
+
+// rd = b - A x with the FP64 values; r := rd (FP32); true-residual stop:
+// converged and verified, or the recursion continues from rd
+template <int B>
+__device__ __forceinline__ double chunk_refine(const SrvSlot& S, int row0, int row1) {
+  double part = 0.0;
+  for (int i = row0 + threadIdx.x; i < row1; i += kSrvTpb) {
+    double y[B];
+    sell_row_mv<double, B>(i, S.sptr, S.swidth, S.scol, S.sval, S.x, y);
+#pragma unroll
+    for (int d = 0; d < B; ++d) {
+      const double rv = S.rhs[(size_t)i * B + d] - y[d];
+      S.r32[(size_t)i * B + d] = (float)rv;
+      part += rv * rv;
+    }
+  }
+  return part;
+}
+
+__global__ void __launch_bounds__(kSrvTpb) k_srvm_refine(const SrvTable* T, double* partials) {
+  const int nch = T->total_chunks;
+  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
+    const SrvSlot S = T->slot[find_slot(T, c)];
+    if (!mixed_due(S.st)) continue;
+    int row0, row1;
+    chunk_rows(S, c, row0, row1);
+    const double part = S.b == 1 ? chunk_refine<1>(S, row0, row1)
+                        : S.b == 2 ? chunk_refine<2>(S, row0, row1) : chunk_refine<3>(S, row0, row1);
+    double tot;
+    if (slot_sum(part, c, S, partials, &tot) && threadIdx.x == 0) {
+      PcgState* st = S.st;
+      st->rr_true = tot;
+      st->refine = 0;
+      st->nreplace += 1;
+      if (tot * st->inv_rr0 <= st->tol2) {
+        st->done = 1;
+        st->verified = 1;
+      } else if (!(tot == tot)) {
+        st->done = 3;
+      } else if (st->it >= st->maxit) {
+        st->done = 2;
+        st->iter_out = st->maxit;
+      } else {
+        st->rr_ref = tot;
+        st->done = 0;
+      }
+    }
+  }
+}
+
+__global__ void k_srvm_init_vectors(long long m, const double* rhs, double* x, double* d, float* r32, float* p32,
+                                    float* y, float* z) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m; k += (long long)gridDim.x * blockDim.x) {
+    x[k] = 0.0;
+    d[k] = 0.0;
+    r32[k] = (float)rhs[k];
+    p32[k] = 0.0f;
+    y[k] = sentinel_value<float>();
+    z[k] = sentinel_value<float>();
+  }
+}
+
+__global__ void k_srv_init_state(PcgState* st, const double* rr0p, double tol, int maxit, double delta2) {
   const double rr0 = *rr0p;
   PcgState s{};
   s.rr0 = rr0;
+  s.rr_ref = rr0;
+  s.delta2 = delta2;
   s.tol2 = tol * tol;
   s.maxit = maxit;
   if (rr0 < 1.0e-30) {  // Solve_PCG returns at once; x = 0
@@ -373,8 +589,39 @@ cudaError_t srv_init_vectors(long long m, const double* rhs, double* r, double* 
   else k_srv_init_vectors<double><<<grid, 256, 0, s>>>(m, rhs, r, x, p, (double*)y, (double*)z, r32);
   return cudaGetLastError();
 }
-cudaError_t srv_init_state(PcgState* st, const double* rr0, double tol, int maxit, cudaStream_t s) {
-  k_srv_init_state<<<1, 1, 0, s>>>(st, rr0, tol, maxit);
+cudaError_t srv_init_state(PcgState* st, const double* rr0, double tol, int maxit, double delta2, cudaStream_t s) {
+  k_srv_init_state<<<1, 1, 0, s>>>(st, rr0, tol, maxit, delta2);
+  return cudaGetLastError();
+}
+cudaError_t srvm_rz_beta(const SrvTable* T, double* partials, int* tickets, int ntickets, int grid, cudaStream_t s) {
+  k_srvm_rz_beta<<<grid, kSrvTpb, 0, s>>>(T, partials, tickets, ntickets);
+  return cudaGetLastError();
+}
+cudaError_t srvm_update_p(const SrvTable* T, int grid, cudaStream_t s) {
+  k_srvm_update_p<<<grid, kSrvTpb, 0, s>>>(T);
+  return cudaGetLastError();
+}
+cudaError_t srvm_spmv_pap(const SrvTable* T, double* partials, int grid, cudaStream_t s) {
+  k_srvm_spmv_pap<<<grid, kSrvTpb, 0, s>>>(T, partials);
+  return cudaGetLastError();
+}
+cudaError_t srvm_update_rx(const SrvTable* T, double* partials, int grid, cudaStream_t s) {
+  k_srvm_update_rx<<<grid, kSrvTpb, 0, s>>>(T, partials);
+  return cudaGetLastError();
+}
+cudaError_t srvm_fold(const SrvTable* T, int grid, cudaStream_t s) {
+  k_srvm_fold<<<grid, kSrvTpb, 0, s>>>(T);
+  return cudaGetLastError();
+}
+cudaError_t srvm_refine(const SrvTable* T, double* partials, int grid, cudaStream_t s) {
+  k_srvm_refine<<<grid, kSrvTpb, 0, s>>>(T, partials);
+  return cudaGetLastError();
+}
+cudaError_t srvm_init_vectors(long long m, const double* rhs, double* x, double* d, float* r32, float* p32,
+                              float* y, float* z, cudaStream_t s) {
+  if (m == 0) return cudaSuccess;
+  const int grid = (int)std::min<long long>((m + 255) / 256, 1216);
+  k_srvm_init_vectors<<<grid, 256, 0, s>>>(m, rhs, x, d, r32, p32, y, z);
   return cudaGetLastError();
 }
 

@@ -30,9 +30,17 @@ struct SrvSlot {
   double* rd;           // true residual b - A x
   void* y;              // forward-sweep output (sweep precision)
   void* z;              // backward-sweep output
-  float* r32;           // FP32 sweep input (FP32 factor), else nullptr
+  float* r32;           // FP32 sweep input (FP32 factor), else nullptr; the
+                        // recursive residual itself in the mixed form
   PcgState* st;
   unsigned* cnt;        // reduction arrival counter (0 between launches)
+  // mixed form (DFG_PREC_MIXED) only, else nullptr: FP32 sliced-ELL values,
+  // FP32 direction and product, FP64 correction accumulated since the last
+  // reliable update
+  const float* sval32;
+  float* p32;
+  float* q32;
+  double* d;
 };
 
 struct SrvTable {
@@ -67,6 +75,29 @@ cudaError_t srv_collect(const SrvTable* T, SrvStatus* out, cudaStream_t s);
 // state from rr0 = r.r (computed by the caller into *rr0)
 cudaError_t srv_init_vectors(long long m, const double* rhs, double* r, double* x, double* p, void* y, void* z,
                              float* r32, bool fp32z, cudaStream_t s);
-cudaError_t srv_init_state(PcgState* st, const double* rr0, double tol, int maxit, cudaStream_t s);
+// delta2 > 0 (mixed form): a reliable update falls due once the recursive
+// residual norm^2 drops below delta2 times its value at the last update
+cudaError_t srv_init_state(PcgState* st, const double* rr0, double tol, int maxit, double delta2, cudaStream_t s);
+
+// ---- the mixed form (DFG_PREC_MIXED): FP32 SpMV on FP32-stored values with
+// FP32 accumulation, FP32 Krylov vectors r, p, q and preconditioned vectors;
+// FP64 for the dot reductions (alpha, beta, r.r), the solution x += d and the
+// reliable-update residual b - A x.  Each iteration: sweeps, srvm_rz_beta,
+// srvm_update_p, srvm_spmv_pap, srvm_update_rx; each replay ends with
+// srvm_fold and srvm_refine.
+cudaError_t srvm_rz_beta(const SrvTable* T, double* partials, int* tickets, int ntickets, int grid, cudaStream_t s);
+cudaError_t srvm_update_p(const SrvTable* T, int grid, cudaStream_t s);
+cudaError_t srvm_spmv_pap(const SrvTable* T, double* partials, int grid, cudaStream_t s);
+// r -= alpha q, d += alpha p, rr; the recursive stop (done = 5) and the
+// reliable-update trigger (refine = 1)
+cudaError_t srvm_update_rx(const SrvTable* T, double* partials, int grid, cudaStream_t s);
+// slots due for a reliable update or stopped: x += d, d = 0
+cudaError_t srvm_fold(const SrvTable* T, int grid, cudaStream_t s);
+// slots due for a reliable update or stopped on the recursion: r = b - A x in
+// FP64 (rounded to FP32 for the recursion) and the true-residual stop
+cudaError_t srvm_refine(const SrvTable* T, double* partials, int grid, cudaStream_t s);
+// admission: x = d = p = 0, r = rhs (FP32), sweep outputs = sentinel
+cudaError_t srvm_init_vectors(long long m, const double* rhs, double* x, double* d, float* r32, float* p32,
+                              float* y, float* z, cudaStream_t s);
 
 }  // namespace dfg

@@ -1,0 +1,305 @@
+// k_solo.cu -- batched forward / backward substitution of the block ILU(0)
+// factor (CMatDiaFrac_BlkCrs::ForwardSubstitution / BackwardSubstitution,
+// src/matvec/matdiafrac_blkcrs.cpp:332-669) with one CTA per solve.
+//
+// Serving keeps up to a few hundred independent solves in flight, so the
+// device is filled by solves, not by splitting one solve over SMs: a CTA
+// claims a whole solve and runs its sweep level after level (the dependency
+// levels of the reference's natural order, build_levels), so every
+// dependency was produced by the same CTA and no value crosses SMs.
+//
+// CTA: kSoloWarps compute warps + one producer warp.
+//   * producer -- walks the solve's steps (<= 32 rows of one level each) in
+//     order: one TMA bulk copy per packed step record (cp.async.bulk,
+//     completion on the stage's rec_full mbarrier with a byte count), then,
+//     once the record has landed, per-lane cp.async gathers of the rows'
+//     right-hand sides, arriving on the stage's `full` mbarrier when they
+//     complete; it runs up to NS steps ahead of the compute warps.
+//   * compute warps -- level by level: warp w takes steps first+w,
+//     first+w+kSoloWarps, ... of the level; per step it waits for `full`,
+//     evaluates its 32 rows, writes the results to the shared-memory ring
+//     (slot step mod R) and to the output vector, and releases the stage on
+//     `empty`; a named barrier over the compute warps closes each level.
+// A dependency is read from the ring when its step lies among the R steps
+// before the end of the consuming level (never overwritten before it is
+// read), else from the output vector in global memory (written at least one
+// level barrier earlier).  No sentinels, flags or fences between CTAs: nothing
+// is shared between CTAs but the ticket counter.  Every wait is bounded; a
+// wait that gives up records kErrTimeout and the launch drains and returns.
+//
+// Record layout (bytes; pack_solo_headers in sched.cpp, values by k_pack):
+//   [hdr int4: nent][row: 32 int][code: nent x 32 int]
+//   [blocks: nent x B*B x 32 of T][D^-1: B*B x 32 of T, forward only]
+// code >= 0: byte offset into the ring region (0 = 32 zero bytes, padding);
+// code < 0: -(row + 1) of a dependency in the output vector.
+#include "dfg_common.cuh"
+#include "k_mbar.cuh"
+#include "k_sweep.h"
+
+namespace dfg {
+
+template <typename T, int B, bool FWD, int MAXE>
+__global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
+  constexpr int BS = B * B;
+  constexpr int SZ = (int)sizeof(T);
+  constexpr int NW = kSoloWarps;
+  constexpr int VS = (B * 32 * SZ + 15) / 16 * 16;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int NS = a.NS;  // a power of two: stage = pos & NSM, phase = (pos >> NSL) & 1
+  const int NSM = NS - 1, NSL = __ffs(NS) - 1;
+  const int RM = a.R - 1;
+  // layout: [bars: 3*NS u64][rstage: NS x rec_stage][vstage: NS x VS][zero 32 B][ring: R x 32 x B of T]
+  uint64_t* rec_full = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* full = rec_full + NS;
+  uint64_t* empty = full + NS;
+  unsigned char* rstage = smem + (((size_t)3 * NS * 8 + 127) / 128) * 128;
+  unsigned char* vstage = rstage + (size_t)NS * a.rec_stage;
+  unsigned char* ringreg = vstage + (size_t)NS * VS;
+  __shared__ int s_slot, s_stop;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NS; ++s) {
+      mbar_init(&rec_full[s], 1);
+      mbar_init(&full[s], 64);  // 32 copy-completion arrivals + 32 producer-lane arrivals
+      mbar_init(&empty[s], 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (threadIdx.x < 8) reinterpret_cast<unsigned*>(ringreg)[threadIdx.x] = 0u;
+  __syncthreads();
+
+  int g = 0;  // steps this CTA has pushed through the pipeline (both sides count alike)
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int t = atomicAdd(a.ticket, 1);
+      int j = -1;
+      if (t < a.batch->nslots) j = ld_relaxed_int(a.batch->slot[t].done) ? -2 : t;
+      s_slot = j;
+    }
+    __syncthreads();
+    const int jslot = s_slot;
+    __syncthreads();
+    if (jslot == -1) break;
+    if (jslot == -2) continue;  // a finished solve
+    const SoloSlot& S = a.batch->slot[jslot];
+    const unsigned char* __restrict__ recs = S.rec;
+    const long long* __restrict__ rec_off = S.rec_off;
+    const int nst = S.nsteps;
+    bool abort = false;
+    if (warp == NW) {
+      // ------------------------------------------------------------ producer
+      const T* __restrict__ in = reinterpret_cast<const T*>(S.in);
+      int n_issued = 0, n_waited = 0;
+      auto issue_rec = [&](int i) {
+        const int pos = g + i;
+        const int st = pos & NSM;
+        const int use = pos >> NSL;
+        if (use >= 1 && !abort) {
+          if (!mbar_wait(&empty[st], (unsigned)((use - 1) & 1), a.err, kSiteEmpty, jslot, i)) abort = true;
+        }
+        if (abort) return;  // no new copies once the launch is failing
+        ++n_issued;
+        if (lane == 0) {
+          const long long o0 = rec_off[i], o1 = rec_off[i + 1];
+          mbar_expect_tx(&rec_full[st], (unsigned)(o1 - o0));
+          tma_load_1d(rstage + (size_t)st * a.rec_stage, recs + o0, (unsigned)(o1 - o0), &rec_full[st]);
+        }
+      };
+      const int LA = NS > 3 ? NS / 2 : 1;  // record copies run LA steps ahead of the gathers
+      for (int i = 0; i < LA && i < nst; ++i) issue_rec(i);
+      for (int i = 0; i < nst; ++i) {
+        if (i + LA < nst) issue_rec(i + LA);
+        const int pos = g + i;
+        const int st = pos & NSM;
+        if (!abort) {
+          if (mbar_wait(&rec_full[st], (unsigned)((pos >> NSL) & 1), a.err, kSiteRecLoad, jslot, i)) ++n_waited;
+          else abort = true;
+        }
+        const unsigned char* rec = rstage + (size_t)st * a.rec_stage;
+        const int row = reinterpret_cast<const int*>(rec + 16)[lane];
+        if (row >= 0 && !abort) {
+          T* rhs = reinterpret_cast<T*>(vstage + (size_t)st * VS) + lane * B;
+#pragma unroll
+          for (int d = 0; d < B; ++d) {
+            if constexpr (SZ == 8) cp_async8(rhs + d, &in[(size_t)row * B + d]);
+            else cp_async4(rhs + d, &in[(size_t)row * B + d]);
+          }
+        }
+        cp_async_arrive_noinc(&full[st]);
+        // release: the record this lane waited for is visible to whoever
+        // acquires `full`; a failing lane does not arrive, so the compute
+        // warps give up on the error word instead of reading a missing record
+        if (!abort) mbar_arrive(&full[st]);
+      }
+      if (abort && lane == 0) {  // record copies already issued land before the CTA moves on (bounded)
+        for (int k = n_waited; k < n_issued; ++k) {
+          const int pos = g + k;
+          mbar_drain(&rec_full[pos & NSM], (unsigned)((pos >> NSL) & 1));
+        }
+      }
+    } else {
+      // ------------------------------------------------------------- compute
+      T* out = reinterpret_cast<T*>(S.out);
+      const int* __restrict__ ls = S.lev_steps;
+      const int nl = S.nlevels;
+      // level bounds come one level ahead, so their load is off the critical path
+      int s0 = ls[0], s1 = nl > 0 ? ls[1] : 0;
+      for (int l = 0; l < nl; ++l) {
+        const int s2 = l + 2 <= nl ? __ldg(&ls[l + 2]) : 0;
+        for (int s = s0 + warp; s < s1; s += NW) {
+          const int pos = g + s;
+          const int st = pos & NSM;
+          if (!abort && !mbar_wait(&full[st], (unsigned)((pos >> NSL) & 1), a.err, kSiteFull, jslot, s)) abort = true;
+          const unsigned char* rec = rstage + (size_t)st * a.rec_stage;
+          const int nent = reinterpret_cast<const int*>(rec)[0];
+          const int row = reinterpret_cast<const int*>(rec + 16)[lane];
+          const int* code = reinterpret_cast<const int*>(rec + 144);
+          const T* blk = reinterpret_cast<const T*>(rec + 144 + nent * 128);
+          if (row >= 0 && !abort) {
+            const T* val = reinterpret_cast<const T*>(vstage + (size_t)st * VS);
+            T t[B];
+#pragma unroll
+            for (int d = 0; d < B; ++d) t[d] = val[lane * B + d];
+            if constexpr (MAXE > 0) {
+              // all dependency values first (independent loads), then the FMAs
+              T v[MAXE][B];
+#pragma unroll
+              for (int e = 0; e < MAXE; ++e) {
+                if (e < nent) {
+                  const int c = code[e * 32 + lane];
+                  if (c >= 0) {
+                    const T* vp = reinterpret_cast<const T*>(ringreg + c);
+#pragma unroll
+                    for (int d = 0; d < B; ++d) v[e][d] = vp[d];
+                  } else {
+                    const T* gp = out + (size_t)(-c - 1) * B;
+#pragma unroll
+                    for (int d = 0; d < B; ++d) v[e][d] = __ldcg(gp + d);
+                  }
+                }
+              }
+#pragma unroll
+              for (int e = 0; e < MAXE; ++e) {
+                if (e < nent) {
+#pragma unroll
+                  for (int p = 0; p < B; ++p) {
+                    T acc = t[p];
+#pragma unroll
+                    for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[e][q];
+                    t[p] = acc;
+                  }
+                }
+              }
+            } else {
+              for (int e = 0; e < nent; ++e) {
+                const int c = code[e * 32 + lane];
+                T v[B];
+                if (c >= 0) {
+                  const T* vp = reinterpret_cast<const T*>(ringreg + c);
+#pragma unroll
+                  for (int d = 0; d < B; ++d) v[d] = vp[d];
+                } else {
+                  const T* gp = out + (size_t)(-c - 1) * B;
+#pragma unroll
+                  for (int d = 0; d < B; ++d) v[d] = __ldcg(gp + d);
+                }
+#pragma unroll
+                for (int p = 0; p < B; ++p) {
+                  T acc = t[p];
+#pragma unroll
+                  for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[q];
+                  t[p] = acc;
+                }
+              }
+            }
+            T y[B];
+            if constexpr (FWD) {
+              const T* dinv = blk + nent * BS * 32;
+#pragma unroll
+              for (int p = 0; p < B; ++p) {
+                T acc = dinv[(p * B) * 32 + lane] * t[0];
+#pragma unroll
+                for (int q = 1; q < B; ++q) acc += dinv[(p * B + q) * 32 + lane] * t[q];
+                y[p] = acc;
+              }
+            } else {
+#pragma unroll
+              for (int p = 0; p < B; ++p) y[p] = t[p];
+            }
+            T* rg = reinterpret_cast<T*>(ringreg + 32) + (((s & RM) * 32 + lane) * B);
+#pragma unroll
+            for (int d = 0; d < B; ++d) {
+              rg[d] = y[d];
+              out[(size_t)row * B + d] = y[d];
+            }
+          }
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&empty[st]);
+        }
+        named_sync(1, NW * 32);
+        s0 = s1;
+        s1 = s2;
+      }
+    }
+    g += nst;
+    if (__any_sync(0xffffffffu, abort)) {
+      if (lane == 0) record_fail(a.err, kErrTimeout, kSiteRange, jslot, -1);
+    }
+    // one read of the error word decides for the whole CTA
+    __syncthreads();
+    if (threadIdx.x == 0) s_stop = ld_relaxed_int(a.err) != 0;
+    __syncthreads();
+    if (s_stop) break;
+  }
+  cp_async_wait_all();
+}
+
+// ------------------------------------------------------------------ launchers
+
+template <typename T, int B, bool FWD>
+static cudaError_t launch_e(const SoloArgs& a, int grid, size_t smem, cudaStream_t st) {
+  constexpr int NT = (kSoloWarps + 1) * 32;
+  if (a.max_nent <= 4) k_solo<T, B, FWD, 4><<<grid, NT, smem, st>>>(a);
+  else if (a.max_nent <= 8) k_solo<T, B, FWD, 8><<<grid, NT, smem, st>>>(a);
+  else k_solo<T, B, FWD, 0><<<grid, NT, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T, bool FWD>
+static cudaError_t launch_b(int B, const SoloArgs& a, int grid, size_t smem, cudaStream_t st) {
+  switch (B) {
+    case 1: return launch_e<T, 1, FWD>(a, grid, smem, st);
+    case 2: return launch_e<T, 2, FWD>(a, grid, smem, st);
+    case 3: return launch_e<T, 3, FWD>(a, grid, smem, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_solo(bool forward, bool fp32, int B, const SoloArgs& a, int grid, size_t smem, cudaStream_t st) {
+  if (fp32) return forward ? launch_b<float, true>(B, a, grid, smem, st) : launch_b<float, false>(B, a, grid, smem, st);
+  return forward ? launch_b<double, true>(B, a, grid, smem, st) : launch_b<double, false>(B, a, grid, smem, st);
+}
+
+template <typename T, int B, bool FWD>
+static cudaError_t set_attr(size_t max_smem) {
+  cudaError_t e = cudaFuncSetAttribute(k_solo<T, B, FWD, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_solo<T, B, FWD, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_solo<T, B, FWD, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+  return e;
+}
+
+cudaError_t solo_set_smem_limits(size_t max_smem) {
+  cudaError_t e = cudaSuccess;
+#define DFG_ATTR(T, B)                                        \
+  if (e == cudaSuccess) e = set_attr<T, B, true>(max_smem);   \
+  if (e == cudaSuccess) e = set_attr<T, B, false>(max_smem);
+  DFG_ATTR(double, 1) DFG_ATTR(double, 2) DFG_ATTR(double, 3)
+  DFG_ATTR(float, 1) DFG_ATTR(float, 2) DFG_ATTR(float, 3)
+#undef DFG_ATTR
+  return e;
+}
+
+}  // namespace dfg

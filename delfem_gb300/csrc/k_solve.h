@@ -15,7 +15,8 @@ struct PcgState {
   int it, maxit, done, iter_out;
   int verified;    // serving: the true residual met the tolerance
   int nreplace;    // serving: residual replacements so far
-  int pad[2];
+  int refine;      // serving, mixed: a reliable update is due at the end of the replay
+  int pad;
 };
 // done codes: 0 running, 1 converged, 2 iteration limit, 3 NaN,
 //             4 reliable update due (mixed), 5 recursive residual below tol (mixed)

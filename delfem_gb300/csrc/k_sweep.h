@@ -70,22 +70,64 @@ struct PackArgs {
   const int* step_rows;       // nsteps*32
   const double* fdiag;
   const double* foffd;
+  int code_bytes;             // bytes of dependency codes per entry: 256 ranged (code + row), 128 solo; 0 = 256
 };
 cudaError_t launch_pack(bool forward, bool fp32, int B, const PackArgs& a, cudaStream_t st);
+
+// Solo sweeps (k_solo.cu): a CTA owns one solve's whole sweep, level after
+// level (SweepPlan from solo_sweep_plan, records from pack_solo_headers).
+// Batched: a ticket claims the next solve of the batch, in batch order.
+struct SoloSlot {
+  const unsigned char* rec;
+  const long long* rec_off;
+  const int* lev_steps;   // nlevels + 1: first step of each level
+  int nlevels, nsteps;
+  const void* in;
+  void* out;
+  const int* done;        // the solve's state: nonzero = skip
+};
+struct SoloBatch {
+  int nslots;
+  SoloSlot slot[kSweepMaxSlots];
+};
+struct SoloArgs {
+  const SoloBatch* batch;
+  int* ticket;       // 0 at launch
+  int* err;          // device error word
+  int rec_stage;     // bytes per record stage (>= the largest record, 16-aligned)
+  int NS;            // pipeline stages (a power of two)
+  int R;             // ring depth in steps (a power of two)
+  int max_nent;      // selects the unrolled variant
+};
+// compute warps per CTA (plus one producer warp)
+constexpr int kSoloWarps = 8;
+inline int solo_val_stage(int B, int elem) { return (B * 32 * elem + 15) / 16 * 16; }
+inline size_t solo_smem_bytes(int NS, int rec_stage, int val_stage, int R, int B, int elem) {
+  return ((size_t)3 * NS * 8 + 127) / 128 * 128 + (size_t)NS * rec_stage + (size_t)NS * val_stage + 32 +
+         (size_t)R * 32 * B * elem;
+}
+cudaError_t launch_solo(bool forward, bool fp32, int B, const SoloArgs& a, int grid, size_t smem, cudaStream_t st);
+cudaError_t solo_set_smem_limits(size_t max_smem);
 
 // Level-scheduled sweep (k_level.cu): the factor in block CRS (values of
 // the sweep's type), rows listed level after level; one launch per level.
 struct LevelSweepArgs {
-  const int* rows;
-  const int* rowptr;
+  const int4* info;    // per position (rows level after level): {row, first entry, end entry, 0}
   const int* colind;
-  const int* diaind;
   const void* fdiag;   // D^-1 blocks (forward)
   const void* foffd;   // L | D^-1 U blocks
   const void* in;
   void* out;
   const int* done;     // nonzero: return at once
+  int G;               // lanes per row: level_group_lanes of the widest row
 };
+// lanes per row of the level-scheduled sweep: the smallest power of two that
+// holds `max_entries`, 4 to 32
+inline int level_group_lanes(int max_entries) {
+  int g = 4;
+  while (g < 32 && g < max_entries) g *= 2;
+  return g;
+}
 cudaError_t launch_sweep_level(bool forward, bool fp32, int b, const LevelSweepArgs& a, int first, int cnt,
                                cudaStream_t s);
 

@@ -379,6 +379,95 @@ std::vector<unsigned char> pack_record_headers(const SweepPlan& P, int elem, std
   return h;
 }
 
+SweepPlan solo_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind, bool forward,
+                          int R) {
+  SweepPlan P;
+  P.forward = forward;
+  P.n = n;
+  P.b = b;
+  P.R = R;
+  const Levels L = build_levels(n, rowptr, colind, diaind, forward);
+  const int nl = (int)L.ptr.size() - 1;
+  P.nranges = std::max(nl, 0);
+  P.range_steps.assign(P.nranges + 1, 0);
+  std::vector<int> row_step(n, 0), row_lane(n, 0);
+  for (int l = 0; l < nl; ++l) {
+    P.range_steps[l] = P.nsteps;
+    const int cnt = L.ptr[l + 1] - L.ptr[l];
+    for (int q = 0; q < cnt; ++q) {
+      const int row = L.rows[L.ptr[l] + q];
+      row_step[row] = P.nsteps + q / 32;
+      row_lane[row] = q % 32;
+    }
+    P.nsteps += (cnt + 31) / 32;
+  }
+  P.range_steps[P.nranges] = P.nsteps;
+  std::vector<int> step_level(P.nsteps, 0);
+  for (int l = 0; l < nl; ++l)
+    for (int s = P.range_steps[l]; s < P.range_steps[l + 1]; ++s) step_level[s] = l;
+  P.step_rows.assign((size_t)P.nsteps * 32, -1);
+  P.step_nent.assign(P.nsteps, 0);
+  for (int row = 0; row < n; ++row) {
+    P.step_rows[(size_t)row_step[row] * 32 + row_lane[row]] = row;
+    int c0, c1;
+    deps_of(row, forward, rowptr, diaind, c0, c1);
+    P.step_nent[row_step[row]] = std::max(P.step_nent[row_step[row]], c1 - c0);
+  }
+  P.ent_off.assign(P.nsteps + 1, 0);
+  for (int s = 0; s < P.nsteps; ++s) {
+    P.ent_off[s + 1] = P.ent_off[s] + P.step_nent[s];
+    P.max_nent = std::max(P.max_nent, P.step_nent[s]);
+  }
+  const long long nent_total = P.ent_off[P.nsteps];
+  P.ent_src.assign((size_t)nent_total * 32, SweepPlan::kSrcPad);
+  P.ent_slot.assign((size_t)nent_total * 32, -1);
+  for (int row = 0; row < n; ++row) {
+    const int s = row_step[row], lane = row_lane[row];
+    const int level_end = P.range_steps[step_level[s] + 1];
+    int c0, c1;
+    deps_of(row, forward, rowptr, diaind, c0, c1);
+    for (int c = c0; c < c1; ++c) {
+      const int k = colind[c];
+      const long long e = P.ent_off[s] + (c - c0);
+      const int sk = row_step[k];
+      P.ent_src[(size_t)e * 32 + lane] = (sk >= level_end - R) ? (sk % R) * 32 + row_lane[k] : -(k + 1);
+      P.ent_slot[(size_t)e * 32 + lane] = c;
+    }
+  }
+  P.est_cost = (double)P.nranges;
+  return P;
+}
+
+std::vector<unsigned char> pack_solo_headers(const SweepPlan& P, int elem, std::vector<long long>& off,
+                                             long long& max_rec) {
+  const int b = P.b, bs = b * b;
+  off.assign(P.nsteps + 1, 0);
+  max_rec = 0;
+  for (int s = 0; s < P.nsteps; ++s) {
+    const long long rb = solo_rec_bytes(P.step_nent[s], bs, elem, P.forward);
+    off[s + 1] = off[s] + rb;
+    max_rec = std::max(max_rec, rb);
+  }
+  std::vector<unsigned char> h((size_t)off[P.nsteps], 0);
+  for (int s = 0; s < P.nsteps; ++s) {
+    unsigned char* r = h.data() + off[s];
+    const int nent = P.step_nent[s];
+    std::memcpy(r, &nent, 4);
+    std::memcpy(r + 16, &P.step_rows[(size_t)s * 32], 128);
+    int* code = reinterpret_cast<int*>(r + 144);
+    for (int e = 0; e < nent; ++e)
+      for (int lane = 0; lane < 32; ++lane) {
+        const int src = P.ent_src[(size_t)(P.ent_off[s] + e) * 32 + lane];
+        int c = 0;
+        if (src == SweepPlan::kSrcPad) c = 0;
+        else if (src >= 0) c = 32 + src * b * elem;
+        else c = src;  // -(row + 1)
+        code[e * 32 + lane] = c;
+      }
+  }
+  return h;
+}
+
 bool build_gather_map(int n, const int* rowptr, const int* colind, int nelem, int nnoel,
                       const int* conn, GatherMap& G, std::string& err) {
   const long long nnz = rowptr[n];

@@ -57,6 +57,9 @@ constexpr int kClasses = 9;         // block size 1..3 x dependency entries <= 4
 constexpr int kMaxChunks = 1 << 20; // chunk space of one launch (kSrvRows rows each)
 constexpr int kRingSteps = 32;
 constexpr int kServeStages = 3;   // sweep pipeline depth in batched launches
+// mixed form: a reliable update falls due once the recursive residual norm
+// has dropped by 10x since the last one (delta 0.1, as dfg_solve_pcg_mixed)
+constexpr double kMixedDelta2 = 0.01;
 // Solves are iterated in groups of similar size, each with its own table and
 // graph on its own streams (dfg_server_config::size_groups): a batched sweep
 // lasts as long as the largest solve's dependency chain, so small solves that
@@ -163,12 +166,13 @@ struct Req {
   std::vector<long long> of, ob;
   long long maxrf = 0, maxrb = 0;
   int cls = -1, maxe = 0, group = 0;
+  bool solo = false;  // sweeps by one CTA per solve (k_solo.cu), else ranged (k_sweep.cu)
   // algorithmic bytes of one launch of each batched kernel for this solve:
   // 0 r.z, 1 p update, 2 SpMV, 3 r/x update, then forward and backward sweep
   double alg[6] = {};
   // device memory plan (offsets into the persistent / transient blocks)
   Layout P, T;
-  size_t o_sptr, o_swidth, o_scol, o_sval, o_rhs, o_r, o_x, o_p, o_q, o_rd, o_y, o_z, o_r32;
+  size_t o_sptr, o_swidth, o_scol, o_sval, o_sval32, o_rhs, o_r, o_x, o_p, o_q, o_rd, o_y, o_z, o_r32;
   size_t o_recf, o_offf, o_rsf, o_recb, o_offb, o_rsb, o_st, o_cnt;
   size_t t_rowptr, t_colind, t_diag, t_offd, t_ssrc;
   size_t t_coords, t_conn, t_coef, t_bc, t_load, t_em, t_er, t_sp, t_ss, t_rp, t_rs, t_dia, t_lev, t_fd, t_fo;
@@ -191,9 +195,11 @@ inline int class_b(int c) { return c / 3 + 1; }
 struct Group {
   SrvTable* d_tab = nullptr;
   SrvTable* h_tab = nullptr;       // pinned mirror
-  SweepBatch* d_sb = nullptr;      // kClasses x 2 (forward, backward)
+  SweepBatch* d_sb = nullptr;      // kClasses x 2 (forward, backward): ranged sweeps
   SweepBatch* h_sb = nullptr;
-  int* d_tickets = nullptr;        // kClasses x 2
+  SoloBatch* d_solo = nullptr;     // kClasses x 2: one-CTA-per-solve sweeps
+  SoloBatch* h_solo = nullptr;
+  int* d_tickets = nullptr;        // kClasses x 2 ranged, then kClasses x 2 solo
   double* d_partials = nullptr;    // kMaxChunks
   unsigned char* d_stat = nullptr; // SrvStatus[kSrvMaxSlots] then the error word
   unsigned char* h_stat = nullptr;
@@ -202,7 +208,7 @@ struct Group {
   cudaEvent_t ev_fork = nullptr, ev_done = nullptr, ev_join[kClasses] = {};
   cudaEvent_t ev_prof[2 * DFG_SERVER_NKERNELS] = {};
   cudaGraphExec_t exec = nullptr, exec_prof = nullptr;
-  int graph_mask = -1;
+  int graph_mask = -1;             // bits 0..8: ranged classes present; 9..17: solo classes
   std::vector<Req*> act;           // table order
   std::deque<Req*> incoming;       // admitted, waiting for a table slot (guarded by the server mutex)
   bool changed = false, in_flight = false, prof = false;
@@ -216,7 +222,8 @@ struct dfg_server_s {
   dfg_ctx ctx = nullptr;
   int device = 0, nsm = 0;
   int mode = DFG_PREC_FP32_FACTOR;
-  bool fp32 = true;
+  bool fp32 = true;    // FP32 factor and sweeps (both FP32 modes)
+  bool mixed = false;  // DFG_PREC_MIXED: FP32 SpMV and Krylov vectors too
   double tol = 1e-8;
   int maxit = 20000, max_inflight = 128, chunk = 8, nthreads = 4, ngroups = 1;
   int vec_grid = 0;
@@ -236,6 +243,10 @@ struct dfg_server_s {
   // per-class sweep launch shape
   int cls_grid[kClasses] = {}, cls_ns[kClasses][2] = {}, cls_rec_stage[kClasses][2] = {}, cls_val_stage[kClasses] = {};
   size_t cls_smem[kClasses][2] = {};
+  // per-class solo sweep shape: grid, stages, ring steps, record stage bytes, shared memory
+  int solo_grid[kClasses] = {}, solo_ns[kClasses][2] = {}, solo_R[kClasses] = {}, solo_rec_stage[kClasses][2] = {};
+  size_t solo_smem[kClasses][2] = {};
+  int sweeps = 0;  // dfg_server_config::sweeps
 
   // host state
   Clock::time_point t0;
@@ -277,6 +288,18 @@ namespace {
 
 // ---------------------------------------------------------------- symbolic
 
+// Which sweep kernel serves a solve.  FP32 sweeps run one CTA per solve
+// (k_solo.cu): a solve's whole dependency chain stays on one SM and the
+// in-flight solves fill the device.  FP64 sweeps stay ranged (k_sweep.cu):
+// GB300 issues about 1.6 FP64 FMA lanes per clock per SM, so a large
+// solve's FP64 sweep needs the FMA rate of many SMs.
+bool use_solo(const dfg_server_s* S, const Req* r) {
+  (void)r;
+  if (S->sweeps == 1) return false;
+  if (S->sweeps == 2) return true;
+  return S->fp32;
+}
+
 // Fills the request's host-side set-up; returns false with r->error on failure.
 bool symbolic(dfg_server_s* S, Req* r) {
   const int n = r->n;
@@ -297,39 +320,62 @@ bool symbolic(dfg_server_s* S, Req* r) {
   r->lev = build_levels(n, r->rowptr.data(), r->colind.data(), r->diaind.data(), true);
   r->sell = build_sell(n, r->rowptr.data(), r->colind.data());
   const int elem = S->fp32 ? 4 : 8;
-  r->pf = fullest_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), true, kRingSteps);
-  r->pb = fullest_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), false, kRingSteps);
-  r->maxe = std::max(r->pf.max_nent, r->pb.max_nent);
+  r->maxe = 0;
+  for (int i = 0; i < n; ++i)
+    r->maxe = std::max(r->maxe, std::max(r->diaind[i] - r->rowptr[i], r->rowptr[i + 1] - r->diaind[i]));
   if (r->maxe > 16) {
     r->error = "a row has more than 16 lower or upper neighbours; the serving sweeps take at most 16";
     return false;
   }
   r->cls = class_index(r->b, r->maxe);
   r->group = group_of((long long)n * r->b, S->ngroups);
-  r->hf = pack_record_headers(r->pf, elem, r->of, r->maxrf);
-  r->hb = pack_record_headers(r->pb, elem, r->ob, r->maxrb);
+  r->solo = use_solo(S, r);
+  if (r->solo) {
+    const int R = S->solo_R[r->cls];
+    r->pf = solo_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), true, R);
+    r->pb = solo_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), false, R);
+    r->hf = pack_solo_headers(r->pf, elem, r->of, r->maxrf);
+    r->hb = pack_solo_headers(r->pb, elem, r->ob, r->maxrb);
+  } else {
+    r->pf = fullest_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), true, kRingSteps);
+    r->pb = fullest_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), false, kRingSteps);
+    r->hf = pack_record_headers(r->pf, elem, r->of, r->maxrf);
+    r->hb = pack_record_headers(r->pb, elem, r->ob, r->maxrb);
+  }
 
   const size_t m = (size_t)n * r->b, bs = (size_t)r->b * r->b, Z = (size_t)std::max<long long>(r->nnz, 1);
+  const bool mixed = S->mixed;
   {
-    const double dm = (double)m, mat = (n + 1) * 4.0 + r->nnz * 4.0 + ((double)n + r->nnz) * bs * 8.0;
-    r->alg[0] = dm * (8 + elem);
-    r->alg[1] = dm * (16 + elem);
-    r->alg[2] = mat + dm * 16;  // values + CRS-equivalent indices + p read + q write
-    r->alg[3] = dm * (16 + 8 + 16 + 8 + 2 * elem + (S->fp32 ? 4 : 0));
+    const double dm = (double)m, idx = (n + 1) * 4.0 + r->nnz * 4.0, vals = ((double)n + r->nnz) * bs;
+    if (mixed) {
+      r->alg[0] = dm * 8;                      // r, z
+      r->alg[1] = dm * 12;                     // z, p read + write
+      r->alg[2] = idx + vals * 4 + dm * 8;     // FP32 values + indices + p read + q write
+      r->alg[3] = dm * (8 + 4 + 16 + 4 + 8);   // r r/w, q, d r/w, p, y/z sentinels
+    } else {
+      r->alg[0] = dm * (8 + elem);
+      r->alg[1] = dm * (16 + elem);
+      r->alg[2] = idx + vals * 8 + dm * 16;  // values + CRS-equivalent indices + p read + q write
+      r->alg[3] = dm * (16 + 8 + 16 + 8 + 2 * elem + (S->fp32 ? 4 : 0));
+    }
     r->alg[4] = (double)r->hf.size() + dm * 2 * elem;
     r->alg[5] = (double)r->hb.size() + dm * 2 * elem;
   }
   Layout& P = r->P;
   const size_t sblk = (size_t)std::max<long long>(r->sell.ptr.back(), 1);
+  // mixed form: FP32 values beside the FP64 ones (the reliable updates'
+  // b - A x), FP32 p and q, and d (the FP64 correction) in rd's place; the
+  // FP64 r is not kept
   r->o_sptr = P.add(r->sell.ptr.size() * 8);
   r->o_swidth = P.add(std::max<size_t>(r->sell.width.size(), 1) * 4);
   r->o_scol = P.add(sblk * 4);
   r->o_sval = P.add(sblk * bs * 8);
+  r->o_sval32 = P.add(mixed ? sblk * bs * 4 : 16);
   r->o_rhs = P.add(m * 8);
-  r->o_r = P.add(m * 8);
+  r->o_r = P.add(mixed ? 16 : m * 8);
   r->o_x = P.add(m * 8);
-  r->o_p = P.add(m * 8);
-  r->o_q = P.add(m * 8);
+  r->o_p = P.add(m * (mixed ? 4 : 8));
+  r->o_q = P.add(m * (mixed ? 4 : 8));
   r->o_rd = P.add(m * 8);
   r->o_y = P.add(m * elem + 64);
   r->o_z = P.add(m * elem + 64);
@@ -483,10 +529,16 @@ int admit_device(dfg_server_s* S, Req* r) {
     SCK(launch_ilu_level(b, at<int>(S, tb, r->t_lev) + r->lev.ptr[l], r->lev.ptr[l + 1] - r->lev.ptr[l],
                          bc.rowptr, bc.colind, at<int>(S, tb, r->t_dia), fd, fo, nsing, st));
   nl += nlev;
-  // the matrix into its sliced-ELL copy (the only copy that stays resident)
+  // the matrix into its sliced-ELL copy (the only copy that stays resident;
+  // the mixed form keeps an FP32 one beside it)
   SCK(sell_pack(r->sell.nslices, b, at<long long>(S, pb, r->o_sptr), at<int>(S, tb, r->t_ssrc), diag, offd,
                 at<void>(S, pb, r->o_sval), false, st));
   ++nl;
+  if (S->mixed) {
+    SCK(sell_pack(r->sell.nslices, b, at<long long>(S, pb, r->o_sptr), at<int>(S, tb, r->t_ssrc), diag, offd,
+                  at<void>(S, pb, r->o_sval32), true, st));
+    ++nl;
+  }
   // the factor into the step records
   for (int dir = 0; dir < 2; ++dir) {
     const SweepPlan& pl = dir == 0 ? r->pf : r->pb;
@@ -499,16 +551,21 @@ int admit_device(dfg_server_s* S, Req* r) {
     pa.step_rows = at<int>(S, tb, dir == 0 ? r->t_srf : r->t_srb);
     pa.fdiag = fd;
     pa.foffd = fo;
+    pa.code_bytes = r->solo ? 128 : 256;
     SCK(launch_pack(dir == 0, S->fp32, b, pa, st));
     ++nl;
   }
   // PCG start: r = b, x = 0, rr0 = r.r
-  SCK(srv_init_vectors(m, rhs, at<double>(S, pb, r->o_r), at<double>(S, pb, r->o_x), at<double>(S, pb, r->o_p),
-                       at<void>(S, pb, r->o_y), at<void>(S, pb, r->o_z),
-                       S->fp32 ? at<float>(S, pb, r->o_r32) : nullptr, S->fp32, st));
+  if (S->mixed)
+    SCK(srvm_init_vectors(m, rhs, at<double>(S, pb, r->o_x), at<double>(S, pb, r->o_rd), at<float>(S, pb, r->o_r32),
+                          at<float>(S, pb, r->o_p), at<float>(S, pb, r->o_y), at<float>(S, pb, r->o_z), st));
+  else
+    SCK(srv_init_vectors(m, rhs, at<double>(S, pb, r->o_r), at<double>(S, pb, r->o_x), at<double>(S, pb, r->o_p),
+                         at<void>(S, pb, r->o_y), at<void>(S, pb, r->o_z),
+                         S->fp32 ? at<float>(S, pb, r->o_r32) : nullptr, S->fp32, st));
   Red red{S->d_adm, reinterpret_cast<unsigned*>(S->d_adm + kRedGrid), S->d_adm + kRedGrid + 8};
   SCK(api_dot(m, rhs, rhs, red, st));
-  SCK(srv_init_state(at<PcgState>(S, pb, r->o_st), red.result, S->tol, S->maxit, st));
+  SCK(srv_init_state(at<PcgState>(S, pb, r->o_st), red.result, S->tol, S->maxit, S->mixed ? kMixedDelta2 : 0.0, st));
   nl += 3;
   SCK(cudaMemcpyAsync(S->h_nsing, nsing, sizeof(int), cudaMemcpyDeviceToHost, st));
   SCK(cudaStreamSynchronize(st));
@@ -675,6 +732,14 @@ SrvSlot slot_of(dfg_server_s* S, Req* r) {
   s.r32 = S->fp32 ? at<float>(S, pb, r->o_r32) : nullptr;
   s.st = at<PcgState>(S, pb, r->o_st);
   s.cnt = at<unsigned>(S, pb, r->o_cnt);
+  if (S->mixed) {
+    s.r = s.p = s.q = nullptr;
+    s.sval32 = at<float>(S, pb, r->o_sval32);
+    s.p32 = at<float>(S, pb, r->o_p);
+    s.q32 = at<float>(S, pb, r->o_q);
+    s.d = at<double>(S, pb, r->o_rd);
+    s.rd = nullptr;
+  }
   return s;
 }
 
@@ -700,9 +765,36 @@ int upload_table(dfg_server_s* S, Group& G) {
     for (int dir = 0; dir < 2; ++dir) {
       G.h_sb[k * 2 + dir].nslots = 0;
       G.h_sb[k * 2 + dir].range_start[0] = 0;
+      G.h_solo[k * 2 + dir].nslots = 0;
     }
+  // solo sweeps: largest solves first, so the last CTA to start has the
+  // least left to do
+  std::vector<int> solo_order;
+  for (int i = 0; i < (int)act.size(); ++i)
+    if (act[i]->solo) solo_order.push_back(i);
+  std::stable_sort(solo_order.begin(), solo_order.end(),
+                   [&](int x, int y) { return act[x]->pf.nsteps > act[y]->pf.nsteps; });
+  for (int i : solo_order) {
+    Req* r = act[i];
+    mask |= 1 << (kClasses + r->cls);
+    const SrvSlot& sl = T->slot[i];
+    for (int dir = 0; dir < 2; ++dir) {
+      SoloBatch& B = G.h_solo[r->cls * 2 + dir];
+      SoloSlot& w = B.slot[B.nslots++];
+      const SweepPlan& pl = dir == 0 ? r->pf : r->pb;
+      w.rec = at<unsigned char>(S, r->pbase, dir == 0 ? r->o_recf : r->o_recb);
+      w.rec_off = at<long long>(S, r->pbase, dir == 0 ? r->o_offf : r->o_offb);
+      w.lev_steps = at<int>(S, r->pbase, dir == 0 ? r->o_rsf : r->o_rsb);
+      w.nlevels = pl.nranges;
+      w.nsteps = pl.nsteps;
+      w.in = dir == 0 ? (S->fp32 ? (const void*)sl.r32 : (const void*)sl.r) : sl.y;
+      w.out = dir == 0 ? sl.y : sl.z;
+      w.done = &sl.st->done;
+    }
+  }
   for (int i = 0; i < (int)act.size(); ++i) {
     Req* r = act[i];
+    if (r->solo) continue;
     mask |= 1 << r->cls;
     for (int dir = 0; dir < 2; ++dir) {
       SweepBatch& B = G.h_sb[r->cls * 2 + dir];
@@ -723,6 +815,7 @@ int upload_table(dfg_server_s* S, Group& G) {
   const size_t tab_bytes = offsetof(SrvTable, slot) + sizeof(SrvSlot) * std::max<size_t>(act.size(), 1);
   SCK(cudaMemcpyAsync(G.d_tab, G.h_tab, tab_bytes, cudaMemcpyHostToDevice, G.s_iter));
   SCK(cudaMemcpyAsync(G.d_sb, G.h_sb, sizeof(SweepBatch) * kClasses * 2, cudaMemcpyHostToDevice, G.s_iter));
+  SCK(cudaMemcpyAsync(G.d_solo, G.h_solo, sizeof(SoloBatch) * kClasses * 2, cudaMemcpyHostToDevice, G.s_iter));
   return mask;
 }
 
@@ -735,6 +828,18 @@ SweepArgs class_args(dfg_server_s* S, Group& G, int k, int dir) {
   a.val_stage = S->cls_val_stage[k];
   a.R = kRingSteps;
   a.NS = S->cls_ns[k][dir];
+  a.max_nent = class_maxe(k);
+  return a;
+}
+
+SoloArgs solo_args(dfg_server_s* S, Group& G, int k, int dir) {
+  SoloArgs a{};
+  a.batch = G.d_solo + k * 2 + dir;
+  a.ticket = G.d_tickets + kClasses * 2 + k * 2 + dir;
+  a.err = reinterpret_cast<int*>(G.d_stat + sizeof(SrvStatus) * kSrvMaxSlots);
+  a.rec_stage = S->solo_rec_stage[k][dir];
+  a.NS = S->solo_ns[k][dir];
+  a.R = S->solo_R[k];
   a.max_nent = class_maxe(k);
   return a;
 }
@@ -770,36 +875,55 @@ cudaGraphExec_t capture_graph(dfg_server_s* S, Group& G, int mask, bool prof) {
     };
     SCK(cudaEventRecord(G.ev_fork, G.s_iter));
     for (int k = 0; k < kClasses; ++k) {
-      if (!(mask >> k & 1)) continue;
+      const bool ranged = mask >> k & 1, solo = mask >> (kClasses + k) & 1;
+      if (!ranged && !solo) continue;
       SCK(cudaStreamWaitEvent(G.s_side[k], G.ev_fork, 0));
       for (int dir = 0; dir < 2; ++dir) {
         mk(6 + 2 * k + dir, 0, G.s_side[k]);
-        SCK(launch_sweep(dir == 0, S->fp32, class_b(k), class_args(S, G, k, dir), S->cls_grid[k], S->cls_smem[k][dir],
-                         G.s_side[k]));
+        if (ranged)
+          SCK(launch_sweep(dir == 0, S->fp32, class_b(k), class_args(S, G, k, dir), S->cls_grid[k],
+                           S->cls_smem[k][dir], G.s_side[k]));
+        if (solo)
+          SCK(launch_solo(dir == 0, S->fp32, class_b(k), solo_args(S, G, k, dir), S->solo_grid[k],
+                          S->solo_smem[k][dir], G.s_side[k]));
         mk(6 + 2 * k + dir, 1, G.s_side[k]);
       }
       SCK(cudaEventRecord(G.ev_join[k], G.s_side[k]));
       SCK(cudaStreamWaitEvent(G.s_iter, G.ev_join[k], 0));
     }
     mk(0, 0, G.s_iter);
-    SCK(srv_rz_beta(G.d_tab, G.d_partials, G.d_tickets, kClasses * 2, S->fp32, grid, G.s_iter));
+    if (S->mixed) SCK(srvm_rz_beta(G.d_tab, G.d_partials, G.d_tickets, kClasses * 4, grid, G.s_iter));
+    else SCK(srv_rz_beta(G.d_tab, G.d_partials, G.d_tickets, kClasses * 4, S->fp32, grid, G.s_iter));
     mk(0, 1, G.s_iter);
     mk(1, 0, G.s_iter);
-    SCK(srv_update_p(G.d_tab, S->fp32, grid, G.s_iter));
+    if (S->mixed) SCK(srvm_update_p(G.d_tab, grid, G.s_iter));
+    else SCK(srv_update_p(G.d_tab, S->fp32, grid, G.s_iter));
     mk(1, 1, G.s_iter);
     mk(2, 0, G.s_iter);
-    SCK(srv_spmv_pap(G.d_tab, G.d_partials, grid, G.s_iter));
+    if (S->mixed) SCK(srvm_spmv_pap(G.d_tab, G.d_partials, grid, G.s_iter));
+    else SCK(srv_spmv_pap(G.d_tab, G.d_partials, grid, G.s_iter));
     mk(2, 1, G.s_iter);
     mk(3, 0, G.s_iter);
-    SCK(srv_update_rx(G.d_tab, G.d_partials, S->fp32, grid, G.s_iter));
+    if (S->mixed) SCK(srvm_update_rx(G.d_tab, G.d_partials, grid, G.s_iter));
+    else SCK(srv_update_rx(G.d_tab, G.d_partials, S->fp32, grid, G.s_iter));
     mk(3, 1, G.s_iter);
   }
-  mark(4, 0, G.s_iter);
-  SCK(srv_check_true(G.d_tab, G.d_partials, grid, G.s_iter));
-  mark(4, 1, G.s_iter);
-  mark(5, 0, G.s_iter);
-  SCK(srv_replace(G.d_tab, G.d_partials, S->fp32, grid, G.s_iter));
-  mark(5, 1, G.s_iter);
+  // end of the replay: true-residual checks (the mixed form: reliable updates)
+  if (S->mixed) {
+    mark(5, 0, G.s_iter);
+    SCK(srvm_fold(G.d_tab, grid, G.s_iter));
+    mark(5, 1, G.s_iter);
+    mark(4, 0, G.s_iter);
+    SCK(srvm_refine(G.d_tab, G.d_partials, grid, G.s_iter));
+    mark(4, 1, G.s_iter);
+  } else {
+    mark(4, 0, G.s_iter);
+    SCK(srv_check_true(G.d_tab, G.d_partials, grid, G.s_iter));
+    mark(4, 1, G.s_iter);
+    mark(5, 0, G.s_iter);
+    SCK(srv_replace(G.d_tab, G.d_partials, S->fp32, grid, G.s_iter));
+    mark(5, 1, G.s_iter);
+  }
   SCK(srv_collect(G.d_tab, reinterpret_cast<SrvStatus*>(G.d_stat), G.s_iter));
   SCK(cudaMemcpyAsync(G.h_stat, G.d_stat, sizeof(SrvStatus) * kSrvMaxSlots + 16, cudaMemcpyDeviceToHost, G.s_iter));
   guard.armed = false;
@@ -833,7 +957,8 @@ void account_profile(dfg_server_s* S, Group& G) {
   }
   std::lock_guard<std::mutex> lk(S->mu);
   for (int k = 0; k < DFG_SERVER_NKERNELS; ++k) {
-    if (k >= 6 && !((G.graph_mask >> ((k - 6) / 2)) & 1)) continue;
+    if (k >= 6 && !((G.graph_mask >> ((k - 6) / 2)) & 1) && !((G.graph_mask >> (kClasses + (k - 6) / 2)) & 1))
+      continue;
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, G.ev_prof[2 * k], G.ev_prof[2 * k + 1]) != cudaSuccess) {
       cudaGetLastError();
@@ -847,7 +972,7 @@ void account_profile(dfg_server_s* S, Group& G) {
 
 int kernels_per_replay(dfg_server_s* S, const Group& G) {
   int nc = 0;
-  for (int k = 0; k < kClasses; ++k) nc += (G.graph_mask >> k) & 1;
+  for (int k = 0; k < 2 * kClasses; ++k) nc += (G.graph_mask >> k) & 1;
   return S->chunk * (2 * nc + 4) + 3;
 }
 
@@ -886,7 +1011,7 @@ void harvest(dfg_server_s* S, Group& G, std::vector<Req*>& retiring) {
   G.act.swap(keep);
   if (err != 0) {
     SCK(cudaMemsetAsync(G.d_stat + sizeof(SrvStatus) * kSrvMaxSlots, 0, 16, G.s_iter));
-    SCK(cudaMemsetAsync(G.d_tickets, 0, sizeof(int) * kClasses * 2, G.s_iter));
+    SCK(cudaMemsetAsync(G.d_tickets, 0, sizeof(int) * kClasses * 4, G.s_iter));
     SCK(cudaStreamSynchronize(G.s_iter));
   }
 }
@@ -1026,6 +1151,37 @@ void class_shapes(dfg_server_s* S) {
     const int per_sm = std::max(1, std::min(16, (int)(per_sm_bytes / (worst + 1024))));
     S->cls_grid[k] = S->nsm * per_sm;
   }
+  // solo sweeps: the ring takes up to a third of a CTA's shared memory (a
+  // power of two of steps, at most 512), the record stages the rest (a power
+  // of two, 4 to 32 of them).  Rows with at most 4 lower or upper neighbours
+  // (triangle meshes: narrow levels, each depending on the one before) run
+  // two CTAs per SM; wider rows (tetrahedral meshes: levels of thousands of
+  // rows reaching two or three levels back) one CTA per SM with the larger
+  // ring.
+  for (int k = 0; k < kClasses; ++k) {
+    const int b = class_b(k), maxe = class_maxe(k);
+    const size_t budget = std::min<size_t>(S->ctx->smem_optin, (size_t)per_sm_bytes / (maxe <= 4 ? 2 : 1)) - 2048;
+    const size_t step_ring = (size_t)32 * b * elem;
+    int R = 512;
+    while (R > 16 && (size_t)R * step_ring > budget / 3) R /= 2;
+    S->solo_R[k] = R;
+    const int vs = solo_val_stage(b, elem);
+    size_t worst = 0;
+    for (int dir = 0; dir < 2; ++dir) {
+      const int rs = (int)((solo_rec_bytes(maxe, b * b, elem, dir == 0) + 15) / 16 * 16);
+      S->solo_rec_stage[k][dir] = rs;
+      const size_t fixed = solo_smem_bytes(0, rs, vs, R, b, elem) + 3 * 8 * 32;
+      const int fit = (int)std::min<size_t>(32, (budget - std::min(budget, fixed)) / (size_t)(rs + vs));
+      int ns = 4;
+      while (ns * 2 <= fit) ns *= 2;  // a power of two
+      S->solo_ns[k][dir] = ns;
+      S->solo_smem[k][dir] = solo_smem_bytes(ns, rs, vs, R, b, elem);
+      worst = std::max(worst, S->solo_smem[k][dir]);
+    }
+    const int per_sm = std::max(1, std::min(2, (int)(per_sm_bytes / (worst + 1024))));
+    S->solo_grid[k] = S->nsm * per_sm;
+    if (worst > S->ctx->smem_optin) throw CudaFail{cudaErrorInvalidValue, "solo sweep shared memory"};
+  }
 }
 
 int server_error(dfg_ctx ctx, int status, const std::string& m) {
@@ -1040,10 +1196,12 @@ int server_error(dfg_ctx ctx, int status, const std::string& m) {
 extern "C" int dfg_server_create(dfg_ctx ctx, const dfg_server_config* cfg, dfg_server* out) {
   if (!ctx || !cfg || !out) return DFG_INVALID_ARGUMENT;
   *out = nullptr;
-  if (cfg->mode != DFG_PREC_FP64 && cfg->mode != DFG_PREC_FP32_FACTOR)
-    return server_error(ctx, DFG_INVALID_ARGUMENT, "serving modes: DFG_PREC_FP64 or DFG_PREC_FP32_FACTOR");
+  if (cfg->mode != DFG_PREC_FP64 && cfg->mode != DFG_PREC_FP32_FACTOR && cfg->mode != DFG_PREC_MIXED)
+    return server_error(ctx, DFG_INVALID_ARGUMENT,
+                        "serving modes: DFG_PREC_FP64, DFG_PREC_FP32_FACTOR or DFG_PREC_MIXED");
   if (cfg->max_inflight < 0 || cfg->max_inflight > kSrvMaxSlots || cfg->chunk_iters < 0 || cfg->chunk_iters > 64 ||
-      !(cfg->tol > 0.0) || cfg->maxit < 0 || cfg->budget_bytes < 0 || cfg->size_groups < 0 || cfg->size_groups > kGroups)
+      !(cfg->tol > 0.0) || cfg->maxit < 0 || cfg->budget_bytes < 0 || cfg->size_groups < 0 || cfg->size_groups > kGroups ||
+      cfg->sweeps < 0 || cfg->sweeps > 2)
     return server_error(ctx, DFG_INVALID_ARGUMENT, "server configuration out of range");
   std::unique_ptr<dfg_server_s> S(new (std::nothrow) dfg_server_s);
   if (!S) return DFG_OOM_REJECTED;
@@ -1051,7 +1209,8 @@ extern "C" int dfg_server_create(dfg_ctx ctx, const dfg_server_config* cfg, dfg_
   S->device = ctx->device;
   S->nsm = ctx->nsm;
   S->mode = cfg->mode;
-  S->fp32 = cfg->mode == DFG_PREC_FP32_FACTOR;
+  S->fp32 = cfg->mode != DFG_PREC_FP64;
+  S->mixed = cfg->mode == DFG_PREC_MIXED;
   S->tol = cfg->tol;
   S->maxit = cfg->maxit > 0 ? cfg->maxit : 20000;
   S->max_inflight = cfg->max_inflight > 0 ? cfg->max_inflight : 128;
@@ -1061,6 +1220,7 @@ extern "C" int dfg_server_create(dfg_ctx ctx, const dfg_server_config* cfg, dfg_
   S->vec_grid = S->nsm * 4;
   S->profile_every = std::max(0, cfg->profile_every);
   S->ngroups = cfg->size_groups > 0 ? cfg->size_groups : kGroups;
+  S->sweeps = cfg->sweeps;
   S->t0 = Clock::now();
   try {
     SCK(cudaSetDevice(S->device));
@@ -1084,17 +1244,21 @@ extern "C" int dfg_server_create(dfg_ctx ctx, const dfg_server_config* cfg, dfg_
       Group& G = S->grp[g];
       SCK(cudaMalloc(&G.d_tab, sizeof(SrvTable)));
       SCK(cudaMalloc(&G.d_sb, sizeof(SweepBatch) * kClasses * 2));
-      SCK(cudaMalloc(&G.d_tickets, sizeof(int) * kClasses * 2));
+      SCK(cudaMalloc(&G.d_solo, sizeof(SoloBatch) * kClasses * 2));
+      SCK(cudaMalloc(&G.d_tickets, sizeof(int) * kClasses * 4));
       SCK(cudaMalloc(&G.d_partials, sizeof(double) * kMaxChunks));
       SCK(cudaMalloc(&G.d_stat, sizeof(SrvStatus) * kSrvMaxSlots + 64));
-      SCK(cudaMemset(G.d_tickets, 0, sizeof(int) * kClasses * 2));
+      SCK(cudaMemset(G.d_tickets, 0, sizeof(int) * kClasses * 4));
+      SCK(cudaMemset(G.d_solo, 0, sizeof(SoloBatch) * kClasses * 2));
       SCK(cudaMemset(G.d_stat, 0, sizeof(SrvStatus) * kSrvMaxSlots + 64));
       SCK(cudaMemset(G.d_sb, 0, sizeof(SweepBatch) * kClasses * 2));
       SCK(cudaHostAlloc(&G.h_tab, sizeof(SrvTable), cudaHostAllocDefault));
       SCK(cudaHostAlloc(&G.h_sb, sizeof(SweepBatch) * kClasses * 2, cudaHostAllocDefault));
+      SCK(cudaHostAlloc(&G.h_solo, sizeof(SoloBatch) * kClasses * 2, cudaHostAllocDefault));
       SCK(cudaHostAlloc(&G.h_stat, sizeof(SrvStatus) * kSrvMaxSlots + 64, cudaHostAllocDefault));
       std::memset(G.h_tab, 0, sizeof(SrvTable));
       std::memset(G.h_sb, 0, sizeof(SweepBatch) * kClasses * 2);
+      std::memset(G.h_solo, 0, sizeof(SoloBatch) * kClasses * 2);
       std::memset(G.h_stat, 0, sizeof(SrvStatus) * kSrvMaxSlots + 64);
       SCK(cudaStreamCreateWithPriority(&G.s_iter, cudaStreamNonBlocking, hi));
       for (int k = 0; k < kClasses; ++k) {
@@ -1107,6 +1271,7 @@ extern "C" int dfg_server_create(dfg_ctx ctx, const dfg_server_config* cfg, dfg_
         for (int k = 0; k < 2 * DFG_SERVER_NKERNELS; ++k) SCK(cudaEventCreate(&G.ev_prof[k]));
     }
     SCK(sweep_set_smem_limits(ctx->smem_optin));
+    SCK(solo_set_smem_limits(ctx->smem_optin));
     class_shapes(S.get());
   } catch (const CudaFail& f) {
     cudaGetLastError();
@@ -1282,9 +1447,10 @@ extern "C" int dfg_server_destroy(dfg_server s) {
     for (cudaEvent_t e : {G.ev_fork, G.ev_done})
       if (e) cudaEventDestroy(e);
     if (G.s_iter) cudaStreamDestroy(G.s_iter);
-    for (void* p : {(void*)G.d_tab, (void*)G.d_sb, (void*)G.d_tickets, (void*)G.d_partials, (void*)G.d_stat})
+    for (void* p : {(void*)G.d_tab, (void*)G.d_sb, (void*)G.d_solo, (void*)G.d_tickets, (void*)G.d_partials,
+                    (void*)G.d_stat})
       if (p) cudaFree(p);
-    for (void* p : {(void*)G.h_tab, (void*)G.h_sb, (void*)G.h_stat})
+    for (void* p : {(void*)G.h_tab, (void*)G.h_sb, (void*)G.h_solo, (void*)G.h_stat})
       if (p) cudaFreeHost(p);
   }
   for (cudaStream_t st : {s->s_adm, s->s_copy})

@@ -17,7 +17,7 @@ from . import capi
 from . import meshgen as mg
 from .capi import check, lib
 
-MODES = {"fp64": capi.DFG_PREC_FP64, "fp32f": capi.DFG_PREC_FP32_FACTOR}
+MODES = {"fp64": capi.DFG_PREC_FP64, "fp32f": capi.DFG_PREC_FP32_FACTOR, "mixed": capi.DFG_PREC_MIXED}
 
 
 def _ptr(a):
@@ -27,10 +27,10 @@ def _ptr(a):
 class Server:
     def __init__(self, ctx, mode: str = "fp32f", tol: float = 1e-8, maxit: int = 20000, budget_bytes: int = 0,
                  max_inflight: int = 128, chunk_iters: int = 8, host_threads: int = 0, profile_every: int = 0,
-                 size_groups: int = 0):
+                 size_groups: int = 0, sweeps: int = 0):
         self.ctx = ctx
         cfg = capi.ServerConfig(MODES[mode], tol, maxit, budget_bytes, max_inflight, chunk_iters, host_threads,
-                                profile_every, size_groups)
+                                profile_every, size_groups, sweeps)
         h = ctypes.c_void_p()
         check(ctx.h, lib().dfg_server_create(ctx.h, ctypes.byref(cfg), ctypes.byref(h)), "dfg_server_create")
         self.h = h

@@ -356,7 +356,9 @@ int dfg_true_residual(dfg_system sys, const double* b, double* rel);
 typedef struct dfg_server_s* dfg_server;
 
 typedef struct {
-  int mode;               /* DFG_PREC_FP64 or DFG_PREC_FP32_FACTOR */
+  int mode;               /* DFG_PREC_FP64, DFG_PREC_FP32_FACTOR, or DFG_PREC_MIXED (FP32 SpMV on
+                             FP32-stored values, FP32 Krylov vectors, FP32 factor and sweeps; FP64
+                             dot reductions, solution and reliable-update residual b - A x) */
   double tol;             /* true relative residual target */
   int maxit;              /* iteration limit per solve; 0 = 20000 */
   long long budget_bytes; /* device bytes reserved for admitted solves; 0 = 85% of free memory */
@@ -366,6 +368,9 @@ typedef struct {
   int profile_every;      /* every n-th replay times its first iteration per kernel; 0 = never */
   int size_groups;        /* solves grouped by size, each group iterating at its own pace on its own
                              streams: 1 = one table for all, 2-3 groups; 0 = 3 */
+  int sweeps;             /* triangular-sweep kernel: 0 = by precision (FP32 sweeps one CTA per solve,
+                             FP64 sweeps ranged over several CTAs), 1 = ranged, 2 = one CTA per solve;
+                             the results agree to rounding */
 } dfg_server_config;
 
 /* kind: 1 Poisson 2D (P1 triangles), 2 Poisson 3D (P1 tetrahedra),

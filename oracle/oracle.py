@@ -288,3 +288,38 @@ def run_reference_harness(p, fill_level: int = 0, solver: str = "pcg") -> dict:
         mg.write_problem(p, fi)
         subprocess.run([HARNESS, fi, fo, str(fill_level), solver], check=True, stdout=subprocess.DEVNULL)
         return mg.read_result(fo)
+
+
+def make_problem(spec: tuple):
+    """A generated problem from a picklable spec: ("factory", kwargs) names a
+    meshgen problem factory; ("stream2d" | "stream3d", kwargs with `index`)
+    one request of a serving stream."""
+    from delfem_gb300 import meshgen as mg
+    name, kw = spec
+    kw = dict(kw)
+    if name in ("stream2d", "stream3d"):
+        idx = kw.pop("index")
+        items = mg.serve_stream_2d(**kw) if name == "stream2d" else mg.serve_stream_3d(**kw)
+        return items[idx].problem()
+    return getattr(mg, name)(**kw)
+
+
+def solve_digest(spec: tuple, fill_level: int = 0) -> dict:
+    """solve() on make_problem(spec), returning SHA-256 digests of the large
+    arrays (pattern as int32, assembled matrix, finalized right-hand side,
+    ILU factor) with the iteration count, ratio and solution vector: for
+    parity tests at sizes where hashing the arrays costs less than shipping
+    them between processes.  Runs in a spawned worker."""
+    import hashlib
+
+    def h(a, dtype):
+        return hashlib.sha256(np.ascontiguousarray(a, dtype=dtype).tobytes()).hexdigest()
+
+    p = make_problem(spec)
+    t0 = lib().dfo_now()
+    out = solve(p, fill_level=fill_level)
+    return dict(rowptr=h(out["rowptr"], np.int32), colind=h(out["colind"], np.int32),
+                diag=h(out["diag"], np.float64), offd=h(out["offd"], np.float64), rhs=h(out["rhs"], np.float64),
+                fdiag=h(out["fdiag"], np.float64), foffd=h(out["foffd"], np.float64), ilu_rc=int(out["ilu_rc"]),
+                iter=int(out["iter"]), conv=float(out["conv"]), converged=bool(out["converged"]), x=out["x"],
+                true_rel=true_residual(out, out["x"]), seconds=lib().dfo_now() - t0)

@@ -230,10 +230,11 @@ extern "C" long long emul_ilu_pattern(int n, const int* rowptr, const int* colin
 // level, every dependency of a row lies in an earlier level and a row's level
 // is one above its deepest dependency (the longest-path levels, so no launch
 // is wasted).  Each row is computed as k_sweep_level computes it: lane l of
-// the row's warp sums entries l, l+32, ... in order, the 32 partials meet in
-// the xor-butterfly, and lane 0 finishes the row.  Rows of later levels are
-// NaN until written, so a read ahead of the schedule shows in the result.
-// info[0] = number of levels, info[1] = widest level, info[2] = error code.
+// the row's group of G lanes sums entries l, l+G, ... in order, the G
+// partials meet in the xor butterfly, and the group's lanes finish the row's
+// components.  Rows of later levels are NaN until written, so a read ahead
+// of the schedule shows in the result.  info[0] = number of levels,
+// info[1] = widest level, info[2] = error code, info[3] = G.
 extern "C" int emul_level_sweep(int n, int b, const int* rowptr, const int* colind, int forward, const double* fdiag,
                                 const double* foffd, const double* in, double* out, long long* info) {
   std::vector<int> diaind(n);
@@ -260,6 +261,11 @@ extern "C" int emul_level_sweep(int n, int b, const int* rowptr, const int* coli
     }
   }
   const int bs = b * b;
+  int widest = 0;
+  for (int i = 0; i < n; ++i)
+    widest = std::max(widest, forward ? diaind[i] - rowptr[i] : rowptr[i + 1] - diaind[i]);
+  const int G = level_group_lanes(widest);  // lanes per row, as the library launches the kernel
+  info[3] = G;
   for (int i = 0; i < n * b; ++i) out[i] = NAN;
   for (int l = 0; l < nl; ++l) {
     for (int k = V.ptr[l]; k < V.ptr[l + 1]; ++k) {
@@ -270,15 +276,15 @@ extern "C" int emul_level_sweep(int n, int b, const int* rowptr, const int* coli
       for (int c = c0; c < c1; ++c) deepest = std::max(deepest, V.level[colind[c]]);
       if (deepest >= l || deepest + 1 != l) return fail(4);
       double part[32][3] = {};
-      for (int lane = 0; lane < 32; ++lane)
-        for (int c = c0 + lane; c < c1; c += 32) {
+      for (int lane = 0; lane < G; ++lane)
+        for (int c = c0 + lane; c < c1; c += G) {
           const double* blk = foffd + (size_t)c * bs;
           for (int p = 0; p < b; ++p)
             for (int q = 0; q < b; ++q) part[lane][p] += blk[p * b + q] * out[(size_t)colind[c] * b + q];
         }
-      for (int o = 16; o > 0; o >>= 1) {
+      for (int o = G / 2; o > 0; o >>= 1) {
         double nxt[32][3];
-        for (int lane = 0; lane < 32; ++lane)
+        for (int lane = 0; lane < G; ++lane)
           for (int p = 0; p < b; ++p) nxt[lane][p] = part[lane][p] + part[lane ^ o][p];
         std::memcpy(part, nxt, sizeof(part));
       }
@@ -297,5 +303,121 @@ extern "C" int emul_level_sweep(int n, int b, const int* rowptr, const int* coli
   }
   for (int i = 0; i < n * b; ++i)
     if (std::isnan(out[i])) return fail(5);
+  return 0;
+}
+
+// Executes the one-CTA-per-solve schedule (solo_sweep_plan + the record codes
+// of pack_solo_headers) the way k_solo.cu does: levels in order, the steps of
+// a level concurrently (each reads the ring and the output as they stood when
+// the level began), every step writing its ring slot (step mod R) and the
+// output.  Checks: every row once; a ring code decodes to the slot its
+// dependency was written to, that slot is not rewritten by any step of the
+// consuming level (the kernel's warps run a level's steps in any order), and
+// holds the dependency's row; a global code names a row finished in an
+// earlier level.  out receives the result (the kernel's summation order).
+extern "C" int emul_solo_sweep(int n, int b, const int* rowptr, const int* colind, int forward, int R, int elem,
+                               const double* fdiag, const double* foffd, const double* rhs, double* out,
+                               long long* info) {
+  std::vector<int> diaind(n);
+  for (int i = 0; i < n; ++i) {
+    int d = rowptr[i + 1];
+    for (int c = rowptr[i]; c < rowptr[i + 1]; ++c)
+      if (colind[c] > i) { d = c; break; }
+    diaind[i] = d;
+  }
+  SweepPlan P = solo_sweep_plan(n, b, rowptr, colind, diaind.data(), forward != 0, R);
+  std::vector<long long> off;
+  long long max_rec = 0;
+  const std::vector<unsigned char> h = pack_solo_headers(P, elem, off, max_rec);
+  const int bs = b * b;
+  info[0] = P.nranges;  // levels
+  info[1] = P.nsteps;
+  info[2] = P.max_nent;
+  info[3] = 0;
+  info[4] = 0;          // ring references
+  info[5] = 0;          // global references
+  info[6] = max_rec;
+  std::vector<int> seen(n, 0), level_of(n, -1);
+  for (int l = 0; l < P.nranges; ++l)
+    for (int s = P.range_steps[l]; s < P.range_steps[l + 1]; ++s)
+      for (int ln = 0; ln < 32; ++ln) {
+        const int row = P.step_rows[(size_t)s * 32 + ln];
+        if (row >= 0) { seen[row]++; level_of[row] = l; }
+      }
+  for (int i = 0; i < n; ++i)
+    if (seen[i] != 1) { info[3] = 1; return 1; }
+  std::vector<int> ring_row((size_t)R * 32, -1);
+  std::vector<double> ring((size_t)R * 32 * b, NAN);
+  std::vector<char> done(n, 0);
+  std::vector<char> written_now(R, 0);
+  for (int l = 0; l < P.nranges; ++l) {
+    std::fill(written_now.begin(), written_now.end(), 0);
+    for (int s = P.range_steps[l]; s < P.range_steps[l + 1]; ++s) written_now[s % R] = 1;
+    struct W { int row; double y[3]; int slot; };
+    std::vector<W> writes;
+    for (int s = P.range_steps[l]; s < P.range_steps[l + 1]; ++s) {
+      const unsigned char* rec = h.data() + off[s];
+      int nent = 0;
+      std::memcpy(&nent, rec, 4);
+      if (nent != P.step_nent[s]) { info[3] = 2; return 2; }
+      const int* rows = reinterpret_cast<const int*>(rec + 16);
+      const int* code = reinterpret_cast<const int*>(rec + 144);
+      for (int ln = 0; ln < 32; ++ln) {
+        const int row = rows[ln];
+        if (row != P.step_rows[(size_t)s * 32 + ln]) { info[3] = 3; return 3; }
+        if (row < 0) continue;
+        const int c0 = forward ? rowptr[row] : diaind[row];
+        const int c1 = forward ? diaind[row] : rowptr[row + 1];
+        double t[3];
+        for (int d = 0; d < b; ++d) t[d] = rhs[(size_t)row * b + d];
+        for (int e = 0; e < nent; ++e) {
+          const int c = code[e * 32 + ln];
+          if (e >= c1 - c0) {
+            if (c != 0) { info[3] = 4; return 4; }
+            continue;
+          }
+          const int k = colind[c0 + e];
+          double v[3];
+          if (c >= 0) {
+            if (c < 32 || (c - 32) % (b * elem) != 0) { info[3] = 5; return 5; }
+            const int idx = (c - 32) / (b * elem);
+            if (idx >= R * 32 || ring_row[idx] != k || written_now[idx / 32]) { info[3] = 6; return 6; }
+            for (int d = 0; d < b; ++d) v[d] = ring[(size_t)idx * b + d];
+            info[4]++;
+          } else {
+            if (-c - 1 != k || !done[k] || level_of[k] >= l) { info[3] = 7; return 7; }
+            for (int d = 0; d < b; ++d) v[d] = out[(size_t)k * b + d];
+            info[5]++;
+          }
+          const double* blk = foffd + (size_t)(c0 + e) * bs;
+          for (int p = 0; p < b; ++p) {
+            double acc = t[p];
+            for (int q = 0; q < b; ++q) acc -= blk[p * b + q] * v[q];
+            t[p] = acc;
+          }
+        }
+        W w{row, {0, 0, 0}, (s % R) * 32 + ln};
+        if (forward) {
+          const double* dv = fdiag + (size_t)row * bs;
+          for (int p = 0; p < b; ++p) {
+            double acc = dv[p * b] * t[0];
+            for (int q = 1; q < b; ++q) acc += dv[p * b + q] * t[q];
+            w.y[p] = acc;
+          }
+        } else {
+          for (int p = 0; p < b; ++p) w.y[p] = t[p];
+        }
+        writes.push_back(w);
+      }
+    }
+    for (const W& w : writes) {
+      for (int d = 0; d < b; ++d) {
+        out[(size_t)w.row * b + d] = w.y[d];
+        ring[(size_t)w.slot * b + d] = w.y[d];
+      }
+      ring_row[w.slot] = w.row;
+      done[w.row] = 1;
+    }
+  }
   return 0;
 }

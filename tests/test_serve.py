@@ -1,4 +1,6 @@
-"""Serving path (dfg_server_*) against the CPU oracle.
+"""Serving path (dfg_server_*) against the CPU oracle, in the three modes:
+plain FP64, FP32 factor ("fp32f") and the mixed form ("mixed": FP32 SpMV and
+Krylov vectors with FP64 reliable updates).
 
 Bars, per request:
   * status OK and true relative residual ||b - A x|| / ||b|| <= 1e-8 (the
@@ -30,7 +32,7 @@ def _serve(ctx, probs, **kw):
     return res, stats
 
 
-@pytest.mark.parametrize("mode", ["fp64", "fp32f"])
+@pytest.mark.parametrize("mode", ["fp64", "fp32f", "mixed"])
 def test_serve_matches_oracle(gpu_ctx, oracle_lib, mode):
     probs = _stream(10, seed=11)
     res, stats = _serve(gpu_ctx, probs, mode=mode, chunk_iters=4)
@@ -45,11 +47,12 @@ def test_serve_matches_oracle(gpu_ctx, oracle_lib, mode):
             assert ref["iter"] - 2 <= r["iterations"] <= ref["iter"] + 8, (p.name, r["iterations"], ref["iter"])
 
 
-def test_serve_alone_equals_in_mix(gpu_ctx):
+@pytest.mark.parametrize("mode", ["fp32f", "mixed"])
+def test_serve_alone_equals_in_mix(gpu_ctx, mode):
     probs = _stream(8, seed=12)
-    mix, _ = _serve(gpu_ctx, probs, mode="fp32f")
+    mix, _ = _serve(gpu_ctx, probs, mode=mode)
     for k in (0, 5):
-        alone, _ = _serve(gpu_ctx, [probs[k]], mode="fp32f")
+        alone, _ = _serve(gpu_ctx, [probs[k]], mode=mode)
         assert alone[0]["status"] == 0
         assert np.array_equal(bits(alone[0]["x"]), bits(mix[k]["x"])), k
         assert alone[0]["iterations"] == mix[k]["iterations"]
@@ -82,11 +85,30 @@ def test_serve_size_groups_same_results(gpu_ctx):
         assert np.array_equal(bits(a["x"]), bits(b["x"])) and a["iterations"] == b["iterations"]
 
 
+@pytest.mark.parametrize("mode", ["fp64", "fp32f", "mixed"])
+def test_serve_sweep_kernels_agree(gpu_ctx, oracle_lib, mode):
+    """The two batched sweep kernels -- ranged over several CTAs and one CTA
+    per solve -- evaluate each row with the same operations in the same order,
+    so a served solve gives the same bits with either; both meet the oracle
+    bars (2D and 3D kinds, sizes across the stream's range)."""
+    from delfem_gb300 import meshgen as mg
+    probs = _stream(5, seed=15, nmin=300, nmax=40000) + [
+        mg.box_problem_3d(mg.POISSON3D, 9, 8, 7, seed=4), mg.box_problem_3d(mg.SOLID3D, 6, 7, 5, seed=5)]
+    ranged, _ = _serve(gpu_ctx, probs, mode=mode, sweeps=1)
+    solo, _ = _serve(gpu_ctx, probs, mode=mode, sweeps=2)
+    for p, a, c in zip(probs, ranged, solo):
+        assert a["status"] == 0 and c["status"] == 0, (p.name, a, c)
+        assert c["rel_true"] <= 1e-8
+        assert np.array_equal(bits(a["x"]), bits(c["x"])) and a["iterations"] == c["iterations"], p.name
+        xr = oracle_lib.solve(p)["x"]
+        assert np.linalg.norm(c["x"] - xr) <= 1e-6 * np.linalg.norm(xr), p.name
+
+
 def test_serve_3d_kinds(gpu_ctx, oracle_lib):
     from delfem_gb300 import meshgen as mg
     probs = [mg.box_problem_3d(mg.POISSON3D, 6, 7, 8, seed=1), mg.box_problem_3d(mg.SOLID3D, 5, 6, 7, seed=2),
              mg.rect_problem_2d(mg.SOLID2D, 900, seed=3)]
-    for mode in ("fp64", "fp32f"):
+    for mode in ("fp64", "fp32f", "mixed"):
         res, _ = _serve(gpu_ctx, probs, mode=mode)
         for p, r in zip(probs, res):
             assert r["status"] == 0 and r["rel_true"] <= 1e-8, (mode, p.name, r)
@@ -105,4 +127,9 @@ def test_serve_zero_rhs_and_iteration_limit(gpu_ctx):
     assert res[0]["status"] == 0 and res[0]["iterations"] == 0 and not np.any(res[0]["x"])
     p1 = mg.rect_problem_2d(mg.SOLID2D, 2000, seed=10)
     res, _ = _serve(gpu_ctx, [p1], mode="fp64", maxit=3)
+    assert res[0]["status"] == capi.DFG_NOT_CONVERGED and res[0]["iterations"] == 3
+    # the mixed form: the same zero right-hand side and limit semantics
+    res, _ = _serve(gpu_ctx, [p0], mode="mixed")
+    assert res[0]["status"] == 0 and res[0]["iterations"] == 0 and not np.any(res[0]["x"])
+    res, _ = _serve(gpu_ctx, [p1], mode="mixed", maxit=3)
     assert res[0]["status"] == capi.DFG_NOT_CONVERGED and res[0]["iterations"] == 3
