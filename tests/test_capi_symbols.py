@@ -82,7 +82,7 @@ static const entry_fn entry_points[] = {{
 
 int main(void) {{
   /* the positional initializers documented for the server */
-  dfg_server_config cfg = {{DFG_PREC_FP32_FACTOR, 1e-8, 20000, 0, 128, 8, 0, 0, 0}};
+  dfg_server_config cfg = {{DFG_PREC_FP32_FACTOR, 1e-8, 20000, 0, 128, 8, 0, 0, 0, 0}};
   dfg_request q = {{4, 0, 0, NULL, NULL, NULL, NULL, 5, NULL, NULL, NULL}};
   size_t i;
   int nd = 0, nn = 0, nv = 0, ne = 0;
