@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/dfg.h"
+#include "k_sweep.h"
 
 namespace dfg {
 
@@ -81,23 +82,36 @@ std::vector<unsigned char> pack_record_headers(const SweepPlan& P, int elem, std
 // Plan of one solve's sweep run by a single CTA (k_solo.cu): the SweepPlan
 // structure with one "range" per dependency level -- range_steps holds the
 // first step of each level, nranges the number of levels -- and steps of <= 32
-// rows of one level, in row order.  A dependency is a ring slot when its step
-// is among the R steps before the end of the consuming step's level (the
-// ring is never overwritten while that level runs), else a global row.
-SweepPlan solo_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind, bool forward,
-                          int R);
+// rows of one level, in row order.  The steps of a level are cut into chunks
+// (at most `ch_max` steps and `stage_bytes` of records each, elem-byte
+// values), the unit the kernel copies into shared memory; every step of a
+// chunk carries the chunk's largest entry count (padding entries zero), so a
+// chunk's records all have one size.  A dependency is a ring slot when its
+// step is among the R steps before the end of the consuming step's level
+// (the ring is never overwritten while that level runs), else a global read.
+struct SoloPlan {
+  SweepPlan P;                      // steps, padded entries (ent_off / ent_src / ent_slot)
+  std::vector<SoloChunk> chunks;
+  std::vector<int> lev_chunks;      // nlevels + 1: first chunk of each level
+  std::vector<int> pos;             // per row: step * 32 + lane (its slot in step order)
+};
+SoloPlan solo_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind, bool forward,
+                         int R, int elem, int stage_bytes, int ch_max);
 
 // byte layout of one solo step record (k_solo.cu):
-//   [hdr 16][row 32*4][code nent*32*4][blk nent*32*bs*sz][dinv 32*bs*sz (forward only)]
+//   [hdr int4: nent, chunk steps, step, 0][out: 32 int][code nent*32*4][blk nent*32*bs*sz][dinv 32*bs*sz (forward only)]
 inline long long solo_rec_bytes(int nent, int bs, int sz, bool forward) {
   return 16 + 128 + (long long)nent * 128 + (long long)nent * 32 * bs * sz + (forward ? 32LL * bs * sz : 0);
 }
-// Static parts of the solo step records (header, rows, codes) for element
-// size `elem`: code >= 0 is a byte offset into the CTA's ring region (0 = 32
-// zero bytes, for padding); code < 0 is -(row + 1) of a dependency read from
-// the output vector in global memory.
-std::vector<unsigned char> pack_solo_headers(const SweepPlan& P, int elem, std::vector<long long>& off,
-                                             long long& max_rec);
+// Static parts of the solo step records (header, output positions, codes) for
+// element size `elem`.  out_pos[row]: where the sweep writes the row's result
+// (its position in the vector's storage order); glob_pos[row]: where a global
+// dependency read finds a row (the storage order of the sweep's own output).
+// code >= 0 is a byte offset into the CTA's ring region (0 = 32 zero bytes,
+// for padding); code < 0 is -(glob_pos[row] + 1).  rec_off: nsteps + 1 byte
+// offsets (the value packer's view).
+std::vector<unsigned char> pack_solo_headers(const SoloPlan& S, int elem, const int* out_pos, const int* glob_pos,
+                                             std::vector<long long>& rec_off);
 
 // level sets of the triangular dependency DAG (rows sorted by level, then row)
 struct Levels {

@@ -83,6 +83,19 @@ __device__ __forceinline__ double zval(const void* z, long long k) {
   return (double)reinterpret_cast<const Z*>(z)[k];
 }
 
+// A new forward-sweep input value r of element k: in the sweep's step order
+// for one-CTA-per-solve sweeps, else as the FP32 copy ranged FP32 sweeps read
+// (FP64 ranged sweeps read r itself).
+template <typename Z>
+__device__ __forceinline__ void put_sweep_input(const SrvSlot& S, long long k, double r) {
+  if (S.posf) {
+    const long long row = k / S.b;
+    reinterpret_cast<Z*>(S.rperm)[(long long)S.posf[row] * S.b + (k - row * S.b)] = (Z)r;
+  } else if constexpr (sizeof(Z) == 4) {
+    S.r32[k] = (float)r;
+  }
+}
+
 // element range [e0, e1) of chunk c of slot S
 __device__ __forceinline__ void chunk_elems(const SrvSlot& S, int c, long long& e0, long long& e1) {
   const long long row0 = (long long)(c - S.chunk0) * kSrvRows;
@@ -208,7 +221,7 @@ __global__ void __launch_bounds__(kSrvTpb) k_srv_update_rx(const SrvTable* T, do
       part += r * r;
       reinterpret_cast<Z*>(S.y)[k] = sentinel_value<Z>();
       reinterpret_cast<Z*>(S.z)[k] = sentinel_value<Z>();
-      if constexpr (sizeof(Z) == 4) S.r32[k] = (float)r;
+      put_sweep_input<Z>(S, k, r);
     }
     double tot;
     if (slot_sum(part, c, S, partials, &tot) && threadIdx.x == 0) {
@@ -269,7 +282,7 @@ __global__ void __launch_bounds__(kSrvTpb) k_srv_replace(const SrvTable* T, doub
     for (long long k = e0 + threadIdx.x; k < e1; k += kSrvTpb) {
       const double r = S.rd[k];
       S.r[k] = r;
-      if constexpr (sizeof(Z) == 4) S.r32[k] = (float)r;
+      put_sweep_input<Z>(S, k, r);
       reinterpret_cast<Z*>(S.y)[k] = sentinel_value<Z>();
       reinterpret_cast<Z*>(S.z)[k] = sentinel_value<Z>();
     }
@@ -413,6 +426,7 @@ __global__ void __launch_bounds__(kSrvTpb) k_srvm_update_rx(const SrvTable* T, d
         r = r - alpha32 * S.q32[k];
         S.r32[k] = r;
         S.d[k] = S.d[k] + alpha * (double)S.p32[k];
+        if (S.posf) put_sweep_input<float>(S, k, r);
       }
       part += (double)r * (double)r;
       y[k] = sentinel_value<float>();
@@ -474,6 +488,7 @@ __device__ __forceinline__ double chunk_refine(const SrvSlot& S, int row0, int r
     for (int d = 0; d < B; ++d) {
       const double rv = S.rhs[(size_t)i * B + d] - y[d];
       S.r32[(size_t)i * B + d] = (float)rv;
+      if (S.posf) reinterpret_cast<float*>(S.rperm)[(size_t)S.posf[i] * B + d] = (float)rv;
       part += rv * rv;
     }
   }
@@ -617,6 +632,23 @@ cudaError_t srvm_refine(const SrvTable* T, double* partials, int grid, cudaStrea
   k_srvm_refine<<<grid, kSrvTpb, 0, s>>>(T, partials);
   return cudaGetLastError();
 }
+template <typename Z>
+__global__ void k_srv_permute_rhs(long long m, int b, const double* rhs, const int* posf, Z* rperm) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m; k += (long long)gridDim.x * blockDim.x) {
+    const long long row = k / b;
+    rperm[(long long)posf[row] * b + (k - row * b)] = (Z)rhs[k];
+  }
+}
+
+cudaError_t srv_permute_rhs(const SrvSlot& s, bool fp32, cudaStream_t st) {
+  const long long m = (long long)s.n * s.b;
+  if (m == 0 || !s.posf) return cudaSuccess;
+  const int grid = (int)std::min<long long>((m + 255) / 256, 1216);
+  if (fp32) k_srv_permute_rhs<float><<<grid, 256, 0, st>>>(m, s.b, s.rhs, s.posf, static_cast<float*>(s.rperm));
+  else k_srv_permute_rhs<double><<<grid, 256, 0, st>>>(m, s.b, s.rhs, s.posf, static_cast<double*>(s.rperm));
+  return cudaGetLastError();
+}
+
 cudaError_t srvm_init_vectors(long long m, const double* rhs, double* x, double* d, float* r32, float* p32,
                               float* y, float* z, cudaStream_t s) {
   if (m == 0) return cudaSuccess;

@@ -41,6 +41,11 @@ struct SrvSlot {
   float* p32;
   float* q32;
   double* d;
+  // one-CTA-per-solve sweeps (k_solo.cu), else nullptr: the forward sweep's
+  // input stored in its step order, rperm[posf[row]*b + c] = r[row*b + c]
+  // (the sweep's element type: FP32 in the FP32 modes)
+  const int* posf;
+  void* rperm;
 };
 
 struct SrvTable {
@@ -96,6 +101,9 @@ cudaError_t srvm_fold(const SrvTable* T, int grid, cudaStream_t s);
 // slots due for a reliable update or stopped on the recursion: r = b - A x in
 // FP64 (rounded to FP32 for the recursion) and the true-residual stop
 cudaError_t srvm_refine(const SrvTable* T, double* partials, int grid, cudaStream_t s);
+// admission of a solve with one-CTA-per-solve sweeps: its first forward
+// input, rperm[posf[row]*b + c] = rhs[row*b + c] (fp32: as float)
+cudaError_t srv_permute_rhs(const SrvSlot& s, bool fp32, cudaStream_t st);
 // admission: x = d = p = 0, r = rhs (FP32), sweep outputs = sentinel
 cudaError_t srvm_init_vectors(long long m, const double* rhs, double* x, double* d, float* r32, float* p32,
                               float* y, float* z, cudaStream_t s);

@@ -9,17 +9,19 @@
 // dependency was produced by the same CTA and no value crosses SMs.
 //
 // CTA: kSoloWarps compute warps + one producer warp.
-//   * producer -- walks the solve's steps (<= 32 rows of one level each) in
-//     order: one TMA bulk copy per packed step record (cp.async.bulk,
-//     completion on the stage's rec_full mbarrier with a byte count), then,
-//     once the record has landed, per-lane cp.async gathers of the rows'
-//     right-hand sides, arriving on the stage's `full` mbarrier when they
-//     complete; it runs up to NS steps ahead of the compute warps.
-//   * compute warps -- level by level: warp w takes steps first+w,
-//     first+w+kSoloWarps, ... of the level; per step it waits for `full`,
-//     evaluates its 32 rows, writes the results to the shared-memory ring
-//     (slot step mod R) and to the output vector, and releases the stage on
-//     `empty`; a named barrier over the compute warps closes each level.
+//   * producer (one lane) -- walks the solve's chunks (runs of <= ch_max steps
+//     of one level) in order: per chunk two TMA bulk copies onto the stage's
+//     `full` mbarrier (one arrival with the byte count): the chunk's packed
+//     records, and its right-hand sides, which the producing kernel stored in
+//     this sweep's step order so that they are contiguous; it runs up to NS
+//     chunks ahead of the compute warps.
+//   * compute warps -- level by level, chunk by chunk: warp w takes steps w,
+//     w + kSoloWarps, ... of the chunk (every record of a chunk has the same
+//     size, so its offset is arithmetic), evaluates the step's 32 rows, writes
+//     the results to the shared-memory ring (slot step mod R) and to the
+//     output vector at the records' output positions, and arrives on the
+//     stage's `empty` mbarrier (kSoloWarps arrivals free the stage); a named
+//     barrier over the compute warps closes each level.
 // A dependency is read from the ring when its step lies among the R steps
 // before the end of the consuming level (never overwritten before it is
 // read), else from the output vector in global memory (written at least one
@@ -28,10 +30,11 @@
 // wait that gives up records kErrTimeout and the launch drains and returns.
 //
 // Record layout (bytes; pack_solo_headers in sched.cpp, values by k_pack):
-//   [hdr int4: nent][row: 32 int][code: nent x 32 int]
+//   [hdr int4: nent, steps in the chunk, step, 0][out: 32 int][code: nent x 32 int]
 //   [blocks: nent x B*B x 32 of T][D^-1: B*B x 32 of T, forward only]
+// out: the element offset / B where a lane's result goes (-1: empty lane);
 // code >= 0: byte offset into the ring region (0 = 32 zero bytes, padding);
-// code < 0: -(row + 1) of a dependency in the output vector.
+// code < 0: -(position + 1) of a dependency in the output vector.
 #include "dfg_common.cuh"
 #include "k_mbar.cuh"
 #include "k_sweep.h"
@@ -43,33 +46,32 @@ __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
   constexpr int BS = B * B;
   constexpr int SZ = (int)sizeof(T);
   constexpr int NW = kSoloWarps;
-  constexpr int VS = (B * 32 * SZ + 15) / 16 * 16;
+  constexpr int STEP_RHS = 32 * B * SZ;  // right-hand-side bytes of one step
   extern __shared__ __align__(128) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int NS = a.NS;  // a power of two: stage = pos & NSM, phase = (pos >> NSL) & 1
   const int NSM = NS - 1, NSL = __ffs(NS) - 1;
   const int RM = a.R - 1;
-  // layout: [bars: 3*NS u64][rstage: NS x rec_stage][vstage: NS x VS][zero 32 B][ring: R x 32 x B of T]
-  uint64_t* rec_full = reinterpret_cast<uint64_t*>(smem);
-  uint64_t* full = rec_full + NS;
+  const int VS = a.ch_max * STEP_RHS;
+  // layout: [bars: 2*NS u64][rstage: NS x rec_stage][vstage: NS x VS][zero 32 B][ring: R x 32 x B of T]
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem);
   uint64_t* empty = full + NS;
-  unsigned char* rstage = smem + (((size_t)3 * NS * 8 + 127) / 128) * 128;
+  unsigned char* rstage = smem + (((size_t)2 * NS * 8 + 127) / 128) * 128;
   unsigned char* vstage = rstage + (size_t)NS * a.rec_stage;
   unsigned char* ringreg = vstage + (size_t)NS * VS;
   __shared__ int s_slot, s_stop;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NS; ++s) {
-      mbar_init(&rec_full[s], 1);
-      mbar_init(&full[s], 64);  // 32 copy-completion arrivals + 32 producer-lane arrivals
-      mbar_init(&empty[s], 1);
+      mbar_init(&full[s], 1);      // the producer's arrival with the byte count
+      mbar_init(&empty[s], NW);    // one arrival per compute warp
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (threadIdx.x < 8) reinterpret_cast<unsigned*>(ringreg)[threadIdx.x] = 0u;
   __syncthreads();
 
-  int g = 0;  // steps this CTA has pushed through the pipeline (both sides count alike)
+  int g = 0;  // chunks this CTA has pushed through the pipeline (both sides count alike)
   for (;;) {
     if (threadIdx.x == 0) {
       const int t = atomicAdd(a.ticket, 1);
@@ -83,166 +85,151 @@ __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
     if (jslot == -1) break;
     if (jslot == -2) continue;  // a finished solve
     const SoloSlot& S = a.batch->slot[jslot];
-    const unsigned char* __restrict__ recs = S.rec;
-    const long long* __restrict__ rec_off = S.rec_off;
-    const int nst = S.nsteps;
+    const int nch = S.nchunks;
     bool abort = false;
     if (warp == NW) {
       // ------------------------------------------------------------ producer
-      const T* __restrict__ in = reinterpret_cast<const T*>(S.in);
-      int n_issued = 0, n_waited = 0;
-      auto issue_rec = [&](int i) {
-        const int pos = g + i;
-        const int st = pos & NSM;
-        const int use = pos >> NSL;
-        if (use >= 1 && !abort) {
-          if (!mbar_wait(&empty[st], (unsigned)((use - 1) & 1), a.err, kSiteEmpty, jslot, i)) abort = true;
+      if (lane == 0) {
+        const unsigned char* __restrict__ recs = S.rec;
+        const unsigned char* __restrict__ in = reinterpret_cast<const unsigned char*>(S.in);
+        const SoloChunk* __restrict__ chunks = S.chunks;
+        int n_issued = 0;
+        SoloChunk nx = nch > 0 ? chunks[0] : SoloChunk{};
+        for (int c = 0; c < nch; ++c) {
+          const SoloChunk ch = nx;
+          if (c + 1 < nch) nx = chunks[c + 1];  // the next chunk's entry, off the critical path
+          const int pos = g + c;
+          const int st = pos & NSM;
+          const int use = pos >> NSL;
+          if (use >= 1 && !mbar_wait(&empty[st], (unsigned)((use - 1) & 1), a.err, kSiteEmpty, jslot, c)) {
+            abort = true;
+            break;
+          }
+          const unsigned rhs_bytes = (unsigned)(ch.nsteps * STEP_RHS);
+          mbar_expect_tx(&full[st], (unsigned)ch.rec_bytes + rhs_bytes);
+          tma_load_1d(rstage + (size_t)st * a.rec_stage, recs + ch.rec_off, (unsigned)ch.rec_bytes, &full[st]);
+          tma_load_1d(vstage + (size_t)st * VS, in + (size_t)ch.first_step * STEP_RHS, rhs_bytes, &full[st]);
+          ++n_issued;
         }
-        if (abort) return;  // no new copies once the launch is failing
-        ++n_issued;
-        if (lane == 0) {
-          const long long o0 = rec_off[i], o1 = rec_off[i + 1];
-          mbar_expect_tx(&rec_full[st], (unsigned)(o1 - o0));
-          tma_load_1d(rstage + (size_t)st * a.rec_stage, recs + o0, (unsigned)(o1 - o0), &rec_full[st]);
-        }
-      };
-      const int LA = NS > 3 ? NS / 2 : 1;  // record copies run LA steps ahead of the gathers
-      for (int i = 0; i < LA && i < nst; ++i) issue_rec(i);
-      for (int i = 0; i < nst; ++i) {
-        if (i + LA < nst) issue_rec(i + LA);
-        const int pos = g + i;
-        const int st = pos & NSM;
-        if (!abort) {
-          if (mbar_wait(&rec_full[st], (unsigned)((pos >> NSL) & 1), a.err, kSiteRecLoad, jslot, i)) ++n_waited;
-          else abort = true;
-        }
-        const unsigned char* rec = rstage + (size_t)st * a.rec_stage;
-        const int row = reinterpret_cast<const int*>(rec + 16)[lane];
-        if (row >= 0 && !abort) {
-          T* rhs = reinterpret_cast<T*>(vstage + (size_t)st * VS) + lane * B;
-#pragma unroll
-          for (int d = 0; d < B; ++d) {
-            if constexpr (SZ == 8) cp_async8(rhs + d, &in[(size_t)row * B + d]);
-            else cp_async4(rhs + d, &in[(size_t)row * B + d]);
+        if (abort) {  // copies already issued land before the CTA moves on (bounded)
+          for (int k = 0; k < n_issued; ++k) {
+            const int pos = g + k;
+            mbar_drain(&full[pos & NSM], (unsigned)((pos >> NSL) & 1));
           }
         }
-        cp_async_arrive_noinc(&full[st]);
-        // release: the record this lane waited for is visible to whoever
-        // acquires `full`; a failing lane does not arrive, so the compute
-        // warps give up on the error word instead of reading a missing record
-        if (!abort) mbar_arrive(&full[st]);
       }
-      if (abort && lane == 0) {  // record copies already issued land before the CTA moves on (bounded)
-        for (int k = n_waited; k < n_issued; ++k) {
-          const int pos = g + k;
-          mbar_drain(&rec_full[pos & NSM], (unsigned)((pos >> NSL) & 1));
-        }
-      }
+      abort = __shfl_sync(0xffffffffu, abort, 0);
     } else {
       // ------------------------------------------------------------- compute
       T* out = reinterpret_cast<T*>(S.out);
-      const int* __restrict__ ls = S.lev_steps;
+      const int* __restrict__ lc = S.lev_chunks;
       const int nl = S.nlevels;
       // level bounds come one level ahead, so their load is off the critical path
-      int s0 = ls[0], s1 = nl > 0 ? ls[1] : 0;
+      int c0 = lc[0], c1 = nl > 0 ? lc[1] : 0;
       for (int l = 0; l < nl; ++l) {
-        const int s2 = l + 2 <= nl ? __ldg(&ls[l + 2]) : 0;
-        for (int s = s0 + warp; s < s1; s += NW) {
-          const int pos = g + s;
+        const int c2 = l + 2 <= nl ? __ldg(&lc[l + 2]) : 0;
+        for (int c = c0; c < c1; ++c) {
+          const int pos = g + c;
           const int st = pos & NSM;
-          if (!abort && !mbar_wait(&full[st], (unsigned)((pos >> NSL) & 1), a.err, kSiteFull, jslot, s)) abort = true;
-          const unsigned char* rec = rstage + (size_t)st * a.rec_stage;
-          const int nent = reinterpret_cast<const int*>(rec)[0];
-          const int row = reinterpret_cast<const int*>(rec + 16)[lane];
-          const int* code = reinterpret_cast<const int*>(rec + 144);
-          const T* blk = reinterpret_cast<const T*>(rec + 144 + nent * 128);
-          if (row >= 0 && !abort) {
-            const T* val = reinterpret_cast<const T*>(vstage + (size_t)st * VS);
-            T t[B];
+          if (!abort && !mbar_wait(&full[st], (unsigned)((pos >> NSL) & 1), a.err, kSiteFull, jslot, c)) abort = true;
+          const unsigned char* stage = rstage + (size_t)st * a.rec_stage;
+          const int nent = reinterpret_cast<const int*>(stage)[0];
+          const int nst = abort ? 0 : reinterpret_cast<const int*>(stage)[1];
+          const int rec_sz = 144 + nent * 128 + nent * 32 * BS * SZ + (FWD ? 32 * BS * SZ : 0);
+          for (int k = warp; k < nst; k += NW) {
+            const unsigned char* rec = stage + (size_t)k * rec_sz;
+            const int s = reinterpret_cast<const int*>(rec)[2];
+            const int o = reinterpret_cast<const int*>(rec + 16)[lane];
+            const int* code = reinterpret_cast<const int*>(rec + 144);
+            const T* blk = reinterpret_cast<const T*>(rec + 144 + nent * 128);
+            if (o >= 0) {
+              const T* val = reinterpret_cast<const T*>(vstage + (size_t)st * VS + (size_t)k * STEP_RHS);
+              T t[B];
 #pragma unroll
-            for (int d = 0; d < B; ++d) t[d] = val[lane * B + d];
-            if constexpr (MAXE > 0) {
-              // all dependency values first (independent loads), then the FMAs
-              T v[MAXE][B];
+              for (int d = 0; d < B; ++d) t[d] = val[lane * B + d];
+              if constexpr (MAXE > 0) {
+                // all dependency values first (independent loads), then the FMAs
+                T v[MAXE][B];
 #pragma unroll
-              for (int e = 0; e < MAXE; ++e) {
-                if (e < nent) {
-                  const int c = code[e * 32 + lane];
-                  if (c >= 0) {
-                    const T* vp = reinterpret_cast<const T*>(ringreg + c);
+                for (int e = 0; e < MAXE; ++e) {
+                  if (e < nent) {
+                    const int cd = code[e * 32 + lane];
+                    if (cd >= 0) {
+                      const T* vp = reinterpret_cast<const T*>(ringreg + cd);
 #pragma unroll
-                    for (int d = 0; d < B; ++d) v[e][d] = vp[d];
-                  } else {
-                    const T* gp = out + (size_t)(-c - 1) * B;
+                      for (int d = 0; d < B; ++d) v[e][d] = vp[d];
+                    } else {
+                      const T* gp = out + (size_t)(-cd - 1) * B;
 #pragma unroll
-                    for (int d = 0; d < B; ++d) v[e][d] = __ldcg(gp + d);
+                      for (int d = 0; d < B; ++d) v[e][d] = __ldcg(gp + d);
+                    }
                   }
                 }
-              }
 #pragma unroll
-              for (int e = 0; e < MAXE; ++e) {
-                if (e < nent) {
+                for (int e = 0; e < MAXE; ++e) {
+                  if (e < nent) {
+#pragma unroll
+                    for (int p = 0; p < B; ++p) {
+                      T acc = t[p];
+#pragma unroll
+                      for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[e][q];
+                      t[p] = acc;
+                    }
+                  }
+                }
+              } else {
+                for (int e = 0; e < nent; ++e) {
+                  const int cd = code[e * 32 + lane];
+                  T v[B];
+                  if (cd >= 0) {
+                    const T* vp = reinterpret_cast<const T*>(ringreg + cd);
+#pragma unroll
+                    for (int d = 0; d < B; ++d) v[d] = vp[d];
+                  } else {
+                    const T* gp = out + (size_t)(-cd - 1) * B;
+#pragma unroll
+                    for (int d = 0; d < B; ++d) v[d] = __ldcg(gp + d);
+                  }
 #pragma unroll
                   for (int p = 0; p < B; ++p) {
                     T acc = t[p];
 #pragma unroll
-                    for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[e][q];
+                    for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[q];
                     t[p] = acc;
                   }
                 }
               }
-            } else {
-              for (int e = 0; e < nent; ++e) {
-                const int c = code[e * 32 + lane];
-                T v[B];
-                if (c >= 0) {
-                  const T* vp = reinterpret_cast<const T*>(ringreg + c);
-#pragma unroll
-                  for (int d = 0; d < B; ++d) v[d] = vp[d];
-                } else {
-                  const T* gp = out + (size_t)(-c - 1) * B;
-#pragma unroll
-                  for (int d = 0; d < B; ++d) v[d] = __ldcg(gp + d);
-                }
+              T y[B];
+              if constexpr (FWD) {
+                const T* dinv = blk + nent * BS * 32;
 #pragma unroll
                 for (int p = 0; p < B; ++p) {
-                  T acc = t[p];
+                  T acc = dinv[(p * B) * 32 + lane] * t[0];
 #pragma unroll
-                  for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[q];
-                  t[p] = acc;
+                  for (int q = 1; q < B; ++q) acc += dinv[(p * B + q) * 32 + lane] * t[q];
+                  y[p] = acc;
                 }
+              } else {
+#pragma unroll
+                for (int p = 0; p < B; ++p) y[p] = t[p];
               }
-            }
-            T y[B];
-            if constexpr (FWD) {
-              const T* dinv = blk + nent * BS * 32;
+              T* rg = reinterpret_cast<T*>(ringreg + 32) + (((s & RM) * 32 + lane) * B);
 #pragma unroll
-              for (int p = 0; p < B; ++p) {
-                T acc = dinv[(p * B) * 32 + lane] * t[0];
-#pragma unroll
-                for (int q = 1; q < B; ++q) acc += dinv[(p * B + q) * 32 + lane] * t[q];
-                y[p] = acc;
+              for (int d = 0; d < B; ++d) {
+                rg[d] = y[d];
+                out[(size_t)o * B + d] = y[d];
               }
-            } else {
-#pragma unroll
-              for (int p = 0; p < B; ++p) y[p] = t[p];
-            }
-            T* rg = reinterpret_cast<T*>(ringreg + 32) + (((s & RM) * 32 + lane) * B);
-#pragma unroll
-            for (int d = 0; d < B; ++d) {
-              rg[d] = y[d];
-              out[(size_t)row * B + d] = y[d];
             }
           }
           __syncwarp();
           if (lane == 0) mbar_arrive(&empty[st]);
         }
         named_sync(1, NW * 32);
-        s0 = s1;
-        s1 = s2;
+        c0 = c1;
+        c1 = c2;
       }
     }
-    g += nst;
+    g += nch;
     if (__any_sync(0xffffffffu, abort)) {
       if (lane == 0) record_fail(a.err, kErrTimeout, kSiteRange, jslot, -1);
     }
@@ -252,7 +239,6 @@ __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
     __syncthreads();
     if (s_stop) break;
   }
-  cp_async_wait_all();
 }
 
 // ------------------------------------------------------------------ launchers

@@ -75,15 +75,23 @@ struct PackArgs {
 cudaError_t launch_pack(bool forward, bool fp32, int B, const PackArgs& a, cudaStream_t st);
 
 // Solo sweeps (k_solo.cu): a CTA owns one solve's whole sweep, level after
-// level (SweepPlan from solo_sweep_plan, records from pack_solo_headers).
-// Batched: a ticket claims the next solve of the batch, in batch order.
+// level (solo_sweep_plan / pack_solo_headers in sched.cpp).  The sweep's
+// input is stored in its step order (element (step*32 + lane)*B + d), so a
+// chunk of steps needs two contiguous bulk copies: its records and its
+// right-hand sides.  Batched: a ticket claims the next solve of the batch,
+// in batch order.
+struct SoloChunk {
+  long long rec_off;  // byte offset of the chunk's first record
+  int rec_bytes;      // bytes of the chunk's records
+  int first_step, nsteps, nent;
+};
 struct SoloSlot {
   const unsigned char* rec;
-  const long long* rec_off;
-  const int* lev_steps;   // nlevels + 1: first step of each level
-  int nlevels, nsteps;
-  const void* in;
-  void* out;
+  const SoloChunk* chunks;
+  const int* lev_chunks;  // nlevels + 1: first chunk of each level
+  int nlevels, nchunks;
+  const void* in;         // right-hand sides in step order (nsteps*32*B of T)
+  void* out;              // results at the records' output positions
   const int* done;        // the solve's state: nonzero = skip
 };
 struct SoloBatch {
@@ -94,16 +102,17 @@ struct SoloArgs {
   const SoloBatch* batch;
   int* ticket;       // 0 at launch
   int* err;          // device error word
-  int rec_stage;     // bytes per record stage (>= the largest record, 16-aligned)
+  int rec_stage;     // bytes per record stage (>= every chunk's records, 16-aligned)
+  int ch_max;        // steps per chunk at most (sizes the right-hand-side stage)
   int NS;            // pipeline stages (a power of two)
   int R;             // ring depth in steps (a power of two)
   int max_nent;      // selects the unrolled variant
 };
 // compute warps per CTA (plus one producer warp)
-constexpr int kSoloWarps = 8;
-inline int solo_val_stage(int B, int elem) { return (B * 32 * elem + 15) / 16 * 16; }
+constexpr int kSoloWarps = 16;
+inline int solo_val_stage(int ch_max, int B, int elem) { return ch_max * 32 * B * elem; }
 inline size_t solo_smem_bytes(int NS, int rec_stage, int val_stage, int R, int B, int elem) {
-  return ((size_t)3 * NS * 8 + 127) / 128 * 128 + (size_t)NS * rec_stage + (size_t)NS * val_stage + 32 +
+  return ((size_t)2 * NS * 8 + 127) / 128 * 128 + (size_t)NS * rec_stage + (size_t)NS * val_stage + 32 +
          (size_t)R * 32 * B * elem;
 }
 cudaError_t launch_solo(bool forward, bool fp32, int B, const SoloArgs& a, int grid, size_t smem, cudaStream_t st);

@@ -379,13 +379,15 @@ std::vector<unsigned char> pack_record_headers(const SweepPlan& P, int elem, std
   return h;
 }
 
-SweepPlan solo_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind, bool forward,
-                          int R) {
-  SweepPlan P;
+SoloPlan solo_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind, bool forward,
+                         int R, int elem, int stage_bytes, int ch_max) {
+  SoloPlan S;
+  SweepPlan& P = S.P;
   P.forward = forward;
   P.n = n;
   P.b = b;
   P.R = R;
+  const int bs = b * b;
   const Levels L = build_levels(n, rowptr, colind, diaind, forward);
   const int nl = (int)L.ptr.size() - 1;
   P.nranges = std::max(nl, 0);
@@ -406,13 +408,36 @@ SweepPlan solo_sweep_plan(int n, int b, const int* rowptr, const int* colind, co
   for (int l = 0; l < nl; ++l)
     for (int s = P.range_steps[l]; s < P.range_steps[l + 1]; ++s) step_level[s] = l;
   P.step_rows.assign((size_t)P.nsteps * 32, -1);
-  P.step_nent.assign(P.nsteps, 0);
+  std::vector<int> own(P.nsteps, 0);  // the step's own largest entry count
+  S.pos.assign(n, 0);
   for (int row = 0; row < n; ++row) {
     P.step_rows[(size_t)row_step[row] * 32 + row_lane[row]] = row;
+    S.pos[row] = row_step[row] * 32 + row_lane[row];
     int c0, c1;
     deps_of(row, forward, rowptr, diaind, c0, c1);
-    P.step_nent[row_step[row]] = std::max(P.step_nent[row_step[row]], c1 - c0);
+    own[row_step[row]] = std::max(own[row_step[row]], c1 - c0);
   }
+  // chunks: consecutive steps of one level, at most ch_max of them and
+  // stage_bytes of records (a chunk holds at least one step)
+  S.lev_chunks.assign(P.nranges + 1, 0);
+  P.step_nent.assign(P.nsteps, 0);
+  for (int l = 0; l < nl; ++l) {
+    S.lev_chunks[l] = (int)S.chunks.size();
+    int s = P.range_steps[l];
+    while (s < P.range_steps[l + 1]) {
+      SoloChunk c{0, 0, s, 0, 0};
+      while (s < P.range_steps[l + 1] && c.nsteps < ch_max) {
+        const int ne = std::max(c.nent, own[s]);
+        if (c.nsteps > 0 && (c.nsteps + 1) * solo_rec_bytes(ne, bs, elem, forward) > stage_bytes) break;
+        c.nent = ne;
+        ++c.nsteps;
+        ++s;
+      }
+      for (int t = c.first_step; t < c.first_step + c.nsteps; ++t) P.step_nent[t] = c.nent;
+      S.chunks.push_back(c);
+    }
+  }
+  S.lev_chunks[P.nranges] = (int)S.chunks.size();
   P.ent_off.assign(P.nsteps + 1, 0);
   for (int s = 0; s < P.nsteps; ++s) {
     P.ent_off[s + 1] = P.ent_off[s] + P.step_nent[s];
@@ -434,37 +459,44 @@ SweepPlan solo_sweep_plan(int n, int b, const int* rowptr, const int* colind, co
       P.ent_slot[(size_t)e * 32 + lane] = c;
     }
   }
+  long long off = 0;
+  for (SoloChunk& c : S.chunks) {
+    c.rec_off = off;
+    c.rec_bytes = (int)(c.nsteps * solo_rec_bytes(c.nent, bs, elem, forward));
+    off += c.rec_bytes;
+  }
   P.est_cost = (double)P.nranges;
-  return P;
+  return S;
 }
 
-std::vector<unsigned char> pack_solo_headers(const SweepPlan& P, int elem, std::vector<long long>& off,
-                                             long long& max_rec) {
+std::vector<unsigned char> pack_solo_headers(const SoloPlan& S, int elem, const int* out_pos, const int* glob_pos,
+                                             std::vector<long long>& off) {
+  const SweepPlan& P = S.P;
   const int b = P.b, bs = b * b;
   off.assign(P.nsteps + 1, 0);
-  max_rec = 0;
-  for (int s = 0; s < P.nsteps; ++s) {
-    const long long rb = solo_rec_bytes(P.step_nent[s], bs, elem, P.forward);
-    off[s + 1] = off[s] + rb;
-    max_rec = std::max(max_rec, rb);
-  }
+  for (int s = 0; s < P.nsteps; ++s) off[s + 1] = off[s] + solo_rec_bytes(P.step_nent[s], bs, elem, P.forward);
   std::vector<unsigned char> h((size_t)off[P.nsteps], 0);
-  for (int s = 0; s < P.nsteps; ++s) {
-    unsigned char* r = h.data() + off[s];
-    const int nent = P.step_nent[s];
-    std::memcpy(r, &nent, 4);
-    std::memcpy(r + 16, &P.step_rows[(size_t)s * 32], 128);
-    int* code = reinterpret_cast<int*>(r + 144);
-    for (int e = 0; e < nent; ++e)
+  for (const SoloChunk& c : S.chunks)
+    for (int s = c.first_step; s < c.first_step + c.nsteps; ++s) {
+      unsigned char* r = h.data() + off[s];
+      const int hdr[4] = {P.step_nent[s], c.nsteps, s, 0};
+      std::memcpy(r, hdr, 16);
+      int* outv = reinterpret_cast<int*>(r + 16);
+      int* code = reinterpret_cast<int*>(r + 144);
       for (int lane = 0; lane < 32; ++lane) {
-        const int src = P.ent_src[(size_t)(P.ent_off[s] + e) * 32 + lane];
-        int c = 0;
-        if (src == SweepPlan::kSrcPad) c = 0;
-        else if (src >= 0) c = 32 + src * b * elem;
-        else c = src;  // -(row + 1)
-        code[e * 32 + lane] = c;
+        const int row = P.step_rows[(size_t)s * 32 + lane];
+        outv[lane] = row >= 0 ? out_pos[row] : -1;
       }
-  }
+      for (int e = 0; e < P.step_nent[s]; ++e)
+        for (int lane = 0; lane < 32; ++lane) {
+          const int src = P.ent_src[(size_t)(P.ent_off[s] + e) * 32 + lane];
+          int cd = 0;
+          if (src == SweepPlan::kSrcPad) cd = 0;
+          else if (src >= 0) cd = 32 + src * b * elem;
+          else cd = -(glob_pos[-src - 1] + 1);
+          code[e * 32 + lane] = cd;
+        }
+    }
   return h;
 }
 

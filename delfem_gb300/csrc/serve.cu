@@ -167,6 +167,10 @@ struct Req {
   long long maxrf = 0, maxrb = 0;
   int cls = -1, maxe = 0, group = 0;
   bool solo = false;  // sweeps by one CTA per solve (k_solo.cu), else ranged (k_sweep.cu)
+  // solo: chunk tables, first chunk per level, and the forward plan's
+  // position of every row (where the forward input is stored)
+  std::vector<SoloChunk> chf, chb;
+  std::vector<int> posf;
   // algorithmic bytes of one launch of each batched kernel for this solve:
   // 0 r.z, 1 p update, 2 SpMV, 3 r/x update, then forward and backward sweep
   double alg[6] = {};
@@ -174,6 +178,7 @@ struct Req {
   Layout P, T;
   size_t o_sptr, o_swidth, o_scol, o_sval, o_sval32, o_rhs, o_r, o_x, o_p, o_q, o_rd, o_y, o_z, o_r32;
   size_t o_recf, o_offf, o_rsf, o_recb, o_offb, o_rsb, o_st, o_cnt;
+  size_t o_chf = 0, o_chb = 0, o_posf = 0, o_rperm = 0;
   size_t t_rowptr, t_colind, t_diag, t_offd, t_ssrc;
   size_t t_coords, t_conn, t_coef, t_bc, t_load, t_em, t_er, t_sp, t_ss, t_rp, t_rs, t_dia, t_lev, t_fd, t_fo;
   size_t t_eof, t_esf, t_srf, t_eob, t_esb, t_srb;
@@ -245,6 +250,7 @@ struct dfg_server_s {
   size_t cls_smem[kClasses][2] = {};
   // per-class solo sweep shape: grid, stages, ring steps, record stage bytes, shared memory
   int solo_grid[kClasses] = {}, solo_ns[kClasses][2] = {}, solo_R[kClasses] = {}, solo_rec_stage[kClasses][2] = {};
+  int solo_ch[kClasses][2] = {};
   size_t solo_smem[kClasses][2] = {};
   int sweeps = 0;  // dfg_server_config::sweeps
 
@@ -288,16 +294,25 @@ namespace {
 
 // ---------------------------------------------------------------- symbolic
 
-// Which sweep kernel serves a solve.  FP32 sweeps run one CTA per solve
-// (k_solo.cu): a solve's whole dependency chain stays on one SM and the
-// in-flight solves fill the device.  FP64 sweeps stay ranged (k_sweep.cu):
-// GB300 issues about 1.6 FP64 FMA lanes per clock per SM, so a large
-// solve's FP64 sweep needs the FMA rate of many SMs.
+// Which sweep kernel serves a solve.  One CTA per solve (k_solo.cu) keeps a
+// solve's whole dependency chain on one SM, and the in-flight solves fill
+// the device; the ranged kernel (k_sweep.cu) spreads one solve over many
+// SMs at the price of cross-SM hand-offs (about 0.75 us per dependency level
+// in batched launches).  FP32 sweeps always take one CTA: their FMAs are
+// cheap.  An FP64 sweep on one SM is bound by GB300's FP64 FMA rate (about
+// 1.6 lanes per clock per SM, shared by the SM's two sweep CTAs), so an FP64
+// solve takes one CTA only while its FMA time there stays below the ranged
+// kernel's chain time: 1x1-block solves up to a few hundred thousand rows,
+// 2x2 and 3x3 ones only when small.
 bool use_solo(const dfg_server_s* S, const Req* r) {
-  (void)r;
   if (S->sweeps == 1) return false;
   if (S->sweeps == 2) return true;
-  return S->fp32;
+  if (S->fp32) return true;
+  const double levels = (double)std::max<size_t>(r->lev.ptr.size(), 2) - 1;
+  const double fma_per_row = (double)(r->maxe + 1) * r->b * r->b;  // deps and D^-1, per block row
+  const double solo_s = (double)r->n * fma_per_row / (1.6 * 2.0e9 / 2.0);
+  const double ranged_s = levels * 0.75e-6;
+  return solo_s < ranged_s;
 }
 
 // Fills the request's host-side set-up; returns false with r->error on failure.
@@ -331,11 +346,25 @@ bool symbolic(dfg_server_s* S, Req* r) {
   r->group = group_of((long long)n * r->b, S->ngroups);
   r->solo = use_solo(S, r);
   if (r->solo) {
-    const int R = S->solo_R[r->cls];
-    r->pf = solo_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), true, R);
-    r->pb = solo_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), false, R);
-    r->hf = pack_solo_headers(r->pf, elem, r->of, r->maxrf);
-    r->hb = pack_solo_headers(r->pb, elem, r->ob, r->maxrb);
+    const int k = r->cls, R = S->solo_R[k];
+    SoloPlan sf = solo_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), true, R, elem,
+                                  S->solo_rec_stage[k][0], S->solo_ch[k][0]);
+    SoloPlan sb = solo_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), false, R, elem,
+                                  S->solo_rec_stage[k][1], S->solo_ch[k][1]);
+    // the forward sweep writes y where the backward sweep reads it (its step
+    // order); the backward sweep writes z in row order
+    std::vector<int> ident(n);
+    for (int i = 0; i < n; ++i) ident[i] = i;
+    r->hf = pack_solo_headers(sf, elem, sb.pos.data(), sb.pos.data(), r->of);
+    r->hb = pack_solo_headers(sb, elem, ident.data(), ident.data(), r->ob);
+    r->maxrf = r->maxrb = 0;
+    r->chf = std::move(sf.chunks);
+    r->chb = std::move(sb.chunks);
+    r->posf = std::move(sf.pos);
+    r->pf = std::move(sf.P);
+    r->pb = std::move(sb.P);
+    r->pf.range_steps = std::move(sf.lev_chunks);  // per level: first chunk
+    r->pb.range_steps = std::move(sb.lev_chunks);
   } else {
     r->pf = fullest_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), true, kRingSteps);
     r->pb = fullest_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), false, kRingSteps);
@@ -377,7 +406,10 @@ bool symbolic(dfg_server_s* S, Req* r) {
   r->o_p = P.add(m * (mixed ? 4 : 8));
   r->o_q = P.add(m * (mixed ? 4 : 8));
   r->o_rd = P.add(m * 8);
-  r->o_y = P.add(m * elem + 64);
+  // a solo solve's y is stored in the backward plan's step order (padded
+  // steps of 32 rows)
+  const size_t ystore = r->solo ? std::max<size_t>(m, (size_t)r->pb.nsteps * 32 * r->b) : m;
+  r->o_y = P.add(ystore * elem + 64);
   r->o_z = P.add(m * elem + 64);
   r->o_r32 = P.add(S->fp32 ? m * 4 + 64 : 16);
   r->o_recf = P.add(r->hf.size() + 64);
@@ -388,6 +420,12 @@ bool symbolic(dfg_server_s* S, Req* r) {
   r->o_rsb = P.add(r->pb.range_steps.size() * 4);
   r->o_st = P.add(sizeof(PcgState));
   r->o_cnt = P.add(16);
+  if (r->solo) {
+    r->o_chf = P.add(r->chf.size() * sizeof(SoloChunk));
+    r->o_chb = P.add(r->chb.size() * sizeof(SoloChunk));
+    r->o_posf = P.add((size_t)n * 4);
+    r->o_rperm = P.add((size_t)r->pf.nsteps * 32 * r->b * elem + 64);
+  }
   Layout& T = r->T;
   const size_t k = r->nnoel;
   r->t_rowptr = T.add((n + 1) * 4);
@@ -431,6 +469,8 @@ void up(dfg_server_s* S, size_t base, size_t off, const std::vector<T>& v) {
   S->h2d += (long long)(v.size() * sizeof(T));
 }
 
+SrvSlot slot_of(dfg_server_s* S, Req* r);
+
 // Device work of one admission on s_adm; returns the ILU singular-pivot count.
 int admit_device(dfg_server_s* S, Req* r) {
   const size_t pb = r->pbase, tb = r->tbase;
@@ -461,6 +501,11 @@ int admit_device(dfg_server_s* S, Req* r) {
   up(S, pb, r->o_recb, r->hb);
   up(S, pb, r->o_offb, r->ob);
   up(S, pb, r->o_rsb, r->pb.range_steps);
+  if (r->solo) {
+    up(S, pb, r->o_chf, r->chf);
+    up(S, pb, r->o_chb, r->chb);
+    up(S, pb, r->o_posf, r->posf);
+  }
   up(S, tb, r->t_eof, r->pf.ent_off);
   up(S, tb, r->t_esf, r->pf.ent_slot);
   up(S, tb, r->t_srf, r->pf.step_rows);
@@ -563,6 +608,10 @@ int admit_device(dfg_server_s* S, Req* r) {
     SCK(srv_init_vectors(m, rhs, at<double>(S, pb, r->o_r), at<double>(S, pb, r->o_x), at<double>(S, pb, r->o_p),
                          at<void>(S, pb, r->o_y), at<void>(S, pb, r->o_z),
                          S->fp32 ? at<float>(S, pb, r->o_r32) : nullptr, S->fp32, st));
+  if (r->solo) {  // the first forward input, in the forward plan's step order
+    SCK(srv_permute_rhs(slot_of(S, r), S->fp32, st));
+    ++nl;
+  }
   Red red{S->d_adm, reinterpret_cast<unsigned*>(S->d_adm + kRedGrid), S->d_adm + kRedGrid + 8};
   SCK(api_dot(m, rhs, rhs, red, st));
   SCK(srv_init_state(at<PcgState>(S, pb, r->o_st), red.result, S->tol, S->maxit, S->mixed ? kMixedDelta2 : 0.0, st));
@@ -584,6 +633,7 @@ void finish_locked(dfg_server_s* S, Req* r) {
   r->rowptr = {}; r->colind = {}; r->diaind = {};
   r->gm = GatherMap{}; r->sell = SellMap{}; r->lev = Levels{}; r->pf = SweepPlan{}; r->pb = SweepPlan{};
   r->hf = {}; r->hb = {}; r->of = {}; r->ob = {};
+  r->chf = {}; r->chb = {}; r->posf = {};
   ++S->n_finished;
   S->cv_done.notify_all();
 }
@@ -732,6 +782,10 @@ SrvSlot slot_of(dfg_server_s* S, Req* r) {
   s.r32 = S->fp32 ? at<float>(S, pb, r->o_r32) : nullptr;
   s.st = at<PcgState>(S, pb, r->o_st);
   s.cnt = at<unsigned>(S, pb, r->o_cnt);
+  if (r->solo) {
+    s.posf = at<int>(S, pb, r->o_posf);
+    s.rperm = at<void>(S, pb, r->o_rperm);
+  }
   if (S->mixed) {
     s.r = s.p = s.q = nullptr;
     s.sval32 = at<float>(S, pb, r->o_sval32);
@@ -783,12 +837,12 @@ int upload_table(dfg_server_s* S, Group& G) {
       SoloSlot& w = B.slot[B.nslots++];
       const SweepPlan& pl = dir == 0 ? r->pf : r->pb;
       w.rec = at<unsigned char>(S, r->pbase, dir == 0 ? r->o_recf : r->o_recb);
-      w.rec_off = at<long long>(S, r->pbase, dir == 0 ? r->o_offf : r->o_offb);
-      w.lev_steps = at<int>(S, r->pbase, dir == 0 ? r->o_rsf : r->o_rsb);
+      w.chunks = at<SoloChunk>(S, r->pbase, dir == 0 ? r->o_chf : r->o_chb);
+      w.lev_chunks = at<int>(S, r->pbase, dir == 0 ? r->o_rsf : r->o_rsb);
       w.nlevels = pl.nranges;
-      w.nsteps = pl.nsteps;
-      w.in = dir == 0 ? (S->fp32 ? (const void*)sl.r32 : (const void*)sl.r) : sl.y;
-      w.out = dir == 0 ? sl.y : sl.z;
+      w.nchunks = (int)(dir == 0 ? r->chf.size() : r->chb.size());
+      w.in = dir == 0 ? sl.rperm : sl.y;  // both in this sweep's step order
+      w.out = dir == 0 ? sl.y : sl.z;     // y in the backward sweep's step order, z in row order
       w.done = &sl.st->done;
     }
   }
@@ -838,6 +892,7 @@ SoloArgs solo_args(dfg_server_s* S, Group& G, int k, int dir) {
   a.ticket = G.d_tickets + kClasses * 2 + k * 2 + dir;
   a.err = reinterpret_cast<int*>(G.d_stat + sizeof(SrvStatus) * kSrvMaxSlots);
   a.rec_stage = S->solo_rec_stage[k][dir];
+  a.ch_max = S->solo_ch[k][dir];
   a.NS = S->solo_ns[k][dir];
   a.R = S->solo_R[k];
   a.max_nent = class_maxe(k);
@@ -1151,36 +1206,41 @@ void class_shapes(dfg_server_s* S) {
     const int per_sm = std::max(1, std::min(16, (int)(per_sm_bytes / (worst + 1024))));
     S->cls_grid[k] = S->nsm * per_sm;
   }
-  // solo sweeps: the ring takes up to a third of a CTA's shared memory (a
-  // power of two of steps, at most 512), the record stages the rest (a power
-  // of two, 4 to 32 of them).  Rows with at most 4 lower or upper neighbours
-  // (triangle meshes: narrow levels, each depending on the one before) run
-  // two CTAs per SM; wider rows (tetrahedral meshes: levels of thousands of
-  // rows reaching two or three levels back) one CTA per SM with the larger
-  // ring.
+  // solo sweeps, one CTA per SM: the ring takes up to a third of the shared
+  // memory (a power of two of steps, at most 512), the chunk stages the rest:
+  // a power of two of them (<= 32), each holding up to ch_max steps' records
+  // and right-hand sides, ch_max (2..8) chosen for the most steps in flight
   for (int k = 0; k < kClasses; ++k) {
     const int b = class_b(k), maxe = class_maxe(k);
-    const size_t budget = std::min<size_t>(S->ctx->smem_optin, (size_t)per_sm_bytes / (maxe <= 4 ? 2 : 1)) - 2048;
+    const size_t budget = std::min<size_t>(S->ctx->smem_optin, (size_t)per_sm_bytes) - 4096;
     const size_t step_ring = (size_t)32 * b * elem;
     int R = 512;
     while (R > 16 && (size_t)R * step_ring > budget / 3) R /= 2;
     S->solo_R[k] = R;
-    const int vs = solo_val_stage(b, elem);
     size_t worst = 0;
     for (int dir = 0; dir < 2; ++dir) {
-      const int rs = (int)((solo_rec_bytes(maxe, b * b, elem, dir == 0) + 15) / 16 * 16);
-      S->solo_rec_stage[k][dir] = rs;
-      const size_t fixed = solo_smem_bytes(0, rs, vs, R, b, elem) + 3 * 8 * 32;
-      const int fit = (int)std::min<size_t>(32, (budget - std::min(budget, fixed)) / (size_t)(rs + vs));
-      int ns = 4;
-      while (ns * 2 <= fit) ns *= 2;  // a power of two
-      S->solo_ns[k][dir] = ns;
-      S->solo_smem[k][dir] = solo_smem_bytes(ns, rs, vs, R, b, elem);
+      const long long rec1 = solo_rec_bytes(maxe, b * b, elem, dir == 0);
+      const size_t fixed = solo_smem_bytes(32, 0, 0, R, b, elem);
+      int best_ch = 2, best_ns = 0;
+      for (int ch = 2; ch <= 8; ++ch) {
+        const size_t per_stage = (size_t)ch * rec1 + (size_t)solo_val_stage(ch, b, elem);
+        const int fit = (int)std::min<size_t>(32, (budget - std::min(budget, fixed)) / per_stage);
+        int ns = 0;
+        if (fit >= 2) {
+          ns = 2;
+          while (ns * 2 <= fit) ns *= 2;
+        }
+        if (ns * ch > best_ns * best_ch) { best_ns = ns; best_ch = ch; }
+      }
+      if (best_ns < 2) throw CudaFail{cudaErrorInvalidValue, "solo sweep stages do not fit in shared memory"};
+      S->solo_ch[k][dir] = best_ch;
+      S->solo_rec_stage[k][dir] = (int)(best_ch * rec1);
+      S->solo_ns[k][dir] = best_ns;
+      S->solo_smem[k][dir] = solo_smem_bytes(best_ns, (int)(best_ch * rec1), solo_val_stage(best_ch, b, elem), R, b, elem);
       worst = std::max(worst, S->solo_smem[k][dir]);
     }
-    const int per_sm = std::max(1, std::min(2, (int)(per_sm_bytes / (worst + 1024))));
-    S->solo_grid[k] = S->nsm * per_sm;
     if (worst > S->ctx->smem_optin) throw CudaFail{cudaErrorInvalidValue, "solo sweep shared memory"};
+    S->solo_grid[k] = S->nsm;
   }
 }
 

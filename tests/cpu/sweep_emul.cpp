@@ -306,18 +306,26 @@ extern "C" int emul_level_sweep(int n, int b, const int* rowptr, const int* coli
   return 0;
 }
 
-// Executes the one-CTA-per-solve schedule (solo_sweep_plan + the record codes
-// of pack_solo_headers) the way k_solo.cu does: levels in order, the steps of
-// a level concurrently (each reads the ring and the output as they stood when
-// the level began), every step writing its ring slot (step mod R) and the
-// output.  Checks: every row once; a ring code decodes to the slot its
-// dependency was written to, that slot is not rewritten by any step of the
-// consuming level (the kernel's warps run a level's steps in any order), and
-// holds the dependency's row; a global code names a row finished in an
-// earlier level.  out receives the result (the kernel's summation order).
-extern "C" int emul_solo_sweep(int n, int b, const int* rowptr, const int* colind, int forward, int R, int elem,
-                               const double* fdiag, const double* foffd, const double* rhs, double* out,
-                               long long* info) {
+// Executes the one-CTA-per-solve schedules (solo_sweep_plan + the records of
+// pack_solo_headers) the way k_solo.cu runs them, forward then backward, with
+// the storage orders the server uses: the forward input in the forward
+// plan's step order, y written in the backward plan's step order (where the
+// backward sweep reads its input and the forward sweep its global
+// dependencies), z in row order.  Per direction: levels in order, a level's
+// chunks and steps concurrently (each step reads the ring and the output as
+// they stood when the level began), every step writing its ring slot (step
+// mod R) and its output position.  Checks: every row once; chunks tile each
+// level, hold at most ch_max steps and stage_bytes of records, and carry one
+// entry count; a ring code decodes to the slot its dependency was written to,
+// that slot is not rewritten by any step of the consuming level, and holds
+// the dependency's row; a global code names a row finished in an earlier
+// level, at its storage position.  z receives the result (the kernel's
+// summation order).  info: [0] forward levels, [1] forward steps, [2] largest
+// entry count, [3] error code, [4] ring references, [5] global references,
+// [6] chunks (forward + backward).
+extern "C" int emul_solo_precond(int n, int b, const int* rowptr, const int* colind, int R, int elem,
+                                 int stage_bytes, int ch_max, const double* fdiag, const double* foffd,
+                                 const double* rhs, double* z, long long* info) {
   std::vector<int> diaind(n);
   for (int i = 0; i < n; ++i) {
     int d = rowptr[i + 1];
@@ -325,98 +333,126 @@ extern "C" int emul_solo_sweep(int n, int b, const int* rowptr, const int* colin
       if (colind[c] > i) { d = c; break; }
     diaind[i] = d;
   }
-  SweepPlan P = solo_sweep_plan(n, b, rowptr, colind, diaind.data(), forward != 0, R);
-  std::vector<long long> off;
-  long long max_rec = 0;
-  const std::vector<unsigned char> h = pack_solo_headers(P, elem, off, max_rec);
+  const SoloPlan SF = solo_sweep_plan(n, b, rowptr, colind, diaind.data(), true, R, elem, stage_bytes, ch_max);
+  const SoloPlan SB = solo_sweep_plan(n, b, rowptr, colind, diaind.data(), false, R, elem, stage_bytes, ch_max);
+  std::vector<int> ident(n);
+  for (int i = 0; i < n; ++i) ident[i] = i;
   const int bs = b * b;
-  info[0] = P.nranges;  // levels
-  info[1] = P.nsteps;
-  info[2] = P.max_nent;
-  info[3] = 0;
-  info[4] = 0;          // ring references
-  info[5] = 0;          // global references
-  info[6] = max_rec;
-  std::vector<int> seen(n, 0), level_of(n, -1);
-  for (int l = 0; l < P.nranges; ++l)
-    for (int s = P.range_steps[l]; s < P.range_steps[l + 1]; ++s)
-      for (int ln = 0; ln < 32; ++ln) {
-        const int row = P.step_rows[(size_t)s * 32 + ln];
-        if (row >= 0) { seen[row]++; level_of[row] = l; }
-      }
+  for (int k = 0; k < 7; ++k) info[k] = 0;
+  info[0] = SF.P.nranges;
+  info[1] = SF.P.nsteps;
+  info[2] = std::max(SF.P.max_nent, SB.P.max_nent);
+  info[6] = (long long)(SF.chunks.size() + SB.chunks.size());
+  // storage: forward input and y in step order (padded), z in row order
+  std::vector<double> xin((size_t)SF.P.nsteps * 32 * b, NAN), y((size_t)SB.P.nsteps * 32 * b, NAN);
   for (int i = 0; i < n; ++i)
-    if (seen[i] != 1) { info[3] = 1; return 1; }
-  std::vector<int> ring_row((size_t)R * 32, -1);
-  std::vector<double> ring((size_t)R * 32 * b, NAN);
-  std::vector<char> done(n, 0);
-  std::vector<char> written_now(R, 0);
-  for (int l = 0; l < P.nranges; ++l) {
-    std::fill(written_now.begin(), written_now.end(), 0);
-    for (int s = P.range_steps[l]; s < P.range_steps[l + 1]; ++s) written_now[s % R] = 1;
-    struct W { int row; double y[3]; int slot; };
-    std::vector<W> writes;
-    for (int s = P.range_steps[l]; s < P.range_steps[l + 1]; ++s) {
-      const unsigned char* rec = h.data() + off[s];
-      int nent = 0;
-      std::memcpy(&nent, rec, 4);
-      if (nent != P.step_nent[s]) { info[3] = 2; return 2; }
-      const int* rows = reinterpret_cast<const int*>(rec + 16);
-      const int* code = reinterpret_cast<const int*>(rec + 144);
-      for (int ln = 0; ln < 32; ++ln) {
-        const int row = rows[ln];
-        if (row != P.step_rows[(size_t)s * 32 + ln]) { info[3] = 3; return 3; }
-        if (row < 0) continue;
-        const int c0 = forward ? rowptr[row] : diaind[row];
-        const int c1 = forward ? diaind[row] : rowptr[row + 1];
-        double t[3];
-        for (int d = 0; d < b; ++d) t[d] = rhs[(size_t)row * b + d];
-        for (int e = 0; e < nent; ++e) {
-          const int c = code[e * 32 + ln];
-          if (e >= c1 - c0) {
-            if (c != 0) { info[3] = 4; return 4; }
-            continue;
-          }
-          const int k = colind[c0 + e];
-          double v[3];
-          if (c >= 0) {
-            if (c < 32 || (c - 32) % (b * elem) != 0) { info[3] = 5; return 5; }
-            const int idx = (c - 32) / (b * elem);
-            if (idx >= R * 32 || ring_row[idx] != k || written_now[idx / 32]) { info[3] = 6; return 6; }
-            for (int d = 0; d < b; ++d) v[d] = ring[(size_t)idx * b + d];
-            info[4]++;
-          } else {
-            if (-c - 1 != k || !done[k] || level_of[k] >= l) { info[3] = 7; return 7; }
-            for (int d = 0; d < b; ++d) v[d] = out[(size_t)k * b + d];
-            info[5]++;
-          }
-          const double* blk = foffd + (size_t)(c0 + e) * bs;
-          for (int p = 0; p < b; ++p) {
-            double acc = t[p];
-            for (int q = 0; q < b; ++q) acc -= blk[p * b + q] * v[q];
-            t[p] = acc;
-          }
+    for (int d = 0; d < b; ++d) xin[(size_t)SF.pos[i] * b + d] = rhs[(size_t)i * b + d];
+  for (int i = 0; i < n * b; ++i) z[i] = NAN;
+  for (int dir = 0; dir < 2; ++dir) {
+    const bool forward = dir == 0;
+    const SoloPlan& S = forward ? SF : SB;
+    const SweepPlan& P = S.P;
+    const int* out_pos = forward ? SB.pos.data() : ident.data();
+    std::vector<long long> off;
+    const std::vector<unsigned char> h = pack_solo_headers(S, elem, out_pos, out_pos, off);
+    const double* in = forward ? xin.data() : y.data();
+    double* out = forward ? y.data() : z;
+    std::vector<int> seen(n, 0), level_of(n, -1);
+    for (int l = 0; l < P.nranges; ++l)
+      for (int s = P.range_steps[l]; s < P.range_steps[l + 1]; ++s)
+        for (int ln = 0; ln < 32; ++ln) {
+          const int row = P.step_rows[(size_t)s * 32 + ln];
+          if (row >= 0) { seen[row]++; level_of[row] = l; }
         }
-        W w{row, {0, 0, 0}, (s % R) * 32 + ln};
-        if (forward) {
-          const double* dv = fdiag + (size_t)row * bs;
-          for (int p = 0; p < b; ++p) {
-            double acc = dv[p * b] * t[0];
-            for (int q = 1; q < b; ++q) acc += dv[p * b + q] * t[q];
-            w.y[p] = acc;
-          }
-        } else {
-          for (int p = 0; p < b; ++p) w.y[p] = t[p];
-        }
-        writes.push_back(w);
+    for (int i = 0; i < n; ++i)
+      if (seen[i] != 1) { info[3] = 1; return 1; }
+    // chunks: tile each level in order, bounded, one size per chunk
+    if ((int)S.lev_chunks.size() != P.nranges + 1) { info[3] = 8; return 8; }
+    for (int l = 0; l < P.nranges; ++l) {
+      int next = P.range_steps[l];
+      for (int c = S.lev_chunks[l]; c < S.lev_chunks[l + 1]; ++c) {
+        const SoloChunk& ch = S.chunks[c];
+        if (ch.first_step != next || ch.nsteps < 1 || ch.nsteps > ch_max || ch.rec_off != off[ch.first_step] ||
+            ch.rec_bytes != off[ch.first_step + ch.nsteps] - off[ch.first_step] ||
+            (ch.nsteps > 1 && ch.rec_bytes > stage_bytes)) { info[3] = 9; return 9; }
+        for (int s = ch.first_step; s < ch.first_step + ch.nsteps; ++s)
+          if (P.step_nent[s] != ch.nent) { info[3] = 10; return 10; }
+        next += ch.nsteps;
       }
+      if (next != P.range_steps[l + 1]) { info[3] = 11; return 11; }
     }
-    for (const W& w : writes) {
-      for (int d = 0; d < b; ++d) {
-        out[(size_t)w.row * b + d] = w.y[d];
-        ring[(size_t)w.slot * b + d] = w.y[d];
+    std::vector<int> ring_row((size_t)R * 32, -1);
+    std::vector<double> ring((size_t)R * 32 * b, NAN);
+    std::vector<char> done(n, 0), written_now(R, 0);
+    for (int l = 0; l < P.nranges; ++l) {
+      std::fill(written_now.begin(), written_now.end(), 0);
+      for (int s = P.range_steps[l]; s < P.range_steps[l + 1]; ++s) written_now[s % R] = 1;
+      struct W { int row, o, slot; double y[3]; };
+      std::vector<W> writes;
+      for (int s = P.range_steps[l]; s < P.range_steps[l + 1]; ++s) {
+        const unsigned char* rec = h.data() + off[s];
+        int hdr[4];
+        std::memcpy(hdr, rec, 16);
+        const int nent = hdr[0];
+        if (nent != P.step_nent[s] || hdr[2] != s) { info[3] = 2; return 2; }
+        const int* outv = reinterpret_cast<const int*>(rec + 16);
+        const int* code = reinterpret_cast<const int*>(rec + 144);
+        for (int ln = 0; ln < 32; ++ln) {
+          const int row = P.step_rows[(size_t)s * 32 + ln];
+          if (outv[ln] != (row >= 0 ? out_pos[row] : -1)) { info[3] = 3; return 3; }
+          if (row < 0) continue;
+          const int c0 = forward ? rowptr[row] : diaind[row];
+          const int c1 = forward ? diaind[row] : rowptr[row + 1];
+          double t[3];
+          for (int d = 0; d < b; ++d) t[d] = in[((size_t)s * 32 + ln) * b + d];
+          for (int e = 0; e < nent; ++e) {
+            const int c = code[e * 32 + ln];
+            if (e >= c1 - c0) {
+              if (c != 0) { info[3] = 4; return 4; }
+              continue;
+            }
+            const int k = colind[c0 + e];
+            double v[3];
+            if (c >= 0) {
+              if (c < 32 || (c - 32) % (b * elem) != 0) { info[3] = 5; return 5; }
+              const int idx = (c - 32) / (b * elem);
+              if (idx >= R * 32 || ring_row[idx] != k || written_now[idx / 32]) { info[3] = 6; return 6; }
+              for (int d = 0; d < b; ++d) v[d] = ring[(size_t)idx * b + d];
+              info[4]++;
+            } else {
+              if (-c - 1 != out_pos[k] || !done[k] || level_of[k] >= l) { info[3] = 7; return 7; }
+              for (int d = 0; d < b; ++d) v[d] = out[(size_t)(-c - 1) * b + d];
+              info[5]++;
+            }
+            const double* blk = foffd + (size_t)(c0 + e) * bs;
+            for (int p = 0; p < b; ++p) {
+              double acc = t[p];
+              for (int q = 0; q < b; ++q) acc -= blk[p * b + q] * v[q];
+              t[p] = acc;
+            }
+          }
+          W w{row, outv[ln], (s % R) * 32 + ln, {0, 0, 0}};
+          if (forward) {
+            const double* dv = fdiag + (size_t)row * bs;
+            for (int p = 0; p < b; ++p) {
+              double acc = dv[p * b] * t[0];
+              for (int q = 1; q < b; ++q) acc += dv[p * b + q] * t[q];
+              w.y[p] = acc;
+            }
+          } else {
+            for (int p = 0; p < b; ++p) w.y[p] = t[p];
+          }
+          writes.push_back(w);
+        }
       }
-      ring_row[w.slot] = w.row;
-      done[w.row] = 1;
+      for (const W& w : writes) {
+        for (int d = 0; d < b; ++d) {
+          out[(size_t)w.o * b + d] = w.y[d];
+          ring[(size_t)w.slot * b + d] = w.y[d];
+        }
+        ring_row[w.slot] = w.row;
+        done[w.row] = 1;
+      }
     }
   }
   return 0;

@@ -28,8 +28,8 @@ def emul():
     L = ctypes.CDLL(EMUL_SO)
     P = ctypes.c_void_p
     L.emul_sweep.argtypes = [ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P, P]
-    L.emul_solo_sweep.argtypes = [ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P,
-                                  P, P]
+    L.emul_solo_precond.argtypes = [ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_int, P, P, P, P, P]
     L.emul_ilu_pattern.restype = ctypes.c_longlong
     L.emul_ilu_pattern.argtypes = [ctypes.c_int, P, P, ctypes.c_int, P, P, ctypes.c_longlong]
     return L
@@ -122,48 +122,46 @@ def test_serving_schedule_has_fuller_steps(emul, oracle_lib):
         assert fill[-1] > 20, fill
 
 
+def _solo(emul, out, R, elem, stage_bytes, ch_max, rhs):
+    n, b = out["n"], out["b"]
+    fo = out["foffd"] if out["foffd"].size else np.zeros(1)
+    z = np.full(n * b, np.nan)
+    info = np.zeros(8, dtype=np.int64)
+    rc = emul.emul_solo_precond(n, b, _p(out["rowptr"]), _p(out["colind"]), R, elem, stage_bytes, ch_max,
+                                _p(out["fdiag"]), _p(fo), _p(rhs), _p(z), _p(info))
+    return rc, z, info
+
+
 @pytest.mark.parametrize("idx", range(4))
-@pytest.mark.parametrize("R", [16, 256])
+@pytest.mark.parametrize("R,stage,ch", [(16, 4096, 2), (256, 20000, 4), (512, 100000, 8)])
 @pytest.mark.parametrize("elem", [4, 8])
-def test_solo_schedule(emul, oracle_lib, idx, R, elem):
-    """The one-CTA-per-solve schedule executed as k_solo.cu runs it, through
-    its packed record codes: complete coverage, ring references that the
+def test_solo_schedule(emul, oracle_lib, idx, R, stage, ch, elem):
+    """The one-CTA-per-solve schedules executed as k_solo.cu runs them,
+    through their packed records and the server's storage orders: chunks
+    that tile each level within their bounds, ring references that the
     consuming level never overwrites, global references to rows of earlier
-    levels only, and forward/backward results equal to the oracle's
-    substitutions up to rounding."""
+    levels at their storage positions, and a preconditioner apply equal to the
+    oracle's substitutions up to rounding."""
     p = _problems()[idx]
     out = oracle_lib.solve(p, stop_after_ilu=True)
     n, b = out["n"], out["b"]
     rhs = np.random.default_rng(idx).standard_normal(n * b)
-    fo = out["foffd"] if out["foffd"].size else np.zeros(1)
-    y = np.full(n * b, np.nan)
-    z = np.full(n * b, np.nan)
-    info = np.zeros(8, dtype=np.int64)
-    assert emul.emul_solo_sweep(n, b, _p(out["rowptr"]), _p(out["colind"]), 1, R, elem, _p(out["fdiag"]), _p(fo),
-                                _p(rhs), _p(y), _p(info)) == 0, info
-    levels_fwd = info[0]
-    assert info[4] + info[5] > 0
-    assert emul.emul_solo_sweep(n, b, _p(out["rowptr"]), _p(out["colind"]), 0, R, elem, _p(out["fdiag"]), _p(fo),
-                                _p(y), _p(z), _p(info)) == 0, info
+    rc, z, info = _solo(emul, out, R, elem, stage, ch, rhs)
+    assert rc == 0, info
+    assert info[4] + info[5] > 0 and info[6] >= 2 * info[0] // 2
     dind = oracle_lib.diaind(out["rowptr"], out["colind"])
     zref = oracle_lib.precond(n, b, out["rowptr"], out["colind"], dind, out["fdiag"], out["foffd"], rhs)
     np.testing.assert_allclose(z, zref, rtol=1e-12, atol=1e-13 * np.abs(zref).max())
-    assert levels_fwd >= 1
 
 
 def test_solo_schedule_ring_covers_2d_levels(emul, oracle_lib):
-    """On a serving-sized 2D mesh the ring (256 steps) holds every dependency:
-    a level's rows depend on the level before it only."""
+    """On a serving-sized 2D mesh a 128-step ring holds every dependency: a
+    level's rows depend on the level before it only."""
     from delfem_gb300 import meshgen as mg
     p = mg.rect_problem_2d(mg.SOLID2D, 30000, seed=3)
     out = oracle_lib.solve(p, stop_after_ilu=True)
-    n, b = out["n"], out["b"]
-    y = np.zeros(n * b)
-    info = np.zeros(8, dtype=np.int64)
-    fo = out["foffd"] if out["foffd"].size else np.zeros(1)
-    assert emul.emul_solo_sweep(n, b, _p(out["rowptr"]), _p(out["colind"]), 1, 128, 4, _p(out["fdiag"]), _p(fo),
-                                _p(np.ones(n * b)), _p(y), _p(info)) == 0
-    assert info[5] == 0 and info[4] > 0, info
+    rc, z, info = _solo(emul, out, 128, 4, 30000, 8, np.ones(out["n"] * out["b"]))
+    assert rc == 0 and info[5] == 0 and info[4] > 0, info
 
 
 def test_library_fill_pattern_matches_reference(emul):
