@@ -99,7 +99,8 @@ SoloPlan solo_sweep_plan(int n, int b, const int* rowptr, const int* colind, con
                          int R, int elem, int stage_bytes, int ch_max);
 
 // byte layout of one solo step record (k_solo.cu):
-//   [hdr int4: nent, chunk steps, step, 0][out: 32 int][code nent*32*4][blk nent*32*bs*sz][dinv 32*bs*sz (forward only)]
+//   [hdr int4: nent, chunk steps, step, chunk's first step - its level's first step]
+//   [out: 32 int][code nent*32*4][blk nent*32*bs*sz][dinv 32*bs*sz (forward only)]
 inline long long solo_rec_bytes(int nent, int bs, int sz, bool forward) {
   return 16 + 128 + (long long)nent * 128 + (long long)nent * 32 * bs * sz + (forward ? 32LL * bs * sz : 0);
 }

@@ -15,9 +15,9 @@
 //     records, and its right-hand sides, which the producing kernel stored in
 //     this sweep's step order so that they are contiguous; it runs up to NS
 //     chunks ahead of the compute warps.
-//   * compute warps -- level by level, chunk by chunk: warp w takes steps w,
-//     w + kSoloWarps, ... of the chunk (every record of a chunk has the same
-//     size, so its offset is arithmetic), evaluates the step's 32 rows, writes
+//   * compute warps -- level by level, chunk by chunk: warp w takes the steps
+//     w, w + kSoloWarps, ... of the level (every record of a chunk has the
+//     same size, so a step's offset is arithmetic), evaluates the step's 32 rows, writes
 //     the results to the shared-memory ring (slot step mod R) and to the
 //     output vector at the records' output positions, and arrives on the
 //     stage's `empty` mbarrier (kSoloWarps arrivals free the stage); a named
@@ -30,7 +30,8 @@
 // wait that gives up records kErrTimeout and the launch drains and returns.
 //
 // Record layout (bytes; pack_solo_headers in sched.cpp, values by k_pack):
-//   [hdr int4: nent, steps in the chunk, step, 0][out: 32 int][code: nent x 32 int]
+//   [hdr int4: nent, steps in the chunk, step, the chunk's offset in its level]
+//   [out: 32 int][code: nent x 32 int]
 //   [blocks: nent x B*B x 32 of T][D^-1: B*B x 32 of T, forward only]
 // out: the element offset / B where a lane's result goes (-1: empty lane);
 // code >= 0: byte offset into the ring region (0 = 32 zero bytes, padding);
@@ -133,10 +134,14 @@ __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
           const int st = pos & NSM;
           if (!abort && !mbar_wait(&full[st], (unsigned)((pos >> NSL) & 1), a.err, kSiteFull, jslot, c)) abort = true;
           const unsigned char* stage = rstage + (size_t)st * a.rec_stage;
-          const int nent = reinterpret_cast<const int*>(stage)[0];
-          const int nst = abort ? 0 : reinterpret_cast<const int*>(stage)[1];
+          const int4 hdr = *reinterpret_cast<const int4*>(stage);
+          const int nent = hdr.x;
+          const int nst = abort ? 0 : hdr.y;
           const int rec_sz = 144 + nent * 128 + nent * 32 * BS * SZ + (FWD ? 32 * BS * SZ : 0);
-          for (int k = warp; k < nst; k += NW) {
+          // steps go to warps by their place in the level (hdr.w: the chunk's
+          // offset there), so a level of <= kSoloWarps steps costs each warp
+          // one step whatever its chunks
+          for (int k = (warp - hdr.w % NW + NW) % NW; k < nst; k += NW) {
             const unsigned char* rec = stage + (size_t)k * rec_sz;
             const int s = reinterpret_cast<const int*>(rec)[2];
             const int o = reinterpret_cast<const int*>(rec + 16)[lane];

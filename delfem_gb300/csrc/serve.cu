@@ -298,21 +298,21 @@ namespace {
 // solve's whole dependency chain on one SM, and the in-flight solves fill
 // the device; the ranged kernel (k_sweep.cu) spreads one solve over many
 // SMs at the price of cross-SM hand-offs (about 0.75 us per dependency level
-// in batched launches).  FP32 sweeps always take one CTA: their FMAs are
-// cheap.  An FP64 sweep on one SM is bound by GB300's FP64 FMA rate (about
-// 1.6 lanes per clock per SM, shared by the SM's two sweep CTAs), so an FP64
-// solve takes one CTA only while its FMA time there stays below the ranged
-// kernel's chain time: 1x1-block solves up to a few hundred thousand rows,
-// 2x2 and 3x3 ones only when small.
+// in batched launches).  FP32 sweeps take one CTA, except the largest
+// solves with 2x2 or 3x3 blocks: their records (about 100 bytes per row for
+// 2x2) outrun what one SM keeps in flight against HBM latency, and spreading
+// them wins.  Measured on GB300 over bands of the 2D serving stream (FP32
+// factor, solves/s, ranged -> one CTA): 1x1 blocks 231 -> 295 (2k-20k
+// nodes), 58 -> 84, 19 -> 28, 5.5 -> 7.1 (150k-400k); 2x2 blocks 142 -> 158,
+// 34 -> 40, 13.0 -> 13.7 (60k-150k), 2.6 -> 2.2 (150k-400k).  FP64 sweeps
+// stay ranged: on one SM every level waits on a chain of dependent FP64 FMAs
+// (64 cycles each on GB300), about twice the ranged kernel's time beyond
+// the smallest solves.
+constexpr int kSoloMaxNodesBlocked = 150000;
 bool use_solo(const dfg_server_s* S, const Req* r) {
   if (S->sweeps == 1) return false;
   if (S->sweeps == 2) return true;
-  if (S->fp32) return true;
-  const double levels = (double)std::max<size_t>(r->lev.ptr.size(), 2) - 1;
-  const double fma_per_row = (double)(r->maxe + 1) * r->b * r->b;  // deps and D^-1, per block row
-  const double solo_s = (double)r->n * fma_per_row / (1.6 * 2.0e9 / 2.0);
-  const double ranged_s = levels * 0.75e-6;
-  return solo_s < ranged_s;
+  return S->fp32 && (r->b == 1 || r->n <= kSoloMaxNodesBlocked);
 }
 
 // Fills the request's host-side set-up; returns false with r->error on failure.

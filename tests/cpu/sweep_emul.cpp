@@ -395,6 +395,12 @@ extern "C" int emul_solo_precond(int n, int b, const int* rowptr, const int* col
         std::memcpy(hdr, rec, 16);
         const int nent = hdr[0];
         if (nent != P.step_nent[s] || hdr[2] != s) { info[3] = 2; return 2; }
+        {  // the chunk's offset in its level, as the kernel distributes steps
+          const SoloChunk* ch = nullptr;
+          for (int c = S.lev_chunks[l]; c < S.lev_chunks[l + 1]; ++c)
+            if (S.chunks[c].first_step <= s && s < S.chunks[c].first_step + S.chunks[c].nsteps) ch = &S.chunks[c];
+          if (!ch || hdr[1] != ch->nsteps || hdr[3] != ch->first_step - P.range_steps[l]) { info[3] = 12; return 12; }
+        }
         const int* outv = reinterpret_cast<const int*>(rec + 16);
         const int* code = reinterpret_cast<const int*>(rec + 144);
         for (int ln = 0; ln < 32; ++ln) {
