@@ -50,8 +50,7 @@ __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
   constexpr int STEP_RHS = 32 * B * SZ;  // right-hand-side bytes of one step
   extern __shared__ __align__(128) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int NS = a.NS;  // a power of two: stage = pos & NSM, phase = (pos >> NSL) & 1
-  const int NSM = NS - 1, NSL = __ffs(NS) - 1;
+  const int NS = a.NS;
   const int RM = a.R - 1;
   const int VS = a.ch_max * STEP_RHS;
   // layout: [bars: 2*NS u64][rstage: NS x rec_stage][vstage: NS x VS][zero 32 B][ring: R x 32 x B of T]
@@ -88,6 +87,9 @@ __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
     const SoloSlot& S = a.batch->slot[jslot];
     const int nch = S.nchunks;
     bool abort = false;
+    // pipeline position g: its stage and that stage's use parity; both sides
+    // then advance them chunk by chunk (every warp visits every chunk)
+    const int st0 = g % NS, ph0 = (g / NS) & 1;
     if (warp == NW) {
       // ------------------------------------------------------------ producer
       if (lane == 0) {
@@ -96,13 +98,12 @@ __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
         const SoloChunk* __restrict__ chunks = S.chunks;
         int n_issued = 0;
         SoloChunk nx = nch > 0 ? chunks[0] : SoloChunk{};
+        int st = st0, ph = ph0;
         for (int c = 0; c < nch; ++c) {
           const SoloChunk ch = nx;
           if (c + 1 < nch) nx = chunks[c + 1];  // the next chunk's entry, off the critical path
-          const int pos = g + c;
-          const int st = pos & NSM;
-          const int use = pos >> NSL;
-          if (use >= 1 && !mbar_wait(&empty[st], (unsigned)((use - 1) & 1), a.err, kSiteEmpty, jslot, c)) {
+          // the stage's previous use (phase ph ^ 1) must have been released
+          if (g + c >= NS && !mbar_wait(&empty[st], (unsigned)(ph ^ 1), a.err, kSiteEmpty, jslot, c)) {
             abort = true;
             break;
           }
@@ -111,11 +112,13 @@ __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
           tma_load_1d(rstage + (size_t)st * a.rec_stage, recs + ch.rec_off, (unsigned)ch.rec_bytes, &full[st]);
           tma_load_1d(vstage + (size_t)st * VS, in + (size_t)ch.first_step * STEP_RHS, rhs_bytes, &full[st]);
           ++n_issued;
+          if (++st == NS) { st = 0; ph ^= 1; }
         }
         if (abort) {  // copies already issued land before the CTA moves on (bounded)
+          int dst = st0, dph = ph0;
           for (int k = 0; k < n_issued; ++k) {
-            const int pos = g + k;
-            mbar_drain(&full[pos & NSM], (unsigned)((pos >> NSL) & 1));
+            mbar_drain(&full[dst], (unsigned)dph);
+            if (++dst == NS) { dst = 0; dph ^= 1; }
           }
         }
       }
@@ -127,12 +130,11 @@ __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
       const int nl = S.nlevels;
       // level bounds come one level ahead, so their load is off the critical path
       int c0 = lc[0], c1 = nl > 0 ? lc[1] : 0;
+      int st = st0, ph = ph0;
       for (int l = 0; l < nl; ++l) {
         const int c2 = l + 2 <= nl ? __ldg(&lc[l + 2]) : 0;
-        for (int c = c0; c < c1; ++c) {
-          const int pos = g + c;
-          const int st = pos & NSM;
-          if (!abort && !mbar_wait(&full[st], (unsigned)((pos >> NSL) & 1), a.err, kSiteFull, jslot, c)) abort = true;
+        for (int c = c0; c < c1; ++c, (++st == NS ? (st = 0, ph ^= 1) : 0)) {
+          if (!abort && !mbar_wait(&full[st], (unsigned)ph, a.err, kSiteFull, jslot, c)) abort = true;
           const unsigned char* stage = rstage + (size_t)st * a.rec_stage;
           const int4 hdr = *reinterpret_cast<const int4*>(stage);
           const int nent = hdr.x;

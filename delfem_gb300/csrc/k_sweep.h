@@ -104,7 +104,7 @@ struct SoloArgs {
   int* err;          // device error word
   int rec_stage;     // bytes per record stage (>= every chunk's records, 16-aligned)
   int ch_max;        // steps per chunk at most (sizes the right-hand-side stage)
-  int NS;            // pipeline stages (a power of two)
+  int NS;            // pipeline stages
   int R;             // ring depth in steps (a power of two)
   int max_nent;      // selects the unrolled variant
 };
