@@ -1012,7 +1012,7 @@ cudaError_t enqueue_sweep(const SweepLaunch& L, cudaStream_t st) {
   if (!L.levels) return launch_sweep(L.forward, L.fp32, L.b, L.args, L.grid, L.smem, st);
   const Levels& V = *L.lev;
   for (size_t l = 0; l + 1 < V.ptr.size(); ++l) {
-    const cudaError_t e = launch_sweep_level(L.forward, L.fp32, L.b, L.la, V.ptr[l], V.ptr[l + 1] - V.ptr[l], st);
+    const cudaError_t e = launch_sweep_level(L.forward, L.fp32, L.b, L.la, V.ptr[l], V.ptr[l + 1] - V.ptr[l], l > 0, st);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;

@@ -137,7 +137,10 @@ inline int level_group_lanes(int max_entries) {
   while (g < 32 && g < max_entries) g *= 2;
   return g;
 }
+// dependent: launch as a programmatic dependent of the previous kernel in the
+// stream (a previous level of the same sweep; the first level is launched in
+// plain stream order)
 cudaError_t launch_sweep_level(bool forward, bool fp32, int b, const LevelSweepArgs& a, int first, int cnt,
-                               cudaStream_t s);
+                               bool dependent, cudaStream_t s);
 
 }  // namespace dfg
