@@ -1007,9 +1007,11 @@ SweepLaunch sweep_launch(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, bool fp32, c
 
 // Launches one sweep on stream st (no error check and no launch count, so
 // that it can be captured into a graph); the ranged kernel or one launch per
-// level.
-cudaError_t enqueue_sweep(const SweepLaunch& L, cudaStream_t st) {
-  if (!L.levels) return launch_sweep(L.forward, L.fp32, L.b, L.args, L.grid, L.smem, st);
+// level.  dep: the ranged kernel as a programmatic dependent of the previous
+// kernel in the stream (a level sweep's first launch always waits in stream
+// order: it reads the solve's stop flag before waiting).
+cudaError_t enqueue_sweep(const SweepLaunch& L, cudaStream_t st, bool dep = false) {
+  if (!L.levels) return launch_sweep(L.forward, L.fp32, L.b, L.args, L.grid, L.smem, st, dep);
   const Levels& V = *L.lev;
   for (size_t l = 0; l + 1 < V.ptr.size(); ++l) {
     const cudaError_t e = launch_sweep_level(L.forward, L.fp32, L.b, L.la, V.ptr[l], V.ptr[l + 1] - V.ptr[l], l > 0, st);
@@ -1500,12 +1502,15 @@ static int solve_pcg_f64vec(dfg_system sys, dfg_precond prec, bool fp32z, bool t
     Chunk g;
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     for (int c = 0; c < chunk; ++c) {
-      pcg_spmv_pap(A, v, st, red, ctx->stream);
-      pcg_update_rx(v, st, red, sc.tickets, fp32z, ctx->stream);
-      enqueue_sweep(F, ctx->stream);
-      enqueue_sweep(B, ctx->stream);
-      pcg_rz_beta(v, st, red, fp32z, ctx->stream);
-      pcg_update_p(v, st, fp32z, ctx->stream);
+      // each kernel after the chunk's first starts as a programmatic
+      // dependent of the one before: its launch overlaps that kernel, and it
+      // waits for it at entry
+      pcg_spmv_pap(A, v, st, red, ctx->stream, c > 0);
+      pcg_update_rx(v, st, red, sc.tickets, fp32z, ctx->stream, true);
+      enqueue_sweep(F, ctx->stream, true);
+      enqueue_sweep(B, ctx->stream, true);
+      pcg_rz_beta(v, st, red, fp32z, ctx->stream, true);
+      pcg_update_p(v, st, fp32z, ctx->stream, true);
     }
     CK(cudaStreamEndCapture(ctx->stream, &g.graph));
     CK(cudaGraphInstantiate(&g.exec, g.graph, 0));

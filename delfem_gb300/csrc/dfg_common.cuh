@@ -71,6 +71,16 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
+// Programmatic dependent launch (kernels launched with
+// cudaLaunchAttributeProgrammaticStreamSerialization): wait until the
+// previous kernel in the stream has finished and its writes are visible,
+// then let the next kernel launch so that its start overlaps this one.  In a
+// kernel launched in plain stream order both are no-ops.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // error word shared by all kernels of a context (0 = ok)
 enum : int { kErrNone = 0, kErrTimeout = 1, kErrBadIndex = 2 };
 

@@ -11,6 +11,8 @@
 // partials in index order.
 #include <cmath>
 
+#include <utility>
+
 #include "dfg_common.cuh"
 #include "k_reduce.cuh"
 #include "k_rowmv.cuh"
@@ -25,6 +27,7 @@ namespace dfg {
 template <typename T, int B>
 __global__ void __launch_bounds__(kSpmvTpb, 2) k_spmv_pap(MatView Am, const T* __restrict__ p, T* __restrict__ q,
                                                          PcgState* st, Red red) {
+  pdl_enter();
   if (st->done) return;
   const T* sval = reinterpret_cast<const T*>(Am.sval);
   double part = 0.0;
@@ -133,6 +136,7 @@ __global__ void k_pcg_after_precond0(PcgVecs v, PcgState* st, Red red) {
 // convergence check; sentinel refill for the sweeps; sweep tickets reset
 template <typename Z>
 __global__ void k_pcg_update_rx(PcgVecs v, PcgState* st, Red red, int* tickets) {
+  pdl_enter();
   if (st->done) return;
   const double alpha = st->alpha;
   double part = 0.0;
@@ -173,6 +177,7 @@ __global__ void k_pcg_update_rx(PcgVecs v, PcgState* st, Red red, int* tickets) 
 // rz_new = r.z; beta = rz_new / rz
 template <typename Z>
 __global__ void k_pcg_rz_beta(PcgVecs v, PcgState* st, Red red) {
+  pdl_enter();
   if (st->done) return;
   double part = 0.0;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < v.m; k += (long long)gridDim.x * blockDim.x)
@@ -187,6 +192,7 @@ __global__ void k_pcg_rz_beta(PcgVecs v, PcgState* st, Red red) {
 // p := beta p; p := p + 1.0 z (SCAL + AXPY); iteration counter
 template <typename Z>
 __global__ void k_pcg_update_p(PcgVecs v, PcgState* st) {
+  pdl_enter();
   if (st->done) return;
   const double beta = st->beta;
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < v.m; k += (long long)gridDim.x * blockDim.x)
@@ -375,6 +381,22 @@ __global__ void k_fill_sentinel32(long long m, float* p) {
 // reductions always use the fixed grid (deterministic regardless of timing)
 #define RED_LAUNCH <<<kRedGrid, kRedTpb, 0, s>>>
 
+// dep: launch as a programmatic dependent of the previous kernel in the
+// stream (the kernel waits for it at entry, see pdl_enter)
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_dep(void (*k)(KArgs...), int grid, int block, cudaStream_t s, bool dep, Args&&... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = dep ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
+
 #define ZDISPATCH(kern, ...)                               \
   do {                                                     \
     if (fp32z) kern<float> RED_LAUNCH(__VA_ARGS__);        \
@@ -389,26 +411,27 @@ cudaError_t pcg_after_precond0(const PcgVecs& v, PcgState* st, Red red, bool fp3
   ZDISPATCH(k_pcg_after_precond0, v, st, red);
   return cudaGetLastError();
 }
-cudaError_t pcg_spmv_pap(const MatView& A, const PcgVecs& v, PcgState* st, Red red, cudaStream_t s) {
+cudaError_t pcg_spmv_pap(const MatView& A, const PcgVecs& v, PcgState* st, Red red, cudaStream_t s, bool dep) {
+  const double* p = v.p;
+  double* q = v.q;
   switch (A.b) {
-    case 1: k_spmv_pap<double, 1><<<kRedGrid, kSpmvTpb, 0, s>>>(A, v.p, v.q, st, red); break;
-    case 2: k_spmv_pap<double, 2><<<kRedGrid, kSpmvTpb, 0, s>>>(A, v.p, v.q, st, red); break;
-    case 3: k_spmv_pap<double, 3><<<kRedGrid, kSpmvTpb, 0, s>>>(A, v.p, v.q, st, red); break;
+    case 1: return launch_dep(k_spmv_pap<double, 1>, kRedGrid, kSpmvTpb, s, dep, A, p, q, st, red);
+    case 2: return launch_dep(k_spmv_pap<double, 2>, kRedGrid, kSpmvTpb, s, dep, A, p, q, st, red);
+    case 3: return launch_dep(k_spmv_pap<double, 3>, kRedGrid, kSpmvTpb, s, dep, A, p, q, st, red);
     default: return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
 }
-cudaError_t pcg_update_rx(const PcgVecs& v, PcgState* st, Red red, int* tickets, bool fp32z, cudaStream_t s) {
-  ZDISPATCH(k_pcg_update_rx, v, st, red, tickets);
-  return cudaGetLastError();
+cudaError_t pcg_update_rx(const PcgVecs& v, PcgState* st, Red red, int* tickets, bool fp32z, cudaStream_t s, bool dep) {
+  if (fp32z) return launch_dep(k_pcg_update_rx<float>, kRedGrid, kRedTpb, s, dep, v, st, red, tickets);
+  return launch_dep(k_pcg_update_rx<double>, kRedGrid, kRedTpb, s, dep, v, st, red, tickets);
 }
-cudaError_t pcg_rz_beta(const PcgVecs& v, PcgState* st, Red red, bool fp32z, cudaStream_t s) {
-  ZDISPATCH(k_pcg_rz_beta, v, st, red);
-  return cudaGetLastError();
+cudaError_t pcg_rz_beta(const PcgVecs& v, PcgState* st, Red red, bool fp32z, cudaStream_t s, bool dep) {
+  if (fp32z) return launch_dep(k_pcg_rz_beta<float>, kRedGrid, kRedTpb, s, dep, v, st, red);
+  return launch_dep(k_pcg_rz_beta<double>, kRedGrid, kRedTpb, s, dep, v, st, red);
 }
-cudaError_t pcg_update_p(const PcgVecs& v, PcgState* st, bool fp32z, cudaStream_t s) {
-  ZDISPATCH(k_pcg_update_p, v, st);
-  return cudaGetLastError();
+cudaError_t pcg_update_p(const PcgVecs& v, PcgState* st, bool fp32z, cudaStream_t s, bool dep) {
+  if (fp32z) return launch_dep(k_pcg_update_p<float>, kRedGrid, kRedTpb, s, dep, v, st);
+  return launch_dep(k_pcg_update_p<double>, kRedGrid, kRedTpb, s, dep, v, st);
 }
 cudaError_t pcg_true_residual(const MatView& A, const PcgVecs& v, PcgState* st, Red red, cudaStream_t s) {
   switch (A.b) {

@@ -67,10 +67,13 @@ struct PcgVecs {
 // fp32z: the preconditioned vectors y, z are float (FP32 factor and sweeps)
 cudaError_t pcg_init(const PcgVecs& v, PcgState* st, Red red, double tol, int maxit, int* tickets, bool fp32z, cudaStream_t s);
 cudaError_t pcg_after_precond0(const PcgVecs& v, PcgState* st, Red red, bool fp32z, cudaStream_t s);
-cudaError_t pcg_spmv_pap(const MatView& A, const PcgVecs& v, PcgState* st, Red red, cudaStream_t s);
-cudaError_t pcg_update_rx(const PcgVecs& v, PcgState* st, Red red, int* tickets, bool fp32z, cudaStream_t s);
-cudaError_t pcg_rz_beta(const PcgVecs& v, PcgState* st, Red red, bool fp32z, cudaStream_t s);
-cudaError_t pcg_update_p(const PcgVecs& v, PcgState* st, bool fp32z, cudaStream_t s);
+// dep (the four iteration kernels): launch as a programmatic dependent of the
+// previous kernel in the stream, which must be a kernel (a graph's chain)
+cudaError_t pcg_spmv_pap(const MatView& A, const PcgVecs& v, PcgState* st, Red red, cudaStream_t s, bool dep = false);
+cudaError_t pcg_update_rx(const PcgVecs& v, PcgState* st, Red red, int* tickets, bool fp32z, cudaStream_t s,
+                          bool dep = false);
+cudaError_t pcg_rz_beta(const PcgVecs& v, PcgState* st, Red red, bool fp32z, cudaStream_t s, bool dep = false);
+cudaError_t pcg_update_p(const PcgVecs& v, PcgState* st, bool fp32z, cudaStream_t s, bool dep = false);
 // rd = b - A x, rr = rd.rd (into st->rr; state otherwise untouched)
 cudaError_t pcg_true_residual(const MatView& A, const PcgVecs& v, PcgState* st, Red red, cudaStream_t s);
 // r = rd (and r32), sentinels, tickets reset, done = 0: continue from the true residual

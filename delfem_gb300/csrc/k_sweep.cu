@@ -85,6 +85,7 @@ __global__ void __launch_bounds__(64) k_sweep(SweepArgs a) {
   unsigned char* ringreg = vstage + (size_t)NS * a.val_stage;  // 32 zero bytes, then the ring
   __shared__ int s_range, s_slot, s_stop;
 
+  pdl_enter();
   if (a.done && *a.done) return;
   if (threadIdx.x == 0) {
     for (int s = 0; s < NS; ++s) {
@@ -366,28 +367,43 @@ __global__ void k_pack(PackArgs a) {
 
 // ------------------------------------------------------------------ launchers
 
+template <typename T, int B, bool FWD, int MAXE>
+static cudaError_t launch_k(const SweepArgs& a, int grid, size_t smem, cudaStream_t st, bool dep) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(64);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = dep ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k_sweep<T, B, FWD, MAXE>, a);
+}
+
 template <typename T, int B, bool FWD>
-static cudaError_t launch_e(const SweepArgs& a, int grid, size_t smem, cudaStream_t st) {
-  if (a.max_nent <= 4) k_sweep<T, B, FWD, 4><<<grid, 64, smem, st>>>(a);
-  else if (a.max_nent <= 8) k_sweep<T, B, FWD, 8><<<grid, 64, smem, st>>>(a);
-  else k_sweep<T, B, FWD, 0><<<grid, 64, smem, st>>>(a);
-  return cudaGetLastError();
+static cudaError_t launch_e(const SweepArgs& a, int grid, size_t smem, cudaStream_t st, bool dep) {
+  if (a.max_nent <= 4) return launch_k<T, B, FWD, 4>(a, grid, smem, st, dep);
+  if (a.max_nent <= 8) return launch_k<T, B, FWD, 8>(a, grid, smem, st, dep);
+  return launch_k<T, B, FWD, 0>(a, grid, smem, st, dep);
 }
 
 template <typename T, bool FWD>
-static cudaError_t launch_b(int B, const SweepArgs& a, int grid, size_t smem, cudaStream_t st) {
+static cudaError_t launch_b(int B, const SweepArgs& a, int grid, size_t smem, cudaStream_t st, bool dep) {
   switch (B) {
-    case 1: return launch_e<T, 1, FWD>(a, grid, smem, st);
-    case 2: return launch_e<T, 2, FWD>(a, grid, smem, st);
-    case 3: return launch_e<T, 3, FWD>(a, grid, smem, st);
+    case 1: return launch_e<T, 1, FWD>(a, grid, smem, st, dep);
+    case 2: return launch_e<T, 2, FWD>(a, grid, smem, st, dep);
+    case 3: return launch_e<T, 3, FWD>(a, grid, smem, st, dep);
     default: return cudaErrorInvalidValue;
   }
 }
 
 cudaError_t launch_sweep(bool forward, bool fp32, int B, const SweepArgs& a, int grid, size_t smem,
-                         cudaStream_t st) {
-  if (fp32) return forward ? launch_b<float, true>(B, a, grid, smem, st) : launch_b<float, false>(B, a, grid, smem, st);
-  return forward ? launch_b<double, true>(B, a, grid, smem, st) : launch_b<double, false>(B, a, grid, smem, st);
+                         cudaStream_t st, bool dep) {
+  if (fp32)
+    return forward ? launch_b<float, true>(B, a, grid, smem, st, dep) : launch_b<float, false>(B, a, grid, smem, st, dep);
+  return forward ? launch_b<double, true>(B, a, grid, smem, st, dep) : launch_b<double, false>(B, a, grid, smem, st, dep);
 }
 
 template <typename T, int B, bool FWD>

@@ -54,8 +54,9 @@ inline int sweep_rhs_bytes(int B, int elem) { return (B * 32 * elem + 15) / 16 *
 inline int sweep_val_stage(int max_nent, int B, int elem) { return sweep_rhs_bytes(B, elem) + max_nent * 32 * 32; }
 
 // launchers (k_sweep.cu)
+// dep: launch as a programmatic dependent of the previous kernel in the stream
 cudaError_t launch_sweep(bool forward, bool fp32, int B, const SweepArgs& a, int grid, size_t smem,
-                         cudaStream_t st);
+                         cudaStream_t st, bool dep = false);
 cudaError_t sweep_set_smem_limits(size_t max_smem);
 // one bounded wait on a value nothing writes (`never` holds the sentinel)
 cudaError_t launch_wait_selftest(const double* never, int* err, cudaStream_t st);
