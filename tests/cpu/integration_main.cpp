@@ -68,6 +68,7 @@ static int matrix_level_check(dfg_ctx ctx, DfgDelFEM::CLinearSystem_FieldGPU& ls
   crs.array.assign(colind.begin(), colind.begin() + nnz);
   MatVec::CMatDia_BlkCrs mat(n, b);
   if (!mat.AddPattern(crs)) return 12;
+  mat.SetZero();  // allocates the value arrays (the reference allocates them lazily here)
   for (int i = 0; i < n; ++i) {
     std::copy(diag.begin() + i * bs, diag.begin() + (i + 1) * bs, mat.GetPtrValDia(i));
     unsigned int np = 0;
@@ -159,6 +160,7 @@ static int host_system_check(dfg_ctx ctx, Fem::Field::CFieldWorld& world, unsign
 }
 
 int main() {
+  std::setvbuf(stdout, nullptr, _IOLBF, 0);  // each report line reaches the log even if a later step fails
   dfg_ctx ctx = nullptr;
   if (dfg_ctx_create(0, &ctx) != DFG_OK) {
     std::printf("no CUDA device: adapter compiled and linked\n");
