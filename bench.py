@@ -245,7 +245,7 @@ def run_gpu(args, rank, world, local):
     p = make_problem(args.config)
     ctx = L.Context(local)
     s = FESolve(ctx, p, fill_level=args.fill_level)
-    sched = {1: "ranged", 2: "level-scheduled"}
+    sched = {1: "ranged", 2: "level-scheduled", 3: "one CTA"}
     sweeps = dict(zip(("forward", "backward"), (sched[k] for k in s.prec.GetSweepMode())))
     stream = ctx.stream
 

@@ -89,6 +89,7 @@ SIGNATURES = {
     "dfg_precond_set_sweep_mode": (_I, [_P, _I]),
     "dfg_precond_get_sweep_mode": (_I, [_P, _PI, _PI]),
     "dfg_precond_get_sweep_timing": (_I, [_P, _P]),
+    "dfg_precond_get_solo_timing": (_I, [_P, _P]),
     "dfg_solve_pcg": (_I, [_P, _P, _PD, _PU]),
     "dfg_solve_pcg_mixed": (_I, [_P, _P, _PD, _PU, _PU]),
     "dfg_solve_pcg_ex": (_I, [_P, _P, _I, _I, _PD, _PU, _PU]),

@@ -921,6 +921,22 @@ void setup_sweep_plan(dfg_ctx ctx_, SweepDev& S) {
 
 void pack_sweep(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, bool fp32) {
   if (S.levels) return;  // the level-scheduled sweep reads the factor itself
+  if (S.solo) {
+    SweepDev::SoloDev& D = S.sd[fp32 ? 1 : 0];
+    PackArgs a{};
+    a.nsteps = D.plan.P.nsteps;
+    a.rec = D.rec.as<unsigned char>();
+    a.rec_off = D.rec_off.as<long long>();
+    a.ent_off = D.ent_off.as<long long>();
+    a.ent_slot = D.ent_slot.as<int>();
+    a.step_rows = D.step_rows.as<int>();
+    a.fdiag = pr->fdiag.as<double>();
+    a.foffd = pr->foffd.as<double>();
+    a.code_bytes = 128;
+    CK(launch_pack(S.forward, fp32, pr->b, a, ctx_->stream));
+    launched(ctx_);
+    return;
+  }
   PackArgs a{};
   a.nsteps = S.plan.nsteps;
   a.rec = fp32 ? S.rec32.as<unsigned char>() : S.rec64.as<unsigned char>();
@@ -945,6 +961,14 @@ struct SweepLaunch {
   bool levels = false;
   const Levels* lev = nullptr;
   LevelSweepArgs la{};
+  // one CTA: permute `src` (row order) into the plan's step order, then the sweep
+  bool solo = false;
+  SoloArgs sa{};
+  size_t ssmem = 0;
+  long long sn = 0;
+  const int* spos = nullptr;
+  const void* ssrc = nullptr;
+  void* sdst = nullptr;
 };
 
 // The factor's block pattern: the system's for ILU(0), the preconditioner's
@@ -962,6 +986,80 @@ FactorPattern factor_pattern(dfg_precond pr) {
           s->rowptr.as<int>(), s->colind.as<int>(), s->diaind.as<int>()};
 }
 
+constexpr int kSoloBatchRing = 8;  // single-slot batches kept per sweep (a BiCGSTAB solve uses two)
+
+// A single-slot batch for the one-CTA sweep of S writing `out`, in the next
+// entry of S's batch ring (uploaded in stream order), and its launch args.
+SoloArgs solo_launch_args(dfg_ctx ctx_, SweepDev& S, bool fp32, void* out, int* ticket, const int* done) {
+  const SweepDev::SoloDev& D = S.sd[fp32 ? 1 : 0];
+  if (!S.solo_batch.p) dalloc(ctx_, S.solo_batch, sizeof(SoloBatch) * kSoloBatchRing);
+  SoloBatch* dev = S.solo_batch.as<SoloBatch>() + (S.solo_next++ % kSoloBatchRing);
+  SoloBatch h{};
+  h.nslots = 1;
+  SoloSlot& w = h.slot[0];
+  w.rec = D.rec.as<unsigned char>();
+  w.chunks = D.chunks.as<SoloChunk>();
+  w.lev_chunks = D.lev_chunks.as<int>();
+  w.nlevels = D.plan.P.nranges;
+  w.nchunks = (int)D.plan.chunks.size();
+  w.in = S.solo_in.p;
+  w.out = out;
+  w.done = done;
+  const size_t head = offsetof(SoloBatch, slot) + sizeof(SoloSlot);
+  CK(cudaMemcpyAsync(dev, &h, head, cudaMemcpyHostToDevice, ctx_->stream));
+  CK(cudaStreamSynchronize(ctx_->stream));  // h is on this frame
+  SoloArgs a{};
+  a.batch = dev;
+  a.ticket = ticket;
+  a.err = ctx_->err_word.as<int>();
+  a.rec_stage = D.shape.rec_stage;
+  a.ch_max = D.shape.ch_max;
+  a.NS = D.shape.ns;
+  a.R = D.shape.R;
+  a.max_nent = D.plan.P.max_nent;
+  return a;
+}
+
+// Builds the one-CTA sweep of one direction for both precisions into S (plans,
+// record headers, chunk tables, packing indices, the row -> position map);
+// false when its stages do not fit in shared memory.
+bool setup_solo(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, const FactorPattern& F, bool forward) {
+  const int n = pr->n, b = pr->b;
+  if (n == 0) return false;
+  int maxe = 0;
+  for (int i = 0; i < n; ++i)
+    maxe = std::max(maxe, forward ? F.diaind[i] - F.rowptr[i] : F.rowptr[i + 1] - F.diaind[i]);
+  int per_sm = 0;
+  cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx_->device);
+  const size_t budget = std::min<size_t>(ctx_->smem_optin, (size_t)per_sm) - 4096;
+  std::vector<int> ident(n);
+  for (int i = 0; i < n; ++i) ident[i] = i;
+  for (int k = 0; k < 2; ++k) {
+    const int elem = k ? 4 : 8;
+    SweepDev::SoloDev& D = S.sd[k];
+    D.shape = solo_shape(b, maxe, elem, forward, budget);
+    if (D.shape.ns < 2 || D.shape.smem > ctx_->smem_optin) return false;
+    D.plan = solo_sweep_plan(n, b, F.rowptr, F.colind, F.diaind, forward, D.shape.R, elem, D.shape.rec_stage,
+                             D.shape.ch_max);
+    std::vector<long long> off;
+    const std::vector<unsigned char> h = pack_solo_headers(D.plan, elem, ident.data(), ident.data(), off);
+    const SweepPlan& P = D.plan.P;
+    upload(ctx_, D.rec, h.data(), std::max<size_t>(h.size(), 1), 64);
+    upload(ctx_, D.rec_off, off.data(), off.size());
+    upload(ctx_, D.chunks, D.plan.chunks.data(), std::max<size_t>(D.plan.chunks.size(), 1));
+    upload(ctx_, D.lev_chunks, D.plan.lev_chunks.data(), D.plan.lev_chunks.size());
+    upload(ctx_, D.ent_off, P.ent_off.data(), P.ent_off.size());
+    upload(ctx_, D.ent_slot, P.ent_slot.data(), std::max<size_t>(P.ent_slot.size(), 1));
+    upload(ctx_, D.step_rows, P.step_rows.data(), std::max<size_t>(P.step_rows.size(), 1));
+  }
+  upload(ctx_, S.solo_pos, S.sd[0].plan.pos.data(), std::max<size_t>(S.sd[0].plan.pos.size(), 1));
+  dalloc(ctx_, S.solo_in, (size_t)std::max(S.sd[0].plan.P.nsteps, 1) * 32 * b * 8 + 64);
+  CK(cudaMemsetAsync(S.solo_in.p, 0, S.solo_in.bytes, ctx_->stream));
+  S.solo_maxe = maxe;
+  CK(solo_set_smem_limits(ctx_->smem_optin));
+  return true;
+}
+
 SweepLaunch sweep_launch(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, bool fp32, const void* in, void* out,
                          int* ticket, const int* done) {
   const int elem = fp32 ? 4 : 8;
@@ -975,6 +1073,16 @@ SweepLaunch sweep_launch(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, bool fp32, c
     L.lev = &S.lev;
     L.la = LevelSweepArgs{S.lev_info.as<int4>(), F.d_colind, fp32 ? pr->fdiag32.p : pr->fdiag.p,
                           fp32 ? pr->foffd32.p : pr->foffd.p, in, out, done, S.lev_G};
+    return L;
+  }
+  if (S.solo) {
+    L.solo = true;
+    L.sa = solo_launch_args(ctx_, S, fp32, out, ticket, done);
+    L.ssmem = S.sd[fp32 ? 1 : 0].shape.smem;
+    L.sn = pr->n;
+    L.spos = S.solo_pos.as<int>();
+    L.ssrc = in;
+    L.sdst = S.solo_in.p;
     return L;
   }
   SweepArgs& a = L.args;
@@ -1011,6 +1119,11 @@ SweepLaunch sweep_launch(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, bool fp32, c
 // kernel in the stream (a level sweep's first launch always waits in stream
 // order: it reads the solve's stop flag before waiting).
 cudaError_t enqueue_sweep(const SweepLaunch& L, cudaStream_t st, bool dep = false) {
+  if (L.solo) {
+    const cudaError_t e = launch_solo_permute(L.fp32, L.sn, L.b, L.spos, L.ssrc, L.sdst, st);
+    if (e != cudaSuccess) return e;
+    return launch_solo(L.forward, L.fp32, L.b, L.sa, 1, L.ssmem, st);
+  }
   if (!L.levels) return launch_sweep(L.forward, L.fp32, L.b, L.args, L.grid, L.smem, st, dep);
   const Levels& V = *L.lev;
   for (size_t l = 0; l + 1 < V.ptr.size(); ++l) {
@@ -1019,7 +1132,9 @@ cudaError_t enqueue_sweep(const SweepLaunch& L, cudaStream_t st, bool dep = fals
   }
   return cudaSuccess;
 }
-long long launches_of(const SweepLaunch& L) { return L.levels ? (long long)L.lev->ptr.size() - 1 : 1; }
+long long launches_of(const SweepLaunch& L) {
+  return L.solo ? 2 : L.levels ? (long long)L.lev->ptr.size() - 1 : 1;
+}
 
 void run_sweep(dfg_ctx ctx_, const SweepLaunch& L) {
   CK(enqueue_sweep(L, ctx_->stream));
@@ -1111,8 +1226,38 @@ void setup_sweep(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, const dfg_system sys
       S.t_ranged = best_ms;
     }
   }
+  // one-CTA candidate (k_solo.cu), timed in FP32 with its input permutation
+  S.solo = false;
+  S.t_solo = -1.f;
+  if (mode == 0 || mode == 3) {
+    const bool fits = setup_solo(ctx_, pr, S, F, forward);
+    REQUIRE(fits || mode != 3, DFG_INVALID_ARGUMENT, "the one-CTA sweep's records do not fit in shared memory");
+    if (fits) {
+      S.solo = true;
+      SweepLaunch L = sweep_launch(ctx_, pr, S, true, vin.p, vout.p, sc.tickets + 2, nullptr);
+      const float ms = elapsed([&] {
+        CK(cudaMemsetAsync(sc.tickets + 2, 0, sizeof(int), ctx_->stream));
+        CK(enqueue_sweep(L, ctx_->stream));
+      });
+      launched(ctx_, 4);
+      if (read_err(ctx_) != 0) {
+        CK(cudaMemsetAsync(ctx_->err_word.p, 0, sizeof(int), ctx_->stream));
+        set_err(ctx_, "a triangular-sweep wait timed out while choosing the schedule");
+        throw Fail{DFG_TIMEOUT};
+      }
+      S.t_solo = ms;
+      if (mode == 3 || ms < best_ms) {
+        best_ms = ms;
+      } else {
+        S.solo = false;
+        for (SweepDev::SoloDev& D : S.sd) D = SweepDev::SoloDev{};
+        S.solo_pos.release();
+        S.solo_in.release();
+      }
+    }
+  }
   // level-scheduled candidate
-  if (mode != 1) {
+  if (mode != 1 && mode != 3) {
     Levels V = build_levels(sys->n, F.rowptr, F.colind, F.diaind, forward);
     // per position: the row and its entry range in this direction
     std::vector<int4> info(std::max<size_t>(V.rows.size(), 1), make_int4(0, 0, 0, 0));
@@ -1156,12 +1301,20 @@ void setup_sweep(dfg_ctx ctx_, dfg_precond pr, SweepDev& S, const dfg_system sys
     }
     if (take) {
       S.levels = true;
+      S.solo = false;
+      for (SweepDev::SoloDev& D : S.sd) D = SweepDev::SoloDev{};
+      S.solo_pos.release();
+      S.solo_in.release();
       S.lev = std::move(V);
       S.lev_info = std::move(rows);
       S.lev_G = G;
       S.plan = SweepPlan{};
       return;
     }
+  }
+  if (S.solo) {
+    S.plan = SweepPlan{};
+    return;
   }
   S.plan = std::move(cands[best]);
   setup_sweep_plan(ctx_, S);
@@ -1198,8 +1351,9 @@ extern "C" int dfg_precond_set_fill_level(dfg_precond prec, int lev) {
 
 extern "C" int dfg_precond_set_sweep_mode(dfg_precond prec, int mode) {
   if (!prec) return DFG_INVALID_ARGUMENT;
-  if (mode < 0 || mode > 2) {
-    prec->ctx->last_error = "sweep mode must be 0 (timed choice), 1 (ranged) or 2 (level-scheduled)";
+  if (mode < 0 || mode > 3) {
+    prec->ctx->last_error =
+        "sweep mode must be 0 (timed choice), 1 (ranged), 2 (level-scheduled) or 3 (one CTA)";
     return DFG_INVALID_ARGUMENT;
   }
   prec->sweep_mode = mode;
@@ -1212,8 +1366,8 @@ extern "C" int dfg_precond_get_sweep_mode(dfg_precond prec, int* fwd, int* bwd) 
     prec->ctx->last_error = "dfg_precond_set_linear_system must come first";
     return DFG_NOT_READY;
   }
-  if (fwd) *fwd = prec->fwd.levels ? 2 : 1;
-  if (bwd) *bwd = prec->bwd.levels ? 2 : 1;
+  if (fwd) *fwd = prec->fwd.solo ? 3 : prec->fwd.levels ? 2 : 1;
+  if (bwd) *bwd = prec->bwd.solo ? 3 : prec->bwd.levels ? 2 : 1;
   return DFG_OK;
 }
 
@@ -1227,6 +1381,17 @@ extern "C" int dfg_precond_get_sweep_timing(dfg_precond prec, float* ms) {
   ms[1] = prec->fwd.t_levels;
   ms[2] = prec->bwd.t_ranged;
   ms[3] = prec->bwd.t_levels;
+  return DFG_OK;
+}
+
+extern "C" int dfg_precond_get_solo_timing(dfg_precond prec, float* ms) {
+  if (!prec || !ms) return DFG_INVALID_ARGUMENT;
+  if (!prec->symbolic) {
+    prec->ctx->last_error = "dfg_precond_set_linear_system must come first";
+    return DFG_NOT_READY;
+  }
+  ms[0] = prec->fwd.t_solo;
+  ms[1] = prec->bwd.t_solo;
   return DFG_OK;
 }
 

@@ -190,6 +190,20 @@ struct SweepDev {
   Levels lev;
   DBuf lev_info;   // level-scheduled: int4 {row, first entry, end entry, 0} per position
   int lev_G = 4;   // level-scheduled: lanes per row
+  // one CTA (k_solo.cu): the input is permuted into the plan's step order
+  // first, the output is written in row order; [0] FP64 records, [1] FP32
+  bool solo = false;
+  float t_solo = -1.f;
+  struct SoloDev {
+    SoloPlan plan;
+    SoloShape shape;
+    DBuf rec, rec_off, chunks, lev_chunks, ent_off, ent_slot, step_rows;
+  };
+  SoloDev sd[2];
+  DBuf solo_pos, solo_in;      // row -> position (int); the permuted input (FP64-sized)
+  DBuf solo_batch;             // kSoloBatchRing single-slot batches, one per launch set-up in use
+  int solo_next = 0;
+  int solo_maxe = 0;
   // ranged: one packed record buffer per precision
   DBuf rec64, rec32;
   DBuf rec_off64, rec_off32;       // long long per step (+1)

@@ -76,7 +76,10 @@ __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
     if (threadIdx.x == 0) {
       const int t = atomicAdd(a.ticket, 1);
       int j = -1;
-      if (t < a.batch->nslots) j = ld_relaxed_int(a.batch->slot[t].done) ? -2 : t;
+      if (t < a.batch->nslots) {
+        const int* dn = a.batch->slot[t].done;
+        j = (dn && ld_relaxed_int(dn)) ? -2 : t;
+      }
       s_slot = j;
     }
     __syncthreads();
@@ -248,7 +251,26 @@ __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
   }
 }
 
+template <typename T>
+__global__ void k_solo_permute(long long n, int b, const int* __restrict__ pos, const T* __restrict__ in,
+                               T* __restrict__ out) {
+  const long long m = n * b;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < m; k += (long long)gridDim.x * blockDim.x) {
+    const long long row = k / b;
+    out[(long long)pos[row] * b + (k - row * b)] = in[k];
+  }
+}
+
 // ------------------------------------------------------------------ launchers
+
+cudaError_t launch_solo_permute(bool fp32, long long n, int b, const int* pos, const void* in, void* out,
+                                cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int grid = (int)std::min<long long>((n * b + 255) / 256, 1216);
+  if (fp32) k_solo_permute<float><<<grid, 256, 0, st>>>(n, b, pos, static_cast<const float*>(in), static_cast<float*>(out));
+  else k_solo_permute<double><<<grid, 256, 0, st>>>(n, b, pos, static_cast<const double*>(in), static_cast<double*>(out));
+  return cudaGetLastError();
+}
 
 template <typename T, int B, bool FWD>
 static cudaError_t launch_e(const SoloArgs& a, int grid, size_t smem, cudaStream_t st) {

@@ -2,6 +2,9 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstddef>
+
 namespace dfg {
 
 // Several independent sweeps in one launch (the serving path): a claimed
@@ -117,6 +120,51 @@ inline size_t solo_smem_bytes(int NS, int rec_stage, int val_stage, int R, int B
          (size_t)R * 32 * B * elem;
 }
 cudaError_t launch_solo(bool forward, bool fp32, int B, const SoloArgs& a, int grid, size_t smem, cudaStream_t st);
+// out[pos[row]*b + c] = in[row*b + c] for rows < n: a vector in row order into
+// a solo sweep's step order (elements of T: float when fp32)
+cudaError_t launch_solo_permute(bool fp32, long long n, int b, const int* pos, const void* in, void* out,
+                                cudaStream_t st);
+
+// Shared-memory shape of a solo sweep CTA for block size b, rows of at most
+// maxe lower or upper entries and elem-byte values, in `budget` bytes.  The
+// ring: rows with at most 4 entries (triangle meshes) depend on the level
+// before theirs only, at most about 20 steps wide on meshes of up to 400k
+// nodes, so 64 steps hold every dependency; wider rows (tetrahedral meshes,
+// levels of up to ~150 steps reaching two or three levels back) get up to a
+// third of the budget (a power of two of steps, at most 512).  The chunk
+// stages take the rest -- the bytes in flight that hide HBM latency: up to 64
+// of them, each holding up to ch_max steps' records and right-hand sides;
+// ch_max (1..8) is the largest (fewest waits per level) within 10 % of the
+// most steps in flight.  ns == 0 when nothing fits.
+struct SoloShape {
+  int R = 0, ch_max = 0, rec_stage = 0, ns = 0;
+  size_t smem = 0;
+};
+inline long long solo_record_bytes(int nent, int bs, int sz, bool forward) {
+  return 16 + 128 + (long long)nent * 128 + (long long)nent * 32 * bs * sz + (forward ? 32LL * bs * sz : 0);
+}
+inline SoloShape solo_shape(int b, int maxe, int elem, bool forward, size_t budget) {
+  SoloShape sh;
+  const size_t step_ring = (size_t)32 * b * elem;
+  int R = maxe <= 4 ? 64 : 512;
+  while (R > 16 && (size_t)R * step_ring > budget / 3) R /= 2;
+  sh.R = R;
+  const long long rec1 = solo_record_bytes(maxe, b * b, elem, forward);
+  const size_t fixed = solo_smem_bytes(64, 0, 0, R, b, elem);
+  int ns_of[9] = {}, most = 0;
+  for (int ch = 1; ch <= 8; ++ch) {
+    const size_t per_stage = (size_t)ch * rec1 + (size_t)solo_val_stage(ch, b, elem);
+    ns_of[ch] = (int)std::min<size_t>(64, (budget - std::min(budget, fixed)) / per_stage);
+    if (ns_of[ch] >= 2) most = ns_of[ch] * ch > most ? ns_of[ch] * ch : most;
+  }
+  for (int ch = 1; ch <= 8; ++ch)
+    if (ns_of[ch] >= 2 && 10 * ns_of[ch] * ch >= 9 * most) { sh.ch_max = ch; sh.ns = ns_of[ch]; }
+  if (sh.ns > 0) {
+    sh.rec_stage = (int)(sh.ch_max * rec1);
+    sh.smem = solo_smem_bytes(sh.ns, sh.rec_stage, solo_val_stage(sh.ch_max, b, elem), R, b, elem);
+  }
+  return sh;
+}
 cudaError_t solo_set_smem_limits(size_t max_smem);
 
 // Level-scheduled sweep (k_level.cu): the factor in block CRS (values of

@@ -1206,43 +1206,20 @@ void class_shapes(dfg_server_s* S) {
     const int per_sm = std::max(1, std::min(16, (int)(per_sm_bytes / (worst + 1024))));
     S->cls_grid[k] = S->nsm * per_sm;
   }
-  // solo sweeps, one CTA per SM.  The ring: rows with at most 4 lower or
-  // upper neighbours (triangle meshes) depend on the level before theirs
-  // only, at most about 20 steps wide on the serving meshes, so 64 steps hold
-  // every dependency (checked by the plan emulator on the stream's largest
-  // requests); wider rows (tetrahedral meshes, levels of up to ~150 steps
-  // reaching two or three levels back) get up to a third of the shared
-  // memory (a power of two of steps, at most 512).  The chunk stages take the
-  // rest -- the bytes in flight that hide HBM latency: up to 64 of them, each
-  // holding up to ch_max steps' records and right-hand sides; ch_max (2..8)
-  // is the largest (fewest waits per level) within 10 % of the most steps in
-  // flight.
+  // solo sweeps: one CTA per SM (solo_shape)
   for (int k = 0; k < kClasses; ++k) {
     const int b = class_b(k), maxe = class_maxe(k);
     const size_t budget = std::min<size_t>(S->ctx->smem_optin, (size_t)per_sm_bytes) - 4096;
-    const size_t step_ring = (size_t)32 * b * elem;
-    int R = maxe <= 4 ? 64 : 512;
-    while (R > 16 && (size_t)R * step_ring > budget / 3) R /= 2;
-    S->solo_R[k] = R;
     size_t worst = 0;
     for (int dir = 0; dir < 2; ++dir) {
-      const long long rec1 = solo_rec_bytes(maxe, b * b, elem, dir == 0);
-      const size_t fixed = solo_smem_bytes(64, 0, 0, R, b, elem);
-      int ns_of[9] = {}, most = 0;
-      for (int ch = 2; ch <= 8; ++ch) {
-        const size_t per_stage = (size_t)ch * rec1 + (size_t)solo_val_stage(ch, b, elem);
-        ns_of[ch] = (int)std::min<size_t>(64, (budget - std::min(budget, fixed)) / per_stage);
-        if (ns_of[ch] >= 2) most = std::max(most, ns_of[ch] * ch);
-      }
-      int best_ch = 2, best_ns = 0;
-      for (int ch = 2; ch <= 8; ++ch)
-        if (ns_of[ch] >= 2 && 10 * ns_of[ch] * ch >= 9 * most) { best_ch = ch; best_ns = ns_of[ch]; }
-      if (best_ns < 2) throw CudaFail{cudaErrorInvalidValue, "solo sweep stages do not fit in shared memory"};
-      S->solo_ch[k][dir] = best_ch;
-      S->solo_rec_stage[k][dir] = (int)(best_ch * rec1);
-      S->solo_ns[k][dir] = best_ns;
-      S->solo_smem[k][dir] = solo_smem_bytes(best_ns, (int)(best_ch * rec1), solo_val_stage(best_ch, b, elem), R, b, elem);
-      worst = std::max(worst, S->solo_smem[k][dir]);
+      const SoloShape sh = solo_shape(b, maxe, elem, dir == 0, budget);
+      if (sh.ns < 2) throw CudaFail{cudaErrorInvalidValue, "solo sweep stages do not fit in shared memory"};
+      S->solo_R[k] = sh.R;
+      S->solo_ch[k][dir] = sh.ch_max;
+      S->solo_rec_stage[k][dir] = sh.rec_stage;
+      S->solo_ns[k][dir] = sh.ns;
+      S->solo_smem[k][dir] = sh.smem;
+      worst = std::max(worst, sh.smem);
     }
     if (worst > S->ctx->smem_optin) throw CudaFail{cudaErrorInvalidValue, "solo sweep shared memory"};
     S->solo_grid[k] = S->nsm;

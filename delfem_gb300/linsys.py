@@ -257,7 +257,7 @@ class PreconditionerILU:
         check(self.ctx.h, lib().dfg_precond_set_fill_level(self.h, lev), "dfg_precond_set_fill_level")
 
     def SetSweepMode(self, mode: int):
-        """0: timed choice (default), 1: ranged, 2: level-scheduled sweeps."""
+        """0: timed choice (default), 1: ranged, 2: level-scheduled, 3: one-CTA sweeps."""
         check(self.ctx.h, lib().dfg_precond_set_sweep_mode(self.h, mode), "dfg_precond_set_sweep_mode")
 
     def GetSweepMode(self):
@@ -273,6 +273,13 @@ class PreconditionerILU:
         level-scheduled (-1: not timed)."""
         ms = np.zeros(4, dtype=np.float32)
         check(self.ctx.h, lib().dfg_precond_get_sweep_timing(self.h, _p(ms)), "dfg_precond_get_sweep_timing")
+        return [float(x) for x in ms]
+
+    def GetSoloTiming(self):
+        """Set-up timings (ms per FP32 sweep) of the one-CTA kind: forward,
+        backward (-1: not timed)."""
+        ms = np.zeros(2, dtype=np.float32)
+        check(self.ctx.h, lib().dfg_precond_get_solo_timing(self.h, _p(ms)), "dfg_precond_get_solo_timing")
         return [float(x) for x in ms]
 
     def SetLinearSystem(self, ls: LinearSystemField):

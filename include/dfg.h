@@ -232,19 +232,25 @@ int dfg_precond_set_fill_level(dfg_precond prec, int lev);
  * CMatDiaFrac_BlkCrs(0,A), src/matvec/matdiafrac_blkcrs.cpp:171-225). */
 int dfg_precond_set_linear_system(dfg_precond prec, dfg_system sys);
 /* How the triangular sweeps are scheduled (no counterpart in the reference,
- * whose substitutions are sequential loops): 0 (default) times both kinds
- * on the device at the symbolic set-up and keeps the faster per direction;
+ * whose substitutions are sequential loops): 0 (default) times the kinds
+ * on the device at the symbolic set-up and keeps the fastest per direction;
  * 1 = ranged (contiguous row ranges pipelined across CTAs, good for the long
- * thin wavefronts of 2D meshes); 2 = level-scheduled (one launch per
- * dependency level, good for the wide levels of 3D meshes).  Takes effect at
- * the next dfg_precond_set_linear_system; results agree to rounding. */
+ * thin wavefronts of large 2D meshes); 2 = level-scheduled (one launch per
+ * dependency level, good for the wide levels of 3D meshes); 3 = one CTA
+ * (the whole sweep on one SM, level after level, its input first permuted
+ * into the schedule's order: good for small 2D meshes, whose sweeps are
+ * bound by the latency of each level).  Takes effect at the next
+ * dfg_precond_set_linear_system; results agree to rounding. */
 int dfg_precond_set_sweep_mode(dfg_precond prec, int mode);
-/* The kind chosen per direction after the symbolic set-up (1 or 2). */
+/* The kind chosen per direction after the symbolic set-up (1, 2 or 3). */
 int dfg_precond_get_sweep_mode(dfg_precond prec, int* fwd, int* bwd);
 /* The set-up's timings behind that choice, ms per FP32 sweep: ms[0..3] =
  * forward ranged, forward level-scheduled, backward ranged, backward
  * level-scheduled (-1 where a kind was not timed). */
 int dfg_precond_get_sweep_timing(dfg_precond prec, float* ms);
+/* The set-up's timings of the one-CTA kind, ms per FP32 sweep: ms[0] forward,
+ * ms[1] backward (-1 where it was not timed). */
+int dfg_precond_get_solo_timing(dfg_precond prec, float* ms);
 /* The factor's block pattern after the symbolic set-up: *nnz off-diagonal
  * blocks; rowptr (n+1) and colind (nnz) in the layout of
  * dfg_system_get_pattern, each written when non-NULL. */

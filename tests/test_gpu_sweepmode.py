@@ -1,8 +1,8 @@
-"""Both sweep schedules (dfg_precond_set_sweep_mode: 1 ranged, 2
-level-scheduled) against the oracle: the preconditioner apply to 1e-12,
-FP64 PCG within +-2 iterations and 1e-6 of the oracle's solution, the
-precision forms to a true residual of 1e-8, BiCGSTAB and ILU(1) on the
-level schedule; the timed choice picks one of the two per direction."""
+"""The three sweep schedules (dfg_precond_set_sweep_mode: 1 ranged, 2
+level-scheduled, 3 one CTA) against the oracle: the preconditioner apply to
+1e-12, FP64 PCG within +-2 iterations and 1e-6 of the oracle's solution, the
+precision forms to a true residual of 1e-8, BiCGSTAB, and ILU(1) on the
+level and one-CTA schedules; the timed choice picks one kind per direction."""
 import numpy as np
 import pytest
 
@@ -17,7 +17,7 @@ def _problem(kind):
             "solid3d": lambda: mg.solid3d_cube(8, seed=74, coef_sigma=1.0)}[kind]()
 
 
-@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("mode", [1, 2, 3])
 @pytest.mark.parametrize("kind", ["poisson2d", "solid2d", "poisson3d", "solid3d"])
 def test_sweep_modes(gpu_ctx, oracle_lib, kind, mode):
     from delfem_gb300 import linsys as L
@@ -53,11 +53,12 @@ def test_sweep_modes(gpu_ctx, oracle_lib, kind, mode):
         s.close()
 
 
-def test_level_schedule_with_fill_in(gpu_ctx, oracle_lib):
+@pytest.mark.parametrize("mode", [2, 3])
+def test_schedule_with_fill_in(gpu_ctx, oracle_lib, mode):
     from delfem_gb300.solver import FESolve
     p = _problem("solid3d")
     ref = oracle_lib.solve(p, fill_level=1)
-    s = FESolve(gpu_ctx, p, fill_level=1, sweep_mode=2)
+    s = FESolve(gpu_ctx, p, fill_level=1, sweep_mode=mode)
     try:
         r = s.run("fp64")
         assert r["converged"] and abs(r["iter"] - ref["iter"]) <= 2
@@ -74,9 +75,11 @@ def test_timed_choice_and_bad_mode(gpu_ctx):
     s = FESolve(gpu_ctx, _problem("poisson3d"))
     try:
         f, b = s.prec.GetSweepMode()
-        assert f in (1, 2) and b in (1, 2)
+        assert f in (1, 2, 3) and b in (1, 2, 3)
+        solo = s.prec.GetSoloTiming()
+        assert all(t > 0 for t in solo) or all(t == -1 for t in solo)
         with pytest.raises(capi.DfgError) as e:
-            s.prec.SetSweepMode(3)
+            s.prec.SetSweepMode(4)
         assert e.value.status == capi.DFG_INVALID_ARGUMENT
     finally:
         s.close()
