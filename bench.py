@@ -614,6 +614,10 @@ def run_serve(args, rank, world, local):
             h2d=st1["h2d_bytes"] - st0["h2d_bytes"], d2h=st1["d2h_bytes"] - st0["d2h_bytes"],
             backlog_frac=(st1["backlog_seconds"] - st0["backlog_seconds"]) / wall,
             queued_frac=(st1["queued_seconds"] - st0["queued_seconds"]) / wall,
+            full_frac=(st1["full_seconds"] - st0["full_seconds"]) / wall,
+            inflight_avg=(st1["inflight_seconds"] - st0["inflight_seconds"]) / wall,
+            symbolic_ms=1e3 * (st1["symbolic_seconds"] - st0["symbolic_seconds"]) / max(len(res), 1),
+            admit_ms=1e3 * (st1["admit_seconds"] - st0["admit_seconds"]) / max(len(res), 1),
             peak_inflight=st1["peak_inflight"], peak_bytes=st1["peak_bytes"], budget=st1["budget_bytes"],
             busy=st1["busy_seconds"] - st0["busy_seconds"], prof=prof, clocks=clk.summary(),
             err_vs_plain=(max(err) if err else None),
@@ -685,7 +689,11 @@ def compose_serve_line(args, world, cfg, items, timed_items, timed_probs, result
                 "graph_replays": int(r["replays"]), "peak_inflight": int(r["peak_inflight"]),
                 "peak_device_bytes": int(r["peak_bytes"]),
                 "saturation": {"backlog_fraction": round(r["backlog_frac"], 4),
-                               "admission_queue_fraction": round(r["queued_frac"], 4)},
+                               "admission_queue_fraction": round(r["queued_frac"], 4),
+                               "device_full_fraction": round(r["full_frac"], 4),
+                               "inflight_mean": round(r["inflight_avg"], 1),
+                               "symbolic_ms_per_request": round(r["symbolic_ms"], 2),
+                               "admission_ms_per_request": round(r["admit_ms"], 2)},
                 "error_vs_fp64_rel_l2_max": r["err_vs_plain"],
                 "kernels": {k: {"ms": round(v["ms"], 4), "gbs": round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1)
                                 if v["bytes"] > 0 and v["ms"] > 0 else None}

@@ -134,7 +134,8 @@ class ServerCounters(ctypes.Structure):
     _fields_ = [("submitted", _LL), ("finished", _LL), ("replays", _LL), ("kernel_launches", _LL),
                 ("graph_builds", _LL), ("peak_inflight", _LL), ("budget_bytes", _LL), ("peak_bytes", _LL),
                 ("h2d_bytes", _LL), ("d2h_bytes", _LL), ("busy_seconds", _D), ("now_seconds", _D),
-                ("backlog_seconds", _D), ("queued_seconds", _D)]
+                ("backlog_seconds", _D), ("queued_seconds", _D), ("full_seconds", _D),
+                ("inflight_seconds", _D), ("symbolic_seconds", _D), ("admit_seconds", _D)]
 
 
 SERVER_NKERNELS = 24

@@ -277,7 +277,9 @@ struct dfg_server_s {
   // backlog = submitted and neither admitted nor finished; ready = set up and
   // waiting for device memory or an in-flight slot
   long long backlog = 0;
-  double t_acc = 0, backlog_s = 0, queued_s = 0;
+  double t_acc = 0, backlog_s = 0, queued_s = 0, full_s = 0, inflight_s = 0;
+  bool adm_full = false;  // admission waits for device memory or an in-flight slot
+  double symbolic_s = 0, admit_s = 0;
 
   double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
   // brings the occupancy integrals up to now; called (under mu) before every
@@ -286,6 +288,8 @@ struct dfg_server_s {
     const double t = now();
     if (backlog > 0) backlog_s += t - t_acc;
     if (!ready.empty()) queued_s += t - t_acc;
+    if (adm_full) full_s += t - t_acc;
+    inflight_s += inflight * (t - t_acc);
     t_acc = t;
   }
 };
@@ -643,7 +647,10 @@ void release_locked(dfg_server_s* S, Req* r) {
   if (r->have_t) S->arena.release(r->tbase, r->T.total);
   const bool was_admitted = r->have_p;
   r->have_p = r->have_t = false;
-  if (was_admitted) --S->inflight;
+  if (was_admitted) {
+    S->account_locked();
+    --S->inflight;
+  }
   S->cv_adm.notify_all();
 }
 
@@ -660,12 +667,14 @@ void symbolic_worker(dfg_server_s* S) {
       S->submitted.pop_front();
     }
     bool ok = false;
+    const Clock::time_point t_sym = Clock::now();
     try {
       ok = symbolic(S, r);
     } catch (const std::bad_alloc&) {
       r->error = "host allocation failed during the symbolic set-up";
     }
     std::lock_guard<std::mutex> lk(S->mu);
+    S->symbolic_s += std::chrono::duration<double>(Clock::now() - t_sym).count();
     S->account_locked();
     if (!ok) {
       r->status = DFG_INVALID_ARGUMENT;
@@ -714,6 +723,7 @@ void admission_thread(dfg_server_s* S) {
               h->tbase = to;
               h->have_p = h->have_t = true;
               S->account_locked();
+              S->adm_full = false;
               --S->backlog;
               S->ready.erase(S->ready.begin());
               ++S->inflight;
@@ -725,12 +735,19 @@ void admission_thread(dfg_server_s* S) {
             S->arena.release(po, h->P.total);
           }
         }
+        if (!S->ready.empty() && !S->adm_full) {
+          S->account_locked();
+          S->adm_full = true;
+        }
         S->cv_adm.wait(lk);
       }
     }
     int nsing = 0;
+    const Clock::time_point t_adm = Clock::now();
     try {
       nsing = admit_device(S, r);
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->admit_s += std::chrono::duration<double>(Clock::now() - t_adm).count();
     } catch (const CudaFail& f) {
       cudaGetLastError();
       std::lock_guard<std::mutex> lk(S->mu);
@@ -1437,6 +1454,10 @@ extern "C" int dfg_server_stats(dfg_server s, dfg_server_counters* out) {
   s->account_locked();
   out->backlog_seconds = s->backlog_s;
   out->queued_seconds = s->queued_s;
+  out->full_seconds = s->full_s;
+  out->inflight_seconds = s->inflight_s;
+  out->symbolic_seconds = s->symbolic_s;
+  out->admit_seconds = s->admit_s;
   out->now_seconds = s->now();
   return DFG_OK;
 }

@@ -417,7 +417,12 @@ typedef struct {
   double now_seconds;     /* on the clock of dfg_result's times */
   double backlog_seconds; /* time with at least one request submitted and not yet admitted */
   double queued_seconds;  /* time with at least one request set up and waiting for device
-                             memory or an in-flight slot (the device was full) */
+                             admission (behind another admission, or the device was full) */
+  double full_seconds;    /* time with a request set up and no device memory or in-flight
+                             slot free for it */
+  double inflight_seconds; /* solves admitted and not yet released, integrated over time */
+  double symbolic_seconds; /* host symbolic set-up, summed over requests */
+  double admit_seconds;   /* device admission (uploads, assembly, ILU, packing), summed */
 } dfg_server_counters;
 
 /* Per-kernel timing of profiled replays (dfg_server_config::profile_every):
