@@ -244,7 +244,7 @@ def run_gpu(args, rank, world, local):
 
     p = make_problem(args.config)
     ctx = L.Context(local)
-    s = FESolve(ctx, p, fill_level=args.fill_level)
+    s = FESolve(ctx, p, fill_level=args.fill_level, sweep_mode=args.sweep_mode)
     sched = {1: "ranged", 2: "level-scheduled", 3: "one CTA"}
     sweeps = dict(zip(("forward", "backward"), (sched[k] for k in s.prec.GetSweepMode())))
     stream = ctx.stream
@@ -919,6 +919,9 @@ def main():
                     help="single-solve workloads: Solve_PCG or Solve_PBiCGSTAB (BiCGSTAB: arm plain_fp64 only)")
     ap.add_argument("--fill-level", type=int, default=0,
                     help="single-solve workloads: ILU fill level (CPreconditioner_ILU::SetFillInLevel; -1 = no limit)")
+    ap.add_argument("--sweep-mode", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="single solves: triangular-sweep schedule, 0 = timed choice, 1 ranged, "
+                         "2 level-scheduled, 3 one CTA")
     ap.add_argument("--max-inflight", type=int, default=128, help="serving: solves resident at once (<= 256)")
     ap.add_argument("--size-groups", type=int, default=0, help="serving: 1 table, 2-3 size groups, 0 = server default (3)")
     ap.add_argument("--ref-sample-every", type=int, default=1,

@@ -302,21 +302,19 @@ namespace {
 // solve's whole dependency chain on one SM, and the in-flight solves fill
 // the device; the ranged kernel (k_sweep.cu) spreads one solve over many
 // SMs at the price of cross-SM hand-offs (about 0.75 us per dependency level
-// in batched launches).  FP32 sweeps take one CTA, except the largest
-// solves with 2x2 or 3x3 blocks: their records (about 100 bytes per row for
-// 2x2) outrun what one SM keeps in flight against HBM latency, and spreading
-// them wins.  Measured on GB300 over bands of the 2D serving stream (FP32
-// factor, solves/s, ranged -> one CTA): 1x1 blocks 231 -> 295 (2k-20k
-// nodes), 58 -> 84, 19 -> 28, 5.5 -> 7.1 (150k-400k); 2x2 blocks 142 -> 158,
-// 34 -> 40, 13.0 -> 13.7 (60k-150k), 2.6 -> 2.2 (150k-400k).  FP64 sweeps
-// stay ranged: on one SM every level waits on a chain of dependent FP64 FMAs
-// (64 cycles each on GB300), about twice the ranged kernel's time beyond
-// the smallest solves.
-constexpr int kSoloMaxNodesBlocked = 150000;
+// in batched launches).  FP32 sweeps take one CTA.  Measured on GB300 over
+// bands of the 2D serving stream (FP32 factor, solves/s, ranged -> one
+// CTA): 1x1 blocks 231 -> 295 (2k-20k nodes), 58 -> 84, 19 -> 28, 5.5 -> 7.1
+// (150k-400k); 2x2 blocks 142 -> 158, 34 -> 40, 13.0 -> 13.7 (60k-150k),
+// 4.65 -> 5.71 (150k-250k), 2.07 -> 2.31 (250k-400k).  FP64 sweeps stay
+// ranged: on one SM every level waits on a chain of dependent FP64 FMAs (64
+// cycles each on GB300), about twice the ranged kernel's time beyond the
+// smallest solves.
 bool use_solo(const dfg_server_s* S, const Req* r) {
+  (void)r;
   if (S->sweeps == 1) return false;
   if (S->sweeps == 2) return true;
-  return S->fp32 && (r->b == 1 || r->n <= kSoloMaxNodesBlocked);
+  return S->fp32;
 }
 
 // Fills the request's host-side set-up; returns false with r->error on failure.

@@ -191,6 +191,11 @@ int main() {
   double conv = 1e-8;
   unsigned int iter = 1000;
   const bool ok_ref = LsSol::Solve_PCG(conv, iter, ls);  // the reference's solver over the GPU system
+  // the reference's loop leaves its final residual in the residual vector:
+  // assemble again so that the device loop solves the same system
+  ls.InitializeMarge();
+  DfgDelFEM::AddLinSys_Poisson(ls, 1.0, 1.0);
+  ls.FinalizeMarge();
   double conv2 = 1e-8;
   unsigned int iter2 = 1000;
   const bool ok_fast = DfgDelFEM::Solve_PCG(conv2, iter2, ls);
