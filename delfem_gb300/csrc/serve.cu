@@ -69,6 +69,9 @@ constexpr double kMixedDelta2 = 0.01;
 // 1.54 s), so three is the default.
 // Groups by DOF: < 30k, < 150k, larger (three); < 60k, larger (two).
 constexpr int kGroups = 3;
+// Admission lanes: requests are admitted (uploads, assembly, Dirichlet, the
+// level-by-level ILU, packing) this many at a time, each on its own stream.
+constexpr int kAdmLanes = 4;
 inline int group_of(long long dof, int ngroups) {
   if (ngroups <= 1) return 0;
   if (ngroups == 2) return dof < 60000 ? 0 : 1;
@@ -237,9 +240,16 @@ struct dfg_server_s {
   void* arena_base = nullptr;
   Arena arena;
   Group grp[kGroups];
-  double* d_adm = nullptr;      // admission reductions: partials, counter, result, singular-pivot count
-  int* h_nsing = nullptr;
-  cudaStream_t s_adm = nullptr, s_copy = nullptr;
+  // admission lanes: each admits one request at a time on its own stream,
+  // with its own reduction scratch (partials, counter, result, singular-pivot
+  // count) and pinned read-back word
+  struct AdmLane {
+    cudaStream_t st = nullptr;
+    double* d_red = nullptr;
+    int* h_nsing = nullptr;
+    std::thread th;
+  } adm[kAdmLanes];
+  cudaStream_t s_copy = nullptr;
   // profiling of every profile_every-th replay of a group (first iteration, per kernel)
   int profile_every = 0;
   double prof_ms[DFG_SERVER_NKERNELS] = {}, prof_bytes[DFG_SERVER_NKERNELS] = {};
@@ -269,7 +279,7 @@ struct dfg_server_s {
   int fatal = DFG_OK;
   std::string fatal_msg;
   std::vector<std::thread> workers;
-  std::thread adm_thread, loop_thread;
+  std::thread loop_thread;
   // statistics
   long long replays = 0, launches = 0, peak_inflight = 0, graph_builds = 0;
   double busy_s = 0;
@@ -302,19 +312,24 @@ namespace {
 // solve's whole dependency chain on one SM, and the in-flight solves fill
 // the device; the ranged kernel (k_sweep.cu) spreads one solve over many
 // SMs at the price of cross-SM hand-offs (about 0.75 us per dependency level
-// in batched launches).  FP32 sweeps take one CTA.  Measured on GB300 over
-// bands of the 2D serving stream (FP32 factor, solves/s, ranged -> one
-// CTA): 1x1 blocks 231 -> 295 (2k-20k nodes), 58 -> 84, 19 -> 28, 5.5 -> 7.1
-// (150k-400k); 2x2 blocks 142 -> 158, 34 -> 40, 13.0 -> 13.7 (60k-150k),
-// 4.65 -> 5.71 (150k-250k), 2.07 -> 2.31 (250k-400k).  FP64 sweeps stay
+// in batched launches).  FP32 sweeps take one CTA, except 3x3-block solves
+// above 100,000 nodes.  Measured on GB300 over bands of the serving streams
+// (FP32 factor, solves/s, ranged -> one CTA).  2D stream: 1x1 blocks
+// 231 -> 295 (2k-20k nodes), 58 -> 84, 19 -> 28, 5.5 -> 7.1 (150k-400k);
+// 2x2 blocks 142 -> 158, 34 -> 40, 13.0 -> 13.7 (60k-150k), 4.65 -> 5.71
+// (150k-250k), 2.07 -> 2.31 (250k-400k).  3D stream: 1x1 blocks
+// 52.8 -> 126.0 (< 40k), 13.9 -> 48.1, 12.8 -> 24.8, 6.1 -> 11.5 (> 300k);
+// 3x3 blocks 18.1 -> 32.9 (< 40k), 7.8 -> 9.0 (40k-120k), but 4.0 -> 2.4
+// (120k-300k) and 2.3 -> 1.1 (> 300k): a wide 3D level of 3x3 blocks is more
+// record bytes than one SM streams in a level's time.  FP64 sweeps stay
 // ranged: on one SM every level waits on a chain of dependent FP64 FMAs (64
 // cycles each on GB300), about twice the ranged kernel's time beyond the
 // smallest solves.
+constexpr int kSoloMaxNodes3x3 = 100000;
 bool use_solo(const dfg_server_s* S, const Req* r) {
-  (void)r;
   if (S->sweeps == 1) return false;
   if (S->sweeps == 2) return true;
-  return S->fp32;
+  return S->fp32 && (r->b < 3 || r->n <= kSoloMaxNodes3x3);
 }
 
 // Fills the request's host-side set-up; returns false with r->error on failure.
@@ -465,55 +480,56 @@ T* at(dfg_server_s* S, size_t base, size_t off) {
 }
 
 template <class T>
-void up(dfg_server_s* S, size_t base, size_t off, const std::vector<T>& v) {
+void up(dfg_server_s* S, cudaStream_t st, size_t base, size_t off, const std::vector<T>& v) {
   if (v.empty()) return;
-  SCK(cudaMemcpyAsync(at<T>(S, base, off), v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, S->s_adm));
+  SCK(cudaMemcpyAsync(at<T>(S, base, off), v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
   S->h2d += (long long)(v.size() * sizeof(T));
 }
 
 SrvSlot slot_of(dfg_server_s* S, Req* r);
 
-// Device work of one admission on s_adm; returns the ILU singular-pivot count.
-int admit_device(dfg_server_s* S, Req* r) {
+// Device work of one admission on an admission lane's stream; returns the
+// ILU singular-pivot count.
+int admit_device(dfg_server_s* S, Req* r, dfg_server_s::AdmLane& lane) {
   const size_t pb = r->pbase, tb = r->tbase;
   const int n = r->n, b = r->b;
   const long long m = (long long)n * b;
   const size_t bs = (size_t)b * b;
-  cudaStream_t st = S->s_adm;
-  up(S, tb, r->t_rowptr, r->rowptr);
-  up(S, tb, r->t_colind, r->colind);
-  up(S, pb, r->o_sptr, r->sell.ptr);
-  up(S, pb, r->o_swidth, r->sell.width);
-  up(S, pb, r->o_scol, r->sell.col);
-  up(S, tb, r->t_ssrc, r->sell.src);
-  up(S, tb, r->t_coords, r->coords);
-  up(S, tb, r->t_conn, r->conn);
-  up(S, tb, r->t_coef, r->coef);
-  up(S, tb, r->t_bc, r->bcflag);
-  up(S, tb, r->t_load, r->load);
-  up(S, tb, r->t_sp, r->gm.slot_ptr);
-  up(S, tb, r->t_ss, r->gm.slot_src);
-  up(S, tb, r->t_rp, r->gm.res_ptr);
-  up(S, tb, r->t_rs, r->gm.res_src);
-  up(S, tb, r->t_dia, r->diaind);
-  up(S, tb, r->t_lev, r->lev.rows);
-  up(S, pb, r->o_recf, r->hf);
-  up(S, pb, r->o_offf, r->of);
-  up(S, pb, r->o_rsf, r->pf.range_steps);
-  up(S, pb, r->o_recb, r->hb);
-  up(S, pb, r->o_offb, r->ob);
-  up(S, pb, r->o_rsb, r->pb.range_steps);
+  cudaStream_t st = lane.st;
+  up(S, st, tb, r->t_rowptr, r->rowptr);
+  up(S, st, tb, r->t_colind, r->colind);
+  up(S, st, pb, r->o_sptr, r->sell.ptr);
+  up(S, st, pb, r->o_swidth, r->sell.width);
+  up(S, st, pb, r->o_scol, r->sell.col);
+  up(S, st, tb, r->t_ssrc, r->sell.src);
+  up(S, st, tb, r->t_coords, r->coords);
+  up(S, st, tb, r->t_conn, r->conn);
+  up(S, st, tb, r->t_coef, r->coef);
+  up(S, st, tb, r->t_bc, r->bcflag);
+  up(S, st, tb, r->t_load, r->load);
+  up(S, st, tb, r->t_sp, r->gm.slot_ptr);
+  up(S, st, tb, r->t_ss, r->gm.slot_src);
+  up(S, st, tb, r->t_rp, r->gm.res_ptr);
+  up(S, st, tb, r->t_rs, r->gm.res_src);
+  up(S, st, tb, r->t_dia, r->diaind);
+  up(S, st, tb, r->t_lev, r->lev.rows);
+  up(S, st, pb, r->o_recf, r->hf);
+  up(S, st, pb, r->o_offf, r->of);
+  up(S, st, pb, r->o_rsf, r->pf.range_steps);
+  up(S, st, pb, r->o_recb, r->hb);
+  up(S, st, pb, r->o_offb, r->ob);
+  up(S, st, pb, r->o_rsb, r->pb.range_steps);
   if (r->solo) {
-    up(S, pb, r->o_chf, r->chf);
-    up(S, pb, r->o_chb, r->chb);
-    up(S, pb, r->o_posf, r->posf);
+    up(S, st, pb, r->o_chf, r->chf);
+    up(S, st, pb, r->o_chb, r->chb);
+    up(S, st, pb, r->o_posf, r->posf);
   }
-  up(S, tb, r->t_eof, r->pf.ent_off);
-  up(S, tb, r->t_esf, r->pf.ent_slot);
-  up(S, tb, r->t_srf, r->pf.step_rows);
-  up(S, tb, r->t_eob, r->pb.ent_off);
-  up(S, tb, r->t_esb, r->pb.ent_slot);
-  up(S, tb, r->t_srb, r->pb.step_rows);
+  up(S, st, tb, r->t_eof, r->pf.ent_off);
+  up(S, st, tb, r->t_esf, r->pf.ent_slot);
+  up(S, st, tb, r->t_srf, r->pf.step_rows);
+  up(S, st, tb, r->t_eob, r->pb.ent_off);
+  up(S, st, tb, r->t_esb, r->pb.ent_slot);
+  up(S, st, tb, r->t_srb, r->pb.step_rows);
   double* diag = at<double>(S, tb, r->t_diag);
   double* offd = at<double>(S, tb, r->t_offd);
   double* rhs = at<double>(S, pb, r->o_rhs);
@@ -569,7 +585,7 @@ int admit_device(dfg_server_s* S, Req* r) {
   double* fo = at<double>(S, tb, r->t_fo);
   SCK(cudaMemcpyAsync(fd, diag, n * bs * 8, cudaMemcpyDeviceToDevice, st));
   if (r->nnz) SCK(cudaMemcpyAsync(fo, offd, r->nnz * bs * 8, cudaMemcpyDeviceToDevice, st));
-  int* nsing = reinterpret_cast<int*>(S->d_adm + kRedGrid + 16);
+  int* nsing = reinterpret_cast<int*>(lane.d_red + kRedGrid + 16);
   SCK(cudaMemsetAsync(nsing, 0, sizeof(int), st));
   const int nlev = (int)r->lev.ptr.size() - 1;
   for (int l = 0; l < nlev; ++l)
@@ -614,17 +630,17 @@ int admit_device(dfg_server_s* S, Req* r) {
     SCK(srv_permute_rhs(slot_of(S, r), S->fp32, st));
     ++nl;
   }
-  Red red{S->d_adm, reinterpret_cast<unsigned*>(S->d_adm + kRedGrid), S->d_adm + kRedGrid + 8};
+  Red red{lane.d_red, reinterpret_cast<unsigned*>(lane.d_red + kRedGrid), lane.d_red + kRedGrid + 8};
   SCK(api_dot(m, rhs, rhs, red, st));
   SCK(srv_init_state(at<PcgState>(S, pb, r->o_st), red.result, S->tol, S->maxit, S->mixed ? kMixedDelta2 : 0.0, st));
   nl += 3;
-  SCK(cudaMemcpyAsync(S->h_nsing, nsing, sizeof(int), cudaMemcpyDeviceToHost, st));
+  SCK(cudaMemcpyAsync(lane.h_nsing, nsing, sizeof(int), cudaMemcpyDeviceToHost, st));
   SCK(cudaStreamSynchronize(st));
   {
     std::lock_guard<std::mutex> lk(S->mu);
     S->launches += nl;
   }
-  return *S->h_nsing;
+  return *lane.h_nsing;
 }
 
 void finish_locked(dfg_server_s* S, Req* r) {
@@ -693,8 +709,9 @@ void symbolic_worker(dfg_server_s* S) {
   }
 }
 
-void admission_thread(dfg_server_s* S) {
+void admission_thread(dfg_server_s* S, int li) {
   cudaSetDevice(S->device);
+  dfg_server_s::AdmLane& lane = S->adm[li];
   for (;;) {
     Req* r = nullptr;
     {
@@ -743,7 +760,7 @@ void admission_thread(dfg_server_s* S) {
     int nsing = 0;
     const Clock::time_point t_adm = Clock::now();
     try {
-      nsing = admit_device(S, r);
+      nsing = admit_device(S, r, lane);
       std::lock_guard<std::mutex> lk(S->mu);
       S->admit_s += std::chrono::duration<double>(Clock::now() - t_adm).count();
     } catch (const CudaFail& f) {
@@ -1290,12 +1307,14 @@ extern "C" int dfg_server_create(dfg_ctx ctx, const dfg_server_config* cfg, dfg_
                               std::to_string(fre) + ")");
     SCK(cudaMalloc(&S->arena_base, budget));
     S->arena.init(budget);
-    SCK(cudaMalloc(&S->d_adm, sizeof(double) * (kRedGrid + 32)));
-    SCK(cudaMemset(S->d_adm, 0, sizeof(double) * (kRedGrid + 32)));
-    SCK(cudaHostAlloc(&S->h_nsing, 64, cudaHostAllocDefault));
     int lo = 0, hi = 0;
     SCK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-    SCK(cudaStreamCreateWithPriority(&S->s_adm, cudaStreamNonBlocking, lo));
+    for (auto& a : S->adm) {
+      SCK(cudaMalloc(&a.d_red, sizeof(double) * (kRedGrid + 32)));
+      SCK(cudaMemset(a.d_red, 0, sizeof(double) * (kRedGrid + 32)));
+      SCK(cudaHostAlloc(&a.h_nsing, 64, cudaHostAllocDefault));
+      SCK(cudaStreamCreateWithPriority(&a.st, cudaStreamNonBlocking, lo));
+    }
     SCK(cudaStreamCreateWithPriority(&S->s_copy, cudaStreamNonBlocking, lo));
     for (int g = 0; g < S->ngroups; ++g) {
       Group& G = S->grp[g];
@@ -1340,7 +1359,7 @@ extern "C" int dfg_server_create(dfg_ctx ctx, const dfg_server_config* cfg, dfg_
   }
   dfg_server s = S.release();
   for (int i = 0; i < s->nthreads; ++i) s->workers.emplace_back(symbolic_worker, s);
-  s->adm_thread = std::thread(admission_thread, s);
+  for (int i = 0; i < kAdmLanes; ++i) s->adm[i].th = std::thread(admission_thread, s, i);
   s->loop_thread = std::thread(loop_thread, s);
   *out = s;
   return DFG_OK;
@@ -1487,7 +1506,8 @@ extern "C" int dfg_server_destroy(dfg_server s) {
     s->adm_stop = true;
     s->cv_adm.notify_all();
   }
-  if (s->adm_thread.joinable()) s->adm_thread.join();
+  for (auto& a : s->adm)
+    if (a.th.joinable()) a.th.join();
   {
     std::lock_guard<std::mutex> lk(s->mu);
     s->loop_stop = true;
@@ -1514,11 +1534,13 @@ extern "C" int dfg_server_destroy(dfg_server s) {
     for (void* p : {(void*)G.h_tab, (void*)G.h_sb, (void*)G.h_solo, (void*)G.h_stat})
       if (p) cudaFreeHost(p);
   }
-  for (cudaStream_t st : {s->s_adm, s->s_copy})
-    if (st) cudaStreamDestroy(st);
-  for (void* p : {(void*)s->arena_base, (void*)s->d_adm})
-    if (p) cudaFree(p);
-  if (s->h_nsing) cudaFreeHost(s->h_nsing);
+  for (auto& a : s->adm) {
+    if (a.st) cudaStreamDestroy(a.st);
+    if (a.d_red) cudaFree(a.d_red);
+    if (a.h_nsing) cudaFreeHost(a.h_nsing);
+  }
+  if (s->s_copy) cudaStreamDestroy(s->s_copy);
+  if (s->arena_base) cudaFree(s->arena_base);
   delete s;
   return DFG_OK;
 }

@@ -374,9 +374,9 @@ typedef struct {
   int profile_every;      /* every n-th replay times its first iteration per kernel; 0 = never */
   int size_groups;        /* solves grouped by size, each group iterating at its own pace on its own
                              streams: 1 = one table for all, 2-3 groups; 0 = 3 */
-  int sweeps;             /* triangular-sweep kernel: 0 = by precision (FP32 sweeps one CTA per solve,
-                             FP64 sweeps ranged over several CTAs), 1 = ranged, 2 = one CTA per solve;
-                             the same bits either way */
+  int sweeps;             /* triangular-sweep kernel: 0 = per solve (FP32 sweeps one CTA per solve
+                             except 3x3-block solves above 100,000 nodes; FP64 sweeps ranged over
+                             several CTAs), 1 = ranged, 2 = one CTA per solve; the same bits either way */
 } dfg_server_config;
 
 /* kind: 1 Poisson 2D (P1 triangles), 2 Poisson 3D (P1 tetrahedra),
