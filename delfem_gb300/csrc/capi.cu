@@ -1477,7 +1477,7 @@ extern "C" int dfg_precond_set_value(dfg_precond prec, dfg_system sys) {
     for (int l = 0; l < nl; ++l)
       CK(launch_ilu_level(sys->b, prec->lev_rows.as<int>() + L.ptr[l], L.ptr[l + 1] - L.ptr[l], F.d_rowptr,
                           F.d_colind, F.d_diaind, prec->fdiag.as<double>(), prec->foffd.as<double>(), nsing,
-                          ctx->stream));
+                          ctx->stream, l > 0));
     launched(ctx, nl);
     int h_nsing = 0;
     CK(cudaMemcpyAsync(&h_nsing, nsing, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));

@@ -29,6 +29,7 @@ __global__ void k_ilu_level(const int* __restrict__ rows, int cnt, const int* __
                             const int* __restrict__ colind, const int* __restrict__ diaind,
                             double* fdiag, double* foffd, int* nsing) {
   constexpr int BS = B * B;
+  pdl_enter();  // the previous level (a programmatic dependency) is complete
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= cnt) return;
   const int i = rows[t];
@@ -157,17 +158,25 @@ cudaError_t launch_factor_init(int B, long long nnz_a, const int* a2f, const dou
 }
 
 cudaError_t launch_ilu_level(int B, const int* rows, int cnt, const int* rowptr, const int* colind,
-                             const int* diaind, double* fdiag, double* foffd, int* nsing, cudaStream_t st) {
+                             const int* diaind, double* fdiag, double* foffd, int* nsing, cudaStream_t st,
+                             bool dependent) {
   if (cnt <= 0) return cudaSuccess;
   const int tpb = 64;
-  const int grid = (cnt + tpb - 1) / tpb;
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((cnt + tpb - 1) / tpb);
+  cfg.blockDim = dim3(tpb);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = dependent ? 1 : 0;
   switch (B) {
-    case 1: k_ilu_level<1><<<grid, tpb, 0, st>>>(rows, cnt, rowptr, colind, diaind, fdiag, foffd, nsing); break;
-    case 2: k_ilu_level<2><<<grid, tpb, 0, st>>>(rows, cnt, rowptr, colind, diaind, fdiag, foffd, nsing); break;
-    case 3: k_ilu_level<3><<<grid, tpb, 0, st>>>(rows, cnt, rowptr, colind, diaind, fdiag, foffd, nsing); break;
+    case 1: return cudaLaunchKernelEx(&cfg, k_ilu_level<1>, rows, cnt, rowptr, colind, diaind, fdiag, foffd, nsing);
+    case 2: return cudaLaunchKernelEx(&cfg, k_ilu_level<2>, rows, cnt, rowptr, colind, diaind, fdiag, foffd, nsing);
+    case 3: return cudaLaunchKernelEx(&cfg, k_ilu_level<3>, rows, cnt, rowptr, colind, diaind, fdiag, foffd, nsing);
     default: return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
 }
 
 }  // namespace dfg

@@ -590,7 +590,7 @@ int admit_device(dfg_server_s* S, Req* r, dfg_server_s::AdmLane& lane) {
   const int nlev = (int)r->lev.ptr.size() - 1;
   for (int l = 0; l < nlev; ++l)
     SCK(launch_ilu_level(b, at<int>(S, tb, r->t_lev) + r->lev.ptr[l], r->lev.ptr[l + 1] - r->lev.ptr[l],
-                         bc.rowptr, bc.colind, at<int>(S, tb, r->t_dia), fd, fo, nsing, st));
+                         bc.rowptr, bc.colind, at<int>(S, tb, r->t_dia), fd, fo, nsing, st, l > 0));
   nl += nlev;
   // the matrix into its sliced-ELL copy (the only copy that stays resident;
   // the mixed form keeps an FP32 one beside it)
