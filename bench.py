@@ -922,7 +922,7 @@ def main():
     ap.add_argument("--sweep-mode", type=int, default=0, choices=[0, 1, 2, 3],
                     help="single solves: triangular-sweep schedule, 0 = timed choice, 1 ranged, "
                          "2 level-scheduled, 3 one CTA")
-    ap.add_argument("--max-inflight", type=int, default=128, help="serving: solves resident at once (<= 256)")
+    ap.add_argument("--max-inflight", type=int, default=256, help="serving: solves resident at once (<= 256)")
     ap.add_argument("--size-groups", type=int, default=0, help="serving: 1 table, 2-3 size groups, 0 = server default (3)")
     ap.add_argument("--ref-sample-every", type=int, default=1,
                     help="--impl reference, serving configs: solve every n-th timed request (1 = all of them)")

@@ -48,14 +48,24 @@ __device__ double block_sum(double v) {
   return ws[0];
 }
 
-__device__ __forceinline__ int find_slot(const SrvTable* T, int c) {
-  int lo = 0, hi = T->nslots - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (T->chunk_start[mid] <= c) lo = mid; else hi = mid - 1;
+// This block's chunks (blockIdx.x, + gridDim.x, ...) with their slot index,
+// the next chunk's index loaded one chunk ahead so that only the slot's
+// fields and state stand between a chunk and its data.
+struct ChunkWalk {
+  const unsigned char* map;
+  int nch, c, si_next;
+  __device__ explicit ChunkWalk(const SrvTable* T) : map(T->chunk_slot), nch(T->total_chunks), c(blockIdx.x) {
+    si_next = c < nch ? __ldg(map + c) : 0;
   }
-  return lo;
-}
+  __device__ bool next(int& cc, int& si) {
+    if (c >= nch) return false;
+    cc = c;
+    si = si_next;
+    c += gridDim.x;
+    si_next = c < nch ? __ldg(map + c) : 0;
+    return true;
+  }
+};
 
 // Publishes this chunk's partial; true (block-uniform) in the slot's last
 // arriving block, which then holds the slot total in *tot.
@@ -148,13 +158,14 @@ template <typename Z>
 __global__ void __launch_bounds__(kSrvTpb) k_srv_rz_beta(const SrvTable* T, double* partials, int* tickets,
                                                          int ntickets) {
   if (blockIdx.x == 0 && threadIdx.x < ntickets) tickets[threadIdx.x] = 0;
-  const int nch = T->total_chunks;
-  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
-    const SrvSlot S = T->slot[find_slot(T, c)];
+  ChunkWalk w(T);
+  for (int c, si; w.next(c, si);) {
+    const SrvSlot S = T->slot[si];
     if (ld_relaxed_int(&S.st->done) != 0) continue;
     long long e0, e1;
     chunk_elems(S, c, e0, e1);
     double part = 0.0;
+    #pragma unroll 4
     for (long long k = e0 + threadIdx.x; k < e1; k += kSrvTpb) part += S.r[k] * zval<Z>(S.z, k);
     double tot;
     if (slot_sum(part, c, S, partials, &tot) && threadIdx.x == 0) {
@@ -168,14 +179,15 @@ __global__ void __launch_bounds__(kSrvTpb) k_srv_rz_beta(const SrvTable* T, doub
 // p := z in the first iteration, else p := beta p + z (SCAL + AXPY)
 template <typename Z>
 __global__ void __launch_bounds__(kSrvTpb) k_srv_update_p(const SrvTable* T) {
-  const int nch = T->total_chunks;
-  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
-    const SrvSlot S = T->slot[find_slot(T, c)];
+  ChunkWalk w(T);
+  for (int c, si; w.next(c, si);) {
+    const SrvSlot S = T->slot[si];
     if (ld_relaxed_int(&S.st->done) != 0) continue;
     long long e0, e1;
     chunk_elems(S, c, e0, e1);
     const bool first = S.st->it == 0;
     const double beta = S.st->beta;
+    #pragma unroll 4
     for (long long k = e0 + threadIdx.x; k < e1; k += kSrvTpb)
       S.p[k] = first ? zval<Z>(S.z, k) : __dadd_rn(__dmul_rn(S.p[k], beta), zval<Z>(S.z, k));
   }
@@ -183,9 +195,9 @@ __global__ void __launch_bounds__(kSrvTpb) k_srv_update_p(const SrvTable* T) {
 
 // q = A p; pAp; alpha = rz / pAp
 __global__ void __launch_bounds__(kSrvTpb) k_srv_spmv_pap(const SrvTable* T, double* partials) {
-  const int nch = T->total_chunks;
-  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
-    const SrvSlot S = T->slot[find_slot(T, c)];
+  ChunkWalk w(T);
+  for (int c, si; w.next(c, si);) {
+    const SrvSlot S = T->slot[si];
     if (ld_relaxed_int(&S.st->done) != 0) continue;
     int row0, row1;
     chunk_rows(S, c, row0, row1);
@@ -203,14 +215,15 @@ __global__ void __launch_bounds__(kSrvTpb) k_srv_spmv_pap(const SrvTable* T, dou
 // to the sentinel; FP32 copy of r for FP32 sweeps
 template <typename Z>
 __global__ void __launch_bounds__(kSrvTpb) k_srv_update_rx(const SrvTable* T, double* partials) {
-  const int nch = T->total_chunks;
-  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
-    const SrvSlot S = T->slot[find_slot(T, c)];
+  ChunkWalk w(T);
+  for (int c, si; w.next(c, si);) {
+    const SrvSlot S = T->slot[si];
     if (ld_relaxed_int(&S.st->done) != 0) continue;
     long long e0, e1;
     chunk_elems(S, c, e0, e1);
     const double alpha = S.st->alpha;
     double part = 0.0;
+    #pragma unroll 4
     for (long long k = e0 + threadIdx.x; k < e1; k += kSrvTpb) {
       double r = S.r[k];
       if (alpha != 0.0) {
@@ -219,8 +232,10 @@ __global__ void __launch_bounds__(kSrvTpb) k_srv_update_rx(const SrvTable* T, do
         S.x[k] = __dadd_rn(S.x[k], __dmul_rn(alpha, S.p[k]));
       }
       part += r * r;
-      reinterpret_cast<Z*>(S.y)[k] = sentinel_value<Z>();
-      reinterpret_cast<Z*>(S.z)[k] = sentinel_value<Z>();
+      if (!S.posf) {  // ranged sweeps hand values over through these sentinels
+        reinterpret_cast<Z*>(S.y)[k] = sentinel_value<Z>();
+        reinterpret_cast<Z*>(S.z)[k] = sentinel_value<Z>();
+      }
       put_sweep_input<Z>(S, k, r);
     }
     double tot;
@@ -252,9 +267,9 @@ constexpr int kMaxReplace = 8;
 // ||rd||^2 <= tol^2 ||b||^2, else marked for residual replacement (done = 6),
 // or given up (done = 7) after kMaxReplace replacements
 __global__ void __launch_bounds__(kSrvTpb) k_srv_check_true(const SrvTable* T, double* partials) {
-  const int nch = T->total_chunks;
-  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
-    const SrvSlot S = T->slot[find_slot(T, c)];
+  ChunkWalk w(T);
+  for (int c, si; w.next(c, si);) {
+    const SrvSlot S = T->slot[si];
     if (ld_relaxed_int(&S.st->done) != 1 || ld_relaxed_int(&S.st->verified) != 0) continue;
     int row0, row1;
     chunk_rows(S, c, row0, row1);
@@ -273,18 +288,21 @@ __global__ void __launch_bounds__(kSrvTpb) k_srv_check_true(const SrvTable* T, d
 // done == 6: r := rd and the recursion continues (residual replacement)
 template <typename Z>
 __global__ void __launch_bounds__(kSrvTpb) k_srv_replace(const SrvTable* T, double* partials) {
-  const int nch = T->total_chunks;
-  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
-    const SrvSlot S = T->slot[find_slot(T, c)];
+  ChunkWalk w(T);
+  for (int c, si; w.next(c, si);) {
+    const SrvSlot S = T->slot[si];
     if (ld_relaxed_int(&S.st->done) != 6) continue;
     long long e0, e1;
     chunk_elems(S, c, e0, e1);
+    #pragma unroll 4
     for (long long k = e0 + threadIdx.x; k < e1; k += kSrvTpb) {
       const double r = S.rd[k];
       S.r[k] = r;
       put_sweep_input<Z>(S, k, r);
-      reinterpret_cast<Z*>(S.y)[k] = sentinel_value<Z>();
-      reinterpret_cast<Z*>(S.z)[k] = sentinel_value<Z>();
+      if (!S.posf) {
+        reinterpret_cast<Z*>(S.y)[k] = sentinel_value<Z>();
+        reinterpret_cast<Z*>(S.z)[k] = sentinel_value<Z>();
+      }
     }
     double tot;
     if (slot_sum(0.0, c, S, partials, &tot) && threadIdx.x == 0) {
@@ -338,14 +356,15 @@ __device__ __forceinline__ bool mixed_live(const PcgState* st) { return ld_relax
 __global__ void __launch_bounds__(kSrvTpb) k_srvm_rz_beta(const SrvTable* T, double* partials, int* tickets,
                                                           int ntickets) {
   if (blockIdx.x == 0 && threadIdx.x < ntickets) tickets[threadIdx.x] = 0;
-  const int nch = T->total_chunks;
-  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
-    const SrvSlot S = T->slot[find_slot(T, c)];
+  ChunkWalk w(T);
+  for (int c, si; w.next(c, si);) {
+    const SrvSlot S = T->slot[si];
     if (!mixed_live(S.st)) continue;
     long long e0, e1;
     chunk_elems(S, c, e0, e1);
     const float* z = reinterpret_cast<const float*>(S.z);
     double part = 0.0;
+    #pragma unroll 4
     for (long long k = e0 + threadIdx.x; k < e1; k += kSrvTpb) part += (double)S.r32[k] * (double)z[k];
     double tot;
     if (slot_sum(part, c, S, partials, &tot) && threadIdx.x == 0) {
@@ -358,15 +377,16 @@ __global__ void __launch_bounds__(kSrvTpb) k_srvm_rz_beta(const SrvTable* T, dou
 
 // p := z in the first iteration, else p := z + beta p (FP32)
 __global__ void __launch_bounds__(kSrvTpb) k_srvm_update_p(const SrvTable* T) {
-  const int nch = T->total_chunks;
-  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
-    const SrvSlot S = T->slot[find_slot(T, c)];
+  ChunkWalk w(T);
+  for (int c, si; w.next(c, si);) {
+    const SrvSlot S = T->slot[si];
     if (!mixed_live(S.st)) continue;
     long long e0, e1;
     chunk_elems(S, c, e0, e1);
     const bool first = S.st->it == 0;
     const float beta = (float)S.st->beta;
     const float* z = reinterpret_cast<const float*>(S.z);
+    #pragma unroll 4
     for (long long k = e0 + threadIdx.x; k < e1; k += kSrvTpb) S.p32[k] = first ? z[k] : z[k] + beta * S.p32[k];
   }
 }
@@ -388,9 +408,9 @@ __device__ __forceinline__ double chunk_q_pap32(const SrvSlot& S, int row0, int 
 }
 
 __global__ void __launch_bounds__(kSrvTpb) k_srvm_spmv_pap(const SrvTable* T, double* partials) {
-  const int nch = T->total_chunks;
-  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
-    const SrvSlot S = T->slot[find_slot(T, c)];
+  ChunkWalk w(T);
+  for (int c, si; w.next(c, si);) {
+    const SrvSlot S = T->slot[si];
     if (!mixed_live(S.st)) continue;
     int row0, row1;
     chunk_rows(S, c, row0, row1);
@@ -409,9 +429,9 @@ __global__ void __launch_bounds__(kSrvTpb) k_srvm_spmv_pap(const SrvTable* T, do
 // the reliable-update trigger, the iteration limit; sweep outputs back to the
 // sentinel
 __global__ void __launch_bounds__(kSrvTpb) k_srvm_update_rx(const SrvTable* T, double* partials) {
-  const int nch = T->total_chunks;
-  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
-    const SrvSlot S = T->slot[find_slot(T, c)];
+  ChunkWalk w(T);
+  for (int c, si; w.next(c, si);) {
+    const SrvSlot S = T->slot[si];
     if (!mixed_live(S.st)) continue;
     long long e0, e1;
     chunk_elems(S, c, e0, e1);
@@ -420,6 +440,7 @@ __global__ void __launch_bounds__(kSrvTpb) k_srvm_update_rx(const SrvTable* T, d
     float* y = reinterpret_cast<float*>(S.y);
     float* z = reinterpret_cast<float*>(S.z);
     double part = 0.0;
+    #pragma unroll 4
     for (long long k = e0 + threadIdx.x; k < e1; k += kSrvTpb) {
       float r = S.r32[k];
       if (alpha != 0.0) {
@@ -429,8 +450,10 @@ __global__ void __launch_bounds__(kSrvTpb) k_srvm_update_rx(const SrvTable* T, d
         if (S.posf) put_sweep_input<float>(S, k, r);
       }
       part += (double)r * (double)r;
-      y[k] = sentinel_value<float>();
-      z[k] = sentinel_value<float>();
+      if (!S.posf) {
+        y[k] = sentinel_value<float>();
+        z[k] = sentinel_value<float>();
+      }
     }
     double tot;
     if (slot_sum(part, c, S, partials, &tot) && threadIdx.x == 0) {
@@ -462,13 +485,14 @@ __device__ __forceinline__ bool mixed_due(const PcgState* st) {
 // x := x + d, d := 0 for slots due for a reliable update, stopped, or at
 // the end (limit, NaN)
 __global__ void __launch_bounds__(kSrvTpb) k_srvm_fold(const SrvTable* T) {
-  const int nch = T->total_chunks;
-  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
-    const SrvSlot S = T->slot[find_slot(T, c)];
+  ChunkWalk w(T);
+  for (int c, si; w.next(c, si);) {
+    const SrvSlot S = T->slot[si];
     const int dn = ld_relaxed_int(&S.st->done);
     if (!(mixed_due(S.st) || dn == 2 || dn == 3)) continue;
     long long e0, e1;
     chunk_elems(S, c, e0, e1);
+    #pragma unroll 4
     for (long long k = e0 + threadIdx.x; k < e1; k += kSrvTpb) {
       S.x[k] = S.x[k] + S.d[k];
       S.d[k] = 0.0;
@@ -496,9 +520,9 @@ __device__ __forceinline__ double chunk_refine(const SrvSlot& S, int row0, int r
 }
 
 __global__ void __launch_bounds__(kSrvTpb) k_srvm_refine(const SrvTable* T, double* partials) {
-  const int nch = T->total_chunks;
-  for (int c = blockIdx.x; c < nch; c += gridDim.x) {
-    const SrvSlot S = T->slot[find_slot(T, c)];
+  ChunkWalk w(T);
+  for (int c, si; w.next(c, si);) {
+    const SrvSlot S = T->slot[si];
     if (!mixed_due(S.st)) continue;
     int row0, row1;
     chunk_rows(S, c, row0, row1);

@@ -51,9 +51,11 @@ struct SrvSlot {
 struct SrvTable {
   int nslots;
   int total_chunks;
+  const unsigned char* chunk_slot;  // per chunk of the launch: its slot
   int chunk_start[kSrvMaxSlots + 1];
   SrvSlot slot[kSrvMaxSlots];
 };
+static_assert(kSrvMaxSlots <= 256, "chunk_slot holds a slot index in one byte");
 
 // What the host reads after each replay, one entry per table slot.
 struct SrvStatus {

@@ -26,7 +26,7 @@ def _ptr(a):
 
 class Server:
     def __init__(self, ctx, mode: str = "fp32f", tol: float = 1e-8, maxit: int = 20000, budget_bytes: int = 0,
-                 max_inflight: int = 128, chunk_iters: int = 8, host_threads: int = 0, profile_every: int = 0,
+                 max_inflight: int = 0, chunk_iters: int = 8, host_threads: int = 0, profile_every: int = 0,
                  size_groups: int = 0, sweeps: int = 0):
         self.ctx = ctx
         cfg = capi.ServerConfig(MODES[mode], tol, maxit, budget_bytes, max_inflight, chunk_iters, host_threads,

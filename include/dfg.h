@@ -368,7 +368,7 @@ typedef struct {
   double tol;             /* true relative residual target */
   int maxit;              /* iteration limit per solve; 0 = 20000 */
   long long budget_bytes; /* device bytes reserved for admitted solves; 0 = 85% of free memory */
-  int max_inflight;       /* solves resident at once, <= 256; 0 = 128 */
+  int max_inflight;       /* solves resident at once, <= 256; 0 = 256 */
   int chunk_iters;        /* PCG iterations per graph replay, <= 64; 0 = 8 */
   int host_threads;       /* symbolic set-up threads; 0 = hardware threads - 2 */
   int profile_every;      /* every n-th replay times its first iteration per kernel; 0 = never */
