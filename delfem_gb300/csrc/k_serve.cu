@@ -27,6 +27,11 @@ namespace dfg {
 
 namespace {
 
+// element-wise kernels (four-way unrolled loops) are held to the registers of
+// six blocks per SM, so that the launches' four blocks per SM are resident in
+// one wave (unbounded, the r/x update took 70 registers: three blocks per SM)
+constexpr int kSrvVecBlocks = 6;
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -155,7 +160,7 @@ __device__ __forceinline__ void chunk_rows(const SrvSlot& S, int c, int& row0, i
 
 // rz_new = r.z; beta = rz_new / rz (0 in the first iteration)
 template <typename Z>
-__global__ void __launch_bounds__(kSrvTpb) k_srv_rz_beta(const SrvTable* T, double* partials, int* tickets,
+__global__ void __launch_bounds__(kSrvTpb, kSrvVecBlocks) k_srv_rz_beta(const SrvTable* T, double* partials, int* tickets,
                                                          int ntickets) {
   if (blockIdx.x == 0 && threadIdx.x < ntickets) tickets[threadIdx.x] = 0;
   ChunkWalk w(T);
@@ -178,7 +183,7 @@ __global__ void __launch_bounds__(kSrvTpb) k_srv_rz_beta(const SrvTable* T, doub
 
 // p := z in the first iteration, else p := beta p + z (SCAL + AXPY)
 template <typename Z>
-__global__ void __launch_bounds__(kSrvTpb) k_srv_update_p(const SrvTable* T) {
+__global__ void __launch_bounds__(kSrvTpb, kSrvVecBlocks) k_srv_update_p(const SrvTable* T) {
   ChunkWalk w(T);
   for (int c, si; w.next(c, si);) {
     const SrvSlot S = T->slot[si];
@@ -214,7 +219,7 @@ __global__ void __launch_bounds__(kSrvTpb) k_srv_spmv_pap(const SrvTable* T, dou
 // r := r - alpha q; x := x + alpha p; rr = r.r; stop test; sweep outputs back
 // to the sentinel; FP32 copy of r for FP32 sweeps
 template <typename Z>
-__global__ void __launch_bounds__(kSrvTpb) k_srv_update_rx(const SrvTable* T, double* partials) {
+__global__ void __launch_bounds__(kSrvTpb, kSrvVecBlocks) k_srv_update_rx(const SrvTable* T, double* partials) {
   ChunkWalk w(T);
   for (int c, si; w.next(c, si);) {
     const SrvSlot S = T->slot[si];
@@ -287,7 +292,7 @@ __global__ void __launch_bounds__(kSrvTpb) k_srv_check_true(const SrvTable* T, d
 
 // done == 6: r := rd and the recursion continues (residual replacement)
 template <typename Z>
-__global__ void __launch_bounds__(kSrvTpb) k_srv_replace(const SrvTable* T, double* partials) {
+__global__ void __launch_bounds__(kSrvTpb, kSrvVecBlocks) k_srv_replace(const SrvTable* T, double* partials) {
   ChunkWalk w(T);
   for (int c, si; w.next(c, si);) {
     const SrvSlot S = T->slot[si];
@@ -353,7 +358,7 @@ __global__ void k_srv_init_vectors(long long m, const double* rhs, double* r, do
 __device__ __forceinline__ bool mixed_live(const PcgState* st) { return ld_relaxed_int(&st->done) == 0; }
 
 // rz_new = r.z (FP64 accumulation of FP32 products); beta = rz_new / rz
-__global__ void __launch_bounds__(kSrvTpb) k_srvm_rz_beta(const SrvTable* T, double* partials, int* tickets,
+__global__ void __launch_bounds__(kSrvTpb, kSrvVecBlocks) k_srvm_rz_beta(const SrvTable* T, double* partials, int* tickets,
                                                           int ntickets) {
   if (blockIdx.x == 0 && threadIdx.x < ntickets) tickets[threadIdx.x] = 0;
   ChunkWalk w(T);
@@ -376,7 +381,7 @@ __global__ void __launch_bounds__(kSrvTpb) k_srvm_rz_beta(const SrvTable* T, dou
 }
 
 // p := z in the first iteration, else p := z + beta p (FP32)
-__global__ void __launch_bounds__(kSrvTpb) k_srvm_update_p(const SrvTable* T) {
+__global__ void __launch_bounds__(kSrvTpb, kSrvVecBlocks) k_srvm_update_p(const SrvTable* T) {
   ChunkWalk w(T);
   for (int c, si; w.next(c, si);) {
     const SrvSlot S = T->slot[si];
@@ -428,7 +433,7 @@ __global__ void __launch_bounds__(kSrvTpb) k_srvm_spmv_pap(const SrvTable* T, do
 // recursive stop (done 5: the true residual decides at the end of the replay),
 // the reliable-update trigger, the iteration limit; sweep outputs back to the
 // sentinel
-__global__ void __launch_bounds__(kSrvTpb) k_srvm_update_rx(const SrvTable* T, double* partials) {
+__global__ void __launch_bounds__(kSrvTpb, kSrvVecBlocks) k_srvm_update_rx(const SrvTable* T, double* partials) {
   ChunkWalk w(T);
   for (int c, si; w.next(c, si);) {
     const SrvSlot S = T->slot[si];
@@ -484,7 +489,7 @@ __device__ __forceinline__ bool mixed_due(const PcgState* st) {
 
 // x := x + d, d := 0 for slots due for a reliable update, stopped, or at
 // the end (limit, NaN)
-__global__ void __launch_bounds__(kSrvTpb) k_srvm_fold(const SrvTable* T) {
+__global__ void __launch_bounds__(kSrvTpb, kSrvVecBlocks) k_srvm_fold(const SrvTable* T) {
   ChunkWalk w(T);
   for (int c, si; w.next(c, si);) {
     const SrvSlot S = T->slot[si];

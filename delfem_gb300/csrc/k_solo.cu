@@ -30,7 +30,8 @@
 // wait that gives up records kErrTimeout and the launch drains and returns.
 //
 // Record layout (bytes; pack_solo_headers in sched.cpp, values by k_pack):
-//   [hdr int4: nent, steps in the chunk, step, the chunk's offset in its level]
+//   [hdr int4: nent, steps in the chunk (+ 1 << 16 if the chunk closes its
+//    level), step, the chunk's offset in its level]
 //   [out: 32 int][code: nent x 32 int]
 //   [blocks: nent x B*B x 32 of T][D^-1: B*B x 32 of T, forward only]
 // out: the element offset / B where a lane's result goes (-1: empty lane);
@@ -41,6 +42,19 @@
 #include "k_sweep.h"
 
 namespace dfg {
+
+// whether some level starts at chunk v (lev_chunks: nlevels + 1 ascending
+// first chunks, the last entry the chunk count)
+__device__ __forceinline__ bool level_starts_at(const int* lev_chunks, int nlevels, int v) {
+  int lo = 1, hi = nlevels;
+  while (lo <= hi) {
+    const int mid = (lo + hi) >> 1;
+    const int x = __ldg(&lev_chunks[mid]);
+    if (x == v) return true;
+    if (x < v) lo = mid + 1; else hi = mid - 1;
+  }
+  return false;
+}
 
 template <typename T, int B, bool FWD, int MAXE>
 __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
@@ -129,114 +143,109 @@ __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
     } else {
       // ------------------------------------------------------------- compute
       T* out = reinterpret_cast<T*>(S.out);
-      const int* __restrict__ lc = S.lev_chunks;
-      const int nl = S.nlevels;
-      // level bounds come one level ahead, so their load is off the critical path
-      int c0 = lc[0], c1 = nl > 0 ? lc[1] : 0;
       int st = st0, ph = ph0;
-      for (int l = 0; l < nl; ++l) {
-        const int c2 = l + 2 <= nl ? __ldg(&lc[l + 2]) : 0;
-        for (int c = c0; c < c1; ++c, (++st == NS ? (st = 0, ph ^= 1) : 0)) {
-          if (!abort && !mbar_wait(&full[st], (unsigned)ph, a.err, kSiteFull, jslot, c)) abort = true;
-          const unsigned char* stage = rstage + (size_t)st * a.rec_stage;
-          const int4 hdr = *reinterpret_cast<const int4*>(stage);
-          const int nent = hdr.x;
-          const int nst = abort ? 0 : hdr.y;
-          const int rec_sz = 144 + nent * 128 + nent * 32 * BS * SZ + (FWD ? 32 * BS * SZ : 0);
-          // steps go to warps by their place in the level (hdr.w: the chunk's
-          // offset there), so a level of <= kSoloWarps steps costs each warp
-          // one step whatever its chunks
-          for (int k = (warp - hdr.w % NW + NW) % NW; k < nst; k += NW) {
-            const unsigned char* rec = stage + (size_t)k * rec_sz;
-            const int s = reinterpret_cast<const int*>(rec)[2];
-            const int o = reinterpret_cast<const int*>(rec + 16)[lane];
-            const int* code = reinterpret_cast<const int*>(rec + 144);
-            const T* blk = reinterpret_cast<const T*>(rec + 144 + nent * 128);
-            if (o >= 0) {
-              const T* val = reinterpret_cast<const T*>(vstage + (size_t)st * VS + (size_t)k * STEP_RHS);
-              T t[B];
+      for (int c = 0; c < nch; ++c, (++st == NS ? (st = 0, ph ^= 1) : 0)) {
+        if (!abort && !mbar_wait(&full[st], (unsigned)ph, a.err, kSiteFull, jslot, c)) abort = true;
+        const unsigned char* stage = rstage + (size_t)st * a.rec_stage;
+        const int4 hdr = *reinterpret_cast<const int4*>(stage);
+        const int nent = hdr.x;
+        const int nst = abort ? 0 : (hdr.y & 0xffff);
+        const int rec_sz = 144 + nent * 128 + nent * 32 * BS * SZ + (FWD ? 32 * BS * SZ : 0);
+        // steps go to warps by their place in the level (hdr.w: the chunk's
+        // offset there), so a level of <= kSoloWarps steps costs each warp
+        // one step whatever its chunks
+        for (int k = (warp - hdr.w % NW + NW) % NW; k < nst; k += NW) {
+          const unsigned char* rec = stage + (size_t)k * rec_sz;
+          const int s = reinterpret_cast<const int*>(rec)[2];
+          const int o = reinterpret_cast<const int*>(rec + 16)[lane];
+          const int* code = reinterpret_cast<const int*>(rec + 144);
+          const T* blk = reinterpret_cast<const T*>(rec + 144 + nent * 128);
+          if (o >= 0) {
+            const T* val = reinterpret_cast<const T*>(vstage + (size_t)st * VS + (size_t)k * STEP_RHS);
+            T t[B];
 #pragma unroll
-              for (int d = 0; d < B; ++d) t[d] = val[lane * B + d];
-              if constexpr (MAXE > 0) {
-                // all dependency values first (independent loads), then the FMAs
-                T v[MAXE][B];
+            for (int d = 0; d < B; ++d) t[d] = val[lane * B + d];
+            if constexpr (MAXE > 0) {
+              // all dependency values first (independent loads), then the FMAs
+              T v[MAXE][B];
 #pragma unroll
-                for (int e = 0; e < MAXE; ++e) {
-                  if (e < nent) {
-                    const int cd = code[e * 32 + lane];
-                    if (cd >= 0) {
-                      const T* vp = reinterpret_cast<const T*>(ringreg + cd);
-#pragma unroll
-                      for (int d = 0; d < B; ++d) v[e][d] = vp[d];
-                    } else {
-                      const T* gp = out + (size_t)(-cd - 1) * B;
-#pragma unroll
-                      for (int d = 0; d < B; ++d) v[e][d] = __ldcg(gp + d);
-                    }
-                  }
-                }
-#pragma unroll
-                for (int e = 0; e < MAXE; ++e) {
-                  if (e < nent) {
-#pragma unroll
-                    for (int p = 0; p < B; ++p) {
-                      T acc = t[p];
-#pragma unroll
-                      for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[e][q];
-                      t[p] = acc;
-                    }
-                  }
-                }
-              } else {
-                for (int e = 0; e < nent; ++e) {
+              for (int e = 0; e < MAXE; ++e) {
+                if (e < nent) {
                   const int cd = code[e * 32 + lane];
-                  T v[B];
                   if (cd >= 0) {
                     const T* vp = reinterpret_cast<const T*>(ringreg + cd);
 #pragma unroll
-                    for (int d = 0; d < B; ++d) v[d] = vp[d];
+                    for (int d = 0; d < B; ++d) v[e][d] = vp[d];
                   } else {
                     const T* gp = out + (size_t)(-cd - 1) * B;
 #pragma unroll
-                    for (int d = 0; d < B; ++d) v[d] = __ldcg(gp + d);
+                    for (int d = 0; d < B; ++d) v[e][d] = __ldcg(gp + d);
                   }
+                }
+              }
+#pragma unroll
+              for (int e = 0; e < MAXE; ++e) {
+                if (e < nent) {
 #pragma unroll
                   for (int p = 0; p < B; ++p) {
                     T acc = t[p];
 #pragma unroll
-                    for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[q];
+                    for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[e][q];
                     t[p] = acc;
                   }
                 }
               }
-              T y[B];
-              if constexpr (FWD) {
-                const T* dinv = blk + nent * BS * 32;
+            } else {
+              for (int e = 0; e < nent; ++e) {
+                const int cd = code[e * 32 + lane];
+                T v[B];
+                if (cd >= 0) {
+                  const T* vp = reinterpret_cast<const T*>(ringreg + cd);
+#pragma unroll
+                  for (int d = 0; d < B; ++d) v[d] = vp[d];
+                } else {
+                  const T* gp = out + (size_t)(-cd - 1) * B;
+#pragma unroll
+                  for (int d = 0; d < B; ++d) v[d] = __ldcg(gp + d);
+                }
 #pragma unroll
                 for (int p = 0; p < B; ++p) {
-                  T acc = dinv[(p * B) * 32 + lane] * t[0];
+                  T acc = t[p];
 #pragma unroll
-                  for (int q = 1; q < B; ++q) acc += dinv[(p * B + q) * 32 + lane] * t[q];
-                  y[p] = acc;
+                  for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[q];
+                  t[p] = acc;
                 }
-              } else {
-#pragma unroll
-                for (int p = 0; p < B; ++p) y[p] = t[p];
-              }
-              T* rg = reinterpret_cast<T*>(ringreg + 32) + (((s & RM) * 32 + lane) * B);
-#pragma unroll
-              for (int d = 0; d < B; ++d) {
-                rg[d] = y[d];
-                out[(size_t)o * B + d] = y[d];
               }
             }
+            T y[B];
+            if constexpr (FWD) {
+              const T* dinv = blk + nent * BS * 32;
+#pragma unroll
+              for (int p = 0; p < B; ++p) {
+                T acc = dinv[(p * B) * 32 + lane] * t[0];
+#pragma unroll
+                for (int q = 1; q < B; ++q) acc += dinv[(p * B + q) * 32 + lane] * t[q];
+                y[p] = acc;
+              }
+            } else {
+#pragma unroll
+              for (int p = 0; p < B; ++p) y[p] = t[p];
+            }
+            T* rg = reinterpret_cast<T*>(ringreg + 32) + (((s & RM) * 32 + lane) * B);
+#pragma unroll
+            for (int d = 0; d < B; ++d) {
+              rg[d] = y[d];
+              out[(size_t)o * B + d] = y[d];
+            }
           }
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&empty[st]);
         }
-        named_sync(1, NW * 32);
-        c0 = c1;
-        c1 = c2;
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[st]);
+        // the chunk's header says whether it closes its level (no global
+        // load on the way from one level to the next); a lane that gave up
+        // waiting finds the level bounds in global memory instead
+        const bool lev_end = abort ? level_starts_at(S.lev_chunks, S.nlevels, c + 1) : (hdr.y >> 16) != 0;
+        if (lev_end) named_sync(1, NW * 32);
       }
     }
     g += nch;

@@ -476,13 +476,18 @@ std::vector<unsigned char> pack_solo_headers(const SoloPlan& S, int elem, const 
   off.assign(P.nsteps + 1, 0);
   for (int s = 0; s < P.nsteps; ++s) off[s + 1] = off[s] + solo_rec_bytes(P.step_nent[s], bs, elem, P.forward);
   std::vector<unsigned char> h((size_t)off[P.nsteps], 0);
-  std::vector<int> level_first(P.nsteps, 0);
+  std::vector<int> level_first(P.nsteps, 0), level_end(P.nsteps, 0);
   for (int l = 0; l < P.nranges; ++l)
-    for (int s = P.range_steps[l]; s < P.range_steps[l + 1]; ++s) level_first[s] = P.range_steps[l];
+    for (int s = P.range_steps[l]; s < P.range_steps[l + 1]; ++s) {
+      level_first[s] = P.range_steps[l];
+      level_end[s] = P.range_steps[l + 1];
+    }
   for (const SoloChunk& c : S.chunks)
     for (int s = c.first_step; s < c.first_step + c.nsteps; ++s) {
       unsigned char* r = h.data() + off[s];
-      const int hdr[4] = {P.step_nent[s], c.nsteps, s, c.first_step - level_first[c.first_step]};
+      // steps in the chunk, plus 1 << 16 when the chunk closes its level
+      const int closes = c.first_step + c.nsteps == level_end[c.first_step] ? 1 << 16 : 0;
+      const int hdr[4] = {P.step_nent[s], c.nsteps | closes, s, c.first_step - level_first[c.first_step]};
       std::memcpy(r, hdr, 16);
       int* outv = reinterpret_cast<int*>(r + 16);
       int* code = reinterpret_cast<int*>(r + 144);

@@ -399,7 +399,11 @@ extern "C" int emul_solo_precond(int n, int b, const int* rowptr, const int* col
           const SoloChunk* ch = nullptr;
           for (int c = S.lev_chunks[l]; c < S.lev_chunks[l + 1]; ++c)
             if (S.chunks[c].first_step <= s && s < S.chunks[c].first_step + S.chunks[c].nsteps) ch = &S.chunks[c];
-          if (!ch || hdr[1] != ch->nsteps || hdr[3] != ch->first_step - P.range_steps[l]) { info[3] = 12; return 12; }
+          const int closes = ch && ch->first_step + ch->nsteps == P.range_steps[l + 1] ? 1 << 16 : 0;
+          if (!ch || hdr[1] != (ch->nsteps | closes) || hdr[3] != ch->first_step - P.range_steps[l]) {
+            info[3] = 12;
+            return 12;
+          }
         }
         const int* outv = reinterpret_cast<const int*>(rec + 16);
         const int* code = reinterpret_cast<const int*>(rec + 144);
