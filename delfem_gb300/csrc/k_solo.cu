@@ -166,18 +166,29 @@ __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
 #pragma unroll
             for (int d = 0; d < B; ++d) t[d] = val[lane * B + d];
             if constexpr (MAXE > 0) {
-              // all dependency values first (independent loads), then the FMAs
+              // all dependency values first, then the FMAs.  The codes are
+              // loaded together, then every value from the ring together
+              // (a global reference reads the ring's zero bytes first), so
+              // the step waits on two shared-memory round trips, not two per
+              // entry; global references are read after, in a warp-uniform
+              // branch that is taken only where the ring does not reach
+              int cdv[MAXE];
+#pragma unroll
+              for (int e = 0; e < MAXE; ++e) cdv[e] = e < nent ? code[e * 32 + lane] : 0;
               T v[MAXE][B];
+              bool glob = false;
 #pragma unroll
               for (int e = 0; e < MAXE; ++e) {
-                if (e < nent) {
-                  const int cd = code[e * 32 + lane];
-                  if (cd >= 0) {
-                    const T* vp = reinterpret_cast<const T*>(ringreg + cd);
+                const T* vp = reinterpret_cast<const T*>(ringreg + (cdv[e] >= 0 ? cdv[e] : 0));
 #pragma unroll
-                    for (int d = 0; d < B; ++d) v[e][d] = vp[d];
-                  } else {
-                    const T* gp = out + (size_t)(-cd - 1) * B;
+                for (int d = 0; d < B; ++d) v[e][d] = vp[d];
+                glob |= cdv[e] < 0;
+              }
+              if (__any_sync(__activemask(), glob)) {
+#pragma unroll
+                for (int e = 0; e < MAXE; ++e) {
+                  if (cdv[e] < 0) {
+                    const T* gp = out + (size_t)(-cdv[e] - 1) * B;
 #pragma unroll
                     for (int d = 0; d < B; ++d) v[e][d] = __ldcg(gp + d);
                   }
