@@ -9,8 +9,9 @@
 // dependency was produced by the same CTA and no value crosses SMs.
 //
 // CTA: kSoloWarps compute warps + one producer warp.
-//   * producer (one lane) -- walks the solve's chunks (runs of <= ch_max steps
-//     of one level) in order: per chunk two TMA bulk copies onto the stage's
+//   * producer (one warp; lane 0 issues) -- walks the solve's chunks (runs of
+//     <= ch_max steps of one level) in order, their table read 32 entries at a
+//     time by the whole warp: per chunk two TMA bulk copies onto the stage's
 //     `full` mbarrier (one arrival with the byte count): the chunk's packed
 //     records, and its right-hand sides, which the producing kernel stored in
 //     this sweep's step order so that they are contiguous; it runs up to NS
@@ -109,37 +110,51 @@ __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
     const int st0 = g % NS, ph0 = (g / NS) & 1;
     if (warp == NW) {
       // ------------------------------------------------------------ producer
-      if (lane == 0) {
-        const unsigned char* __restrict__ recs = S.rec;
-        const unsigned char* __restrict__ in = reinterpret_cast<const unsigned char*>(S.in);
-        const SoloChunk* __restrict__ chunks = S.chunks;
-        int n_issued = 0;
-        SoloChunk nx = nch > 0 ? chunks[0] : SoloChunk{};
-        int st = st0, ph = ph0;
-        for (int c = 0; c < nch; ++c) {
-          const SoloChunk ch = nx;
-          if (c + 1 < nch) nx = chunks[c + 1];  // the next chunk's entry, off the critical path
-          // the stage's previous use (phase ph ^ 1) must have been released
-          if (g + c >= NS && !mbar_wait(&empty[st], (unsigned)(ph ^ 1), a.err, kSiteEmpty, jslot, c)) {
-            abort = true;
-            break;
+      // The warp reads the chunk table 32 entries at a time (one coalesced
+      // load per 32 chunks, the next batch in flight while this one is
+      // issued); lane 0 issues the copies with each entry taken from its
+      // lane, so no global-load latency lies between two chunks' copies.
+      const unsigned char* __restrict__ recs = S.rec;
+      const unsigned char* __restrict__ in = reinterpret_cast<const unsigned char*>(S.in);
+      const SoloChunk* __restrict__ chunks = S.chunks;
+      int n_issued = 0;
+      SoloChunk cur = lane < nch ? chunks[lane] : SoloChunk{};
+      SoloChunk nxt = 32 + lane < nch ? chunks[32 + lane] : SoloChunk{};
+      int st = st0, ph = ph0;
+      for (int base = 0; base < nch && !abort; base += 32) {
+        const int cnt = min(32, nch - base);
+        for (int i = 0; i < cnt; ++i) {
+          const long long rec_off = __shfl_sync(0xffffffffu, cur.rec_off, i);
+          const int rec_bytes = __shfl_sync(0xffffffffu, cur.rec_bytes, i);
+          const int first_step = __shfl_sync(0xffffffffu, cur.first_step, i);
+          const int nsteps = __shfl_sync(0xffffffffu, cur.nsteps, i);
+          const int c = base + i;
+          if (lane == 0) {
+            // the stage's previous use (phase ph ^ 1) must have been released
+            if (g + c >= NS && !mbar_wait(&empty[st], (unsigned)(ph ^ 1), a.err, kSiteEmpty, jslot, c)) {
+              abort = true;
+            } else {
+              const unsigned rhs_bytes = (unsigned)(nsteps * STEP_RHS);
+              mbar_expect_tx(&full[st], (unsigned)rec_bytes + rhs_bytes);
+              tma_load_1d(rstage + (size_t)st * a.rec_stage, recs + rec_off, (unsigned)rec_bytes, &full[st]);
+              tma_load_1d(vstage + (size_t)st * VS, in + (size_t)first_step * STEP_RHS, rhs_bytes, &full[st]);
+            }
           }
-          const unsigned rhs_bytes = (unsigned)(ch.nsteps * STEP_RHS);
-          mbar_expect_tx(&full[st], (unsigned)ch.rec_bytes + rhs_bytes);
-          tma_load_1d(rstage + (size_t)st * a.rec_stage, recs + ch.rec_off, (unsigned)ch.rec_bytes, &full[st]);
-          tma_load_1d(vstage + (size_t)st * VS, in + (size_t)ch.first_step * STEP_RHS, rhs_bytes, &full[st]);
+          abort = __shfl_sync(0xffffffffu, abort, 0);
+          if (abort) break;
           ++n_issued;
           if (++st == NS) { st = 0; ph ^= 1; }
         }
-        if (abort) {  // copies already issued land before the CTA moves on (bounded)
-          int dst = st0, dph = ph0;
-          for (int k = 0; k < n_issued; ++k) {
-            mbar_drain(&full[dst], (unsigned)dph);
-            if (++dst == NS) { dst = 0; dph ^= 1; }
-          }
+        cur = nxt;
+        nxt = base + 64 + lane < nch ? chunks[base + 64 + lane] : SoloChunk{};
+      }
+      if (abort && lane == 0) {  // copies already issued land before the CTA moves on (bounded)
+        int dst = st0, dph = ph0;
+        for (int k = 0; k < n_issued; ++k) {
+          mbar_drain(&full[dst], (unsigned)dph);
+          if (++dst == NS) { dst = 0; dph ^= 1; }
         }
       }
-      abort = __shfl_sync(0xffffffffu, abort, 0);
     } else {
       // ------------------------------------------------------------- compute
       T* out = reinterpret_cast<T*>(S.out);
