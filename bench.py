@@ -268,6 +268,16 @@ def run_gpu(args, rank, world, local):
         return ok, r
 
     arms_run = [(a, m) for a, m in ARMS if a in args.arms.split(",")]
+    # L2 flush between timed solves: a 256 MB write (twice the 129 MB L2) on
+    # the library's stream, outside each solve's CUDA events
+    flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device=torch.device("cuda", local)) \
+        if torch is not None else None
+
+    def flush_l2():
+        if flush_buf is not None:
+            with torch.cuda.stream(ext):
+                flush_buf.zero_()
+
     results = {}
     for arm, mode in arms_run:
         for _ in range(args.warmup):
@@ -283,6 +293,7 @@ def run_gpu(args, rank, world, local):
             t0 = time.perf_counter()
             for _ in range(args.steps):
                 e0, e1 = ev(), ev()
+                flush_l2()
                 if e0 is not None:
                     e0.record(ext)
                 ok, r = step(mode)
@@ -300,10 +311,11 @@ def run_gpu(args, rank, world, local):
                 e_all1.record(ext)
             barrier()
             wall = time.perf_counter() - t0
-        total_ms = e_all0.elapsed_time(e_all1) if e_all0 is not None else 1e3 * wall
+        # the solves' own device time (the flushes between them excluded)
+        total_ms = sum(lat) if e_all0 is not None else 1e3 * wall
         launches = ctx.kernel_launches - launches0
         results[arm] = dict(mode=mode, total_ms=total_ms, lat=lat, iters=iters, conv=convs, launches=launches,
-                            clocks=clk.summary(), true_rel=s.ls.true_residual(), x=s.solution())
+                            clocks=clk.summary(), true_rel=s.ls.true_residual(), x=s.solution(), sweeps=sweeps)
 
     # per-kernel timing (CUDA events on the library's stream) + algorithmic bytes
     # of the PCG iteration's kernels (for --solver bicgstab: the sweeps and the
@@ -375,7 +387,8 @@ def load_peaks():
 
 
 def ncu_traffic(kernel: str, algorithmic_bytes: float | None = None):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary
+    """Per-launch DRAM bytes of `kernel` (a name, then ':' and the sweep
+    schedule for sweeps) from the committed ncu summary
     (profiles/ncu_traffic.txt), scaled to `algorithmic_bytes` when the
     captured launch's algorithmic bytes are recorded; None without an entry."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
@@ -400,14 +413,24 @@ def compose_line(args, world, p, results, prof, e2e, head):
     steps = args.steps
     hbm_peak, peak_kind = load_peaks()
 
+    sched = (results and next(iter(results.values())).get("sweeps")) or {}
+
+    def traffic_key(name):
+        # sweeps are keyed by their schedule: the kernels differ
+        if name == "sweep_fwd":
+            return f"sweep_fwd:{sched.get('forward', '')}"
+        if name == "sweep_bwd":
+            return f"sweep_bwd:{sched.get('backward', '')}"
+        return name
+
     def roof(ms, by, name):
         b = by.get(name)
         if b is None:
             return None
         achieved = b / (ms[name] * 1e-3) / 1e9
         return dict(bound="hbm", achieved=round(achieved, 1), peak=hbm_peak, unit="GB/s",
-                    frac=round(achieved / hbm_peak, 4), traffic=ncu_traffic(name, b), peak_source=peak_kind,
-                    kernel=name, ms_per_launch=round(ms[name], 4), algorithmic_bytes=int(b))
+                    frac=round(achieved / hbm_peak, 4), traffic=ncu_traffic(traffic_key(name), b),
+                    peak_source=peak_kind, kernel=name, ms_per_launch=round(ms[name], 4), algorithmic_bytes=int(b))
 
     def arm_summary(arm):
         r = results[arm]
@@ -418,6 +441,7 @@ def compose_line(args, world, p, results, prof, e2e, head):
                                               / (r["total_ms"] / 1e3), 1),
                 "iterations": r["iters"][-1], "true_rel_residual": r["true_rel"],
                 "kernels_ms": {k: round(v, 4) for k, v in ms.items()},
+                "kernels_bytes": {k: int(v) for k, v in by.items()},
                 "spmv_roofline": roof(ms, by, "spmv"), "gpu_launches": int(r["launches"])}
 
     arms = {arm: arm_summary(arm) for arm in results}
@@ -448,7 +472,8 @@ def compose_line(args, world, p, results, prof, e2e, head):
                    "stop": ("true relative residual <= tol (all arms)" if args.solver == "pcg" else
                             "recursive relative residual <= tol (the reference's test); true one reported"),
                    "parallelism": f"replicas x{world} (independent solves per GPU)",
-                   "l2": "working set (matrix 112 MB + factor records + vectors) larger than the 129 MB L2; no flush"},
+                   "l2": "L2 flushed (256 MB write, untimed) before every timed solve; value from the "
+                         "solves' CUDA-event times"},
         "p50_ms": arms[head]["p50_ms"],
         "p99_ms": arms[head]["p99_ms"],
         "iterations": arms[head]["iterations"],
@@ -713,7 +738,11 @@ def compose_serve_line(args, world, cfg, items, timed_items, timed_probs, result
         v = swept[dom]
         achieved = v["bytes"] / (v["ms"] * 1e-3) / 1e9
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
-                "frac": round(achieved / hbm_peak, 4), "traffic": ncu_traffic(dom, v["bytes"]), "peak_source": peak_kind,
+                "frac": round(achieved / hbm_peak, 4),
+                # FP32 sweeps of the 2D classes run one CTA per solve, FP64 ones ranged
+                "traffic": ncu_traffic(dom + (":one CTA" if results[head]["mode"] != "fp64" else ":ranged")
+                                       if dom.startswith("sweep") else dom, v["bytes"]),
+                "peak_source": peak_kind,
                 "kernel": dom, "ms_per_launch": round(v["ms"], 4), "algorithmic_bytes": int(v["bytes"]),
                 "launches_timed": int(v["n"])}
     value = arms[head]["value"]
@@ -924,8 +953,9 @@ def main():
                          "2 level-scheduled, 3 one CTA")
     ap.add_argument("--max-inflight", type=int, default=256, help="serving: solves resident at once (<= 256)")
     ap.add_argument("--size-groups", type=int, default=0, help="serving: 1 table, 2-3 size groups, 0 = server default (3)")
-    ap.add_argument("--ref-sample-every", type=int, default=1,
-                    help="--impl reference, serving configs: solve every n-th timed request (1 = all of them)")
+    ap.add_argument("--ref-sample-every", type=int, default=4,
+                    help="--impl reference, serving configs: solve every n-th timed request (1 = all of them; "
+                         "4, the default, keeps the run near a minute and a half on 16 cores)")
     ap.add_argument("--arms", default=",".join(sorted({a for a, _ in ARMS + SERVE_ARMS})),
                     help="comma-separated GPU arms to run (profiling runs pick one)")
     args = ap.parse_args()
