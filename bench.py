@@ -388,7 +388,7 @@ def load_peaks():
 
 def ncu_traffic(kernel: str, algorithmic_bytes: float | None = None):
     """Per-launch DRAM bytes of `kernel` (a name, then ':' and the sweep
-    schedule for sweeps) from the committed ncu summary
+    schedule for sweeps, spaces as '_') from the committed ncu summary
     (profiles/ncu_traffic.txt), scaled to `algorithmic_bytes` when the
     captured launch's algorithmic bytes are recorded; None without an entry."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
@@ -418,9 +418,9 @@ def compose_line(args, world, p, results, prof, e2e, head):
     def traffic_key(name):
         # sweeps are keyed by their schedule: the kernels differ
         if name == "sweep_fwd":
-            return f"sweep_fwd:{sched.get('forward', '')}"
+            return f"sweep_fwd:{sched.get('forward', '')}".replace(" ", "_")
         if name == "sweep_bwd":
-            return f"sweep_bwd:{sched.get('backward', '')}"
+            return f"sweep_bwd:{sched.get('backward', '')}".replace(" ", "_")
         return name
 
     def roof(ms, by, name):
@@ -740,7 +740,7 @@ def compose_serve_line(args, world, cfg, items, timed_items, timed_probs, result
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
                 "frac": round(achieved / hbm_peak, 4),
                 # FP32 sweeps of the 2D classes run one CTA per solve, FP64 ones ranged
-                "traffic": ncu_traffic(dom + (":one CTA" if results[head]["mode"] != "fp64" else ":ranged")
+                "traffic": ncu_traffic(dom + (":one_CTA" if results[head]["mode"] != "fp64" else ":ranged")
                                        if dom.startswith("sweep") else dom, v["bytes"]),
                 "peak_source": peak_kind,
                 "kernel": dom, "ms_per_launch": round(v["ms"], 4), "algorithmic_bytes": int(v["bytes"]),
