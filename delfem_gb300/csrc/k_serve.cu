@@ -9,8 +9,10 @@
 // A slot whose state says `done` is skipped.
 //
 // Per-slot reductions are deterministic and independent of the mix: each
-// chunk publishes one partial (fixed block tree), and the last chunk of the
-// slot to arrive sums the slot's partials in chunk order.
+// chunk publishes one partial (fixed block tree), and the slot's partials are
+// summed in chunk order -- for the three reductions of every PCG iteration by
+// a finishing launch (one block per slot), so that no fence or atomic stands
+// between a block's chunks; for the rest by the slot's last arriving block.
 //
 // The iteration follows LsSol::Solve_PCG (src/ls/solver_ls_iter.cpp:100-172)
 // with the first iteration folded into the common body (beta = 0, p = z).
@@ -93,6 +95,28 @@ __device__ bool slot_sum(double v, int c, const SrvSlot& S, double* partials, do
   return true;
 }
 
+// Publishes this chunk's partial (a fixed block tree) for the slot's total,
+// which a separate launch takes (slot_total): no fence or atomic stands
+// between a block's chunks.
+__device__ __forceinline__ void publish(double v, int c, double* partials) {
+  const double bs = block_sum(v);
+  if (threadIdx.x == 0) partials[c] = bs;
+}
+
+// The slot's partials summed in chunk order, as the slot's last arriving
+// block sums them in slot_sum: one block per slot.
+__device__ __forceinline__ double slot_total(const SrvSlot& S, const double* partials) {
+  double t = 0.0;
+  for (int i = threadIdx.x; i < S.nchunks; i += kSrvTpb) t += partials[S.chunk0 + i];
+  return block_sum(t);
+}
+
+// the slots a finishing launch works on: block s takes slot s while its
+// solve runs (its state is read once, by every thread)
+__device__ __forceinline__ bool live_slot(const SrvTable* T, int s) {
+  return s < T->nslots && ld_relaxed_int(&T->slot[s].st->done) == 0;
+}
+
 template <typename Z>
 __device__ __forceinline__ double zval(const void* z, long long k) {
   return (double)reinterpret_cast<const Z*>(z)[k];
@@ -172,12 +196,18 @@ __global__ void __launch_bounds__(kSrvTpb, kSrvVecBlocks) k_srv_rz_beta(const Sr
     double part = 0.0;
     #pragma unroll 4
     for (long long k = e0 + threadIdx.x; k < e1; k += kSrvTpb) part += S.r[k] * zval<Z>(S.z, k);
-    double tot;
-    if (slot_sum(part, c, S, partials, &tot) && threadIdx.x == 0) {
-      PcgState* st = S.st;
-      st->beta = (st->it == 0) ? 0.0 : tot / st->rz;
-      st->rz = tot;
-    }
+    publish(part, c, partials);
+  }
+}
+
+__global__ void __launch_bounds__(kSrvTpb) k_srv_fin_rz_beta(const SrvTable* T, const double* partials) {
+  if (!live_slot(T, blockIdx.x)) return;
+  const SrvSlot& S = T->slot[blockIdx.x];
+  const double tot = slot_total(S, partials);
+  if (threadIdx.x == 0) {
+    PcgState* st = S.st;
+    st->beta = (st->it == 0) ? 0.0 : tot / st->rz;
+    st->rz = tot;
   }
 }
 
@@ -208,11 +238,17 @@ __global__ void __launch_bounds__(kSrvTpb) k_srv_spmv_pap(const SrvTable* T, dou
     chunk_rows(S, c, row0, row1);
     const double part = S.b == 1 ? chunk_q_pap<1>(S, row0, row1)
                         : S.b == 2 ? chunk_q_pap<2>(S, row0, row1) : chunk_q_pap<3>(S, row0, row1);
-    double tot;
-    if (slot_sum(part, c, S, partials, &tot) && threadIdx.x == 0) {
-      S.st->pap = tot;
-      S.st->alpha = S.st->rz / tot;
-    }
+    publish(part, c, partials);
+  }
+}
+
+__global__ void __launch_bounds__(kSrvTpb) k_srv_fin_pap(const SrvTable* T, const double* partials) {
+  if (!live_slot(T, blockIdx.x)) return;
+  const SrvSlot& S = T->slot[blockIdx.x];
+  const double tot = slot_total(S, partials);
+  if (threadIdx.x == 0) {
+    S.st->pap = tot;
+    S.st->alpha = S.st->rz / tot;
   }
 }
 
@@ -243,26 +279,32 @@ __global__ void __launch_bounds__(kSrvTpb, kSrvVecBlocks) k_srv_update_rx(const 
       }
       put_sweep_input<Z>(S, k, r);
     }
-    double tot;
-    if (slot_sum(part, c, S, partials, &tot) && threadIdx.x == 0) {
-      PcgState* st = S.st;
-      st->rr = tot;
-      const double ratio = tot * st->inv_rr0;
-      if (ratio < st->tol2) {
-        st->done = 1;
-        st->conv = sqrt(ratio);
-        st->iter_out = st->it;
-      } else if (st->it + 1 >= st->maxit) {
-        st->done = 2;
-        st->conv = sqrt(ratio);
-        st->iter_out = st->maxit;
-      } else if (!(ratio == ratio)) {
-        st->done = 3;
-        st->conv = ratio;
-        st->iter_out = st->it;
-      }
-      st->it += 1;
+    publish(part, c, partials);
+  }
+}
+
+__global__ void __launch_bounds__(kSrvTpb) k_srv_fin_rx(const SrvTable* T, const double* partials) {
+  if (!live_slot(T, blockIdx.x)) return;
+  const SrvSlot& S = T->slot[blockIdx.x];
+  const double tot = slot_total(S, partials);
+  if (threadIdx.x == 0) {
+    PcgState* st = S.st;
+    st->rr = tot;
+    const double ratio = tot * st->inv_rr0;
+    if (ratio < st->tol2) {
+      st->done = 1;
+      st->conv = sqrt(ratio);
+      st->iter_out = st->it;
+    } else if (st->it + 1 >= st->maxit) {
+      st->done = 2;
+      st->conv = sqrt(ratio);
+      st->iter_out = st->maxit;
+    } else if (!(ratio == ratio)) {
+      st->done = 3;
+      st->conv = ratio;
+      st->iter_out = st->it;
     }
+    st->it += 1;
   }
 }
 
@@ -596,6 +638,7 @@ cudaError_t srv_rz_beta(const SrvTable* T, double* partials, int* tickets, int n
                         cudaStream_t s) {
   if (fp32z) k_srv_rz_beta<float><<<grid, kSrvTpb, 0, s>>>(T, partials, tickets, ntickets);
   else k_srv_rz_beta<double><<<grid, kSrvTpb, 0, s>>>(T, partials, tickets, ntickets);
+  k_srv_fin_rz_beta<<<kSrvMaxSlots, kSrvTpb, 0, s>>>(T, partials);
   return cudaGetLastError();
 }
 cudaError_t srv_update_p(const SrvTable* T, bool fp32z, int grid, cudaStream_t s) {
@@ -605,11 +648,13 @@ cudaError_t srv_update_p(const SrvTable* T, bool fp32z, int grid, cudaStream_t s
 }
 cudaError_t srv_spmv_pap(const SrvTable* T, double* partials, int grid, cudaStream_t s) {
   k_srv_spmv_pap<<<grid, kSrvTpb, 0, s>>>(T, partials);
+  k_srv_fin_pap<<<kSrvMaxSlots, kSrvTpb, 0, s>>>(T, partials);
   return cudaGetLastError();
 }
 cudaError_t srv_update_rx(const SrvTable* T, double* partials, bool fp32z, int grid, cudaStream_t s) {
   if (fp32z) k_srv_update_rx<float><<<grid, kSrvTpb, 0, s>>>(T, partials);
   else k_srv_update_rx<double><<<grid, kSrvTpb, 0, s>>>(T, partials);
+  k_srv_fin_rx<<<kSrvMaxSlots, kSrvTpb, 0, s>>>(T, partials);
   return cudaGetLastError();
 }
 cudaError_t srv_check_true(const SrvTable* T, double* partials, int grid, cudaStream_t s) {

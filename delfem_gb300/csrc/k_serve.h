@@ -65,7 +65,9 @@ struct SrvStatus {
 };
 
 // fp32z: sweep outputs y, z are float (FP32 factor); tickets: the batched
-// sweep launches' counters, reset once the sweeps of an iteration are over
+// sweep launches' counters, reset once the sweeps of an iteration are over.
+// srv_rz_beta, srv_spmv_pap and srv_update_rx are two launches each: the
+// batched kernel, then one block per slot for the slot's reduction.
 cudaError_t srv_rz_beta(const SrvTable* T, double* partials, int* tickets, int ntickets, bool fp32z, int grid,
                         cudaStream_t s);
 cudaError_t srv_update_p(const SrvTable* T, bool fp32z, int grid, cudaStream_t s);

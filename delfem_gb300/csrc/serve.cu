@@ -1065,7 +1065,9 @@ void account_profile(dfg_server_s* S, Group& G) {
 int kernels_per_replay(dfg_server_s* S, const Group& G) {
   int nc = 0;
   for (int k = 0; k < 2 * kClasses; ++k) nc += (G.graph_mask >> k) & 1;
-  return S->chunk * (2 * nc + 4) + 3;
+  // per iteration: the sweeps, four batched kernels, and (outside the mixed
+  // form) the three finishing launches of their per-slot reductions
+  return S->chunk * (2 * nc + 4 + (S->mixed ? 0 : 3)) + 3;
 }
 
 // Reads a finished replay's status array: finished solves leave the table
