@@ -44,19 +44,6 @@
 
 namespace dfg {
 
-// whether some level starts at chunk v (lev_chunks: nlevels + 1 ascending
-// first chunks, the last entry the chunk count)
-__device__ __forceinline__ bool level_starts_at(const int* lev_chunks, int nlevels, int v) {
-  int lo = 1, hi = nlevels;
-  while (lo <= hi) {
-    const int mid = (lo + hi) >> 1;
-    const int x = __ldg(&lev_chunks[mid]);
-    if (x == v) return true;
-    if (x < v) lo = mid + 1; else hi = mid - 1;
-  }
-  return false;
-}
-
 template <typename T, int B, bool FWD, int MAXE>
 __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
   constexpr int BS = B * B;
@@ -160,118 +147,136 @@ __global__ void __launch_bounds__((kSoloWarps + 1) * 32) k_solo(SoloArgs a) {
       T* out = reinterpret_cast<T*>(S.out);
       int st = st0, ph = ph0;
       for (int c = 0; c < nch; ++c, (++st == NS ? (st = 0, ph ^= 1) : 0)) {
-        if (!abort && !mbar_wait(&full[st], (unsigned)ph, a.err, kSiteFull, jslot, c)) abort = true;
+        // (the wait is voted across the warp, so that abort stays warp-uniform)
+        if (!abort) abort = !__all_sync(0xffffffffu, mbar_wait(&full[st], (unsigned)ph, a.err, kSiteFull, jslot, c));
         const unsigned char* stage = rstage + (size_t)st * a.rec_stage;
         const int4 hdr = *reinterpret_cast<const int4*>(stage);
         const int nent = hdr.x;
         const int nst = abort ? 0 : (hdr.y & 0xffff);
         const int rec_sz = 144 + nent * 128 + nent * 32 * BS * SZ + (FWD ? 32 * BS * SZ : 0);
-        // steps go to warps by their place in the level (hdr.w: the chunk's
-        // offset there), so a level of <= kSoloWarps steps costs each warp
-        // one step whatever its chunks
-        for (int k = (warp - hdr.w % NW + NW) % NW; k < nst; k += NW) {
-          const unsigned char* rec = stage + (size_t)k * rec_sz;
-          const int s = reinterpret_cast<const int*>(rec)[2];
-          const int o = reinterpret_cast<const int*>(rec + 16)[lane];
-          const int* code = reinterpret_cast<const int*>(rec + 144);
-          const T* blk = reinterpret_cast<const T*>(rec + 144 + nent * 128);
-          if (o >= 0) {
-            const T* val = reinterpret_cast<const T*>(vstage + (size_t)st * VS + (size_t)k * STEP_RHS);
-            T t[B];
+        // a chunk may hold the ends of several narrow levels: lane j reads
+        // step j's header (does it close its level, its place in the level)
+        int yv = 0, wv = 0;
+        if (lane < nst) {
+          const int4 hj = *reinterpret_cast<const int4*>(stage + (size_t)lane * rec_sz);
+          yv = hj.y;
+          wv = hj.w;
+        }
+        const unsigned closes = __ballot_sync(0xffffffffu, lane < nst && (yv >> 16) != 0);
+        // segments of one level each; a segment's steps go to warps by their
+        // place in the level, so a level of <= kSoloWarps steps costs each
+        // warp one step whatever its chunks
+        for (int j0 = 0; j0 < nst;) {
+          const unsigned rest = closes >> j0;
+          const int j1 = rest ? j0 + __ffs(rest) : nst;
+          const int p0 = __shfl_sync(0xffffffffu, wv, j0);
+          for (int k = j0 + (warp - p0 % NW + NW) % NW; k < j1; k += NW) {
+            const unsigned char* rec = stage + (size_t)k * rec_sz;
+            const int s = reinterpret_cast<const int*>(rec)[2];
+            const int o = reinterpret_cast<const int*>(rec + 16)[lane];
+            const int* code = reinterpret_cast<const int*>(rec + 144);
+            const T* blk = reinterpret_cast<const T*>(rec + 144 + nent * 128);
+            if (o >= 0) {
+              const T* val = reinterpret_cast<const T*>(vstage + (size_t)st * VS + (size_t)k * STEP_RHS);
+              T t[B];
 #pragma unroll
-            for (int d = 0; d < B; ++d) t[d] = val[lane * B + d];
-            if constexpr (MAXE > 0) {
-              // all dependency values first, then the FMAs.  The codes are
-              // loaded together, then every value from the ring together
-              // (a global reference reads the ring's zero bytes first), so
-              // the step waits on two shared-memory round trips, not two per
-              // entry; global references are read after, in a warp-uniform
-              // branch that is taken only where the ring does not reach
-              int cdv[MAXE];
+              for (int d = 0; d < B; ++d) t[d] = val[lane * B + d];
+              if constexpr (MAXE > 0) {
+                // all dependency values first, then the FMAs.  The codes are
+                // loaded together, then every value from the ring together
+                // (a global reference reads the ring's zero bytes first), so
+                // the step waits on two shared-memory round trips, not two per
+                // entry; global references are read after, in a warp-uniform
+                // branch that is taken only where the ring does not reach
+                int cdv[MAXE];
 #pragma unroll
-              for (int e = 0; e < MAXE; ++e) cdv[e] = e < nent ? code[e * 32 + lane] : 0;
-              T v[MAXE][B];
-              bool glob = false;
-#pragma unroll
-              for (int e = 0; e < MAXE; ++e) {
-                const T* vp = reinterpret_cast<const T*>(ringreg + (cdv[e] >= 0 ? cdv[e] : 0));
-#pragma unroll
-                for (int d = 0; d < B; ++d) v[e][d] = vp[d];
-                glob |= cdv[e] < 0;
-              }
-              if (__any_sync(__activemask(), glob)) {
+                for (int e = 0; e < MAXE; ++e) cdv[e] = e < nent ? code[e * 32 + lane] : 0;
+                T v[MAXE][B];
+                bool glob = false;
 #pragma unroll
                 for (int e = 0; e < MAXE; ++e) {
-                  if (cdv[e] < 0) {
-                    const T* gp = out + (size_t)(-cdv[e] - 1) * B;
+                  const T* vp = reinterpret_cast<const T*>(ringreg + (cdv[e] >= 0 ? cdv[e] : 0));
 #pragma unroll
-                    for (int d = 0; d < B; ++d) v[e][d] = __ldcg(gp + d);
+                  for (int d = 0; d < B; ++d) v[e][d] = vp[d];
+                  glob |= cdv[e] < 0;
+                }
+                if (__any_sync(__activemask(), glob)) {
+#pragma unroll
+                  for (int e = 0; e < MAXE; ++e) {
+                    if (cdv[e] < 0) {
+                      const T* gp = out + (size_t)(-cdv[e] - 1) * B;
+#pragma unroll
+                      for (int d = 0; d < B; ++d) v[e][d] = __ldcg(gp + d);
+                    }
                   }
                 }
-              }
 #pragma unroll
-              for (int e = 0; e < MAXE; ++e) {
-                if (e < nent) {
+                for (int e = 0; e < MAXE; ++e) {
+                  if (e < nent) {
+#pragma unroll
+                    for (int p = 0; p < B; ++p) {
+                      T acc = t[p];
+#pragma unroll
+                      for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[e][q];
+                      t[p] = acc;
+                    }
+                  }
+                }
+              } else {
+                for (int e = 0; e < nent; ++e) {
+                  const int cd = code[e * 32 + lane];
+                  T v[B];
+                  if (cd >= 0) {
+                    const T* vp = reinterpret_cast<const T*>(ringreg + cd);
+#pragma unroll
+                    for (int d = 0; d < B; ++d) v[d] = vp[d];
+                  } else {
+                    const T* gp = out + (size_t)(-cd - 1) * B;
+#pragma unroll
+                    for (int d = 0; d < B; ++d) v[d] = __ldcg(gp + d);
+                  }
 #pragma unroll
                   for (int p = 0; p < B; ++p) {
                     T acc = t[p];
 #pragma unroll
-                    for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[e][q];
+                    for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[q];
                     t[p] = acc;
                   }
                 }
               }
-            } else {
-              for (int e = 0; e < nent; ++e) {
-                const int cd = code[e * 32 + lane];
-                T v[B];
-                if (cd >= 0) {
-                  const T* vp = reinterpret_cast<const T*>(ringreg + cd);
-#pragma unroll
-                  for (int d = 0; d < B; ++d) v[d] = vp[d];
-                } else {
-                  const T* gp = out + (size_t)(-cd - 1) * B;
-#pragma unroll
-                  for (int d = 0; d < B; ++d) v[d] = __ldcg(gp + d);
-                }
+              T y[B];
+              if constexpr (FWD) {
+                const T* dinv = blk + nent * BS * 32;
 #pragma unroll
                 for (int p = 0; p < B; ++p) {
-                  T acc = t[p];
+                  T acc = dinv[(p * B) * 32 + lane] * t[0];
 #pragma unroll
-                  for (int q = 0; q < B; ++q) acc -= blk[(e * BS + p * B + q) * 32 + lane] * v[q];
-                  t[p] = acc;
+                  for (int q = 1; q < B; ++q) acc += dinv[(p * B + q) * 32 + lane] * t[q];
+                  y[p] = acc;
                 }
+              } else {
+#pragma unroll
+                for (int p = 0; p < B; ++p) y[p] = t[p];
               }
-            }
-            T y[B];
-            if constexpr (FWD) {
-              const T* dinv = blk + nent * BS * 32;
+              T* rg = reinterpret_cast<T*>(ringreg + 32) + (((s & RM) * 32 + lane) * B);
 #pragma unroll
-              for (int p = 0; p < B; ++p) {
-                T acc = dinv[(p * B) * 32 + lane] * t[0];
-#pragma unroll
-                for (int q = 1; q < B; ++q) acc += dinv[(p * B + q) * 32 + lane] * t[q];
-                y[p] = acc;
+              for (int d = 0; d < B; ++d) {
+                rg[d] = y[d];
+                out[(size_t)o * B + d] = y[d];
               }
-            } else {
-#pragma unroll
-              for (int p = 0; p < B; ++p) y[p] = t[p];
-            }
-            T* rg = reinterpret_cast<T*>(ringreg + 32) + (((s & RM) * 32 + lane) * B);
-#pragma unroll
-            for (int d = 0; d < B; ++d) {
-              rg[d] = y[d];
-              out[(size_t)o * B + d] = y[d];
             }
           }
+          if (rest) named_sync(1, NW * 32);  // the segment closes its level
+          j0 = j1;
+        }
+        // a warp that gave up waiting takes the chunk's level ends from its
+        // table entry, so that every warp passes the same barriers
+        if (abort) {
+          const int nb = __ldg(&S.chunks[c].nclose);
+          for (int i = 0; i < nb; ++i) named_sync(1, NW * 32);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[st]);
-        // the chunk's header says whether it closes its level (no global
-        // load on the way from one level to the next); a lane that gave up
-        // waiting finds the level bounds in global memory instead
-        const bool lev_end = abort ? level_starts_at(S.lev_chunks, S.nlevels, c + 1) : (hdr.y >> 16) != 0;
-        if (lev_end) named_sync(1, NW * 32);
       }
     }
     g += nch;

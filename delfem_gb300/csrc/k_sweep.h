@@ -88,11 +88,12 @@ struct SoloChunk {
   long long rec_off;  // byte offset of the chunk's first record
   int rec_bytes;      // bytes of the chunk's records
   int first_step, nsteps, nent;
+  int nclose;         // levels that end inside the chunk
 };
 struct SoloSlot {
   const unsigned char* rec;
   const SoloChunk* chunks;
-  const int* lev_chunks;  // nlevels + 1: first chunk of each level
+  const int* lev_chunks;  // nlevels + 1: the chunk holding each level's first step
   int nlevels, nchunks;
   const void* in;         // right-hand sides in step order (nsteps*32*B of T)
   void* out;              // results at the records' output positions

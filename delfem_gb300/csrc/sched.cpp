@@ -417,16 +417,17 @@ SoloPlan solo_sweep_plan(int n, int b, const int* rowptr, const int* colind, con
     deps_of(row, forward, rowptr, diaind, c0, c1);
     own[row_step[row]] = std::max(own[row_step[row]], c1 - c0);
   }
-  // chunks: consecutive steps of one level, at most ch_max of them and
-  // stage_bytes of records (a chunk holds at least one step)
+  // chunks: consecutive steps, across level ends, at most ch_max of them and
+  // stage_bytes of records (a chunk holds at least one step); a narrow level
+  // shares its chunk with the next ones, so the copies and the handshake of
+  // one chunk serve several levels
   S.lev_chunks.assign(P.nranges + 1, 0);
   P.step_nent.assign(P.nsteps, 0);
-  for (int l = 0; l < nl; ++l) {
-    S.lev_chunks[l] = (int)S.chunks.size();
-    int s = P.range_steps[l];
-    while (s < P.range_steps[l + 1]) {
-      SoloChunk c{0, 0, s, 0, 0};
-      while (s < P.range_steps[l + 1] && c.nsteps < ch_max) {
+  {
+    int s = 0, l = 0;
+    while (s < P.nsteps) {
+      SoloChunk c{0, 0, s, 0, 0, 0};
+      while (s < P.nsteps && c.nsteps < ch_max) {
         const int ne = std::max(c.nent, own[s]);
         if (c.nsteps > 0 && (c.nsteps + 1) * solo_rec_bytes(ne, bs, elem, forward) > stage_bytes) break;
         c.nent = ne;
@@ -434,6 +435,12 @@ SoloPlan solo_sweep_plan(int n, int b, const int* rowptr, const int* colind, con
         ++s;
       }
       for (int t = c.first_step; t < c.first_step + c.nsteps; ++t) P.step_nent[t] = c.nent;
+      // levels ending inside the chunk; the next level's first step is in
+      // this chunk unless the chunk ends with the level
+      for (; l < nl && P.range_steps[l + 1] <= s; ++l) {
+        ++c.nclose;
+        S.lev_chunks[l + 1] = (int)S.chunks.size() + (P.range_steps[l + 1] < s ? 0 : 1);
+      }
       S.chunks.push_back(c);
     }
   }
@@ -485,9 +492,10 @@ std::vector<unsigned char> pack_solo_headers(const SoloPlan& S, int elem, const 
   for (const SoloChunk& c : S.chunks)
     for (int s = c.first_step; s < c.first_step + c.nsteps; ++s) {
       unsigned char* r = h.data() + off[s];
-      // steps in the chunk, plus 1 << 16 when the chunk closes its level
-      const int closes = c.first_step + c.nsteps == level_end[c.first_step] ? 1 << 16 : 0;
-      const int hdr[4] = {P.step_nent[s], c.nsteps | closes, s, c.first_step - level_first[c.first_step]};
+      // steps in the chunk, plus 1 << 16 when this step closes its level; the
+      // step's place in its level
+      const int closes = s + 1 == level_end[s] ? 1 << 16 : 0;
+      const int hdr[4] = {P.step_nent[s], c.nsteps | closes, s, s - level_first[s]};
       std::memcpy(r, hdr, 16);
       int* outv = reinterpret_cast<int*>(r + 16);
       int* code = reinterpret_cast<int*>(r + 144);

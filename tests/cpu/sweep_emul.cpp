@@ -366,20 +366,31 @@ extern "C" int emul_solo_precond(int n, int b, const int* rowptr, const int* col
         }
     for (int i = 0; i < n; ++i)
       if (seen[i] != 1) { info[3] = 1; return 1; }
-    // chunks: tile each level in order, bounded, one size per chunk
+    // chunks: tile the steps in order (across level ends), bounded, one size
+    // per chunk, with the count of levels ending inside; lev_chunks names the
+    // chunk holding each level's first step
     if ((int)S.lev_chunks.size() != P.nranges + 1) { info[3] = 8; return 8; }
-    for (int l = 0; l < P.nranges; ++l) {
-      int next = P.range_steps[l];
-      for (int c = S.lev_chunks[l]; c < S.lev_chunks[l + 1]; ++c) {
+    std::vector<int> chunk_of(P.nsteps, -1);
+    {
+      int next = 0;
+      for (size_t c = 0; c < S.chunks.size(); ++c) {
         const SoloChunk& ch = S.chunks[c];
         if (ch.first_step != next || ch.nsteps < 1 || ch.nsteps > ch_max || ch.rec_off != off[ch.first_step] ||
             ch.rec_bytes != off[ch.first_step + ch.nsteps] - off[ch.first_step] ||
             (ch.nsteps > 1 && ch.rec_bytes > stage_bytes)) { info[3] = 9; return 9; }
-        for (int s = ch.first_step; s < ch.first_step + ch.nsteps; ++s)
+        int ends = 0;
+        for (int s = ch.first_step; s < ch.first_step + ch.nsteps; ++s) {
           if (P.step_nent[s] != ch.nent) { info[3] = 10; return 10; }
+          chunk_of[s] = (int)c;
+        }
+        for (int l = 0; l < P.nranges; ++l)
+          if (P.range_steps[l + 1] > ch.first_step && P.range_steps[l + 1] <= ch.first_step + ch.nsteps) ++ends;
+        if (ends != ch.nclose) { info[3] = 11; return 11; }
         next += ch.nsteps;
       }
-      if (next != P.range_steps[l + 1]) { info[3] = 11; return 11; }
+      if (next != P.nsteps) { info[3] = 11; return 11; }
+      for (int l = 0; l < P.nranges; ++l)
+        if (P.range_steps[l] < P.nsteps && S.lev_chunks[l] != chunk_of[P.range_steps[l]]) { info[3] = 8; return 8; }
     }
     std::vector<int> ring_row((size_t)R * 32, -1);
     std::vector<double> ring((size_t)R * 32 * b, NAN);
@@ -395,12 +406,11 @@ extern "C" int emul_solo_precond(int n, int b, const int* rowptr, const int* col
         std::memcpy(hdr, rec, 16);
         const int nent = hdr[0];
         if (nent != P.step_nent[s] || hdr[2] != s) { info[3] = 2; return 2; }
-        {  // the chunk's offset in its level, as the kernel distributes steps
-          const SoloChunk* ch = nullptr;
-          for (int c = S.lev_chunks[l]; c < S.lev_chunks[l + 1]; ++c)
-            if (S.chunks[c].first_step <= s && s < S.chunks[c].first_step + S.chunks[c].nsteps) ch = &S.chunks[c];
-          const int closes = ch && ch->first_step + ch->nsteps == P.range_steps[l + 1] ? 1 << 16 : 0;
-          if (!ch || hdr[1] != (ch->nsteps | closes) || hdr[3] != ch->first_step - P.range_steps[l]) {
+        {  // the step's chunk size, whether it closes its level, its place in
+           // the level (the kernel distributes a level's steps by it)
+          const SoloChunk& ch = S.chunks[chunk_of[s]];
+          const int closes = s + 1 == P.range_steps[l + 1] ? 1 << 16 : 0;
+          if (hdr[1] != (ch.nsteps | closes) || hdr[3] != s - P.range_steps[l]) {
             info[3] = 12;
             return 12;
           }
