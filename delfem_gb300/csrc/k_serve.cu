@@ -29,9 +29,10 @@ namespace dfg {
 
 namespace {
 
-// element-wise kernels (four-way unrolled loops) are held to the registers of
-// six blocks per SM, so that the launches' four blocks per SM are resident in
-// one wave (unbounded, the r/x update took 70 registers: three blocks per SM)
+// the batched kernels of every iteration are held to the registers of six
+// blocks per SM and launched six blocks per SM, all resident in one wave:
+// more rows in flight per SM (the SpMV and vector kernels are latency-bound
+// at four blocks; 78.4 against 74.7 solves/s on the saturated 2D stream)
 constexpr int kSrvVecBlocks = 6;
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -229,7 +230,7 @@ __global__ void __launch_bounds__(kSrvTpb, kSrvVecBlocks) k_srv_update_p(const S
 }
 
 // q = A p; pAp; alpha = rz / pAp
-__global__ void __launch_bounds__(kSrvTpb) k_srv_spmv_pap(const SrvTable* T, double* partials) {
+__global__ void __launch_bounds__(kSrvTpb, kSrvVecBlocks) k_srv_spmv_pap(const SrvTable* T, double* partials) {
   ChunkWalk w(T);
   for (int c, si; w.next(c, si);) {
     const SrvSlot S = T->slot[si];

@@ -960,6 +960,8 @@ cudaGraphExec_t capture_graph(dfg_server_s* S, Group& G, int mask, bool prof) {
   SCK(cudaStreamBeginCapture(G.s_iter, cudaStreamCaptureModeThreadLocal));
   EndOnThrow guard{G.s_iter};
   const int grid = S->vec_grid;
+  // kernels above the six-block register bound run four blocks per SM
+  const int grid4 = S->nsm * 4;
   for (int it = 0; it < S->chunk; ++it) {
     const bool pf = prof && it == 0;
     auto mk = [&](int k, int edge, cudaStream_t st) {
@@ -992,7 +994,7 @@ cudaGraphExec_t capture_graph(dfg_server_s* S, Group& G, int mask, bool prof) {
     else SCK(srv_update_p(G.d_tab, S->fp32, grid, G.s_iter));
     mk(1, 1, G.s_iter);
     mk(2, 0, G.s_iter);
-    if (S->mixed) SCK(srvm_spmv_pap(G.d_tab, G.d_partials, grid, G.s_iter));
+    if (S->mixed) SCK(srvm_spmv_pap(G.d_tab, G.d_partials, grid4, G.s_iter));
     else SCK(srv_spmv_pap(G.d_tab, G.d_partials, grid, G.s_iter));
     mk(2, 1, G.s_iter);
     mk(3, 0, G.s_iter);
@@ -1006,11 +1008,11 @@ cudaGraphExec_t capture_graph(dfg_server_s* S, Group& G, int mask, bool prof) {
     SCK(srvm_fold(G.d_tab, grid, G.s_iter));
     mark(5, 1, G.s_iter);
     mark(4, 0, G.s_iter);
-    SCK(srvm_refine(G.d_tab, G.d_partials, grid, G.s_iter));
+    SCK(srvm_refine(G.d_tab, G.d_partials, grid4, G.s_iter));
     mark(4, 1, G.s_iter);
   } else {
     mark(4, 0, G.s_iter);
-    SCK(srv_check_true(G.d_tab, G.d_partials, grid, G.s_iter));
+    SCK(srv_check_true(G.d_tab, G.d_partials, grid4, G.s_iter));
     mark(4, 1, G.s_iter);
     mark(5, 0, G.s_iter);
     SCK(srv_replace(G.d_tab, G.d_partials, S->fp32, grid, G.s_iter));
@@ -1301,7 +1303,7 @@ extern "C" int dfg_server_create(dfg_ctx ctx, const dfg_server_config* cfg, dfg_
   S->chunk = cfg->chunk_iters > 0 ? cfg->chunk_iters : 8;
   const int hw = (int)std::thread::hardware_concurrency();
   S->nthreads = cfg->host_threads > 0 ? cfg->host_threads : std::max(1, hw - 2);
-  S->vec_grid = S->nsm * 4;
+  S->vec_grid = S->nsm * 6;  // blocks of the batched kernels (k_serve.cu kSrvVecBlocks)
   S->profile_every = std::max(0, cfg->profile_every);
   S->ngroups = cfg->size_groups > 0 ? cfg->size_groups : kGroups;
   S->sweeps = cfg->sweeps;
