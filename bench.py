@@ -593,7 +593,8 @@ def run_serve(args, rank, world, local):
     x_plain = {}
     for arm, mode in arms_run:
         with Server(ctx, mode=mode, budget_bytes=int(args.serve_budget) or cfg["budget"], profile_every=16,
-                    max_inflight=args.max_inflight, size_groups=args.size_groups) as S:
+                    max_inflight=args.max_inflight, size_groups=args.size_groups,
+                    chunk_iters=args.chunk_iters) as S:
             wids = serve_segment(S, warm_items, warm_probs, cfg["saturate"])
             for i in wids:
                 S.wait(i)
@@ -765,7 +766,7 @@ def compose_serve_line(args, world, cfg, items, timed_items, timed_probs, result
         "serving": {"head_arm": head, "admission_budget_bytes": int(hr["budget"]),
                     "timing": "host clock around the timed stream, device synchronised at both ends",
                     "parallelism": f"one server per GPU, x{world}", "max_inflight": args.max_inflight,
-                    "size_groups": args.size_groups, "generation_s": round(t_gen, 1),
+                    "chunk_iters": args.chunk_iters, "size_groups": args.size_groups, "generation_s": round(t_gen, 1),
                     "dof_timed": int(sum(p.ndof for p in timed_probs))},
         "p50_ms": arms[head]["p50_ms"],
         "p99_ms": arms[head]["p99_ms"],
@@ -952,6 +953,7 @@ def main():
                     help="single solves: triangular-sweep schedule, 0 = timed choice, 1 ranged, "
                          "2 level-scheduled, 3 one CTA")
     ap.add_argument("--max-inflight", type=int, default=256, help="serving: solves resident at once (<= 256)")
+    ap.add_argument("--chunk-iters", type=int, default=8, help="serving: PCG iterations per graph replay (<= 64)")
     ap.add_argument("--size-groups", type=int, default=0, help="serving: 1 table, 2-3 size groups, 0 = server default (3)")
     ap.add_argument("--ref-sample-every", type=int, default=4,
                     help="--impl reference, serving configs: solve every n-th timed request (1 = all of them; "
