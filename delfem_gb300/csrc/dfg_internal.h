@@ -92,7 +92,7 @@ std::vector<unsigned char> pack_record_headers(const SweepPlan& P, int elem, std
 struct SoloPlan {
   SweepPlan P;                      // steps, padded entries (ent_off / ent_src / ent_slot)
   std::vector<SoloChunk> chunks;
-  std::vector<int> lev_chunks;      // nlevels + 1: first chunk of each level
+  std::vector<int> lev_chunks;      // nlevels + 1: the chunk holding each level's first step
   std::vector<int> pos;             // per row: step * 32 + lane (its slot in step order)
 };
 SoloPlan solo_sweep_plan(int n, int b, const int* rowptr, const int* colind, const int* diaind, bool forward,

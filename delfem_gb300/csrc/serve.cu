@@ -382,7 +382,7 @@ bool symbolic(dfg_server_s* S, Req* r) {
     r->posf = std::move(sf.pos);
     r->pf = std::move(sf.P);
     r->pb = std::move(sb.P);
-    r->pf.range_steps = std::move(sf.lev_chunks);  // per level: first chunk
+    r->pf.range_steps = std::move(sf.lev_chunks);  // per level: the chunk of its first step
     r->pb.range_steps = std::move(sb.lev_chunks);
   } else {
     r->pf = fullest_sweep_plan(n, r->b, r->rowptr.data(), r->colind.data(), r->diaind.data(), true, kRingSteps);
