@@ -135,8 +135,8 @@ cudaError_t launch_solo_permute(bool fp32, long long n, int b, const int* pos, c
 // third of the budget (a power of two of steps, at most 512).  The chunk
 // stages take the rest -- the bytes in flight that hide HBM latency: up to 64
 // of them, each holding up to ch_max steps' records and right-hand sides;
-// ch_max (1..8) is the largest (fewest waits per level) within 10 % of the
-// most steps in flight.  ns == 0 when nothing fits.
+// ch_max (1..16) is the largest (fewest chunk handshakes per level) within
+// 10 % of the most steps in flight.  ns == 0 when nothing fits.
 struct SoloShape {
   int R = 0, ch_max = 0, rec_stage = 0, ns = 0;
   size_t smem = 0;
@@ -152,14 +152,17 @@ inline SoloShape solo_shape(int b, int maxe, int elem, bool forward, size_t budg
   sh.R = R;
   const long long rec1 = solo_record_bytes(maxe, b * b, elem, forward);
   const size_t fixed = solo_smem_bytes(64, 0, 0, R, b, elem);
-  int ns_of[9] = {}, most = 0;
-  for (int ch = 1; ch <= 8; ++ch) {
+  // chunks above 8 steps only with at least 4 stages, so that the producer
+  // still refills stages while others are consumed
+  int ns_of[17] = {}, most = 0;
+  auto usable = [&](int ch) { return ns_of[ch] >= (ch <= 8 ? 2 : 4); };
+  for (int ch = 1; ch <= 16; ++ch) {
     const size_t per_stage = (size_t)ch * rec1 + (size_t)solo_val_stage(ch, b, elem);
     ns_of[ch] = (int)std::min<size_t>(64, (budget - std::min(budget, fixed)) / per_stage);
-    if (ns_of[ch] >= 2) most = ns_of[ch] * ch > most ? ns_of[ch] * ch : most;
+    if (usable(ch)) most = ns_of[ch] * ch > most ? ns_of[ch] * ch : most;
   }
-  for (int ch = 1; ch <= 8; ++ch)
-    if (ns_of[ch] >= 2 && 10 * ns_of[ch] * ch >= 9 * most) { sh.ch_max = ch; sh.ns = ns_of[ch]; }
+  for (int ch = 1; ch <= 16; ++ch)
+    if (usable(ch) && 10 * ns_of[ch] * ch >= 9 * most) { sh.ch_max = ch; sh.ns = ns_of[ch]; }
   if (sh.ns > 0) {
     sh.rec_stage = (int)(sh.ch_max * rec1);
     sh.smem = solo_smem_bytes(sh.ns, sh.rec_stage, solo_val_stage(sh.ch_max, b, elem), R, b, elem);
