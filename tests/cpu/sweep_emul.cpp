@@ -477,3 +477,14 @@ extern "C" int emul_solo_precond(int n, int b, const int* rowptr, const int* col
   }
   return 0;
 }
+
+// The one-CTA sweep's launch shape for a class (solo_shape, k_sweep.h):
+// out = {R, ch_max, rec_stage, ns, smem}.
+extern "C" void emul_solo_shape(int b, int maxe, int elem, int forward, long long budget, long long* out) {
+  const SoloShape s = solo_shape(b, maxe, elem, forward != 0, (size_t)budget);
+  out[0] = s.R;
+  out[1] = s.ch_max;
+  out[2] = s.rec_stage;
+  out[3] = s.ns;
+  out[4] = (long long)s.smem;
+}

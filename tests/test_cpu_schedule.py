@@ -30,6 +30,7 @@ def emul():
     L.emul_sweep.argtypes = [ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P, P]
     L.emul_solo_precond.argtypes = [ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_int, P, P, P, P, P]
+    L.emul_solo_shape.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_longlong, P]
     L.emul_ilu_pattern.restype = ctypes.c_longlong
     L.emul_ilu_pattern.argtypes = [ctypes.c_int, P, P, ctypes.c_int, P, P, ctypes.c_longlong]
     return L
@@ -133,7 +134,7 @@ def _solo(emul, out, R, elem, stage_bytes, ch_max, rhs):
 
 
 @pytest.mark.parametrize("idx", range(4))
-@pytest.mark.parametrize("R,stage,ch", [(16, 4096, 2), (256, 20000, 4), (512, 100000, 8)])
+@pytest.mark.parametrize("R,stage,ch", [(16, 4096, 2), (256, 20000, 4), (512, 100000, 8), (64, 120000, 16)])
 @pytest.mark.parametrize("elem", [4, 8])
 def test_solo_schedule(emul, oracle_lib, idx, R, stage, ch, elem):
     """The one-CTA-per-solve schedules executed as k_solo.cu runs them,
@@ -289,3 +290,25 @@ def test_level_schedule_shapes(emul):
     info = run(wide, 101, b=3)
     assert info[0] == 2 and info[1] == 100
     assert run([], 0)[0] == 0
+
+
+@pytest.mark.parametrize("b", [1, 2, 3])
+@pytest.mark.parametrize("maxe", [4, 8, 16])
+@pytest.mark.parametrize("elem", [4, 8])
+@pytest.mark.parametrize("forward", [0, 1])
+def test_solo_shape(emul, b, maxe, elem, forward):
+    """The one-CTA sweep's per-class launch shape within one SM's shared
+    memory (GB300: 232,448 bytes a CTA may opt into, less the 4 KB the
+    server leaves): a power-of-two ring of at most 512 steps, 1-16 steps per
+    chunk, at least two stages and at least four for chunks above 8 steps, a
+    stage that holds a full chunk's records, and the kernel's own byte count
+    (k_sweep.h solo_smem_bytes) inside the budget."""
+    budget = 232448 - 4096
+    out = np.zeros(5, dtype=np.int64)
+    emul.emul_solo_shape(b, maxe, elem, forward, budget, _p(out))
+    R, ch, rec_stage, ns, smem = (int(v) for v in out)
+    assert 16 <= R <= 512 and R & (R - 1) == 0
+    assert 1 <= ch <= 16 and ns >= (4 if ch > 8 else 2), (ch, ns)
+    rec1 = 16 + 128 + maxe * 128 + maxe * 32 * b * b * elem + (32 * b * b * elem if forward else 0)
+    assert rec_stage == ch * rec1
+    assert 0 < smem <= budget
