@@ -1,7 +1,7 @@
 """GPU parity through the C ABI against the reference (golden fixtures) and
 the CPU oracle.
 
-Bars (the benchmark spec's tolerances, written per test):
+Bars (the parity tolerances, written per test):
   * assembled matrix and right-hand side: bit-identical to the reference
     (stronger than the 1e-12 relative-per-entry bar);
   * ILU(0) factor: bit-identical;

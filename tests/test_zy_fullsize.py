@@ -9,7 +9,7 @@ generated inputs:
   * two >= 300k-node requests of the 2D serving stream (a Poisson and an
     elasticity one), served alone by the server.
 
-Bars, per the benchmark spec (solver_ls_iter.cpp:100-172 is the reference solve):
+Bars (solver_ls_iter.cpp:100-172 is the reference solve):
   * pattern, assembled matrix, finalized right-hand side and ILU(0) factor
     bit-identical (compared as SHA-256 digests of the arrays);
   * FP64 Solve_PCG: iterations within +-2 of the oracle's and solution within
