@@ -72,3 +72,18 @@ def test_gpu_arm_fails_loudly_without_a_gpu():
     assert r.returncode != 0
     assert not [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
     assert "dfg_ctx_create" in r.stderr or "CUDA" in r.stderr
+
+
+def test_ncu_traffic_entries_by_schedule():
+    """DRAM traffic of a kernel comes from the committed capture of the same
+    kernel: sweeps are keyed by their schedule (ranged, one CTA), scaled by
+    algorithmic bytes; no entry gives None rather than another kernel's."""
+    import bench
+    one = bench.ncu_traffic("sweep_fwd:one_CTA")
+    assert one is not None and one > 0
+    assert bench.ncu_traffic("sweep_fwd:one_CTA", 2 * 661524) == 2 * one
+    ranged = bench.ncu_traffic("sweep_fwd:ranged")
+    assert ranged is not None and ranged != one
+    assert bench.ncu_traffic("sweep_bwd_b2_e4:one_CTA") is not None
+    assert bench.ncu_traffic("sweep_fwd:level-scheduled") is None
+    assert bench.ncu_traffic("no_such_kernel") is None
